@@ -1,0 +1,175 @@
+/*
+ * stormbird_gb300 — C ABI of the GB300 (sm_103a) lifting-line hot path.
+ *
+ * This library is a drop-in for the path behind the reference's `Simulation`
+ * (stormbird/src/lifting_line/simulation.rs:20-217): JSON setup in, one `do_step`
+ * per time step with the freestream at the points `get_freestream_velocity_points`
+ * returns, per-step circulation and forces out. Conventions follow the reference's
+ * C interface `cstormbird` (interfaces/cstormbird/src/lifting_line/complete_sail_model.rs:18-110):
+ * an opaque handle built from a JSON string (NULL on error), caller-owned buffers,
+ * negative integer status codes, `#[repr(C)]`-style POD results in f64.
+ *
+ * Numbers are f64 at the boundary ([x, y, z] triples, i.e. `[f64; 3]` arrays as the
+ * PyO3 binding passes them, interfaces/pystormbird/src/lifting_line/simulation.rs:117-164).
+ * Inside, the Biot-Savart sweeps run in FP32 with compensated accumulation; wake
+ * positions, the circulation solve and the residual reductions run in FP64.
+ *
+ * Threading: one handle owns one CUDA stream and its device memory. A handle is not
+ * thread-safe; different handles may be driven from different host threads.
+ * Errors: every entry point returns SB_OK (0) or a negative SB_ERR_* code; the
+ * message of the last error on the calling thread is available from sb_last_error().
+ */
+#ifndef STORMBIRD_GB300_H
+#define STORMBIRD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SB_OK 0
+#define SB_ERR_NULL_ARG (-1)    /* a required pointer was NULL (cstormbird: -1)                  */
+#define SB_ERR_SIZE (-2)        /* a buffer length does not match the model (cstormbird: -2)     */
+#define SB_ERR_BAD_JSON (-3)    /* setup JSON malformed or violates the SimulationBuilder schema  */
+#define SB_ERR_CUDA (-4)        /* a CUDA call failed; the handle should be freed                 */
+#define SB_ERR_NONFINITE (-5)   /* NaN/Inf in an input array                                      */
+#define SB_ERR_TIMEOUT (-6)     /* a bounded device-side wait ran out                             */
+#define SB_ERR_UNSUPPORTED (-7) /* valid reference setup outside this path (e.g. rotor sections)  */
+#define SB_ERR_STATE (-8)       /* call not valid in this state (e.g. induced velocities in QS)   */
+
+typedef struct sb_sim sb_sim; /* opaque simulation handle */
+
+/*
+ * Per-step output, mirroring the reference's SimulationResult
+ * (stormbird/src/common_utils/results/simulation.rs:27-40) and SolverResult
+ * (common_utils/results/solver.rs:12-18). N = span lines, S = wings.
+ * Array members are caller-owned and may be NULL (not written). The six force
+ * components are ordered circulatory, viscous_lift, sectional_drag, added_mass,
+ * gyroscopic, total (common_utils/forces_and_moments.rs:108-160).
+ */
+typedef struct sb_step_output {
+    double* circulation_strength;       /* [N]        SolverResult.circulation_strength            */
+    double* ctrl_points_velocity;       /* [N*3]      SolverResult.output_ctrl_points_velocity      */
+    double* solver_input_velocity;      /* [N*3]      felt freestream at the control points         */
+    double* angles_of_attack;           /* [N]        force_input.angles_of_attack                  */
+    double* force_input_velocity;       /* [N*3]      force_input.velocity (output frame)           */
+    double* acceleration;               /* [N*3]      force_input.acceleration (output frame)       */
+    double* ctrl_points;                /* [N*3]      ctrl points (global)                          */
+    double* sectional_forces;           /* [6*N*3]    component-major                               */
+    double* integrated_forces;          /* [S*6*3]    wing-major                                    */
+    double* integrated_moments;         /* [S*6*3]    wing-major                                    */
+    /* always written */
+    double force_sum[3];                /* SimulationResult::integrated_forces_sum  (simulation.rs:61-69) */
+    double moment_sum[3];               /* SimulationResult::integrated_moments_sum (simulation.rs:71-79) */
+    double residual;                    /* SolverResult.residual                                     */
+    int64_t iterations;                 /* SolverResult.iterations                                   */
+    int32_t converged;                  /* 1 if a tolerance was met before the iteration cap         */
+    int32_t reserved;
+} sb_step_output;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* sb_last_error(void);
+
+/* Library version string. */
+const char* sb_version(void);
+
+/*
+ * Builds a simulation from a SimulationBuilder JSON string.
+ * Replaces Simulation::new_from_string (stormbird/src/lifting_line/simulation.rs:33-39)
+ * and cstormbird's new_from_string constructor (complete_sail_model.rs:29-45).
+ * Returns NULL on error (sb_last_error() says why). device = CUDA ordinal.
+ */
+sb_sim* sb_sim_new(const char* setup_json, int device);
+
+/* Frees the handle and all device memory it owns. NULL is accepted. */
+void sb_sim_free(sb_sim* sim);
+
+/* Model sizes: span lines N, wings S, freestream points (N + wake points; N in quasi-steady). */
+int sb_sim_sizes(const sb_sim* sim, size_t* nr_span_lines, size_t* nr_wings, size_t* nr_freestream_points);
+
+/*
+ * Writes the points where do_step needs the freestream: control points, then all wake
+ * points (row-major along the span, streamwise-major). Replaces
+ * Simulation::get_freestream_velocity_points (simulation.rs:45-63). n = number of points.
+ */
+int sb_sim_get_freestream_points(const sb_sim* sim, double* points_xyz, size_t n);
+
+/*
+ * One time step. freestream_xyz holds n = nr_freestream_points velocities (host memory).
+ * Replaces Simulation::do_step (simulation.rs:107-203) and pystormbird's
+ * Simulation.do_step (interfaces/pystormbird/src/lifting_line/simulation.rs:131-149).
+ */
+int sb_sim_do_step(sb_sim* sim, double time, double time_step, const double* freestream_xyz, size_t n,
+                   sb_step_output* out);
+
+/*
+ * Same as sb_sim_do_step with the freestream already in device memory (n*3 doubles) and
+ * no host copy of the output: results stay on the device until sb_sim_read_output.
+ * Used by callers that generate the freestream on the GPU.
+ */
+int sb_sim_do_step_device(sb_sim* sim, double time, double time_step, const double* freestream_xyz_device, size_t n);
+
+/* Copies the output of the last step to host buffers (same layout as sb_sim_do_step). */
+int sb_sim_read_output(sb_sim* sim, sb_step_output* out);
+
+/*
+ * Induced velocity of the whole dynamic wake at arbitrary points (host arrays, n points).
+ * Replaces Simulation::induced_velocities (simulation.rs:207-216); SB_ERR_STATE in
+ * quasi-steady mode where the reference panics.
+ */
+int sb_sim_induced_velocities(sb_sim* sim, const double* points_xyz, size_t n, double* velocities_xyz);
+
+/* Rigid-body motion and wing-angle setters (line_force_model/data_update.rs:171-234). */
+int sb_sim_set_translation_and_rotation_with_finite_difference(sb_sim* sim, double time_step,
+                                                                const double translation[3], const double rotation[3]);
+int sb_sim_set_translation_only(sb_sim* sim, const double translation[3]);
+int sb_sim_set_rotation_only(sb_sim* sim, const double rotation[3]);
+int sb_sim_set_velocity_linear(sb_sim* sim, const double velocity[3]);
+int sb_sim_set_velocity_angular(sb_sim* sim, const double velocity[3]);
+int sb_sim_set_local_wing_angles(sb_sim* sim, const double* angles, size_t nr_wings);
+
+/* previous_circulation_strength (simulation.rs:26): reset to zero, set (warm start) or read. */
+int sb_sim_reset_previous_circulation(sb_sim* sim);
+int sb_sim_set_previous_circulation(sb_sim* sim, const double* circulation, size_t n);
+int sb_sim_get_previous_circulation(const sb_sim* sim, double* circulation, size_t n);
+
+/*
+ * Wake state for inspection and tests: points [nr_wake_points*3], strengths [nr_panels],
+ * velocity at points [nr_wake_points*3]. Any pointer may be NULL. Sizes come from
+ * sb_sim_wake_sizes. SB_ERR_STATE in quasi-steady mode.
+ */
+int sb_sim_wake_sizes(const sb_sim* sim, size_t* nr_wake_points, size_t* nr_wake_panels, size_t* nr_points_along_span,
+                      size_t* nr_panels_per_line_element);
+int sb_sim_get_wake_state(sb_sim* sim, double* points_xyz, double* strengths, double* velocities_xyz);
+
+/*
+ * Biot-Savart precision variant used by the Biot-Savart sweeps of this handle:
+ * 0 = FP32 with compensated (Kahan) accumulation (default), 1 = plain FP32,
+ * 2 = FP64. Kept as a switch for the precision study.
+ */
+int sb_sim_set_precision(sb_sim* sim, int precision_mode);
+
+/*
+ * Timing of the device work of the last step (CUDA events on the handle's stream, ms):
+ * [0] whole step, [1] wake update, [2] free-wake sweep at control points,
+ * [3] unit-strength matrix, [4] circulation solve, [5] wake roll-up sweep, [6] forces.
+ * Only filled when profiling was enabled with sb_sim_enable_timing(sim, 1).
+ */
+int sb_sim_enable_timing(sb_sim* sim, int enable);
+int sb_sim_last_step_timing(const sb_sim* sim, double* ms, size_t n);
+
+/*
+ * Work counters of the last step: [0] target x segment interactions (near field),
+ * [1] near panel pairs, [2] far panel pairs, [3] roll-up target points,
+ * [4] nonzero-strength panels. Counted on the host from the wake state sizes and the
+ * near/far split reported by the sweep kernels.
+ */
+int sb_sim_last_step_counters(const sb_sim* sim, double* counters, size_t n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* STORMBIRD_GB300_H */
