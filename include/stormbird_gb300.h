@@ -72,6 +72,9 @@ typedef struct sb_step_output {
 /* Message of the last failed call on this thread ("" if none). */
 const char* sb_last_error(void);
 
+/* Status code of the last call on this thread that reports one (e.g. why sb_sim_new gave NULL). */
+int sb_last_status(void);
+
 /* Library version string. */
 const char* sb_version(void);
 
@@ -161,10 +164,10 @@ int sb_sim_enable_timing(sb_sim* sim, int enable);
 int sb_sim_last_step_timing(const sb_sim* sim, double* ms, size_t n);
 
 /*
- * Work counters of the last step: [0] target x segment interactions (near field),
- * [1] near panel pairs, [2] far panel pairs, [3] roll-up target points,
- * [4] nonzero-strength panels. Counted on the host from the wake state sizes and the
- * near/far split reported by the sweep kernels.
+ * Sizes of the last step's Biot-Savart sweeps: [0] roll-up target points, [1] panels
+ * swept for the roll-up, [2] control points, [3] free-wake panels swept at the control
+ * points, [4] steps completed. Zero-strength panels are included in the panel counts
+ * (the sweeps skip them).
  */
 int sb_sim_last_step_counters(const sb_sim* sim, double* counters, size_t n);
 

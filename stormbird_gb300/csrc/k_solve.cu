@@ -1,0 +1,532 @@
+// Circulation solvers and force output (sm_103a), f64.
+//
+// k_solve_si: the damped fixed-point solve SimpleIterative::solve
+// (stormbird/src/lifting_line/solvers/simple_iterative.rs:86-212) for one case on one
+// thread-block cluster. Every CTA of the cluster keeps the full circulation vector in
+// shared memory; CTA r owns a contiguous block of control points. Per iteration:
+//   1. induced velocity of its rows: fixed + M * Gamma (frozen_wake.rs:268-301), one warp
+//      per row, matrix rows read from L2;
+//   2. per row: total velocity (velocity_corrections.rs:28-100), span component removed
+//      (line_force_model/mod.rs:235-254), angle of attack (force_calculations.rs:79-107),
+//      Foil lift, circulation estimate (force_calculations.rs:271-292), residual term
+//      (force_calculations.rs:552-627) and the damped update;
+//   3. new Gamma and residual terms are stored into every CTA's shared memory through
+//      distributed shared memory, the per-CTA max |dGamma| likewise, one cluster barrier;
+//   4. every CTA sums the residual terms in control-point order (the reference's order,
+//      so the convergence test takes the same branch) and takes the max.
+// All waits are hardware cluster barriers; no spin loops.
+//
+// k_solve_lin: Linearized::solve (solvers/linearized.rs:54-222) with the Gaussian
+// elimination with partial pivoting of stormath/src/matrix/linalg.rs:41-103, one CTA.
+//
+// k_forces: SimulationResult of one step (force_calculations.rs:322-452, 669-698;
+// common_utils/forces_and_moments.rs:163-245; flow_derivatives.rs:31-63).
+#include <cooperative_groups.h>
+
+#include "sb_device.cuh"
+#include "sb_kernels.h"
+
+namespace cg = cooperative_groups;
+
+namespace sbgpu {
+
+constexpr int kSolveThreads = 256;
+constexpr int kSolveRowsPerThread = 4;
+constexpr int kMaxCluster = 8;
+
+int solve_cluster_size(int N) {
+    if (N <= 64) return 1;
+    if (N <= 256) return 4;
+    return 8;
+}
+
+struct RowGeom {
+    d3 felt, span_rel, span_dir, chord, span_rel_out;
+    double chord_len, area;
+    int wing;
+};
+
+__device__ inline RowGeom row_geom(const DevModel& m, int i) {
+    RowGeom g;
+    g.felt = m.felt_ctrl[i];
+    g.span_rel = m.span_e[i] - m.span_s[i];
+    g.span_dir = normalize(g.span_rel);
+    g.chord = m.chord_global[i];
+    g.span_rel_out = m.output_body ? (m.span_e_local[i] - m.span_s_local[i]) : g.span_rel;
+    g.chord_len = m.chord_len[i];
+    g.area = m.chord_len[i] * m.span_len_local[i];
+    g.wing = m.wing_of_line[i];
+    return g;
+}
+
+// velocity_corrections.rs:28-100 (returns freestream + induced, corrected)
+__device__ inline d3 total_velocity(const SolveSettings& st, d3 fs, d3 ind) {
+    if (st.velocity_correction == 1) {
+        double im = len(ind), fm = len(fs);
+        double mx = st.velocity_correction_ratio * fm;
+        d3 c = im > mx ? normalize(ind) * mx : ind;
+        return fs + c;
+    }
+    if (st.velocity_correction == 2) return normalize(fs + ind) * len(fs);
+    return fs + ind;
+}
+
+__device__ inline double circulation_cl(const DevModel& m, const FoilP& f, double aoa) {
+    double cl = foil_cl_pre_stall(f, aoa);
+    if (m.include_viscous_lift) cl += foil_cl_post_stall(f, aoa);
+    return cl;
+}
+
+// |cl_gamma - cl_direct| of force_calculations.rs:552-607
+__device__ inline double residual_term(const DevModel& m, const RowGeom& g, const FoilP& f, double gam, d3 u, double aoa) {
+    double ul = len(u);
+    d3 force = ul == 0.0 ? mk(0, 0, 0) : (gam * cross(u, g.span_rel_out)) * m.density;
+    double sign = -1.0 * signum(gam);
+    double ff = 0.5 * g.area * m.density * len2(u);
+    double clg = ff == 0.0 ? 0.0 : len(force) * sign / ff;
+    return fabs(clg - foil_cl_pre_stall(f, aoa));
+}
+
+__global__ void __launch_bounds__(kSolveThreads) k_solve_si(DevModel m, SolveSettings st, SolveBuffers b) {
+    cg::cluster_group cl = cg::this_cluster();
+    const int CS = static_cast<int>(cl.num_blocks());
+    const int rank = static_cast<int>(cl.block_rank());
+    const int N = m.N;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = kSolveThreads / 32;
+    extern __shared__ double smem[];
+    double* G[2] = {smem, smem + N};
+    double* RR[2] = {smem + 2 * N, smem + 3 * N};
+    double* MX[2] = {smem + 4 * N, smem + 4 * N + kMaxCluster};
+    const int rp = (N + CS - 1) / CS;
+    const int r0 = min(N, rank * rp), r1 = min(N, r0 + rp);
+    d3* uind = reinterpret_cast<d3*>(smem + 4 * N + 2 * kMaxCluster);
+    __shared__ double s_res, s_red[kSolveThreads / 32];
+    __shared__ int s_conv;
+
+    const bool scale0 = fabs(st.correction_factor_initial - 1.0) > kMinPositive;
+    for (int i = tid; i < N; i += kSolveThreads) {
+        double g = b.gamma_prev[i];
+        if (scale0) g *= st.correction_factor_initial;
+        G[0][i] = g;
+    }
+    // per-thread rows
+    RowGeom rg[kSolveRowsPerThread];
+    d3 u_last[kSolveRowsPerThread];
+    double aoa_last[kSolveRowsPerThread];
+    int nrows = 0;
+    for (int k = 0; k < kSolveRowsPerThread; ++k) {
+        int i = r0 + tid + k * kSolveThreads;
+        if (i < r1) {
+            rg[k] = row_geom(m, i);
+            u_last[k] = mk(0, 0, 0);
+            aoa_last[k] = 0.0;
+            nrows = k + 1;
+        }
+    }
+    __syncthreads();
+
+    // residual of the initial solution with zero velocity (simple_iterative.rs:180-184)
+    double residual = 0.0;
+    if (st.max_iterations == 0) {
+        if (tid == 0) {
+            double s = 0.0;
+            for (int i = 0; i < N; ++i) s += fabs(0.0 - foil_cl_pre_stall(m.foils[m.wing_of_line[i]], 0.0));
+            s_res = s / static_cast<double>(N);
+        }
+        __syncthreads();
+        residual = s_res;
+    }
+    cl.sync();
+
+    int it = 0, cur = 0;
+    bool conv = false;
+    while (it < st.max_iterations && !conv) {
+        it += 1;
+        const double* Gc = G[cur];
+        // 1. induced velocity of own rows
+        for (int row = r0 + warp; row < r1; row += nwarps) {
+            const d3* fr = b.factors + static_cast<long long>(row) * N;
+            double sx = 0.0, sy = 0.0, sz = 0.0;
+            for (int j = lane; j < N; j += 32) {
+                d3 f = fr[j];
+                double g = Gc[j];
+                sx += f.x * g;
+                sy += f.y * g;
+                sz += f.z * g;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                sx += __shfl_down_sync(0xffffffffu, sx, o);
+                sy += __shfl_down_sync(0xffffffffu, sy, o);
+                sz += __shfl_down_sync(0xffffffffu, sz, o);
+            }
+            if (lane == 0) {
+                d3 fx = b.fixed[row];
+                uind[row - r0] = mk(fx.x + sx, fx.y + sy, fx.z + sz);
+            }
+        }
+        __syncthreads();
+        // 2. row updates
+        double lmax = 0.0;
+        for (int k = 0; k < nrows; ++k) {
+            int i = r0 + tid + k * kSolveThreads;
+            const RowGeom& g = rg[k];
+            const FoilP f = m.foils[g.wing];
+            d3 u = total_velocity(st, g.felt, uind[i - r0]);
+            u = u - project(u, g.span_rel);
+            double aoa = len(u) > kMinPositive ? signed_angle_between(g.chord, u, g.span_dir) : 0.0;
+            double est = -0.5 * g.chord_len * len(u) * circulation_cl(m, f, aoa);
+            double gold = Gc[i];
+            double r = residual_term(m, g, f, gold, u, aoa);
+            double d = est - gold;
+            lmax = fmax(lmax, fabs(d));
+            double gnew = gold + st.damping * d;
+            u_last[k] = u;
+            aoa_last[k] = aoa;
+            for (int q = 0; q < CS; ++q) {
+                double* Gr = cl.map_shared_rank(G[cur ^ 1], q);
+                double* Rr = cl.map_shared_rank(RR[cur], q);
+                Gr[i] = gnew;
+                Rr[i] = r;
+            }
+        }
+        // block max
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_down_sync(0xffffffffu, lmax, o));
+        if (lane == 0) s_red[warp] = lmax;
+        __syncthreads();
+        if (tid == 0) {
+            double v = 0.0;
+            for (int w = 0; w < nwarps; ++w) v = fmax(v, s_red[w]);
+            for (int q = 0; q < CS; ++q) cl.map_shared_rank(MX[cur], q)[rank] = v;
+        }
+        cl.sync();
+        if (tid == 0) {
+            double s = 0.0;
+            for (int i = 0; i < N; ++i) s += RR[cur][i];
+            double res = s / static_cast<double>(N);
+            double mx = 0.0;
+            for (int q = 0; q < CS; ++q) mx = fmax(mx, MX[cur][q]);
+            s_res = res;
+            s_conv = (res < st.residual_tolerance) || (mx < st.strength_tolerance);
+        }
+        __syncthreads();
+        residual = s_res;
+        conv = s_conv != 0;
+        cur ^= 1;
+    }
+
+    // final circulation from the last velocities (simple_iterative.rs:200-203)
+    for (int k = 0; k < nrows; ++k) {
+        int i = r0 + tid + k * kSolveThreads;
+        const RowGeom& g = rg[k];
+        double gam = -0.5 * g.chord_len * len(u_last[k]) * circulation_cl(m, m.foils[g.wing], aoa_last[k]);
+        b.gamma_prev[i] = gam;
+        b.vel_out[i] = u_last[k];
+        if (b.wake_str_row0) b.wake_str_row0[i] = gam;
+        if (b.rec32_row0) b.rec32_row0[i].v[24] = static_cast<float>(gam);
+        if (b.rec64_row0) b.rec64_row0[i].v[24] = gam;
+    }
+    if (rank == 0 && tid == 0) {
+        b.scalars[0] = residual;
+        b.scalars[1] = static_cast<double>(it);
+        b.scalars[2] = conv ? 1.0 : 0.0;
+    }
+    cl.sync();  // no CTA leaves while others may still write into its shared memory
+}
+
+cudaError_t launch_solve_simple_iterative(const DevModel& m, const SolveSettings& st, const SolveBuffers& b, cudaStream_t s) {
+    const int CS = solve_cluster_size(m.N);
+    const int rp = (m.N + CS - 1) / CS;
+    if (rp > kSolveThreads * kSolveRowsPerThread) return cudaErrorInvalidValue;
+    size_t smem = (4 * static_cast<size_t>(m.N) + 2 * kMaxCluster) * sizeof(double) + static_cast<size_t>(rp) * sizeof(d3);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_solve_si, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(CS, 1, 1);
+    cfg.blockDim = dim3(kSolveThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CS;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_solve_si, m, st, b);
+}
+
+// ---------------------------------------------------------------------------------------
+// Linearized solver, one CTA
+// ---------------------------------------------------------------------------------------
+constexpr int kLinThreads = 512;
+
+__device__ inline double block_sum(double v, double* red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0) {
+        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) t += red[w];
+        red[32] = t;
+    }
+    __syncthreads();
+    return red[32];
+}
+
+__global__ void __launch_bounds__(kLinThreads) k_solve_lin(DevModel m, SolveSettings st, SolveBuffers b) {
+    const int N = m.N, tid = threadIdx.x, nt = blockDim.x;
+    const int W1 = N + 1;
+    double* A = b.lin_work;  // [N][N+1]
+    extern __shared__ double smem[];
+    d3* vel = reinterpret_cast<d3*>(smem);               // [N]
+    d3* ind = vel + N;                                    // [N]
+    double* gam = reinterpret_cast<double*>(ind + N);     // [N]
+    double* fac = gam + N;                                // [N]
+    __shared__ double red[33];
+    __shared__ int s_piv;
+
+    // velocities with the fixed part, span removed, and the equation system (linearized.rs:61-136)
+    for (int i = tid; i < N; i += nt) {
+        RowGeom g = row_geom(m, i);
+        d3 v = g.felt + b.fixed[i];
+        v = v - project(v, g.span_rel);
+        d3 un = normalize(v);
+        d3 sd = normalize(g.span_rel);
+        d3 nd = cross(un, sd);
+        double aoa = len(v) > kMinPositive ? signed_angle_between(g.chord, v, g.span_dir) : 0.0;
+        const FoilP f = m.foils[g.wing];
+        double cll = foil_cl_linear(f, aoa);
+        double ut = dot(v, un);
+        double dcl = f.cl_initial_slope;
+        for (int c = 0; c < N; ++c) {
+            double uin = dot(b.factors[static_cast<long long>(i) * N + c], nd);
+            double a = -dcl * uin / ut;
+            if (i == c) a += 2.0 / (g.chord_len * ut);
+            A[static_cast<long long>(i) * W1 + c] = a;
+        }
+        A[static_cast<long long>(i) * W1 + N] = -cll;
+    }
+    __syncthreads();
+    // forward elimination with partial pivoting
+    for (int k = 0; k < N; ++k) {
+        if (tid == 0) {
+            int mr = k;
+            for (int i = k + 1; i < N; ++i)
+                if (fabs(A[static_cast<long long>(i) * W1 + k]) > fabs(A[static_cast<long long>(mr) * W1 + k])) mr = i;
+            s_piv = mr;
+        }
+        __syncthreads();
+        int mr = s_piv;
+        if (mr != k)
+            for (int j = tid; j <= N; j += nt) {
+                double t = A[static_cast<long long>(k) * W1 + j];
+                A[static_cast<long long>(k) * W1 + j] = A[static_cast<long long>(mr) * W1 + j];
+                A[static_cast<long long>(mr) * W1 + j] = t;
+            }
+        __syncthreads();
+        double piv = A[static_cast<long long>(k) * W1 + k];
+        if (fabs(piv) < 1e-12) {
+            if (tid == 0) {
+                atomicExch(b.err, kDevSingular);
+                b.scalars[3] = 1.0;
+            }
+            return;
+        }
+        for (int i = k + 1 + tid; i < N; i += nt) fac[i] = A[static_cast<long long>(i) * W1 + k] / piv;
+        __syncthreads();
+        const long long rows = N - k - 1, cols = N + 1 - k;
+        for (long long q = tid; q < rows * cols; q += nt) {
+            int i = k + 1 + static_cast<int>(q / cols), j = k + static_cast<int>(q % cols);
+            A[static_cast<long long>(i) * W1 + j] -= fac[i] * A[static_cast<long long>(k) * W1 + j];
+        }
+        __syncthreads();
+    }
+    // back substitution
+    for (int i = N - 1; i >= 0; --i) {
+        double part = 0.0;
+        for (int j = i + 1 + tid; j < N; j += nt) part += A[static_cast<long long>(i) * W1 + j] * gam[j];
+        double sum = block_sum(part, red);
+        if (tid == 0) gam[i] = (A[static_cast<long long>(i) * W1 + N] - sum) / A[static_cast<long long>(i) * W1 + i];
+        __syncthreads();
+    }
+    // induced velocity and the total velocity (linearized.rs:141-156)
+    auto update_induced = [&]() {
+        for (int i = tid; i < N; i += nt) {
+            double sx = 0.0, sy = 0.0, sz = 0.0;
+            for (int c = 0; c < N; ++c) {
+                d3 f = b.factors[static_cast<long long>(i) * N + c];
+                sx += f.x * gam[c];
+                sy += f.y * gam[c];
+                sz += f.z * gam[c];
+            }
+            d3 fx = b.fixed[i];
+            ind[i] = mk(fx.x + sx, fx.y + sy, fx.z + sz);
+        }
+        __syncthreads();
+    };
+    update_induced();
+    for (int i = tid; i < N; i += nt) vel[i] = total_velocity(st, m.felt_ctrl[i], ind[i]);
+    __syncthreads();
+    // viscous correction (linearized.rs:158-202)
+    if (!st.disable_viscous_corrections) {
+        for (int i = tid; i < N; i += nt) {
+            RowGeom g = row_geom(m, i);
+            const FoilP f = m.foils[g.wing];
+            double aoa = len(vel[i]) > kMinPositive ? signed_angle_between(g.chord, vel[i], g.span_dir) : 0.0;
+            double cll = foil_cl_linear(f, aoa);
+            double clf = foil_cl_pre_stall(f, aoa);
+            if (fabs(cll) > kMinPositive) gam[i] *= clf / cll;
+        }
+        __syncthreads();
+        if (st.full_induced_correction) update_induced();
+        for (int i = tid; i < N; i += nt) vel[i] = total_velocity(st, m.felt_ctrl[i], ind[i]);
+        __syncthreads();
+    }
+    // residual (linearized.rs:204-213), summed in control-point order
+    if (tid == 0) {
+        double s = 0.0;
+        for (int i = 0; i < N; ++i) {
+            RowGeom g = row_geom(m, i);
+            const FoilP f = m.foils[g.wing];
+            double aoa = len(vel[i]) > kMinPositive ? signed_angle_between(g.chord, vel[i], g.span_dir) : 0.0;
+            s += residual_term(m, g, f, gam[i], vel[i], aoa);
+        }
+        b.scalars[0] = s / static_cast<double>(N);
+        b.scalars[1] = 1.0;
+        b.scalars[2] = 1.0;
+    }
+    for (int i = tid; i < N; i += nt) {
+        b.gamma_prev[i] = gam[i];
+        b.vel_out[i] = vel[i];
+        if (b.wake_str_row0) b.wake_str_row0[i] = gam[i];
+        if (b.rec32_row0) b.rec32_row0[i].v[24] = static_cast<float>(gam[i]);
+        if (b.rec64_row0) b.rec64_row0[i].v[24] = gam[i];
+    }
+}
+
+cudaError_t launch_solve_linearized(const DevModel& m, const SolveSettings& st, const SolveBuffers& b, cudaStream_t s) {
+    size_t smem = static_cast<size_t>(m.N) * (2 * sizeof(d3) + 2 * sizeof(double));
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_solve_lin, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+    }
+    k_solve_lin<<<1, kLinThreads, smem, s>>>(m, st, b);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------
+// Forces, one CTA
+// ---------------------------------------------------------------------------------------
+__global__ void k_forces(DevModel m, StepParams p, ForceArgs f) {
+    const int N = m.N, S = m.S, tid = threadIdx.x, nt = blockDim.x;
+    const OutLayout L = OutLayout::make(N, S);
+    double* o = f.out;
+    const bool body = m.output_body != 0;
+    for (int i = tid; i < N; i += nt) {
+        double g = f.gamma[i];
+        d3 v = f.vel[i];
+        d3 sr = m.span_e[i] - m.span_s[i];
+        double aoa = len(v) > kMinPositive ? signed_angle_between(m.chord_global[i], v, normalize(sr)) : 0.0;
+        d3 acc = mk(0, 0, 0);
+        if (f.fd_count >= 2) acc = (v * 3.0 - f.hist1[i] * 4.0 + f.hist0[i]) / (2.0 * p.dt);
+        f.hist0[i] = f.hist1[i];
+        f.hist1[i] = v;
+        d3 fv = body ? to_body(v, p.rotation) : v;
+        d3 fa = body ? to_body(acc, p.rotation) : acc;
+        d3 sl_local = m.span_e_local[i] - m.span_s_local[i];
+        d3 sl_out = body ? sl_local : sr;
+        d3 cv_out = body ? m.chord_local[i] : m.chord_global[i];
+        const FoilP fo = m.foils[m.wing_of_line[i]];
+        double area = m.chord_len[i] * m.span_len_local[i];
+        double ff = 0.5 * area * m.density * len2(fv);
+        d3 circ = len(fv) == 0.0 ? mk(0, 0, 0) : (g * cross(fv, sl_out)) * m.density;
+        d3 visc = mk(0, 0, 0);
+        if (!m.include_viscous_lift) visc = normalize(cross(sl_local, fv)) * foil_cl_post_stall(fo, aoa) * ff;
+        d3 drag = normalize(fv) * foil_cd(fo, aoa) * ff;
+        double strip = m.chord_len[i] * len(sl_out);
+        d3 ra = fa - project(fa, normalize(sl_out));
+        ra = ra - project(ra, cv_out);
+        d3 am = mk(0, 0, 0);
+        if (len(ra) != 0.0) am = (fo.added_mass_factor * len(ra)) * m.density * strip * normalize(ra);
+        d3 gy = mk(0, 0, 0);
+        d3 tot = circ;
+        tot = tot + visc;
+        tot = tot + drag;
+        tot = tot + am;
+        tot = tot + gy;
+        d3 comps[6] = {circ, visc, drag, am, gy, tot};
+        o[L.gamma + i] = g;
+        d3 ctrl = m.ctrl[i];
+        d3 felt = m.felt_ctrl[i];
+        const d3* src[6] = {&v, &felt, &fv, &fa, &ctrl, nullptr};
+        long long offs[5] = {L.vel, L.felt, L.fvel, L.acc, L.ctrl};
+        for (int q = 0; q < 5; ++q) {
+            o[offs[q] + 3 * i] = src[q]->x;
+            o[offs[q] + 3 * i + 1] = src[q]->y;
+            o[offs[q] + 3 * i + 2] = src[q]->z;
+        }
+        o[L.aoa + i] = aoa;
+        for (int c = 0; c < 6; ++c) {
+            long long base = L.sect + (static_cast<long long>(c) * N + i) * 3;
+            o[base] = comps[c].x;
+            o[base + 1] = comps[c].y;
+            o[base + 2] = comps[c].z;
+        }
+    }
+    __syncthreads();
+    for (int w = tid; w < S; w += nt) {
+        d3 fs[6], ms[6];
+        for (int c = 0; c < 6; ++c) fs[c] = ms[c] = mk(0, 0, 0);
+        for (int i = m.wing_start[w]; i < m.wing_end[w]; ++i) {
+            if (m.is_virtual[i]) continue;
+            d3 cp = body ? 0.5 * (m.span_s_local[i] + m.span_e_local[i]) : 0.5 * (m.span_s[i] + m.span_e[i]);
+            for (int c = 0; c < 6; ++c) {
+                long long base = L.sect + (static_cast<long long>(c) * N + i) * 3;
+                d3 sf = mk(o[base], o[base + 1], o[base + 2]);
+                fs[c] = fs[c] + sf;
+                ms[c] = ms[c] + cross(cp, sf);
+            }
+        }
+        for (int c = 0; c < 6; ++c) {
+            long long bf = L.intf + (static_cast<long long>(w) * 6 + c) * 3, bm = L.intm + (static_cast<long long>(w) * 6 + c) * 3;
+            o[bf] = fs[c].x;
+            o[bf + 1] = fs[c].y;
+            o[bf + 2] = fs[c].z;
+            o[bm] = ms[c].x;
+            o[bm + 1] = ms[c].y;
+            o[bm + 2] = ms[c].z;
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        d3 fsum = mk(0, 0, 0), msum = mk(0, 0, 0);
+        for (int w = 0; w < S; ++w) {
+            long long bf = L.intf + (static_cast<long long>(w) * 6 + 5) * 3, bm = L.intm + (static_cast<long long>(w) * 6 + 5) * 3;
+            fsum = fsum + mk(o[bf], o[bf + 1], o[bf + 2]);
+            msum = msum + mk(o[bm], o[bm + 1], o[bm + 2]);
+        }
+        o[L.fsum] = fsum.x;
+        o[L.fsum + 1] = fsum.y;
+        o[L.fsum + 2] = fsum.z;
+        o[L.msum] = msum.x;
+        o[L.msum + 1] = msum.y;
+        o[L.msum + 2] = msum.z;
+        o[L.residual] = f.scalars[0];
+        o[L.iterations] = f.scalars[1];
+        o[L.converged] = f.scalars[2];
+    }
+}
+
+cudaError_t launch_forces(const DevModel& m, const StepParams& p, const ForceArgs& f, cudaStream_t s) {
+    k_forces<<<1, 256, 0, s>>>(m, p, f);
+    return cudaGetLastError();
+}
+
+}  // namespace sbgpu

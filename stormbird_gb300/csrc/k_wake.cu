@@ -1,0 +1,276 @@
+// Line-force-model geometry and dynamic-wake update kernels (sm_103a). HBM-bound.
+//
+// Reference: stormbird/src/line_force_model/data_update.rs:13-90 (global geometry),
+// force_calculations.rs:50-69 (felt velocity), value_mapping.rs:87-137 (control point ->
+// span point values), lifting_line/wake/dynamic_wake/update_data.rs:28-328 (wake points
+// before solving, panels, strength shift) and initialization.rs:12-71.
+//
+// The wake points live in two buffers (current / next). A step reads the current points
+// and velocities and writes the next points, so the reference's in-place reverse sweep
+// (new row i = old row i-1 + dt * velocity) becomes one independent update per point.
+// Positions are integrated in f64; the panel records for the sweep are written in FP32
+// (and f64 for the first row and in the FP64 precision mode).
+#include "sb_device.cuh"
+#include "sb_kernels.h"
+
+namespace sbgpu {
+
+// ---------------------------------------------------------------------------------------
+// Geometry of the line force model for one step. One CTA: O(N) work.
+// ---------------------------------------------------------------------------------------
+__global__ void k_prep_geometry(DevModel m, StepParams p, const d3* fs_ctrl, d3* mean_out) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int i = tid; i < m.N; i += nt) {
+        int w = m.wing_of_line[i];
+        int ws = m.wing_start[w];
+        d3 axis = m.span_e_local[ws] - m.span_s_local[ws];  // data_access.rs:256-258
+        d3 cl = rotate_around_axis(m.chord_not_rotated[i], p.local_wing_angles[w], axis);
+        m.chord_local[i] = cl;
+        m.chord_global[i] = rotate_xyz(cl, p.rotation);
+        d3 s = rotate_xyz(m.span_s_local[i], p.rotation) + p.translation;
+        d3 e = rotate_xyz(m.span_e_local[i], p.rotation) + p.translation;
+        m.span_s[i] = s;
+        m.span_e[i] = e;
+        d3 c = 0.5 * (s + e);
+        m.ctrl[i] = c;
+        if (fs_ctrl) {
+            // rigid_body_motion.rs:53-60
+            d3 mv = p.velocity_linear + cross(p.velocity_angular, c - p.translation);
+            m.felt_ctrl[i] = fs_ctrl[i] - mv;
+        }
+    }
+    __syncthreads();
+    for (int k = tid; k < m.Np; k += nt) {
+        int l = m.sp_line[k];
+        m.span_pts[k] = m.sp_end[k] ? m.span_e[l] : m.span_s[l];
+        int a = m.sp_val_a[k], b = m.sp_val_b[k];
+        m.chord_span_pts[k] = (a == b) ? m.chord_global[a] : (m.chord_global[a] + m.chord_global[b]) * 0.5;
+        if (fs_ctrl) m.felt_span[k] = (a == b) ? m.felt_ctrl[a] : (m.felt_ctrl[a] + m.felt_ctrl[b]) * 0.5;
+    }
+    if (mean_out && tid == 0) {
+        // simulation.rs:74-75: sum in order, then divide
+        d3 s = mk(0, 0, 0);
+        for (int i = 0; i < m.N; ++i) s = s + fs_ctrl[i];
+        *mean_out = s / static_cast<double>(m.N);
+    }
+}
+
+cudaError_t launch_prep_geometry(const DevModel& m, const StepParams& p, const d3* fs_ctrl, d3* mean_out, cudaStream_t s) {
+    k_prep_geometry<<<1, 512, 0, s>>>(m, p, fs_ctrl, mean_out);
+    return cudaGetLastError();
+}
+
+// Direction of the first free wake row (update_data.rs:152-199).
+__device__ inline d3 first_row_direction(const DevModel& m, int j, const d3* vel_row0, const d3* vel_row1, int steps_done,
+                                         d3 felt_span_j) {
+    if (m.first_dir == 0) return normalize(m.chord_span_pts[j]);
+    if (m.first_dir == 2 && steps_done > 2) return normalize(0.5 * (vel_row0[j] + vel_row1[j]));
+    return normalize(felt_span_j);
+}
+
+// ---------------------------------------------------------------------------------------
+// Initialisation (initialization.rs:12-41): W+1 passes of update_wake_points_before_solving
+// with a uniform velocity U. One thread per spanwise column, in place on the current buffer.
+// Without shape damping the passes collapse to rows 0, 1, then rows 2..W-1 reached by
+// repeated addition of dt*U along the column (the same additions, in the same order, as
+// the reference's passes), and the last row. With damping the passes are run literally.
+// ---------------------------------------------------------------------------------------
+__global__ void k_wake_init(DevModel m, WakeBuffers w, const d3* mean_dev, d3 U_host, double dt, int fill_rows) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const d3 U = mean_dev ? *mean_dev : U_host;
+    // strengths and velocities (both strength buffers hold zeros afterwards)
+    for (long long id = j; id < m.P_pan; id += static_cast<long long>(gridDim.x) * blockDim.x) {
+        w.str_old[id] = 0.0;
+        w.str_new[id] = 0.0;
+    }
+    for (long long id = j; id < m.P_pts; id += static_cast<long long>(gridDim.x) * blockDim.x) w.vel[id] = U;
+    if (j >= m.Np) return;
+    const int Np = m.Np, W = m.W;
+    d3* P = w.pts_old;
+    const d3 S = m.span_pts[j];
+    const d3 dir1 = first_row_direction(m, j, nullptr, nullptr, 0, U);
+    const double L1 = m.rep_chord * m.first_rel;
+    const double Ll = m.last_rel * m.rep_chord;
+    const d3 dU = dt * U;
+    if (fill_rows)  // builder state: every row on the span points (builder.rs:128-135)
+        for (int s = 0; s <= W; ++s) P[static_cast<long long>(s) * Np + j] = S;
+    if (m.damping <= 0.0) {
+        P[j] = S;
+        if (W == 1) {
+            P[Np + j] = S + Ll * normalize(U);
+            return;
+        }
+        d3 r1 = S + dir1 * L1;
+        P[Np + j] = r1;
+        d3 prev2 = S, prev = r1;
+        for (int s = 2; s <= W - 1; ++s) {
+            d3 r = prev + dU;
+            P[static_cast<long long>(s) * Np + j] = r;
+            prev2 = prev;
+            prev = r;
+        }
+        P[static_cast<long long>(W) * Np + j] = prev + Ll * normalize(prev - prev2);
+        return;
+    }
+    const double D = m.damping;
+    for (int pass = 0; pass <= W; ++pass) {
+        P[j] = S;
+        for (int s = W; s >= 2; --s) {
+            d3 integ = P[static_cast<long long>(s - 1) * Np + j] + dU;
+            long long ci = static_cast<long long>(s) * Np + j;
+            P[ci] = P[ci] * D + integ * (1.0 - D);
+        }
+        d3 est = P[j] + dir1 * L1;
+        P[Np + j] = P[Np + j] * D + est * (1.0 - D);
+        if (W > 1) {
+            d3 a = P[static_cast<long long>(W - 1) * Np + j], b = P[static_cast<long long>(W - 2) * Np + j];
+            P[static_cast<long long>(W) * Np + j] = a + Ll * normalize(a - b);
+        } else {
+            P[Np + j] = P[j] + Ll * normalize(U);
+        }
+    }
+}
+
+cudaError_t launch_wake_init(const DevModel& m, const WakeBuffers& w, const d3* mean_dev, d3 U, double dt, int fill_rows,
+                             cudaStream_t s) {
+    int threads = 128;
+    int blocks = (m.Np + threads - 1) / threads;
+    if (blocks < 64) blocks = 64;  // the zero-fill loops are grid-strided
+    k_wake_init<<<blocks, threads, 0, s>>>(m, w, mean_dev, U, dt, fill_rows);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------
+// Rows 0..W-1 of the next wake points (update_data.rs:65-82, 90-99, 205-252, 295-316).
+// ---------------------------------------------------------------------------------------
+__global__ void k_wake_advect(DevModel m, WakeBuffers w, double dt, int steps_done) {
+    long long id = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+    const long long Np = m.Np;
+    if (id >= static_cast<long long>(m.W) * Np) return;
+    const int s = static_cast<int>(id / Np), j = static_cast<int>(id % Np);
+    const double D = m.damping;
+    d3 out;
+    if (s == 0) {
+        out = m.span_pts[j];
+    } else if (s == 1) {
+        d3 dir = first_row_direction(m, j, w.vel, w.vel + Np, steps_done, m.felt_span[j]);
+        d3 est = m.span_pts[j] + dir * (m.rep_chord * m.first_rel);
+        out = D > 0.0 ? w.pts_old[Np + j] * D + est * (1.0 - D) : est;
+    } else {
+        long long pi = id - Np;
+        d3 integ = w.pts_old[pi] + dt * w.vel[pi];
+        out = D > 0.0 ? w.pts_old[id] * D + integ * (1.0 - D) : integ;
+    }
+    w.pts_new[id] = out;
+}
+
+// Last row (update_data.rs:262-292).
+__global__ void k_wake_last_row(DevModel m, WakeBuffers w) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m.Np) return;
+    const long long Np = m.Np;
+    const int W = m.W;
+    d3 prev = w.pts_new[static_cast<long long>(W - 1) * Np + j];
+    d3 dir = W > 1 ? normalize(prev - w.pts_new[static_cast<long long>(W - 2) * Np + j]) : normalize(m.felt_span[j]);
+    w.pts_new[static_cast<long long>(W) * Np + j] = prev + (m.last_rel * m.rep_chord) * dir;
+}
+
+cudaError_t launch_wake_advect(const DevModel& m, const WakeBuffers& w, double dt, int steps_done, cudaStream_t s) {
+    long long tot = static_cast<long long>(m.W) * m.Np;
+    int threads = 256;
+    k_wake_advect<<<static_cast<unsigned>((tot + threads - 1) / threads), threads, 0, s>>>(m, w, dt, steps_done);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_wake_last_row<<<(m.Np + 127) / 128, 128, 0, s>>>(m, w);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------
+// Panel records from the new points (panel.rs:26-50, geometry_functions.rs:11-30,
+// dynamic_wake/mod.rs:82-103) and the strength shift (update_data.rs:319-328).
+// ---------------------------------------------------------------------------------------
+__global__ void k_wake_panels(DevModel m, WakeBuffers w, int shift) {
+    long long id = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+    if (id >= m.P_pan) return;
+    const int N = m.N;
+    const long long Np = m.Np;
+    const int s = static_cast<int>(id / N), j = static_cast<int>(id % N);
+    const int wg = m.wing_of_line[j];
+    const d3* P = w.pts_new;
+    d3 p0 = P[s * Np + j + wg], p1 = P[s * Np + j + 1 + wg];
+    d3 p2 = P[(s + 1) * Np + j + 1 + wg], p3 = P[(s + 1) * Np + j + wg];
+    d3 c = 0.25 * (((p0 + p1) + p2) + p3);
+    double la = len(p1 - p0), lb = len(p2 - p1), lc = len(p3 - p2), ld = len(p0 - p3);
+    double sp = (la + lb + lc + ld) * 0.5;
+    double area = sqrt((sp - la) * (sp - lb) * (sp - lc) * (sp - ld));
+    d3 n = normalize(cross(p2 - p0, p3 - p1));
+    double rep = fmax(la, lb);
+    double t = rep * m.far_field_ratio;
+    double ff2 = t * t;
+    double rc = m.panel_core[id];
+    double g;
+    if (shift) g = (s == 0) ? w.str_old[j] : w.str_old[id - N];
+    else g = w.str_old[id];
+    w.str_new[id] = g;
+
+    PanelRec<float> r;
+    float px[4] = {static_cast<float>(p0.x), static_cast<float>(p1.x), static_cast<float>(p2.x), static_cast<float>(p3.x)};
+    float py[4] = {static_cast<float>(p0.y), static_cast<float>(p1.y), static_cast<float>(p2.y), static_cast<float>(p3.y)};
+    float pz[4] = {static_cast<float>(p0.z), static_cast<float>(p1.z), static_cast<float>(p2.z), static_cast<float>(p3.z)};
+    for (int k = 0; k < 4; ++k) {
+        r.v[3 * k] = px[k];
+        r.v[3 * k + 1] = py[k];
+        r.v[3 * k + 2] = pz[k];
+        float dx = px[(k + 1) & 3] - px[k], dy = py[(k + 1) & 3] - py[k], dz = pz[(k + 1) & 3] - pz[k];
+        float l2 = dx * dx + dy * dy + dz * dz;
+        r.v[12 + k] = l2 > 0.f ? 1.0f / l2 : 0.f;
+    }
+    r.v[16] = static_cast<float>(c.x);
+    r.v[17] = static_cast<float>(c.y);
+    r.v[18] = static_cast<float>(c.z);
+    r.v[19] = static_cast<float>(ff2);
+    r.v[20] = static_cast<float>(n.x);
+    r.v[21] = static_cast<float>(n.y);
+    r.v[22] = static_cast<float>(n.z);
+    r.v[23] = static_cast<float>(area * kFourPiInv);
+    r.v[24] = static_cast<float>(g);
+    double rc2 = rc * rc;
+    r.v[25] = static_cast<float>(rc2 * rc2);
+    r.v[26] = static_cast<float>(wg);
+    r.v[27] = rc == 0.0 ? 1.f : 0.f;
+    w.rec32[id] = r;
+
+    if (s == 0 || w.rec64) {
+        PanelRec<double> q;
+        d3 pp[4] = {p0, p1, p2, p3};
+        for (int k = 0; k < 4; ++k) {
+            q.v[3 * k] = pp[k].x;
+            q.v[3 * k + 1] = pp[k].y;
+            q.v[3 * k + 2] = pp[k].z;
+            q.v[12 + k] = 0.0;
+        }
+        q.v[16] = c.x;
+        q.v[17] = c.y;
+        q.v[18] = c.z;
+        q.v[19] = ff2;
+        q.v[20] = n.x;
+        q.v[21] = n.y;
+        q.v[22] = n.z;
+        q.v[23] = area * kFourPiInv;
+        q.v[24] = g;
+        q.v[25] = rc;
+        q.v[26] = static_cast<double>(wg);
+        q.v[27] = 0.0;
+        if (s == 0) w.row0_64[j] = q;
+        if (w.rec64) w.rec64[id] = q;
+    }
+}
+
+cudaError_t launch_wake_panels(const DevModel& m, const WakeBuffers& w, int shift, cudaStream_t s) {
+    int threads = 128;
+    long long blocks = (m.P_pan + threads - 1) / threads;
+    k_wake_panels<<<static_cast<unsigned>(blocks), threads, 0, s>>>(m, w, shift);
+    return cudaGetLastError();
+}
+
+}  // namespace sbgpu

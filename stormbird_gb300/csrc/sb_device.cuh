@@ -1,0 +1,244 @@
+// Device-side data layout and math shared by the lifting-line kernels (sm_103a).
+//
+// Layout in HBM (one simulation handle):
+//   * line force model, constant: local span lines, chord vectors, chord lengths, wing of
+//     each line, Foil parameters per wing                       (SoA, f64)
+//   * per-step geometry written by k_prep_geometry: global span lines, span points,
+//     control points, chord vectors, felt velocities            (SoA, f64)
+//   * wake points, two buffers (old/new) of [W+1][Np] double3, streamwise-major, and the
+//     velocity at the points [W+1][Np] double3                   (f64: position integration)
+//   * wake strengths, two buffers of [W][N] f64
+//   * wake panel records [W][N], 28 floats each (112 B, 16-B aligned) for the FP32
+//     Biot-Savart sweep, plus f64 records for the first row (unit-strength matrix) and,
+//     in the FP64 precision mode, for every panel
+//   * frozen wake: fixed velocities [N] double3, unit matrix [N][N] double3
+//   * solver state: previous circulation [N], flow-derivative history [2][N] double3
+//   * output block: every per-step result in one contiguous f64 array, copied to the host
+//     with a single D2H per step.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sbgpu {
+
+constexpr int kMaxWings = 64;
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kTau = 2.0 * kPi;
+constexpr double kMinPositive = 2.2250738585072014e-308;
+constexpr double kFourPiInv = 1.0 / (4.0 * kPi);
+
+// ---------------------------------------------------------------------------------------
+// f64 3-vector
+// ---------------------------------------------------------------------------------------
+struct d3 {
+    double x, y, z;
+};
+__host__ __device__ inline d3 mk(double x, double y, double z) { return d3{x, y, z}; }
+__host__ __device__ inline d3 operator+(d3 a, d3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__host__ __device__ inline d3 operator-(d3 a, d3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__host__ __device__ inline d3 operator-(d3 a) { return {-a.x, -a.y, -a.z}; }
+__host__ __device__ inline d3 operator*(d3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+__host__ __device__ inline d3 operator*(double s, d3 a) { return {s * a.x, s * a.y, s * a.z}; }
+__host__ __device__ inline d3 operator/(d3 a, double s) { return {a.x / s, a.y / s, a.z / s}; }
+__host__ __device__ inline double dot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__host__ __device__ inline double len2(d3 a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+__host__ __device__ inline double len(d3 a) { return sqrt(len2(a)); }
+__host__ __device__ inline d3 cross(d3 a, d3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__host__ __device__ inline d3 normalize(d3 a) {
+    double l = len(a);
+    if (l > 0.0) return {a.x / l, a.y / l, a.z / l};
+    return {0.0, 0.0, 0.0};
+}
+__host__ __device__ inline d3 project(d3 a, d3 onto) {
+    d3 n = normalize(onto);
+    return n * dot(a, n);
+}
+__host__ __device__ inline double signum(double v) { return copysign(1.0, v); }
+
+// Angle between two vectors, signed by the right-hand rule about `axis`
+// (stormath/src/spatial_vector/vector_math.rs:65-95).
+__device__ inline double signed_angle_between(d3 a, d3 b, d3 axis) {
+    double triple = dot(a, cross(b, axis));
+    double al = len2(a), bl = len2(b);
+    double ang = 0.0;
+    if (!(al == 0.0 || bl == 0.0)) {
+        double c = dot(a, b) / sqrt(al * bl);
+        c = fmin(fmax(c, -1.0), 1.0);
+        ang = acos(c);
+    }
+    return triple > 0.0 ? ang : -ang;
+}
+
+// Rodrigues rotation (stormath/src/spatial_vector/transformations.rs:139-150).
+__device__ inline d3 rotate_around_axis(d3 v, double angle, d3 axis) {
+    d3 n = normalize(axis);
+    double c = cos(angle), s = sin(angle);
+    d3 t1 = v * c;
+    d3 t2 = cross(n, v) * s;
+    d3 t3 = n * dot(n, v) * (1.0 - c);
+    return t1 + t2 + t3;
+}
+
+// Euler XYZ rotation (transformations.rs:182-207). The line force model's rigid-body
+// motion always uses this form: the builder never copies its rotation_type into the
+// motion (line_force_model/builder/mod.rs:107-108).
+__device__ inline d3 rotate_xyz(d3 v, d3 r) {
+    d3 n = v;
+    if (r.x != 0.0) {
+        double ty = n.y, tz = n.z, c = cos(r.x), s = sin(r.x);
+        n.y = ty * c - tz * s;
+        n.z = ty * s + tz * c;
+    }
+    if (r.y != 0.0) {
+        double tx = n.x, tz = n.z, c = cos(r.y), s = sin(r.y);
+        n.x = tx * c + tz * s;
+        n.z = -tx * s + tz * c;
+    }
+    if (r.z != 0.0) {
+        double tx = n.x, ty = n.y, c = cos(r.z), s = sin(r.z);
+        n.x = tx * c - ty * s;
+        n.y = tx * s + ty * c;
+    }
+    return n;
+}
+
+// Vector expressed in the body frame (transformations.rs:233-265, XYZ).
+__device__ inline d3 to_body(d3 v, d3 r) {
+    d3 ax = rotate_xyz(mk(1, 0, 0), r), ay = rotate_xyz(mk(0, 1, 0), r), az = rotate_xyz(mk(0, 0, 1), r);
+    return {dot(v, ax), dot(v, ay), dot(v, az)};
+}
+
+// ---------------------------------------------------------------------------------------
+// Foil section model (stormbird/src/section_models/foil.rs), f64
+// ---------------------------------------------------------------------------------------
+struct FoilP {
+    double cl_zero_angle, cl_initial_slope, cl_high_order_factor_positive, cl_high_order_factor_negative,
+        cl_high_order_power, cl_max_after_stall, cd_min, angle_cd_min, cd_second_order_factor, cd_max_after_stall,
+        cd_power_after_stall, cdi_correction_factor, mean_positive_stall_angle, mean_negative_stall_angle, stall_range,
+        cd_bump_during_stall, cd_stall_angle_offset, added_mass_factor;
+};
+
+// stormath/src/transition_functions.rs:20-27
+__device__ inline double sigmoid_zero_to_one(double x, double x0, double range) {
+    double slope = 4.5951212 / range;
+    return 1.0 / (1.0 + exp(-(slope * (x - x0))));
+}
+// foil.rs:119-129
+__device__ inline double stall_angle(double a) {
+    double e = fabs(a);
+    while (e > kPi) e -= kPi;
+    return e * signum(a);
+}
+// foil.rs:256-270
+__device__ inline double foil_amount_of_stall(const FoilP& f, double a) {
+    double e = a + f.angle_cd_min;
+    double mean = e >= 0.0 ? fabs(f.mean_positive_stall_angle) : fabs(f.mean_negative_stall_angle);
+    return sigmoid_zero_to_one(fabs(e), mean, f.stall_range);
+}
+// foil.rs:161-163
+__device__ inline double foil_cl_linear(const FoilP& f, double a) { return f.cl_zero_angle + f.cl_initial_slope * sin(a); }
+// foil.rs:166-190
+__device__ inline double foil_cl_pre_stall(const FoilP& f, double a) {
+    double hp = f.cl_high_order_power > 0.0 ? pow(fabs(a), f.cl_high_order_power) * signum(a) : 0.0;
+    double hf = a >= 0.0 ? f.cl_high_order_factor_positive : f.cl_high_order_factor_negative;
+    double raw = foil_cl_linear(f, a) + hf * hp;
+    return raw * (1.0 - foil_amount_of_stall(f, a));
+}
+// foil.rs:193-206
+__device__ inline double foil_cl_post_stall(const FoilP& f, double a) {
+    double raw = f.cl_max_after_stall * sin(2.0 * stall_angle(a));
+    return raw * foil_amount_of_stall(f, a);
+}
+// foil.rs:212-243
+__device__ inline double foil_cd(const FoilP& f, double a) {
+    double sa = stall_angle(a);
+    double eff = fabs(a + f.angle_cd_min);
+    double pre = f.cd_min + f.cd_second_order_factor * (eff * eff);
+    double post = f.cd_max_after_stall * pow(fabs(sin(sa)), f.cd_power_after_stall);
+    double at = a + f.cd_stall_angle_offset * signum(a);
+    double s = foil_amount_of_stall(f, at);
+    double raw = pre * (1.0 - s) + s * post;
+    double during = f.cd_bump_during_stall * ((1.0 - cos(s * kTau)) * 0.5);
+    if (f.cdi_correction_factor != 0.0) {
+        double cl = fabs(foil_cl_post_stall(f, a) + foil_cl_pre_stall(f, a));
+        return raw + f.cdi_correction_factor * (cl * cl) + during;
+    }
+    return raw + during;
+}
+
+// ---------------------------------------------------------------------------------------
+// Panel records
+// ---------------------------------------------------------------------------------------
+// Record of one vortex-ring panel for the Biot-Savart sweeps, `R` = float or double.
+//   [0..11]  corners p0..p3 (x, y, z)
+//   [12..15] 1/|p_{k+1} - p_k|^2 per ring segment k (0 for a degenerate segment)
+//   [16..18] centre, [19] far-field length squared
+//   [20..22] unit normal, [23] area / (4 pi)
+//   [24] strength Gamma, [25] core length^4, [26] wing index, [27] 1 if core length == 0
+template <class R>
+struct __align__(16) PanelRec {
+    R v[28];
+};
+static_assert(sizeof(PanelRec<float>) == 112, "FP32 panel record is 112 bytes");
+static_assert(sizeof(PanelRec<double>) == 224, "FP64 panel record is 224 bytes");
+
+// ---------------------------------------------------------------------------------------
+// Model and step parameters
+// ---------------------------------------------------------------------------------------
+struct DevModel {
+    int N = 0;        // span lines
+    int S = 0;        // wings
+    int Np = 0;       // span points (N + S)
+    int W = 0;        // panels per line element (wake rows of panels)
+    int Wp = 0;       // points per line element (W + 1)
+    long long P_pan = 0, P_pts = 0;
+    double density = 1.225;
+    double rep_chord = 0.0;          // representative chord (mean chord length)
+    double first_rel = 0.75, last_rel = 0.25, damping = 0.0, far_field_ratio = 5.0;
+    int first_dir = 0;               // 0 chord, 1 freestream, 2 actual velocity
+    int symmetry = 0;                // 0 none, 1 X, 2 Y, 3 Z
+    int neglect_self = 0;
+    int output_body = 0;             // output coordinate system 0 global, 1 body
+    int include_viscous_lift = 0;
+    long long end_index = 0;         // wake points that get induced velocities
+    // constant line force model
+    const d3* span_s_local = nullptr;
+    const d3* span_e_local = nullptr;
+    const d3* chord_not_rotated = nullptr;
+    const double* chord_len = nullptr;
+    const double* span_len_local = nullptr;
+    const int* wing_of_line = nullptr;
+    const int* wing_start = nullptr;
+    const int* wing_end = nullptr;
+    const unsigned char* is_virtual = nullptr;
+    const FoilP* foils = nullptr;
+    const int* sp_line = nullptr;    // [Np] line whose start (or end, sp_end) is span point k
+    const unsigned char* sp_end = nullptr;
+    const int* sp_val_a = nullptr;   // [Np] value mapping control -> span points
+    const int* sp_val_b = nullptr;   //       value = (c[a] + c[b]) * 0.5, or c[a] if a == b
+    const double* panel_core = nullptr;  // [W*N]
+    // per-step geometry
+    d3* chord_local = nullptr;
+    d3* chord_global = nullptr;
+    d3* chord_span_pts = nullptr;
+    d3* span_s = nullptr;
+    d3* span_e = nullptr;
+    d3* span_pts = nullptr;
+    d3* ctrl = nullptr;
+    d3* felt_ctrl = nullptr;
+    d3* felt_span = nullptr;
+};
+
+struct StepParams {
+    double time = 0.0, dt = 0.0;
+    d3 translation{0, 0, 0}, rotation{0, 0, 0}, velocity_linear{0, 0, 0}, velocity_angular{0, 0, 0};
+    double local_wing_angles[kMaxWings] = {0};
+};
+
+// Error word written by kernels whose bounded waits ran out (0 = none).
+enum DeviceError : int { kDevOk = 0, kDevTimeout = 1, kDevSingular = 2 };
+
+}  // namespace sbgpu

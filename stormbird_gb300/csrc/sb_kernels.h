@@ -1,0 +1,146 @@
+// Launch interfaces of the lifting-line kernels (host side). Each .cu file holds its
+// kernels and the host launchers declared here, so no relocatable device code is needed.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sb_device.cuh"
+
+namespace sbgpu {
+
+constexpr int kBsThreads = 128;  // threads per Biot-Savart CTA
+
+// One Biot-Savart sweep: velocities at M targets induced by panels [p_begin, p_end).
+struct BsArgs {
+    const void* panels = nullptr;      // PanelRec<float> or PanelRec<double>
+    long long p_begin = 0, p_end = 0;
+    const d3* targets = nullptr;       // [M] f64 positions
+    const int* target_wing = nullptr;  // [M] wing index (neglect-self variant only)
+    long long M = 0;
+    int chunk_panels = 0;              // panels per source chunk (multiple of the tile)
+    int n_chunks = 1;
+    long long n_ttiles = 0;            // target tiles of kBsThreads * T targets
+    double* partial = nullptr;         // [n_chunks][M][3]
+    unsigned long long* work_counter = nullptr;  // zero before launch
+    int* err = nullptr;
+    int symmetry = 0;
+    int neglect = 0;
+};
+
+int bs_targets_per_thread(int symmetry);
+int bs_tile_panels(int precision);
+int bs_occupancy_blocks_per_sm(int precision, int symmetry, int neglect);
+cudaError_t launch_bs_sweep(const BsArgs& a, int precision, int grid, cudaStream_t s);
+cudaError_t launch_bs_reduce(const double* partial, int n_chunks, long long M, long long M_total, const d3* base, d3* out,
+                             cudaStream_t s);
+cudaError_t launch_unit_matrix(const PanelRec<double>* row0, const d3* ctrl, int N, int sym, int neglect,
+                               const int* wing_of_line, d3* factors, cudaStream_t s);
+// Quasi-steady horseshoe matrix; core_kind 0 relative, 1 absolute, 2 none.
+cudaError_t launch_horseshoe_matrix(const DevModel& m, int core_kind, double core_value, double wake_length, d3* wake_vec,
+                                    double* rc_dev, int sym, d3* factors, cudaStream_t s);
+
+// ---- wake and geometry (k_wake.cu) ------------------------------------------------------
+struct WakeBuffers {
+    d3* pts_old = nullptr;   // [Wp][Np]
+    d3* pts_new = nullptr;   // [Wp][Np]
+    d3* vel = nullptr;       // [Wp][Np] velocity at the (old) points
+    double* str_old = nullptr;  // [W][N]
+    double* str_new = nullptr;  // [W][N]
+    PanelRec<float>* rec32 = nullptr;    // [W][N]
+    PanelRec<double>* rec64 = nullptr;   // [W][N] (FP64 precision mode) or nullptr
+    PanelRec<double>* row0_64 = nullptr; // [N]
+};
+
+// Global geometry and felt velocities of the line force model for one step
+// (line_force_model/data_update.rs:13-90, force_calculations.rs:50-69, value_mapping.rs:87-137).
+// When mean_out is not null, also writes the mean control-point freestream (simulation.rs:74-75).
+cudaError_t launch_prep_geometry(const DevModel& m, const StepParams& p, const d3* freestream_ctrl, d3* mean_out,
+                                 cudaStream_t s);
+
+// Wake initialisation with a uniform velocity (dynamic_wake/initialization.rs:12-41).
+// `velocity` is read from device memory (mean_dev) when not null, else `velocity_host`.
+// fill_rows = 1 first puts every row on the span points (the builder's state).
+cudaError_t launch_wake_init(const DevModel& m, const WakeBuffers& w, const d3* mean_dev, d3 velocity_host, double dt,
+                             int fill_rows, cudaStream_t s);
+
+// Wake points before solving (update_data.rs:65-82, 90-99, 152-316) into pts_new.
+cudaError_t launch_wake_advect(const DevModel& m, const WakeBuffers& w, double dt, int steps_completed, cudaStream_t s);
+
+// Panels of the new points and downstream strength shift (update_data.rs:102-115, 319-328).
+// `shift_strengths` = 0 rebuilds the panels without moving strengths (initialisation).
+cudaError_t launch_wake_panels(const DevModel& m, const WakeBuffers& w, int shift_strengths, cudaStream_t s);
+
+// ---- solver and forces (k_solve.cu) ----------------------------------------------------
+struct SolveSettings {
+    int max_iterations = 40;
+    double damping = 0.05;
+    double residual_tolerance = 1e-4;
+    double strength_tolerance = 1e-6;
+    int velocity_correction = 0;  // 0 none, 1 max induced ratio, 2 fixed magnitude
+    double velocity_correction_ratio = 0.0;
+    double correction_factor_initial = 1.0;
+    int start_with_linearized = 0;
+    // Linearized
+    int disable_viscous_corrections = 0;
+    int full_induced_correction = 1;
+};
+
+struct SolveBuffers {
+    const d3* fixed = nullptr;      // [N]
+    const d3* factors = nullptr;    // [N][N]
+    double* gamma_prev = nullptr;   // [N] in: initial solution, out: solution
+    d3* vel_out = nullptr;          // [N] output control-point velocity
+    double* scalars = nullptr;      // [4]: residual, iterations, converged, status
+    double* lin_work = nullptr;     // [N*(N+1)] Gaussian elimination scratch (linearized)
+    double* wake_str_row0 = nullptr;        // strengths row 0 (dynamic) or nullptr
+    PanelRec<float>* rec32_row0 = nullptr;  // FP32 record row 0 (dynamic) or nullptr
+    PanelRec<double>* rec64_row0 = nullptr; // FP64 record row 0 in the FP64 sweep mode
+    int* err = nullptr;
+};
+
+int solve_cluster_size(int N);
+cudaError_t launch_solve_simple_iterative(const DevModel& m, const SolveSettings& st, const SolveBuffers& b, cudaStream_t s);
+cudaError_t launch_solve_linearized(const DevModel& m, const SolveSettings& st, const SolveBuffers& b, cudaStream_t s);
+
+struct ForceArgs {
+    const double* gamma = nullptr;  // [N]
+    const d3* vel = nullptr;        // [N] solver output velocity
+    d3* hist0 = nullptr;            // [N] flow derivative history
+    d3* hist1 = nullptr;
+    int fd_count = 0;               // updates done so far
+    double* out = nullptr;          // output block
+    const double* scalars = nullptr;
+};
+
+// Output block layout (doubles), N span lines, S wings.
+struct OutLayout {
+    long long gamma, vel, felt, aoa, fvel, acc, ctrl, sect, intf, intm, fsum, msum, residual, iterations, converged,
+        total;
+    __host__ __device__ static OutLayout make(int N, int S) {
+        OutLayout o{};
+        long long at = 0;
+        o.gamma = at; at += N;
+        o.vel = at; at += 3LL * N;
+        o.felt = at; at += 3LL * N;
+        o.aoa = at; at += N;
+        o.fvel = at; at += 3LL * N;
+        o.acc = at; at += 3LL * N;
+        o.ctrl = at; at += 3LL * N;
+        o.sect = at; at += 18LL * N;
+        o.intf = at; at += 18LL * S;
+        o.intm = at; at += 18LL * S;
+        o.fsum = at; at += 3;
+        o.msum = at; at += 3;
+        o.residual = at; at += 1;
+        o.iterations = at; at += 1;
+        o.converged = at; at += 1;
+        o.total = at;
+        return o;
+    }
+};
+
+// Sectional and integrated forces (force_calculations.rs:322-452, 669-698;
+// forces_and_moments.rs:163-245; flow_derivatives.rs:31-63).
+cudaError_t launch_forces(const DevModel& m, const StepParams& p, const ForceArgs& f, cudaStream_t s);
+
+}  // namespace sbgpu

@@ -1,0 +1,68 @@
+"""Loader for the CUDA C-ABI library (stormbird_gb300/_build/libstormbird_gb300.so).
+
+There is no CPU fallback: when the library is missing or cannot be loaded, `lib()`
+raises, naming the build step (`python -m stormbird_gb300.build` or
+`__graft_entry__.build()`).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from ._abi import StepOutput
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libstormbird_gb300.so")
+
+# Every entry point of include/stormbird_gb300.h: (name, restype, argtypes)
+_dp = ctypes.POINTER(ctypes.c_double)
+_szp = ctypes.POINTER(ctypes.c_size_t)
+_vp = ctypes.c_void_p
+SIGNATURES = [
+    ("sb_last_error", ctypes.c_char_p, []),
+    ("sb_last_status", ctypes.c_int, []),
+    ("sb_version", ctypes.c_char_p, []),
+    ("sb_sim_new", _vp, [ctypes.c_char_p, ctypes.c_int]),
+    ("sb_sim_free", None, [_vp]),
+    ("sb_sim_sizes", ctypes.c_int, [_vp, _szp, _szp, _szp]),
+    ("sb_sim_get_freestream_points", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
+    ("sb_sim_do_step", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double, _dp, ctypes.c_size_t,
+                                      ctypes.POINTER(StepOutput)]),
+    ("sb_sim_do_step_device", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double, _vp, ctypes.c_size_t]),
+    ("sb_sim_read_output", ctypes.c_int, [_vp, ctypes.POINTER(StepOutput)]),
+    ("sb_sim_induced_velocities", ctypes.c_int, [_vp, _dp, ctypes.c_size_t, _dp]),
+    ("sb_sim_set_translation_and_rotation_with_finite_difference", ctypes.c_int, [_vp, ctypes.c_double, _dp, _dp]),
+    ("sb_sim_set_translation_only", ctypes.c_int, [_vp, _dp]),
+    ("sb_sim_set_rotation_only", ctypes.c_int, [_vp, _dp]),
+    ("sb_sim_set_velocity_linear", ctypes.c_int, [_vp, _dp]),
+    ("sb_sim_set_velocity_angular", ctypes.c_int, [_vp, _dp]),
+    ("sb_sim_set_local_wing_angles", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
+    ("sb_sim_reset_previous_circulation", ctypes.c_int, [_vp]),
+    ("sb_sim_set_previous_circulation", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
+    ("sb_sim_get_previous_circulation", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
+    ("sb_sim_wake_sizes", ctypes.c_int, [_vp, _szp, _szp, _szp, _szp]),
+    ("sb_sim_get_wake_state", ctypes.c_int, [_vp, _dp, _dp, _dp]),
+    ("sb_sim_set_precision", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("sb_sim_enable_timing", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("sb_sim_last_step_timing", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
+    ("sb_sim_last_step_counters", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
+]
+
+_LIB = None
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded CUDA library; raises if it was not built."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"CUDA library {LIB_PATH} is missing: build it with `python -m stormbird_gb300.build` "
+                "(there is no CPU fallback)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB

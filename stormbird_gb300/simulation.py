@@ -1,0 +1,152 @@
+"""Python host interface mirroring the reference's pystormbird `Simulation`.
+
+Reference: interfaces/pystormbird/src/lifting_line/simulation.rs:24-165 — same class
+name, constructor argument (the SimulationBuilder JSON string), method names, keyword-only
+`do_step(*, time, time_step, freestream_velocity)` and setter names. Every call goes
+through the C ABI of include/stormbird_gb300.h into the CUDA library; errors raise
+`SbError` carrying the SB_ERR_* code (the reference panics or unwraps in these cases).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from ._abi import SB_ERR_BAD_JSON, OutputBuffers, SbError, as_ptr, vec3_array
+from .native import lib
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise SbError(rc, lib().sb_last_error().decode())
+
+
+def _d(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+
+
+class Simulation:
+    """A lifting-line simulation on one GPU (quasi-steady or dynamic, per the setup)."""
+
+    def __init__(self, setup_string: str, device: int = 0):
+        L = lib()
+        h = L.sb_sim_new(setup_string.encode(), int(device))
+        if not h:
+            raise SbError(L.sb_last_status() or SB_ERR_BAD_JSON, L.sb_last_error().decode())
+        self._h = ctypes.c_void_p(h)
+        n, s, nfs = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t()
+        _check(L.sb_sim_sizes(self._h, ctypes.byref(n), ctypes.byref(s), ctypes.byref(nfs)))
+        self.nr_span_lines, self.nr_wings, self.nr_freestream_points = n.value, s.value, nfs.value
+        self._out = OutputBuffers(self.nr_span_lines, self.nr_wings)
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h is not None:
+            lib().sb_sim_free(h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- reference API -----------------------------------------------------------------
+    def get_freestream_velocity_points(self) -> np.ndarray:
+        out = np.zeros((self.nr_freestream_points, 3))
+        _check(lib().sb_sim_get_freestream_points(self._h, as_ptr(out), self.nr_freestream_points))
+        return out
+
+    def do_step(self, *, time: float, time_step: float, freestream_velocity):
+        fs = vec3_array(freestream_velocity, self.nr_freestream_points, "freestream_velocity")
+        _check(lib().sb_sim_do_step(self._h, float(time), float(time_step), as_ptr(fs), fs.shape[0],
+                                    ctypes.byref(self._out.struct)))
+        return self._out.to_result(time)
+
+    def induced_velocities(self, points) -> np.ndarray:
+        p = vec3_array(points)
+        out = np.zeros_like(p)
+        _check(lib().sb_sim_induced_velocities(self._h, as_ptr(p), p.shape[0], as_ptr(out)))
+        return out
+
+    def set_translation_and_rotation_with_finite_difference_for_the_velocity(self, time_step, translation, rotation):
+        _check(lib().sb_sim_set_translation_and_rotation_with_finite_difference(
+            self._h, float(time_step), as_ptr(_d(translation)), as_ptr(_d(rotation))))
+
+    def set_translation_only(self, translation):
+        _check(lib().sb_sim_set_translation_only(self._h, as_ptr(_d(translation))))
+
+    def set_rotation_only(self, rotation):
+        _check(lib().sb_sim_set_rotation_only(self._h, as_ptr(_d(rotation))))
+
+    def set_velocity_linear(self, linear_velocity):
+        _check(lib().sb_sim_set_velocity_linear(self._h, as_ptr(_d(linear_velocity))))
+
+    def set_velocity_angular(self, angular_velocity):
+        _check(lib().sb_sim_set_velocity_angular(self._h, as_ptr(_d(angular_velocity))))
+
+    def set_local_wing_angles(self, local_wing_angles):
+        a = _d(local_wing_angles)
+        _check(lib().sb_sim_set_local_wing_angles(self._h, as_ptr(a), a.size))
+
+    def reset_previous_circulation_strength(self):
+        _check(lib().sb_sim_reset_previous_circulation(self._h))
+
+    # -- additions of this library -------------------------------------------------------
+    @property
+    def previous_circulation_strength(self) -> np.ndarray:
+        out = np.zeros(self.nr_span_lines)
+        _check(lib().sb_sim_get_previous_circulation(self._h, as_ptr(out), out.size))
+        return out
+
+    @previous_circulation_strength.setter
+    def previous_circulation_strength(self, g):
+        a = _d(g)
+        _check(lib().sb_sim_set_previous_circulation(self._h, as_ptr(a), a.size))
+
+    def do_step_device(self, *, time: float, time_step: float, freestream_device_ptr: int):
+        """do_step with the freestream already on the GPU (a device pointer to n*3 f64)."""
+        _check(lib().sb_sim_do_step_device(self._h, float(time), float(time_step),
+                                           ctypes.c_void_p(int(freestream_device_ptr)), self.nr_freestream_points))
+
+    def read_output(self, time: float = 0.0):
+        _check(lib().sb_sim_read_output(self._h, ctypes.byref(self._out.struct)))
+        return self._out.to_result(time)
+
+    def wake_state(self):
+        """(points [P_pts, 3], strengths [P_pan], velocity at points [P_pts, 3])."""
+        npts, npan, nspan, W = (ctypes.c_size_t() for _ in range(4))
+        _check(lib().sb_sim_wake_sizes(self._h, ctypes.byref(npts), ctypes.byref(npan), ctypes.byref(nspan),
+                                       ctypes.byref(W)))
+        p = np.zeros((npts.value, 3))
+        s = np.zeros(npan.value)
+        v = np.zeros((npts.value, 3))
+        _check(lib().sb_sim_get_wake_state(self._h, as_ptr(p), as_ptr(s), as_ptr(v)))
+        return p, s, v
+
+    def wake_sizes(self) -> dict:
+        npts, npan, nspan, W = (ctypes.c_size_t() for _ in range(4))
+        _check(lib().sb_sim_wake_sizes(self._h, ctypes.byref(npts), ctypes.byref(npan), ctypes.byref(nspan),
+                                       ctypes.byref(W)))
+        return {"points": npts.value, "panels": npan.value, "points_along_span": nspan.value,
+                "panels_per_line_element": W.value}
+
+    def set_precision(self, mode: str | int):
+        """Biot-Savart arithmetic: 'kahan' (FP32 compensated, default), 'fp32', 'fp64'."""
+        m = {"kahan": 0, "fp32": 1, "fp64": 2}.get(mode, mode)
+        _check(lib().sb_sim_set_precision(self._h, int(m)))
+
+    def enable_timing(self, on: bool = True):
+        _check(lib().sb_sim_enable_timing(self._h, 1 if on else 0))
+
+    def last_step_timing(self) -> dict:
+        ms = np.zeros(7)
+        _check(lib().sb_sim_last_step_timing(self._h, as_ptr(ms), 7))
+        keys = ("step", "wake_update", "free_wake_sweep", "unit_matrix", "solve", "rollup_sweep", "forces")
+        return dict(zip(keys, ms.tolist()))
+
+    def last_step_counters(self) -> dict:
+        c = np.zeros(5)
+        _check(lib().sb_sim_last_step_counters(self._h, as_ptr(c), 5))
+        keys = ("rollup_targets", "rollup_panels", "ctrl_targets", "free_wake_panels", "steps_completed")
+        return dict(zip(keys, c.tolist()))

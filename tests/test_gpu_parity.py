@@ -1,0 +1,216 @@
+"""GPU parity: the CUDA library (through its C ABI) against the f64 oracle.
+
+Tolerance (the hot path's stated bar): relative circulation error
+max|Gamma_gpu - Gamma_ref| / max|Gamma_ref| <= 1e-5 and relative total-force error
+|F_gpu - F_ref| / |F_ref| <= 1e-5 per step, with the Biot-Savart sweeps in FP32 with
+compensated accumulation. Cases run the solver for a fixed number of iterations where the
+convergence test would otherwise be the only difference (tolerances set to 0), and with
+the reference's own tolerances elsewhere.
+"""
+import json
+import math
+
+import numpy as np
+import pytest
+
+from stormbird_gb300 import Simulation, SbError
+from stormbird_gb300 import setups as S
+from tests.helpers import fixed_iterations, rel_inf, rel_vec, run_pair, small_row
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+
+def pair(setup, oracle_mod):
+    return Simulation(setup), oracle_mod.OracleSimulation(setup)
+
+
+def check_step(k, rg, ro, tol=TOL):
+    eg = rel_inf(rg.circulation_strength, ro.circulation_strength)
+    ef = rel_vec(rg.integrated_forces_sum(), ro.integrated_forces_sum())
+    assert eg <= tol, f"step {k}: circulation error {eg:.3e}"
+    assert ef <= tol, f"step {k}: force error {ef:.3e}"
+    return eg, ef
+
+
+def test_dynamic_row_fixed_iterations(gpu_lib, oracle_mod):
+    setup = fixed_iterations(small_row(2, 8, 20), 25)
+    g, o = pair(setup, oracle_mod)
+    wind = S.GustyWind(seed=1)
+    worst = 0.0
+    for k, rg, ro in run_pair(g, o, wind, steps=12, dt=0.05):
+        assert rg.iterations == ro.iterations == 25
+        worst = max(worst, *check_step(k, rg, ro))
+    assert worst < TOL
+
+
+def test_dynamic_row_reference_tolerances(gpu_lib, oracle_mod):
+    setup = small_row(3, 12, 30)
+    g, o = pair(setup, oracle_mod)
+    wind = S.GustyWind(seed=2, apparent_wind_angle_deg=60.0)
+    for k, rg, ro in run_pair(g, o, wind, steps=10, dt=0.05):
+        check_step(k, rg, ro)
+        assert abs(rg.iterations - ro.iterations) <= 1
+
+
+def test_wake_state_matches_oracle(gpu_lib, oracle_mod):
+    setup = fixed_iterations(small_row(2, 6, 15), 20)
+    g, o = pair(setup, oracle_mod)
+    wind = S.GustyWind(seed=3)
+    for _ in run_pair(g, o, wind, steps=9, dt=0.05):
+        pass
+    pg, sg, vg = g.wake_state()
+    po, so, vo = o.wake_state()
+    assert rel_inf(pg, po) < 1e-9, "wake points"
+    assert rel_inf(sg, so) < TOL, "wake strengths"
+    assert rel_inf(vg, vo) < TOL, "wake point velocities"
+
+
+def test_freestream_points_match_oracle(gpu_lib, oracle_mod):
+    setup = small_row(2, 8, 12)
+    g, o = pair(setup, oracle_mod)
+    assert rel_inf(g.get_freestream_velocity_points(), o.get_freestream_velocity_points()) < 1e-12
+
+
+@pytest.mark.parametrize("mode,tol", [("kahan", 2e-6), ("fp32", 1e-5), ("fp64", 1e-11)])
+def test_induced_velocities_precision_modes(gpu_lib, oracle_mod, mode, tol):
+    setup = fixed_iterations(small_row(2, 8, 25), 20)
+    g, o = pair(setup, oracle_mod)
+    wind = S.GustyWind(seed=4)
+    for _ in run_pair(g, o, wind, steps=8, dt=0.05):
+        pass
+    g.set_precision(mode)
+    rng = np.random.default_rng(0)
+    pts = np.concatenate([o.get_freestream_velocity_points()[::7],
+                          rng.uniform([-20, -20, -5], [60, 40, 35], (200, 3))])
+    ug = g.induced_velocities(pts)
+    uo = o.induced_velocities(pts)
+    assert rel_inf(ug, uo) < tol
+
+
+def test_quasi_steady_simple_iterative_single_wing(gpu_lib, oracle_mod):
+    setup, u = S.quasi_steady_single_wing()
+    g, o = pair(setup, oracle_mod)
+    n = g.nr_freestream_points
+    rg = g.do_step(time=0.0, time_step=1.0, freestream_velocity=np.tile(u, (n, 1)))
+    ro = o.do_step(time=0.0, time_step=1.0, freestream_velocity=np.tile(u, (n, 1)))
+    check_step(0, rg, ro)
+    assert rg.iterations == ro.iterations
+
+
+def test_quasi_steady_linearized_default(gpu_lib, oracle_mod):
+    lfm = S.rectangular_wing(5.0, 1.2, math.radians(2.0), 64)
+    setup = S.simulation(lfm, dynamic=False)
+    g, o = pair(setup, oracle_mod)
+    v = np.array([1.2, 0.0, 0.0])
+    rg = g.do_step(time=0.0, time_step=0.2, freestream_velocity=np.tile(v, (g.nr_freestream_points, 1)))
+    ro = o.do_step(time=0.0, time_step=0.2, freestream_velocity=np.tile(v, (o.nr_freestream_points, 1)))
+    check_step(0, rg, ro, tol=1e-9)
+
+
+def test_translation_equals_inflow_on_gpu(gpu_lib):
+    """Reference test right_force_magnitude_with_steady_forward_motion
+    (stormbird/src/lifting_line/tests/dynamic_simulation.rs:23-114), tolerance 1e-5."""
+    vm, AR = 5.2, 5.0
+    lfm = S.rectangular_wing(AR, 0.5, 0.0, 20, negative_span_orientation=True)
+    js = S.simulation(lfm, True)
+    st, si = Simulation(js), Simulation(js)
+    n = si.nr_freestream_points
+    for i in range(1, 20):
+        t = i * 0.1
+        st.set_translation_and_rotation_with_finite_difference_for_the_velocity(0.1, [-vm * t, 0, 0], [0, 0, 0])
+        rt = st.do_step(time=t, time_step=0.1, freestream_velocity=np.zeros((n, 3)))
+        ri = si.do_step(time=t, time_step=0.1, freestream_velocity=np.tile([vm, 0, 0], (n, 1)))
+        d = abs(rt.integrated_forces_sum()[1] - ri.integrated_forces_sum()[1]) / abs(ri.integrated_forces_sum()[1])
+        assert d < 1e-5
+
+
+def test_elliptic_wing_dynamic_on_gpu(gpu_lib):
+    """Reference test steady_lift (stormbird/src/lifting_line/tests/compare_models.rs:28-168):
+    dynamic CL within 7 % and CD within 6 % of elliptic wing theory."""
+    AR, cl0, aoa = 5.0, 1.2, math.radians(2.0)
+    cl2d = cl0 + 2 * math.pi * aoa
+    clt = cl2d / (1 + 2 / AR)
+    cdt = clt ** 2 / (math.pi * AR)
+    sim = Simulation(S.simulation(S.rectangular_wing(AR, cl0, aoa, 64), True))
+    v = np.array([1.2, 0.0, 0.0])
+    dt = 0.25 / 1.2
+    fs = np.tile(v, (sim.nr_freestream_points, 1))
+    for i in range(200):
+        r = sim.do_step(time=i * dt, time_step=dt, freestream_velocity=fs)
+    ff = 0.5 * 13.2 * 1.2 ** 2 * AR
+    f = r.integrated_forces_sum()
+    assert abs(f[1] / ff - clt) / clt < 0.07
+    assert abs(f[0] / ff - cdt) / cdt < 0.06
+
+
+@pytest.mark.parametrize("variant", ["symmetry_z", "neglect_self", "damping", "freestream_dir", "actual_dir",
+                                     "sin_core", "single_row"])
+def test_wake_options_match_oracle(gpu_lib, oracle_mod, variant):
+    d = json.loads(fixed_iterations(small_row(2, 6, 12), 15))
+    w = d["simulation_settings"]["Dynamic"]["wake"]
+    if variant == "symmetry_z":
+        w["symmetry_condition"] = "Z"
+        for wb in d["line_force_model"]["wing_builders"]:
+            for p in wb["section_points"]:
+                p["z"] += 1.0
+    elif variant == "neglect_self":
+        w["neglect_self_induced_velocities"] = True
+    elif variant == "damping":
+        w["shape_damping_factor"] = 0.3
+    elif variant == "freestream_dir":
+        w["first_wake_points_direction"] = "Freestream"
+    elif variant == "actual_dir":
+        w["first_wake_points_direction"] = "ActualVelocity"
+    elif variant == "sin_core":
+        w["viscous_core_length_evolution"] = {"SinIncrease": {"last_panel_value": {"Relative": 0.5}}}
+    elif variant == "single_row":
+        w["nr_panels_per_line_element"] = 1
+    setup = json.dumps(d)
+    g, o = pair(setup, oracle_mod)
+    wind = S.GustyWind(seed=5)
+    for k, rg, ro in run_pair(g, o, wind, steps=7, dt=0.05):
+        check_step(k, rg, ro)
+
+
+def test_motion_and_wing_angles_match_oracle(gpu_lib, oracle_mod):
+    setup = fixed_iterations(small_row(2, 8, 15), 20)
+    g, o = pair(setup, oracle_mod)
+
+    def motion(gs, os_, t):
+        tr = [0.3 * math.sin(t), 0.1 * t, 0.0]
+        ro = [0.02 * math.sin(2 * t), 0.0, 0.05 * t]
+        for s in (gs, os_):
+            s.set_translation_and_rotation_with_finite_difference_for_the_velocity(0.05, tr, ro)
+            s.set_local_wing_angles([math.radians(37.0 + 3 * math.sin(t)), math.radians(35.0)])
+
+    for k, rg, ro in run_pair(g, o, S.GustyWind(seed=6), steps=8, dt=0.05, motion=motion):
+        check_step(k, rg, ro)
+
+
+def test_body_frame_output_matches_oracle(gpu_lib, oracle_mod):
+    d = json.loads(fixed_iterations(small_row(2, 8, 10), 20))
+    d["line_force_model"]["output_coordinate_system"] = "Body"
+    d["line_force_model"]["rotation"] = {"x": 0.1, "y": 0.0, "z": 0.3}
+    setup = json.dumps(d)
+    g, o = pair(setup, oracle_mod)
+    for k, rg, ro in run_pair(g, o, S.GustyWind(seed=7), steps=5, dt=0.05):
+        check_step(k, rg, ro)
+        assert rel_vec(rg.integrated_moments_sum(), ro.integrated_moments_sum()) < TOL
+
+
+def test_error_codes(gpu_lib):
+    g = Simulation(small_row(1, 4, 5))
+    with pytest.raises(SbError) as e:
+        g.do_step(time=0.0, time_step=0.1, freestream_velocity=np.zeros((3, 3)))
+    assert e.value.code == -2
+    fs = np.ones((g.nr_freestream_points, 3))
+    fs[5, 1] = np.nan
+    with pytest.raises(SbError) as e:
+        g.do_step(time=0.0, time_step=0.1, freestream_velocity=fs)
+    assert e.value.code == -5
+    q = Simulation(S.simulation(S.rectangular_wing(), False))
+    with pytest.raises(SbError) as e:
+        q.induced_velocities([[0.0, 0.0, 0.0]])
+    assert e.value.code == -8
