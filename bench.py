@@ -1,0 +1,406 @@
+#!/usr/bin/env python
+"""Benchmark of the lifting-line hot path on GB300: Biot-Savart interactions/s.
+
+Workload (the dynamic free-wake case): 4 wing sails in a row 40 m apart, span 30 m,
+chord 10 m, 64 panels each (256 span lines), 300 shed wake rows (76,800 vortex rings,
+78,260 wake points), dt = 0.05 s, wind 12 m/s at 45 deg with a seeded 1.5 m/s gust, core
+0.1 chord, roll-up of every wake point. The sweeps run in the all-near-field mode
+(far_field_ratio = 1e30, a reference-supported setting), the uniform N-body workload the
+metric is defined on. Before timing, the wake is shed until every panel carries
+circulation (300 + 2 steps).
+
+A step is one Simulation.do_step: wake update, free-wake sweep at the control points,
+unit-strength matrix, damped fixed-point solve, roll-up sweep at every wake point and
+forces. Interactions per step = (roll-up targets + control points) x 4 segments x
+nonzero-strength panels swept.
+
+  value   — whole step, freestream already in HBM, device time from CUDA events on the
+            library's stream, L2 flushed (256 MB write) before every step.
+  e2e     — the same metric through the host-buffer C-ABI call sb_sim_do_step (H2D of the
+            freestream and D2H of the output block inside the timed region), host clock.
+  roofline— the roll-up sweep kernel (k_bs_sweep) against the measured FP32 FMA rate.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SAILS, PANELS, ROWS, DT = 4, 64, 300, 0.05
+FLOPS_PER_SEGMENT = 57  # algorithmic FLOPs per target x segment interaction (FMA = 2)
+METRIC = "Biot-Savart interactions/s"
+UNIT = "interactions/s"
+
+
+def workload_config(extra=None):
+    c = {
+        "workload": "dynamic lifting line, free wake: 4 sails x 64 panels, 300 wake rows (76,800 rings), "
+                    "dt 0.05 s, 12 m/s at 45 deg + 1.5 m/s gust, all-near-field sweeps",
+        "sails": SAILS, "panels_per_sail": PANELS, "wake_rows": ROWS, "time_step": DT,
+        "far_field_ratio": 1e30, "wake_spin_up_steps": ROWS + 2,
+        "l2": "256 MB buffer written before every timed step",
+    }
+    if extra:
+        c.update(extra)
+    return c
+
+
+def setup_json():
+    from stormbird_gb300 import setups as S
+
+    return S.wing_sail_row(SAILS, PANELS, ROWS, time_step=DT, far_field_ratio=1e30)
+
+
+# --------------------------------------------------------------------------------------
+# distributed plumbing (one process per GPU, independent replicas)
+# --------------------------------------------------------------------------------------
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws, backend):
+    if ws > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend=backend)
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allreduce_max(ws, v, device=None):
+    if ws <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(ws, v, device=None):
+    if ws <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# --------------------------------------------------------------------------------------
+# clocks during the timed region
+# --------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100",
+                 "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        time.sleep(0.25)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------------------
+# CPU baseline: the oracle (C++ f64 restatement of the reference, OpenMP over targets)
+# --------------------------------------------------------------------------------------
+def cpu_baseline_sweep(points, strengths, target_seconds=8.0, seed=0):
+    from oracle.binding import bs_sweep
+    from tests.helpers import panel_corners, row_wing_ranges
+
+    corners = panel_corners(points, SAILS * (PANELS + 1), row_wing_ranges(SAILS, PANELS), ROWS)
+    cores = np.full(len(strengths), 1.0)
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(seed)
+    nz = int(np.count_nonzero(strengths))
+
+    def run(m):
+        idx = rng.choice(len(points) - 1, m, replace=False)
+        t0 = time.perf_counter()
+        bs_sweep(corners, cores, strengths, 1e30, points[idx], nthreads=threads)
+        return time.perf_counter() - t0
+
+    m = 2 * threads
+    dt = run(m)
+    for _ in range(4):  # grow the sample until it takes about target_seconds
+        if dt >= 0.6 * target_seconds or m >= len(points) - 1:
+            break
+        m = int(min(len(points) - 1, max(m + 1, m * target_seconds / max(dt, 1e-6))))
+        dt = run(m)
+    inter = m * 4 * nz
+    return {"value": inter / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{m} random wake points x {nz} panels x 4 segments (all near field), "
+                      f"{dt:.2f} s wall on {threads} threads"}, dt
+
+
+# --------------------------------------------------------------------------------------
+# GB300 arm
+# --------------------------------------------------------------------------------------
+def read_traffic():
+    """DRAM bytes per roll-up sweep launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "bs_sweep_rollup_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for ln in open(path):
+        if ln.startswith("dram_bytes_per_full_launch:"):
+            return float(ln.split(":")[1])
+    return None
+
+
+def run_gb300(args):
+    import torch
+
+    from stormbird_gb300 import Simulation
+    from stormbird_gb300 import setups as S
+    from stormbird_gb300.simulation import measure_fp32_peak
+
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    dist_init(ws, "nccl")
+    dev = torch.device("cuda", local)
+
+    sim = Simulation(setup_json(), device=local)
+    sim.enable_timing(True)
+    wind = S.GustyWind(seed=rank)
+    nfs = sim.nr_freestream_points
+    N = sim.nr_span_lines
+    t = 0.0
+    k = 0
+
+    def fs_host(tt):
+        return wind.freestream(tt, nfs)
+
+    # spin-up: shed until every panel carries circulation
+    for _ in range(ROWS + 2):
+        sim.do_step(time=t, time_step=DT, freestream_velocity=fs_host(t))
+        k += 1
+        t = k * DT
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    fs_dev = torch.empty((nfs, 3), dtype=torch.float64, device=dev)
+
+    def device_step(tt):
+        fs_dev.copy_(torch.from_numpy(fs_host(tt)))
+        flush.zero_()
+        torch.cuda.synchronize()
+        sim.do_step_device(time=tt, time_step=DT, freestream_device_ptr=fs_dev.data_ptr())
+        return sim.last_step_timing(), sim.last_step_counters()
+
+    for _ in range(args.warmup):
+        device_step(t)
+        k += 1
+        t = k * DT
+
+    # ---- timed: freestream resident in HBM, device time per step from CUDA events
+    barrier(ws)
+    torch.cuda.synchronize()
+    step_ms, rollup_ms, ctrl_ms, launches, inter = [], [], [], 0, 0.0
+    pts, strengths, _ = sim.wake_state()
+    nz = int(np.count_nonzero(strengths))
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            tm, ct = device_step(t)
+            k += 1
+            t = k * DT
+            step_ms.append(tm["step"])
+            rollup_ms.append(tm["rollup_sweep_kernel"])
+            ctrl_ms.append(tm["free_wake_sweep_kernel"])
+            launches += int(ct["kernel_launches"])
+            inter += (ct["rollup_targets"] + ct["ctrl_targets"]) * 4.0 * nz
+    torch.cuda.synchronize()
+    barrier(ws)
+    total_ms = sum(step_ms)
+    total_ms_max = allreduce_max(ws, total_ms, dev)
+    inter_all = allreduce_sum(ws, inter, dev)
+    value = inter_all / (total_ms_max * 1e-3)
+
+    # ---- e2e: host buffers through sb_sim_do_step
+    e2e_times = []
+    for _ in range(args.steps):
+        fs = fs_host(t)
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = sim.do_step(time=t, time_step=DT, freestream_velocity=fs)
+        e2e_times.append(time.perf_counter() - t0)
+        k += 1
+        t = k * DT
+    assert np.all(np.isfinite(r.circulation_strength))
+    e2e_total = allreduce_max(ws, sum(e2e_times), dev)
+    e2e_value = inter_all / e2e_total
+    h2d = nfs * 3 * 8
+    d2h = (35 * N + 36 * sim.nr_wings + 9) * 8 + 4
+
+    # ---- roofline of the roll-up sweep kernel
+    rollup_targets = ct["rollup_targets"]
+    per_launch_flops = rollup_targets * 4.0 * nz * FLOPS_PER_SEGMENT
+    mean_rollup_s = statistics.mean(rollup_ms) * 1e-3
+    achieved = per_launch_flops / mean_rollup_s / 1e12
+    peak = measure_fp32_peak(local, 5)
+    traffic = read_traffic()
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32 sweeps (compensated, float-float positions) / fp64 solve+positions",
+        "data": "synthetic (seeded gusty wind, reference JSON setup)",
+        "config": workload_config({"parallelism": f"{ws} independent replica(s), one per GPU"}),
+        "roofline": {"kernel": "k_bs_sweep (wake roll-up)", "bound": "fp32", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak if peak > 0 else None, "traffic": traffic,
+                     "peak_source": "measured FP32 FMA rate (sb_measure_fp32_peak); MEASURED_PEAKS.json has no FP32 entry",
+                     "flops_per_interaction": FLOPS_PER_SEGMENT, "interactions_per_launch": rollup_targets * 4.0 * nz,
+                     "mean_launch_ms": statistics.mean(rollup_ms)},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": 1e3 * e2e_total / args.steps},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "breakdown_ms": {k2: v for k2, v in sim.last_step_timing().items()},
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cb, _ = cpu_baseline_sweep(pts, strengths)
+        line["cpu_baseline"] = cb
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+# --------------------------------------------------------------------------------------
+# reference arm: the oracle port of the reference's CPU path on the host cores
+# --------------------------------------------------------------------------------------
+def synthetic_wake():
+    """The workload's wake geometry without a GPU: the reference's initialisation of the
+    wake (straight rows along the mean freestream, oracle) with every panel given a seeded
+    circulation of the magnitude the solve produces (all-near sweeps cost the same for
+    any geometry, so the timing is representative)."""
+    from oracle.binding import OracleSimulation
+    from stormbird_gb300 import setups as S
+
+    sim = OracleSimulation(setup_json())
+    wind = S.GustyWind(seed=0)
+    n = sim.nr_freestream_points
+    r = sim.do_step(time=0.0, time_step=DT, freestream_velocity=wind.freestream(0.0, n))
+    pts, strengths, _ = sim.wake_state()
+    rng = np.random.default_rng(0)
+    g = np.tile(r.circulation_strength, ROWS) * rng.uniform(0.9, 1.1, ROWS * len(r.circulation_strength))
+    return pts, g
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return
+    pts, g = synthetic_wake()
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_baseline_sweep(pts, g, target_seconds=1.0)
+    vals, secs = [], []
+    for i in range(args.steps):
+        cb, dt = cpu_baseline_sweep(pts, g, target_seconds=1.5, seed=i + 1)
+        vals.append(cb["value"])
+        secs.append(dt)
+    v = float(np.mean(vals))
+    line = {
+        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * float(np.mean(secs)), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": workload_config({"sample": "each step: a seeded random sample of wake points, ~1.5 s of work"}),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": cb["sample"] + " (C++ f64 restatement of the reference algorithm; "
+                                                  "the Rust reference cannot be built here)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    import __graft_entry__
+
+    __graft_entry__.build()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -156,9 +156,10 @@ int sb_sim_set_precision(sb_sim* sim, int precision_mode);
 
 /*
  * Timing of the device work of the last step (CUDA events on the handle's stream, ms):
- * [0] whole step, [1] wake update, [2] free-wake sweep at control points,
- * [3] unit-strength matrix, [4] circulation solve, [5] wake roll-up sweep, [6] forces.
- * Only filled when profiling was enabled with sb_sim_enable_timing(sim, 1).
+ * [0] whole step, [1] wake update, [2] free-wake sweep at control points (with its
+ * reduction), [3] unit-strength matrix, [4] circulation solve, [5] wake roll-up sweep
+ * (with its reduction), [6] forces, [7] roll-up sweep kernel alone, [8] control-point
+ * sweep kernel alone. Only filled when enabled with sb_sim_enable_timing(sim, 1).
  */
 int sb_sim_enable_timing(sb_sim* sim, int enable);
 int sb_sim_last_step_timing(const sb_sim* sim, double* ms, size_t n);
@@ -166,10 +167,17 @@ int sb_sim_last_step_timing(const sb_sim* sim, double* ms, size_t n);
 /*
  * Sizes of the last step's Biot-Savart sweeps: [0] roll-up target points, [1] panels
  * swept for the roll-up, [2] control points, [3] free-wake panels swept at the control
- * points, [4] steps completed. Zero-strength panels are included in the panel counts
- * (the sweeps skip them).
+ * points, [4] steps completed, [5] kernels launched by the step. Zero-strength panels are
+ * included in the panel counts (the sweeps skip them).
  */
 int sb_sim_last_step_counters(const sb_sim* sim, double* counters, size_t n);
+
+/*
+ * Measured FP32 FMA throughput of a device in TFLOP/s (best of `reps` timed launches of
+ * an FMA-chain kernel): the denominator of the Biot-Savart sweep's roofline. Diagnostic
+ * entry point with no counterpart in the reference.
+ */
+int sb_measure_fp32_peak(int device, int reps, double* tflops);
 
 #ifdef __cplusplus
 }

@@ -136,18 +136,19 @@ __device__ __forceinline__ void two_sum_acc(R& s, R& c, R t) {
     c += err;
 }
 
-// One FP32 vortex ring (4 segments) at one target; returns the unscaled sum
-// sum_k core_k * k_k * (r_k x r_{k+1}) (multiply by Gamma / 4 pi for the velocity).
-__device__ __forceinline__ void ring_f32(const float (&px)[4], const float (&py)[4], const float (&pz)[4],
-                                         const float (&dx)[4], const float (&dy)[4], const float (&dz)[4],
-                                         const float (&il)[4], float rc4, bool nocore, float x, float y, float z,
+// One FP32 vortex ring (4 segments) at one target, from float-float corners; returns the
+// unscaled sum sum_k core_k * kk_k * (r_k x r_{k+1}) (times Gamma / 4 pi gives the velocity).
+// r_k = (x_hi - p_hi_k) + (x_lo - p_lo_k); d_k = p_{k+1} - p_k (precomputed per panel).
+__device__ __forceinline__ void ring_f32(const float (&ph)[12], const float (&pl)[12], const float (&dx)[4],
+                                         const float (&dy)[4], const float (&dz)[4], const float (&il)[4], float rc4,
+                                         bool nocore, float xh, float yh, float zh, float xl, float yl, float zl,
                                          float& ax, float& ay, float& az) {
     float rx[4], ry[4], rz[4], rs[4], rl[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        rx[k] = x - px[k];
-        ry[k] = y - py[k];
-        rz[k] = z - pz[k];
+        rx[k] = (xh - ph[3 * k]) + (xl - pl[3 * k]);
+        ry[k] = (yh - ph[3 * k + 1]) + (yl - pl[3 * k + 1]);
+        rz[k] = (zh - ph[3 * k + 2]) + (zl - pl[3 * k + 2]);
         rs[k] = fmaf(rx[k], rx[k], fmaf(ry[k], ry[k], rz[k] * rz[k]));
         rl[k] = rs[k] * rsqrtf(fmaxf(rs[k], 1e-30f));
     }
@@ -181,6 +182,7 @@ template <class R, int T, bool KAHAN, int SYM, bool NEGLECT>
 __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
     constexpr int TILE = TileSize<R>::value;
     constexpr int TT = SYM ? 2 * T : T;  // mirrored targets ride along as extra targets
+    constexpr bool F32 = sizeof(R) == 4;
     __shared__ __align__(128) PanelRec<R> tile[2][TILE];
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ long long s_item;
@@ -209,7 +211,8 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
         const long long pb = a.p_begin + static_cast<long long>(chunk) * a.chunk_panels;
         const long long pe = min(pb + static_cast<long long>(a.chunk_panels), a.p_end);
 
-        R x[TT], y[TT], z[TT];
+        // targets: FP32 as float-float pairs, FP64 as is (the lo parts stay 0)
+        R xh[TT], yh[TT], zh[TT], xl[TT], yl[TT], zl[TT];
         bool valid[TT];
         int tw[TT];
 #pragma unroll
@@ -217,17 +220,19 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
             long long idx = ttile * TM + static_cast<long long>(t) * kBsThreads + tid;
             valid[t] = idx < a.M;
             d3 p = valid[t] ? a.targets[idx] : mk(0, 0, 0);
-            x[t] = static_cast<R>(p.x);
-            y[t] = static_cast<R>(p.y);
-            z[t] = static_cast<R>(p.z);
             tw[t] = (NEGLECT && valid[t]) ? a.target_wing[idx] : -1;
-            if (SYM) {
-                d3 m = mirror(SYM, p);
-                x[T + t] = static_cast<R>(m.x);
-                y[T + t] = static_cast<R>(m.y);
-                z[T + t] = static_cast<R>(m.z);
-                valid[T + t] = valid[t];
-                tw[T + t] = tw[t];
+            d3 q[2] = {p, SYM ? mirror(SYM, p) : p};
+#pragma unroll
+            for (int m = 0; m < (SYM ? 2 : 1); ++m) {
+                const int u = t + m * T;
+                xh[u] = static_cast<R>(q[m].x);
+                yh[u] = static_cast<R>(q[m].y);
+                zh[u] = static_cast<R>(q[m].z);
+                xl[u] = static_cast<R>(q[m].x - static_cast<double>(xh[u]));
+                yl[u] = static_cast<R>(q[m].y - static_cast<double>(yh[u]));
+                zl[u] = static_cast<R>(q[m].z - static_cast<double>(zh[u]));
+                valid[u] = valid[t];
+                tw[u] = tw[t];
             }
         }
         R sx[TT], sy[TT], sz[TT], cx[TT], cy[TT], cz[TT];
@@ -263,18 +268,26 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
 
             for (int p = 0; p < np; ++p) {
                 const R* v = tile[buf][p].v;
-                const R gam = v[24];
+                const R gam = F32 ? v[kRec32Gamma] : v[kRec64Gamma];
                 if (gam == R(0)) continue;  // uniform across the CTA
-                const R ccx = v[16], ccy = v[17], ccz = v[18], ff2 = v[19];
-                const int pw = NEGLECT ? static_cast<int>(v[26]) : 0;
+                R ccx, ccy, ccz, ff2, clx = 0, cly = 0, clz = 0;
+                int pw = 0;
+                if constexpr (F32) {
+                    ccx = v[24]; ccy = v[25]; ccz = v[26]; ff2 = v[27];
+                    clx = v[28]; cly = v[29]; clz = v[30];
+                    if (NEGLECT) pw = static_cast<int>(v[41]);
+                } else {
+                    ccx = v[16]; ccy = v[17]; ccz = v[18]; ff2 = v[19];
+                    if (NEGLECT) pw = static_cast<int>(v[26]);
+                }
                 R ex[TT], ey[TT], ez[TT], e2[TT];
                 bool nr[TT], act[TT];
                 bool my_near = false, my_far = false;
 #pragma unroll
                 for (int t = 0; t < TT; ++t) {
-                    ex[t] = x[t] - ccx;
-                    ey[t] = y[t] - ccy;
-                    ez[t] = z[t] - ccz;
+                    ex[t] = (xh[t] - ccx) + (xl[t] - clx);
+                    ey[t] = (yh[t] - ccy) + (yl[t] - cly);
+                    ez[t] = (zh[t] - ccz) + (zl[t] - clz);
                     e2[t] = ex[t] * ex[t] + ey[t] * ey[t] + ez[t] * ez[t];
                     nr[t] = e2[t] <= ff2;
                     act[t] = valid[t] && (!NEGLECT || tw[t] != pw);
@@ -284,15 +297,19 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
                 const bool any_near = __any_sync(0xffffffffu, my_near);
                 const bool any_far = __any_sync(0xffffffffu, my_far);
                 if (any_far) {
-                    const R nx = v[20], ny = v[21], nz = v[22];
-                    const R at = v[23] * gam;
+                    R nx, ny, nz, at;
+                    if constexpr (F32) {
+                        nx = v[32]; ny = v[33]; nz = v[34]; at = v[31] * gam;
+                    } else {
+                        nx = v[20]; ny = v[21]; nz = v[22]; at = v[23] * gam;
+                    }
 #pragma unroll
                     for (int t = 0; t < TT; ++t) {
                         if (act[t] && !nr[t]) {
                             R h = ex[t] * nx + ey[t] * ny + ez[t] * nz;
                             R h3 = R(3) * h;
                             R s;
-                            if constexpr (sizeof(R) == 4) {
+                            if constexpr (F32) {
                                 float ir = rsqrtf(e2[t]);
                                 float ir2 = ir * ir;
                                 s = at * (ir2 * ir2 * ir);
@@ -306,26 +323,30 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
                     }
                 }
                 if (any_near) {
-                    if constexpr (sizeof(R) == 4) {
-                        float px[4] = {v[0], v[3], v[6], v[9]};
-                        float py[4] = {v[1], v[4], v[7], v[10]};
-                        float pz[4] = {v[2], v[5], v[8], v[11]};
-                        float il[4] = {v[12], v[13], v[14], v[15]};
-                        float dx[4], dy[4], dz[4];
+                    if constexpr (F32) {
+                        float ph[12], pl[12], il[4], dx[4], dy[4], dz[4];
+#pragma unroll
+                        for (int i = 0; i < 12; ++i) {
+                            ph[i] = v[i];
+                            pl[i] = v[12 + i];
+                        }
 #pragma unroll
                         for (int k2 = 0; k2 < 4; ++k2) {
-                            dx[k2] = px[(k2 + 1) & 3] - px[k2];
-                            dy[k2] = py[(k2 + 1) & 3] - py[k2];
-                            dz[k2] = pz[(k2 + 1) & 3] - pz[k2];
+                            const int n2 = (k2 + 1) & 3;
+                            il[k2] = v[36 + k2];
+                            dx[k2] = (ph[3 * n2] - ph[3 * k2]) + (pl[3 * n2] - pl[3 * k2]);
+                            dy[k2] = (ph[3 * n2 + 1] - ph[3 * k2 + 1]) + (pl[3 * n2 + 1] - pl[3 * k2 + 1]);
+                            dz[k2] = (ph[3 * n2 + 2] - ph[3 * k2 + 2]) + (pl[3 * n2 + 2] - pl[3 * k2 + 2]);
                         }
-                        const float rc4 = v[25];
-                        const bool nocore = v[27] != 0.f;
+                        const float rc4 = v[40];
+                        const bool nocore = v[42] != 0.f;
                         const float g4 = gam * static_cast<float>(kFourPiInv);
 #pragma unroll
                         for (int t = 0; t < TT; ++t) {
                             if (act[t] && nr[t]) {
                                 float ax, ay, az;
-                                ring_f32(px, py, pz, dx, dy, dz, il, rc4, nocore, x[t], y[t], z[t], ax, ay, az);
+                                ring_f32(ph, pl, dx, dy, dz, il, rc4, nocore, xh[t], yh[t], zh[t], xl[t], yl[t], zl[t],
+                                         ax, ay, az);
                                 tx[t] = fmaf(g4, ax, tx[t]);
                                 ty[t] = fmaf(g4, ay, ty[t]);
                                 tz[t] = fmaf(g4, az, tz[t]);
@@ -338,7 +359,7 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
                                 d3 u = mk(0, 0, 0);
                                 d3 pp[4] = {mk(v[0], v[1], v[2]), mk(v[3], v[4], v[5]), mk(v[6], v[7], v[8]),
                                             mk(v[9], v[10], v[11])};
-                                d3 X = mk(x[t], y[t], z[t]);
+                                d3 X = mk(xh[t], yh[t], zh[t]);
                                 for (int i = 0; i < 4; ++i) u = u + line_unit_f64(pp[i], pp[(i + 1) & 3], X, v[25]);
                                 tx[t] += gam * u.x;
                                 ty[t] += gam * u.y;

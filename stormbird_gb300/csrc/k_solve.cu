@@ -224,8 +224,8 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve_si(DevModel m, SolveSet
         b.gamma_prev[i] = gam;
         b.vel_out[i] = u_last[k];
         if (b.wake_str_row0) b.wake_str_row0[i] = gam;
-        if (b.rec32_row0) b.rec32_row0[i].v[24] = static_cast<float>(gam);
-        if (b.rec64_row0) b.rec64_row0[i].v[24] = gam;
+        if (b.rec32_row0) b.rec32_row0[i].v[kRec32Gamma] = static_cast<float>(gam);
+        if (b.rec64_row0) b.rec64_row0[i].v[kRec64Gamma] = gam;
     }
     if (rank == 0 && tid == 0) {
         b.scalars[0] = residual;
@@ -406,8 +406,8 @@ __global__ void __launch_bounds__(kLinThreads) k_solve_lin(DevModel m, SolveSett
         b.gamma_prev[i] = gam[i];
         b.vel_out[i] = vel[i];
         if (b.wake_str_row0) b.wake_str_row0[i] = gam[i];
-        if (b.rec32_row0) b.rec32_row0[i].v[24] = static_cast<float>(gam[i]);
-        if (b.rec64_row0) b.rec64_row0[i].v[24] = gam[i];
+        if (b.rec32_row0) b.rec32_row0[i].v[kRec32Gamma] = static_cast<float>(gam[i]);
+        if (b.rec64_row0) b.rec64_row0[i].v[kRec64Gamma] = gam[i];
     }
 }
 

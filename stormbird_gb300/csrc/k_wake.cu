@@ -213,31 +213,35 @@ __global__ void k_wake_panels(DevModel m, WakeBuffers w, int shift) {
     else g = w.str_old[id];
     w.str_new[id] = g;
 
+    // FP32 record with float-float positions (layout in sb_device.cuh)
     PanelRec<float> r;
-    float px[4] = {static_cast<float>(p0.x), static_cast<float>(p1.x), static_cast<float>(p2.x), static_cast<float>(p3.x)};
-    float py[4] = {static_cast<float>(p0.y), static_cast<float>(p1.y), static_cast<float>(p2.y), static_cast<float>(p3.y)};
-    float pz[4] = {static_cast<float>(p0.z), static_cast<float>(p1.z), static_cast<float>(p2.z), static_cast<float>(p3.z)};
+    auto split = [](double x, float* hi, float* lo) {
+        float h = static_cast<float>(x);
+        *hi = h;
+        *lo = static_cast<float>(x - static_cast<double>(h));
+    };
+    const d3 pp[4] = {p0, p1, p2, p3};
     for (int k = 0; k < 4; ++k) {
-        r.v[3 * k] = px[k];
-        r.v[3 * k + 1] = py[k];
-        r.v[3 * k + 2] = pz[k];
-        float dx = px[(k + 1) & 3] - px[k], dy = py[(k + 1) & 3] - py[k], dz = pz[(k + 1) & 3] - pz[k];
-        float l2 = dx * dx + dy * dy + dz * dz;
-        r.v[12 + k] = l2 > 0.f ? 1.0f / l2 : 0.f;
+        split(pp[k].x, &r.v[3 * k], &r.v[12 + 3 * k]);
+        split(pp[k].y, &r.v[3 * k + 1], &r.v[12 + 3 * k + 1]);
+        split(pp[k].z, &r.v[3 * k + 2], &r.v[12 + 3 * k + 2]);
+        double l2 = len2(pp[(k + 1) & 3] - pp[k]);
+        r.v[36 + k] = l2 > 0.0 ? static_cast<float>(1.0 / l2) : 0.f;
     }
-    r.v[16] = static_cast<float>(c.x);
-    r.v[17] = static_cast<float>(c.y);
-    r.v[18] = static_cast<float>(c.z);
-    r.v[19] = static_cast<float>(ff2);
-    r.v[20] = static_cast<float>(n.x);
-    r.v[21] = static_cast<float>(n.y);
-    r.v[22] = static_cast<float>(n.z);
-    r.v[23] = static_cast<float>(area * kFourPiInv);
-    r.v[24] = static_cast<float>(g);
+    split(c.x, &r.v[24], &r.v[28]);
+    split(c.y, &r.v[25], &r.v[29]);
+    split(c.z, &r.v[26], &r.v[30]);
+    r.v[27] = static_cast<float>(ff2);
+    r.v[31] = static_cast<float>(area * kFourPiInv);
+    r.v[32] = static_cast<float>(n.x);
+    r.v[33] = static_cast<float>(n.y);
+    r.v[34] = static_cast<float>(n.z);
+    r.v[kRec32Gamma] = static_cast<float>(g);
     double rc2 = rc * rc;
-    r.v[25] = static_cast<float>(rc2 * rc2);
-    r.v[26] = static_cast<float>(wg);
-    r.v[27] = rc == 0.0 ? 1.f : 0.f;
+    r.v[40] = static_cast<float>(rc2 * rc2);
+    r.v[41] = static_cast<float>(wg);
+    r.v[42] = rc == 0.0 ? 1.f : 0.f;
+    for (int k = 43; k < 48; ++k) r.v[k] = 0.f;
     w.rec32[id] = r;
 
     if (s == 0 || w.rec64) {

@@ -172,18 +172,37 @@ __device__ inline double foil_cd(const FoilP& f, double a) {
 // ---------------------------------------------------------------------------------------
 // Panel records
 // ---------------------------------------------------------------------------------------
-// Record of one vortex-ring panel for the Biot-Savart sweeps, `R` = float or double.
-//   [0..11]  corners p0..p3 (x, y, z)
-//   [12..15] 1/|p_{k+1} - p_k|^2 per ring segment k (0 for a degenerate segment)
-//   [16..18] centre, [19] far-field length squared
-//   [20..22] unit normal, [23] area / (4 pi)
-//   [24] strength Gamma, [25] core length^4, [26] wing index, [27] 1 if core length == 0
+// Records of one vortex-ring panel for the Biot-Savart sweeps.
+//
+// FP32 record (PanelRec<float>, 48 floats = 192 B). Positions are float-float pairs
+// (hi = fl32(x), lo = fl32(x - hi)), so that a sweep forms r = (x_hi - p_hi) + (x_lo - p_lo):
+// for nearby points the hi difference is exact (Sterbenz), which makes the FP32 sweep
+// independent of where the geometry sits in space.
+//   [0..11]  corners p0..p3 hi (x, y, z)     [12..23] corners lo
+//   [24..26] centre hi, [27] far-field length squared
+//   [28..30] centre lo, [31] area / (4 pi)
+//   [32..34] unit normal, [35] strength Gamma
+//   [36..39] 1/|p_{k+1} - p_k|^2 per ring segment k (0 for a degenerate segment)
+//   [40] core length^4, [41] wing index, [42] 1 if the core length is 0, [43..47] 0
+// FP64 record (PanelRec<double>, 28 doubles = 224 B):
+//   [0..11] corners, [16..18] centre, [19] far-field length squared, [20..22] normal,
+//   [23] area / (4 pi), [24] Gamma, [25] core length, [26] wing index.
+template <class R>
+struct PanelRecSize;
+template <>
+struct PanelRecSize<float> { static constexpr int value = 48; };
+template <>
+struct PanelRecSize<double> { static constexpr int value = 28; };
+
 template <class R>
 struct __align__(16) PanelRec {
-    R v[28];
+    R v[PanelRecSize<R>::value];
 };
-static_assert(sizeof(PanelRec<float>) == 112, "FP32 panel record is 112 bytes");
+static_assert(sizeof(PanelRec<float>) == 192, "FP32 panel record is 192 bytes");
 static_assert(sizeof(PanelRec<double>) == 224, "FP64 panel record is 224 bytes");
+
+constexpr int kRec32Gamma = 35;  // strength slot of the FP32 record
+constexpr int kRec64Gamma = 24;  // strength slot of the FP64 record
 
 // ---------------------------------------------------------------------------------------
 // Model and step parameters

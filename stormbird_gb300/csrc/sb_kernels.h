@@ -139,6 +139,9 @@ struct OutLayout {
     }
 };
 
+// FP32 FMA throughput of `device` in TFLOP/s (k_probe.cu); negative on error.
+double measure_fp32_peak(int device, int reps);
+
 // Sectional and integrated forces (force_calculations.rs:322-452, 669-698;
 // forces_and_moments.rs:163-245; flow_derivatives.rs:31-63).
 cudaError_t launch_forces(const DevModel& m, const StepParams& p, const ForceArgs& f, cudaStream_t s);

@@ -136,8 +136,10 @@ struct sb_sim {
     OutLayout L{};
     std::vector<double> chord_lengths_h;
     bool timing = false;
-    double last_ms[7] = {0};
-    double last_counters[5] = {0};
+    double last_ms[9] = {0};
+    double last_counters[6] = {0};
+    int launches = 0;
+    bool swept[2] = {false, false};
 
     // constants
     DevBuf<d3> span_s_local, span_e_local, chord_nr;
@@ -163,7 +165,7 @@ struct sb_sim {
     DevBuf<d3> vel_out, hist0, hist1, fs, aux_targets, aux_out;
     PinnedBuf<double> h_out, h_fs;
     PinnedBuf<int> h_err;
-    cudaEvent_t ev[8] = {nullptr};
+    cudaEvent_t ev[12] = {nullptr};
 
     ~sb_sim() {
         for (auto& e : ev) if (e) cudaEventDestroy(e);
@@ -464,10 +466,15 @@ struct sb_sim {
             a.symmetry = sym;
             a.neglect = neglect;
             ck(cudaMemsetAsync(a.work_counter, 0, sizeof(unsigned long long), stream), "memset counter");
+            if (timing && counter_slot < 2) ck(cudaEventRecord(ev[8 + 2 * counter_slot], stream), "event");
             ck(launch_bs_sweep(a, precision, sp.grid, stream), "Biot-Savart sweep");
+            if (timing && counter_slot < 2) ck(cudaEventRecord(ev[9 + 2 * counter_slot], stream), "event");
             ck(launch_bs_reduce(partial.p, sp.n_chunks, M, M_total, base, dst, stream), "sweep reduce");
+            launches += 2;
+            if (counter_slot < 2) swept[counter_slot] = true;
         } else {
             ck(launch_bs_reduce(nullptr, 0, 0, M_total, base, dst, stream), "sweep reduce");
+            launches += 1;
         }
     }
 
@@ -480,12 +487,16 @@ struct sb_sim {
         ensure_rec64();
         record(0);
         const bool first = !first_step_completed;
+        launches = 0;
+        swept[0] = swept[1] = false;
         ck(launch_prep_geometry(dm, params, fs.p, first ? mean.p : nullptr, stream), "prep geometry");
+        launches += 1;
         if (first) {
             // Simulation::initialize (simulation.rs:65-94)
             if (dynamic) {
                 ck(launch_wake_init(dm, wake(false), mean.p, mk(0, 0, 0), dt, 0, stream), "wake init");
                 ck(launch_wake_panels(dm, wake(false), 0, stream), "wake panels");
+                launches += 2;
             }
             ck(cudaMemcpyAsync(hist0.p, fs.p, N * sizeof(d3), cudaMemcpyDeviceToDevice, stream), "fd init");
             ck(cudaMemcpyAsync(hist1.p, fs.p, N * sizeof(d3), cudaMemcpyDeviceToDevice, stream), "fd init");
@@ -497,6 +508,7 @@ struct sb_sim {
         if (dynamic) {
             ck(launch_wake_advect(dm, wake(true), dt, steps_completed, stream), "wake advect");
             ck(launch_wake_panels(dm, wake(true), 1, stream), "wake panels");
+            launches += 3;
             cur ^= 1;
             record(2);
             // frozen wake (frozen_wake.rs:189-261)
@@ -506,6 +518,7 @@ struct sb_sim {
             record(3);
             ck(launch_unit_matrix(row0_64.p, ctrl.p, N, dm.symmetry, dm.neglect_self, wing_of_line.p, factors.p, stream),
                "unit matrix");
+            launches += 1;
         } else {
             record(2);
             const auto& q = setup.quasi_steady_wake;
@@ -513,6 +526,7 @@ struct sb_sim {
             ck(launch_horseshoe_matrix(dm, static_cast<int>(q.viscous_core_length.kind), q.viscous_core_length.value, wl,
                                        qs_wake_vec.p, qs_rc.p, static_cast<int>(q.symmetry_condition), factors.p, stream),
                "horseshoe matrix");
+            launches += 2;
             record(3);
         }
         record(4);
@@ -539,6 +553,7 @@ struct sb_sim {
                 lb.rec64_row0 = nullptr;
                 SolveSettings ls;  // Linearized::default()
                 ck(launch_solve_linearized(dm, ls, lb, stream), "linearized start");
+                launches += 1;
                 ck(cudaMemcpyAsync(gamma_prev.p, gamma_tmp.p, N * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
                 st.correction_factor_initial = 1.0;
             }
@@ -546,6 +561,7 @@ struct sb_sim {
         } else {
             ck(launch_solve_linearized(dm, solve, sb, stream), "linearized solve");
         }
+        launches += 1;
         record(5);
         if (dynamic) {
             // DynamicWake::update_after_solving (update_data.rs:49-59, 125-141)
@@ -572,6 +588,8 @@ struct sb_sim {
         fa.out = out.p;
         fa.scalars = scalars.p;
         ck(launch_forces(dm, params, fa, stream), "forces");
+        launches += 1;
+        last_counters[5] = static_cast<double>(launches);
         fd_count += 1;
         record(7);
     }
@@ -589,6 +607,9 @@ struct sb_sim {
             cudaEventElapsedTime(&ms, ev[4], ev[5]); last_ms[4] = ms;
             cudaEventElapsedTime(&ms, ev[5], ev[6]); last_ms[5] = ms;
             cudaEventElapsedTime(&ms, ev[6], ev[7]); last_ms[6] = ms;
+            last_ms[7] = last_ms[8] = 0.0;
+            if (swept[1]) { cudaEventElapsedTime(&ms, ev[10], ev[11]); last_ms[7] = ms; }
+            if (swept[0]) { cudaEventElapsedTime(&ms, ev[8], ev[9]); last_ms[8] = ms; }
         }
         check_device_status();
     }
@@ -873,13 +894,21 @@ int sb_sim_enable_timing(sb_sim* sim, int enable) {
 
 int sb_sim_last_step_timing(const sb_sim* sim, double* ms, size_t n) {
     if (!sim || !ms) { g_last_error = "null argument"; return SB_ERR_NULL_ARG; }
-    for (size_t i = 0; i < n && i < 7; ++i) ms[i] = sim->last_ms[i];
+    for (size_t i = 0; i < n && i < 9; ++i) ms[i] = sim->last_ms[i];
     return SB_OK;
 }
 
 int sb_sim_last_step_counters(const sb_sim* sim, double* c, size_t n) {
     if (!sim || !c) { g_last_error = "null argument"; return SB_ERR_NULL_ARG; }
-    for (size_t i = 0; i < n && i < 5; ++i) c[i] = sim->last_counters[i];
+    for (size_t i = 0; i < n && i < 6; ++i) c[i] = sim->last_counters[i];
+    return SB_OK;
+}
+
+int sb_measure_fp32_peak(int device, int reps, double* tflops) {
+    if (!tflops) { g_last_error = "null argument"; return SB_ERR_NULL_ARG; }
+    double v = measure_fp32_peak(device, reps < 1 ? 1 : reps);
+    if (v < 0.0) { g_last_error = "FP32 probe failed"; return SB_ERR_CUDA; }
+    *tflops = v;
     return SB_OK;
 }
 

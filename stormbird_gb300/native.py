@@ -46,6 +46,7 @@ SIGNATURES = [
     ("sb_sim_enable_timing", ctypes.c_int, [_vp, ctypes.c_int]),
     ("sb_sim_last_step_timing", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
     ("sb_sim_last_step_counters", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
+    ("sb_measure_fp32_peak", ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp]),
 ]
 
 _LIB = None

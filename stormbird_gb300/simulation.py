@@ -140,13 +140,22 @@ class Simulation:
         _check(lib().sb_sim_enable_timing(self._h, 1 if on else 0))
 
     def last_step_timing(self) -> dict:
-        ms = np.zeros(7)
-        _check(lib().sb_sim_last_step_timing(self._h, as_ptr(ms), 7))
-        keys = ("step", "wake_update", "free_wake_sweep", "unit_matrix", "solve", "rollup_sweep", "forces")
+        ms = np.zeros(9)
+        _check(lib().sb_sim_last_step_timing(self._h, as_ptr(ms), 9))
+        keys = ("step", "wake_update", "free_wake_sweep", "unit_matrix", "solve", "rollup_sweep", "forces",
+                "rollup_sweep_kernel", "free_wake_sweep_kernel")
         return dict(zip(keys, ms.tolist()))
 
     def last_step_counters(self) -> dict:
-        c = np.zeros(5)
-        _check(lib().sb_sim_last_step_counters(self._h, as_ptr(c), 5))
-        keys = ("rollup_targets", "rollup_panels", "ctrl_targets", "free_wake_panels", "steps_completed")
+        c = np.zeros(6)
+        _check(lib().sb_sim_last_step_counters(self._h, as_ptr(c), 6))
+        keys = ("rollup_targets", "rollup_panels", "ctrl_targets", "free_wake_panels", "steps_completed",
+                "kernel_launches")
         return dict(zip(keys, c.tolist()))
+
+
+def measure_fp32_peak(device: int = 0, reps: int = 5) -> float:
+    """Measured FP32 FMA throughput (TFLOP/s) of a device, from the library's probe kernel."""
+    v = ctypes.c_double()
+    _check(lib().sb_measure_fp32_peak(int(device), int(reps), ctypes.byref(v)))
+    return v.value

@@ -52,3 +52,21 @@ def run_pair(gpu_sim, oracle_sim, wind, steps, dt, every=1, motion=None):
 
 def small_row(nr_sails=2, panels=8, wake_rows=20, **kw) -> str:
     return S.wing_sail_row(nr_sails=nr_sails, panels_per_sail=panels, wake_rows=wake_rows, **kw)
+
+
+def panel_corners(points, nr_points_along_span, wing_ranges, nr_rows):
+    """Corners [P_pan, 4, 3] of the wake panels from the wake points, in the reference's
+    panel indexing (stormbird/src/lifting_line/wake/dynamic_wake/mod.rs:82-103)."""
+    P = np.asarray(points).reshape(nr_rows + 1, nr_points_along_span, 3)
+    cols = []
+    for w, (a, b) in enumerate(wing_ranges):
+        for j in range(a, b):
+            cols.append((j + w, j + 1 + w))
+    c0 = np.array([c[0] for c in cols])
+    c1 = np.array([c[1] for c in cols])
+    corners = np.stack([P[:-1][:, c0], P[:-1][:, c1], P[1:][:, c1], P[1:][:, c0]], axis=2)
+    return corners.reshape(-1, 4, 3)
+
+
+def row_wing_ranges(nr_sails, panels):
+    return [(i * panels, (i + 1) * panels) for i in range(nr_sails)]

@@ -15,7 +15,7 @@ import pytest
 
 from stormbird_gb300 import Simulation, SbError
 from stormbird_gb300 import setups as S
-from tests.helpers import fixed_iterations, rel_inf, rel_vec, run_pair, small_row
+from tests.helpers import fixed_iterations, panel_corners, rel_inf, rel_vec, row_wing_ranges, run_pair, small_row
 
 pytestmark = pytest.mark.gpu
 
@@ -62,7 +62,8 @@ def test_wake_state_matches_oracle(gpu_lib, oracle_mod):
         pass
     pg, sg, vg = g.wake_state()
     po, so, vo = o.wake_state()
-    assert rel_inf(pg, po) < 1e-9, "wake points"
+    # positions are integrated in f64 from FP32 induced velocities: a few nm on a 50 m wake
+    assert rel_inf(pg, po) < 1e-8, "wake points"
     assert rel_inf(sg, so) < TOL, "wake strengths"
     assert rel_inf(vg, vo) < TOL, "wake point velocities"
 
@@ -73,20 +74,50 @@ def test_freestream_points_match_oracle(gpu_lib, oracle_mod):
     assert rel_inf(g.get_freestream_velocity_points(), o.get_freestream_velocity_points()) < 1e-12
 
 
-@pytest.mark.parametrize("mode,tol", [("kahan", 2e-6), ("fp32", 1e-5), ("fp64", 1e-11)])
+@pytest.mark.parametrize("mode,tol", [("kahan", 1e-6), ("fp32", 5e-6), ("fp64", 1e-12)])
 def test_induced_velocities_precision_modes(gpu_lib, oracle_mod, mode, tol):
-    setup = fixed_iterations(small_row(2, 8, 25), 20)
-    g, o = pair(setup, oracle_mod)
+    """The sweep kernel alone: GPU induced velocities on the GPU's own wake state against
+    the oracle's sweep (induced_velocity_calc.rs:111-126) over the same panels."""
+    sails, panels, rows = 2, 8, 25
+    setup = fixed_iterations(small_row(sails, panels, rows), 20)
+    g = Simulation(setup)
     wind = S.GustyWind(seed=4)
-    for _ in run_pair(g, o, wind, steps=8, dt=0.05):
-        pass
+    n = g.nr_freestream_points
+    for k in range(8):
+        g.do_step(time=0.05 * k, time_step=0.05, freestream_velocity=wind.freestream(0.05 * k, n))
     g.set_precision(mode)
+    pts, strengths, _ = g.wake_state()
+    corners = panel_corners(pts, sails * (panels + 1), row_wing_ranges(sails, panels), rows)
     rng = np.random.default_rng(0)
-    pts = np.concatenate([o.get_freestream_velocity_points()[::7],
-                          rng.uniform([-20, -20, -5], [60, 40, 35], (200, 3))])
-    ug = g.induced_velocities(pts)
-    uo = o.induced_velocities(pts)
+    targets = np.concatenate([pts[::3], rng.uniform([-20, -20, -5], [60, 40, 35], (200, 3))])
+    ug = g.induced_velocities(targets)
+    uo = oracle_mod.bs_sweep(corners, np.full(len(strengths), 1.0), strengths, 5.0, targets, nthreads=4)
     assert rel_inf(ug, uo) < tol
+
+
+def test_full_size_wing_sail_row_sampled(gpu_lib, oracle_mod):
+    """Full-size dynamic case (4 sails x 64 panels, 300 wake rows, 76,800 panels): after the
+    wake is fully shed, the GPU sweep at sampled targets matches the oracle's sweep over the
+    GPU's own wake, and the stored roll-up velocities equal freestream + induced velocity."""
+    sails, panels, rows = 4, 64, 300
+    g = Simulation(S.wing_sail_row(sails, panels, rows))
+    wind = S.GustyWind(seed=8)
+    n = g.nr_freestream_points
+    for k in range(rows + 5):
+        r = g.do_step(time=0.05 * k, time_step=0.05, freestream_velocity=wind.freestream(0.05 * k, n))
+    assert np.all(np.isfinite(r.circulation_strength)) and r.iterations > 0
+    pts, strengths, vel = g.wake_state()
+    assert np.count_nonzero(strengths) == sails * panels * rows
+    corners = panel_corners(pts, sails * (panels + 1), row_wing_ranges(sails, panels), rows)
+    rng = np.random.default_rng(1)
+    idx = np.sort(rng.choice(len(pts) - 1, 192, replace=False))
+    targets = pts[idx]
+    ug = g.induced_velocities(targets)
+    uo = oracle_mod.bs_sweep(corners, np.full(len(strengths), 1.0), strengths, 5.0, targets, nthreads=8)
+    assert rel_inf(ug, uo) < 2e-6
+    # velocity_at_points = freestream + induced (update_data.rs:125-141), last step's freestream
+    u_fs = wind.velocity(0.05 * (rows + 4))
+    assert rel_inf(vel[idx], ug + u_fs) < 1e-6
 
 
 def test_quasi_steady_simple_iterative_single_wing(gpu_lib, oracle_mod):

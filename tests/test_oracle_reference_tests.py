@@ -229,3 +229,22 @@ def test_oracle_wake_initialisation_is_straight(oracle_mod, damping):
         d_rows = np.diff(p[2:10, :, 0], axis=0)
         assert np.allclose(d_rows, 1.0, atol=1e-9)
     assert np.allclose(v[:, 0], 10.0)
+
+
+def test_panel_corner_reconstruction_matches_oracle_wake(oracle_mod):
+    """The test helper that rebuilds wake panels from wake points (used to check the GPU
+    sweep on the GPU's own wake) reproduces the oracle's induced velocities exactly."""
+    from tests.helpers import panel_corners, row_wing_ranges, small_row
+
+    sails, panels, rows = 2, 5, 8
+    sim = oracle_mod.OracleSimulation(small_row(sails, panels, rows))
+    wind = S.GustyWind(seed=9)
+    n = sim.nr_freestream_points
+    for k in range(6):
+        sim.do_step(time=0.05 * k, time_step=0.05, freestream_velocity=wind.freestream(0.05 * k, n))
+    pts, strengths, _ = sim.wake_state()
+    corners = panel_corners(pts, sails * (panels + 1), row_wing_ranges(sails, panels), rows)
+    targets = pts[::2] + 0.01
+    a = oracle_mod.bs_sweep(corners, np.full(len(strengths), 1.0), strengths, 5.0, targets, nthreads=2)
+    b = sim.induced_velocities(targets)
+    assert np.array_equal(a, b)
