@@ -383,6 +383,29 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_kernel_only(args):
+    """The profiling workload: one standalone sweep (sb_panel_sweep) over a synthetic wake of
+    the benchmark's size (4 x 64 panels x 300 rows = 76,800 panels, 78,259 wake-point
+    targets, all near field), called `--steps` times after one warm-up call. Few kernel
+    launches precede each sweep (the record build and two memsets), so an ncu capture of
+    k_bs_sweep here needs no skipping."""
+    from stormbird_gb300 import setups as S
+    from stormbird_gb300.simulation import panel_sweep
+
+    corners, strengths, cores, pts = S.synthetic_sail_row_wake(SAILS, PANELS, args.rows or ROWS)
+    targets = pts[:-1]
+    panel_sweep(corners, strengths, cores, targets, far_field_ratio=1e30)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        panel_sweep(corners, strengths, cores, targets, far_field_ratio=1e30)
+        times.append(time.perf_counter() - t0)
+    inter = len(targets) * 4.0 * len(strengths)
+    print(json.dumps({"mode": "kernel-only standalone sweep (host-timed call incl. copies and record build)",
+                      "interactions_per_call": inter, "best_s": min(times),
+                      "interactions_per_s": inter / min(times)}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -390,13 +413,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--kernel-only", action="store_true", help="standalone sweep on a synthetic wake (profiling)")
+    ap.add_argument("--rows", type=int, default=0, help="wake rows of the --kernel-only wake (default 300)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     import __graft_entry__
 
     __graft_entry__.build()
-    if args.impl == "reference":
+    if args.kernel_only:
+        run_kernel_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gb300(args)

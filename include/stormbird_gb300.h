@@ -173,6 +173,21 @@ int sb_sim_last_step_timing(const sb_sim* sim, double* ms, size_t n);
 int sb_sim_last_step_counters(const sb_sim* sim, double* counters, size_t n);
 
 /*
+ * Standalone Biot-Savart sweep over caller-given vortex-ring panels: the velocity that
+ * n_panels unit rings (corners [n_panels*12], four corners in ring order), scaled by their
+ * strengths [n_panels], with viscous core lengths [n_panels] and the far-field ratio of the
+ * point-doublet approximation, induce at n_targets points [n_targets*3], written to
+ * velocities [n_targets*3]. It is the computation DynamicWake::induced_velocities runs over
+ * its own panels (stormbird/src/lifting_line/wake/dynamic_wake/induced_velocity_calc.rs:18-26,
+ * singularity_elements/panel.rs:26-118, symmetry_condition.rs:27-43), offered on caller data.
+ * symmetry: 0 none, 1 X, 2 Y, 3 Z. precision as in sb_sim_set_precision. Host arrays; the
+ * device work space is allocated (stream-ordered) and freed on every call.
+ */
+int sb_panel_sweep(int device, const double* corners, const double* strengths, const double* core_lengths,
+                   size_t n_panels, double far_field_ratio, int symmetry, const double* targets, size_t n_targets,
+                   int precision, double* velocities);
+
+/*
  * Measured FP32 FMA throughput of a device in TFLOP/s (best of `reps` timed launches of
  * an FMA-chain kernel): the denominator of the Biot-Savart sweep's roofline. Diagnostic
  * entry point with no counterpart in the reference.

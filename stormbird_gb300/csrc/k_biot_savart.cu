@@ -136,55 +136,69 @@ __device__ __forceinline__ void two_sum_acc(R& s, R& c, R t) {
     c += err;
 }
 
-// One FP32 vortex ring (4 segments) at one target, from float-float corners; returns the
-// unscaled sum sum_k core_k * kk_k * (r_k x r_{k+1}) (times Gamma / 4 pi gives the velocity).
-// r_k = (x_hi - p_hi_k) + (x_lo - p_lo_k); d_k = p_{k+1} - p_k (precomputed per panel).
-__device__ __forceinline__ void ring_f32(const float (&ph)[12], const float (&pl)[12], const float (&dx)[4],
-                                         const float (&dy)[4], const float (&dz)[4], const float (&il)[4], float rc4,
-                                         bool nocore, float xh, float yh, float zh, float xl, float yl, float zl,
-                                         float& ax, float& ay, float& az) {
-    float rx[4], ry[4], rz[4], rs[4], rl[4];
+// ---------------------------------------------------------------------------------------
+// Packed FP32 helpers (Blackwell f32x2: two FP32 operations per instruction)
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ float2 bc(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2s(float2 a, float b) { return __fadd2_rn(a, make_float2(-b, -b)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sel2(bool cx, float2 a, bool cy, float2 b) {
+    return make_float2(cx ? a.x : b.x, cy ? a.y : b.y);
+}
+
+// Vortex ring of one FP32 panel record at two targets (the two lanes of the float2s).
+// r_k = (x_hi - p_hi_k) + (x_lo - p_lo_k). Per segment, with c = d x r1 = r1 x r2:
+//   den = l1 l2 (l1 l2 + r1.r2) = B / A without cancellation
+//        (A, B) = (l1 l2 - r1.r2, l1 l2 |c|^2) if r1.r2 < 0, else (1, l1 l2 (l1 l2 + r1.r2)),
+//   distance^2 to the segment = |c|^2 / |d|^2 inside it, the end-point distance outside,
+//   core * k = d2 (l1 + l2) A / (B sqrt(d2^2 + rc^4)) with a single rsqrt,
+// which is the reference's (vortex_line.rs:18-106) value, evaluated without the FP32
+// cancellations of its literal form. Returns sum_k core_k k_k c_k (times Gamma/4pi = velocity).
+__device__ __forceinline__ void ring2(const float* v, float2 xh, float2 yh, float2 zh, float2 xl, float2 yl, float2 zl,
+                                      float2& ax, float2& ay, float2& az) {
+    float2 rx[4], ry[4], rz[4], rs[4], rl[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        rx[k] = (xh - ph[3 * k]) + (xl - pl[3 * k]);
-        ry[k] = (yh - ph[3 * k + 1]) + (yl - pl[3 * k + 1]);
-        rz[k] = (zh - ph[3 * k + 2]) + (zl - pl[3 * k + 2]);
-        rs[k] = fmaf(rx[k], rx[k], fmaf(ry[k], ry[k], rz[k] * rz[k]));
-        rl[k] = rs[k] * rsqrtf(fmaxf(rs[k], 1e-30f));
+        rx[k] = add2(sub2s(xh, v[3 * k]), sub2s(xl, v[12 + 3 * k]));
+        ry[k] = add2(sub2s(yh, v[3 * k + 1]), sub2s(yl, v[12 + 3 * k + 1]));
+        rz[k] = add2(sub2s(zh, v[3 * k + 2]), sub2s(zl, v[12 + 3 * k + 2]));
+        rs[k] = fma2(rx[k], rx[k], fma2(ry[k], ry[k], mul2(rz[k], rz[k])));
+        float2 t = add2(rs[k], bc(1e-30f));  // r = 0 (target on a corner) gives l = 0
+        rl[k] = mul2(rs[k], make_float2(rsqrtf(t.x), rsqrtf(t.y)));
     }
-    ax = 0.f;
-    ay = 0.f;
-    az = 0.f;
-    // The reference's den = l1 l2 (l1 l2 + r1.r2) and its segment distance |r1|^2 - t^2 both
-    // cancel catastrophically in FP32 when the target is close to the segment's interior
-    // (r1.r2 -> -l1 l2). They are evaluated through exact identities instead:
-    //   c = r1 x r2 = d x r1,  l1 l2 + r1.r2 = |c|^2 / (l1 l2 - r1.r2)  (for r1.r2 < 0),
-    //   distance^2 to the segment's line = |c|^2 / |d|^2.
+    const float rc4 = v[52];
+    ax = ay = az = bc(0.f);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const int k1 = (k + 1) & 3;
-        const float p = rl[k] * rl[k1];
-        const float q = fmaf(rx[k], rx[k1], fmaf(ry[k], ry[k1], rz[k] * rz[k1]));
-        const float cx = dy[k] * rz[k] - dz[k] * ry[k];
-        const float cy = dz[k] * rx[k] - dx[k] * rz[k];
-        const float cz = dx[k] * ry[k] - dy[k] * rx[k];
-        const float c2 = fmaf(cx, cx, fmaf(cy, cy, cz * cz));
-        // den = B / A without cancellation
-        const bool neg = q < 0.f;
-        const float A = neg ? p - q : 1.f;
-        const float B = neg ? p * c2 : p * (p + q);
-        // distance^2 to the segment, clamped to the end points (vortex_line.rs:59-84)
-        const float tp = fmaf(rx[k], dx[k], fmaf(ry[k], dy[k], rz[k] * dz[k]));
-        float d2 = c2 * il[k];
-        d2 = (tp * il[k] > 1.f) ? rs[k1] : d2;
-        d2 = (tp < 0.f) ? rs[k] : d2;
-        const float core = nocore ? 1.f : d2 * rsqrtf(fmaxf(fmaf(d2, d2, rc4), 1e-37f));
-        // closeness cut-off |den| > 1e-10 (vortex_line.rs:35); den >= 0 here
-        const bool ok = (B > 1.0e-10f * A) && il[k] > 0.f;
-        const float s = ok ? core * __fdividef((rl[k] + rl[k1]) * A, B) : 0.f;
-        ax = fmaf(s, cx, ax);
-        ay = fmaf(s, cy, ay);
-        az = fmaf(s, cz, az);
+        const float dx = v[24 + 3 * k], dy = v[24 + 3 * k + 1], dz = v[24 + 3 * k + 2], il = v[36 + k];
+        const float2 p = mul2(rl[k], rl[k1]);
+        const float2 q = fma2(rx[k], rx[k1], fma2(ry[k], ry[k1], mul2(rz[k], rz[k1])));
+        const float2 cx = fma2(bc(dy), rz[k], mul2(bc(-dz), ry[k]));
+        const float2 cy = fma2(bc(dz), rx[k], mul2(bc(-dx), rz[k]));
+        const float2 cz = fma2(bc(dx), ry[k], mul2(bc(-dy), rx[k]));
+        const float2 c2 = fma2(cx, cx, fma2(cy, cy, mul2(cz, cz)));
+        const bool n0 = q.x < 0.f, n1 = q.y < 0.f;
+        const float2 pmq = add2(p, make_float2(-q.x, -q.y));
+        const float2 ppq = add2(p, q);
+        const float2 Ax = make_float2(n0 ? pmq.x : 1.f, n1 ? pmq.y : 1.f);
+        const float2 Bx = mul2(p, make_float2(n0 ? c2.x : ppq.x, n1 ? c2.y : ppq.y));
+        const float2 tp = fma2(rx[k], bc(dx), fma2(ry[k], bc(dy), mul2(rz[k], bc(dz))));
+        const float2 tpl = mul2(tp, bc(il));
+        float2 d2 = mul2(c2, bc(il));
+        d2.x = tpl.x > 1.f ? rs[k1].x : d2.x;
+        d2.y = tpl.y > 1.f ? rs[k1].y : d2.y;
+        d2.x = tp.x < 0.f ? rs[k].x : d2.x;
+        d2.y = tp.y < 0.f ? rs[k].y : d2.y;
+        const float2 X = add2(mul2(mul2(Bx, Bx), fma2(d2, d2, bc(rc4))), bc(1e-37f));
+        const float2 s0 = mul2(mul2(mul2(d2, add2(rl[k], rl[k1])), Ax), make_float2(rsqrtf(X.x), rsqrtf(X.y)));
+        const float2 lim = mul2(Ax, bc(1.0e-10f));
+        const float2 s = make_float2(Bx.x > lim.x ? s0.x : 0.f, Bx.y > lim.y ? s0.y : 0.f);
+        ax = fma2(s, cx, ax);
+        ay = fma2(s, cy, ay);
+        az = fma2(s, cz, az);
     }
 }
 
@@ -193,6 +207,7 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
     constexpr int TILE = TileSize<R>::value;
     constexpr int TT = SYM ? 2 * T : T;  // mirrored targets ride along as extra targets
     constexpr bool F32 = sizeof(R) == 4;
+    static_assert(!F32 || TT == 2, "the packed FP32 path holds exactly two targets per thread");
     __shared__ __align__(128) PanelRec<R> tile[2][TILE];
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ long long s_item;
@@ -221,7 +236,7 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
         const long long pb = a.p_begin + static_cast<long long>(chunk) * a.chunk_panels;
         const long long pe = min(pb + static_cast<long long>(a.chunk_panels), a.p_end);
 
-        // targets: FP32 as float-float pairs, FP64 as is (the lo parts stay 0)
+        // targets: float-float pairs (FP32) or doubles (FP64 path, lo parts 0)
         R xh[TT], yh[TT], zh[TT], xl[TT], yl[TT], zl[TT];
         bool valid[TT];
         int tw[TT];
@@ -245,9 +260,15 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
                 tw[u] = tw[t];
             }
         }
+        // running sums and compensations; for FP32 lane j of a float2 is target j
         R sx[TT], sy[TT], sz[TT], cx[TT], cy[TT], cz[TT];
 #pragma unroll
         for (int t = 0; t < TT; ++t) sx[t] = sy[t] = sz[t] = cx[t] = cy[t] = cz[t] = R(0);
+        float2 X2h, Y2h, Z2h, X2l, Y2l, Z2l;
+        if constexpr (F32) {
+            X2h = make_float2(xh[0], xh[1]); Y2h = make_float2(yh[0], yh[1]); Z2h = make_float2(zh[0], zh[1]);
+            X2l = make_float2(xl[0], xl[1]); Y2l = make_float2(yl[0], yl[1]); Z2l = make_float2(zl[0], zl[1]);
+        }
 
         const int ntiles = static_cast<int>((pe - pb + TILE - 1) / TILE);
         auto issue = [&](int k) {
@@ -272,120 +293,82 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
             }
             const int np = static_cast<int>(min(static_cast<long long>(TILE), pe - (pb + static_cast<long long>(k) * TILE)));
 
-            R tx[TT], ty[TT], tz[TT];
-#pragma unroll
-            for (int t = 0; t < TT; ++t) tx[t] = ty[t] = tz[t] = R(0);
-
-            for (int p = 0; p < np; ++p) {
-                const R* v = tile[buf][p].v;
-                const R gam = F32 ? v[kRec32Gamma] : v[kRec64Gamma];
-                if (gam == R(0)) continue;  // uniform across the CTA
-                R ccx, ccy, ccz, ff2, clx = 0, cly = 0, clz = 0;
-                int pw = 0;
-                if constexpr (F32) {
-                    ccx = v[24]; ccy = v[25]; ccz = v[26]; ff2 = v[27];
-                    clx = v[28]; cly = v[29]; clz = v[30];
-                    if (NEGLECT) pw = static_cast<int>(v[41]);
-                } else {
-                    ccx = v[16]; ccy = v[17]; ccz = v[18]; ff2 = v[19];
-                    if (NEGLECT) pw = static_cast<int>(v[26]);
-                }
-                R ex[TT], ey[TT], ez[TT], e2[TT];
-                bool nr[TT], act[TT];
-                bool my_near = false, my_far = false;
-#pragma unroll
-                for (int t = 0; t < TT; ++t) {
-                    ex[t] = (xh[t] - ccx) + (xl[t] - clx);
-                    ey[t] = (yh[t] - ccy) + (yl[t] - cly);
-                    ez[t] = (zh[t] - ccz) + (zl[t] - clz);
-                    e2[t] = ex[t] * ex[t] + ey[t] * ey[t] + ez[t] * ez[t];
-                    nr[t] = e2[t] <= ff2;
-                    act[t] = valid[t] && (!NEGLECT || tw[t] != pw);
-                    my_near |= act[t] && nr[t];
-                    my_far |= act[t] && !nr[t];
-                }
-                const bool any_near = __any_sync(0xffffffffu, my_near);
-                const bool any_far = __any_sync(0xffffffffu, my_far);
-                if (any_far) {
-                    R nx, ny, nz, at;
-                    if constexpr (F32) {
-                        nx = v[32]; ny = v[33]; nz = v[34]; at = v[31] * gam;
-                    } else {
-                        nx = v[20]; ny = v[21]; nz = v[22]; at = v[23] * gam;
+            if constexpr (F32) {
+                float2 TX = bc(0.f), TY = bc(0.f), TZ = bc(0.f);
+                for (int p = 0; p < np; ++p) {
+                    const float* v = reinterpret_cast<const float*>(tile[buf][p].v);
+                    const float gam = v[kRec32Gamma];
+                    if (gam == 0.f) continue;  // uniform across the CTA
+                    const float2 ex = add2(sub2s(X2h, v[40]), sub2s(X2l, v[44]));
+                    const float2 ey = add2(sub2s(Y2h, v[41]), sub2s(Y2l, v[45]));
+                    const float2 ez = add2(sub2s(Z2h, v[42]), sub2s(Z2l, v[46]));
+                    const float2 e2 = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
+                    const float ff2 = v[43];
+                    const bool n0 = e2.x <= ff2, n1 = e2.y <= ff2;
+                    bool a0 = valid[0], a1 = valid[1];
+                    if (NEGLECT) {
+                        const int pw = static_cast<int>(v[53]);
+                        a0 = a0 && tw[0] != pw;
+                        a1 = a1 && tw[1] != pw;
                     }
+                    const bool any_near = __any_sync(0xffffffffu, (a0 && n0) || (a1 && n1));
+                    const bool any_far = __any_sync(0xffffffffu, (a0 && !n0) || (a1 && !n1));
+                    if (any_far) {  // point doublet (panel.rs:82-96)
+                        const float2 e2s = make_float2(n0 ? 1.f : e2.x, n1 ? 1.f : e2.y);
+                        const float2 ir = make_float2(rsqrtf(e2s.x), rsqrtf(e2s.y));
+                        const float2 ir2 = mul2(ir, ir);
+                        const float at = v[47] * gam;
+                        const float2 sm = make_float2((a0 && !n0) ? at : 0.f, (a1 && !n1) ? at : 0.f);
+                        const float2 s = mul2(sm, mul2(mul2(ir2, ir2), ir));
+                        const float nx = v[48], ny = v[49], nz = v[50];
+                        const float2 h3 = mul2(bc(3.f), fma2(ex, bc(nx), fma2(ey, bc(ny), mul2(ez, bc(nz)))));
+                        TX = fma2(s, fma2(h3, ex, mul2(e2s, bc(-nx))), TX);
+                        TY = fma2(s, fma2(h3, ey, mul2(e2s, bc(-ny))), TY);
+                        TZ = fma2(s, fma2(h3, ez, mul2(e2s, bc(-nz))), TZ);
+                    }
+                    if (any_near) {  // vortex ring (panel.rs:99-118)
+                        float2 ax, ay, az;
+                        ring2(v, X2h, Y2h, Z2h, X2l, Y2l, Z2l, ax, ay, az);
+                        const float g4 = gam * static_cast<float>(kFourPiInv);
+                        const float2 gm = make_float2((a0 && n0) ? g4 : 0.f, (a1 && n1) ? g4 : 0.f);
+                        TX = fma2(gm, ax, TX);
+                        TY = fma2(gm, ay, TY);
+                        TZ = fma2(gm, az, TZ);
+                    }
+                }
+                const float txa[2] = {TX.x, TX.y}, tya[2] = {TY.x, TY.y}, tza[2] = {TZ.x, TZ.y};
+#pragma unroll
+                for (int t = 0; t < 2; ++t) {
+                    if (KAHAN) {
+                        two_sum_acc(sx[t], cx[t], static_cast<R>(txa[t]));
+                        two_sum_acc(sy[t], cy[t], static_cast<R>(tya[t]));
+                        two_sum_acc(sz[t], cz[t], static_cast<R>(tza[t]));
+                    } else {
+                        sx[t] += static_cast<R>(txa[t]);
+                        sy[t] += static_cast<R>(tya[t]);
+                        sz[t] += static_cast<R>(tza[t]);
+                    }
+                }
+            } else {
+                R tx[TT], ty[TT], tz[TT];
+#pragma unroll
+                for (int t = 0; t < TT; ++t) tx[t] = ty[t] = tz[t] = R(0);
+                for (int p = 0; p < np; ++p) {
+                    const double* v = reinterpret_cast<const double*>(tile[buf][p].v);
+                    const double gam = v[kRec64Gamma];
+                    if (gam == 0.0) continue;
+                    const int pw = NEGLECT ? static_cast<int>(v[26]) : 0;
 #pragma unroll
                     for (int t = 0; t < TT; ++t) {
-                        if (act[t] && !nr[t]) {
-                            R h = ex[t] * nx + ey[t] * ny + ez[t] * nz;
-                            R h3 = R(3) * h;
-                            R s;
-                            if constexpr (F32) {
-                                float ir = rsqrtf(e2[t]);
-                                float ir2 = ir * ir;
-                                s = at * (ir2 * ir2 * ir);
-                            } else {
-                                s = at / (e2[t] * e2[t] * sqrt(e2[t]));
-                            }
-                            tx[t] += s * (h3 * ex[t] - e2[t] * nx);
-                            ty[t] += s * (h3 * ey[t] - e2[t] * ny);
-                            tz[t] += s * (h3 * ez[t] - e2[t] * nz);
-                        }
+                        if (!valid[t] || (NEGLECT && tw[t] == pw)) continue;
+                        d3 u = panel_unit_f64(v, mk(xh[t], yh[t], zh[t]));
+                        tx[t] += gam * u.x;
+                        ty[t] += gam * u.y;
+                        tz[t] += gam * u.z;
                     }
                 }
-                if (any_near) {
-                    if constexpr (F32) {
-                        float ph[12], pl[12], il[4], dx[4], dy[4], dz[4];
 #pragma unroll
-                        for (int i = 0; i < 12; ++i) {
-                            ph[i] = v[i];
-                            pl[i] = v[12 + i];
-                        }
-#pragma unroll
-                        for (int k2 = 0; k2 < 4; ++k2) {
-                            const int n2 = (k2 + 1) & 3;
-                            il[k2] = v[36 + k2];
-                            dx[k2] = (ph[3 * n2] - ph[3 * k2]) + (pl[3 * n2] - pl[3 * k2]);
-                            dy[k2] = (ph[3 * n2 + 1] - ph[3 * k2 + 1]) + (pl[3 * n2 + 1] - pl[3 * k2 + 1]);
-                            dz[k2] = (ph[3 * n2 + 2] - ph[3 * k2 + 2]) + (pl[3 * n2 + 2] - pl[3 * k2 + 2]);
-                        }
-                        const float rc4 = v[40];
-                        const bool nocore = v[42] != 0.f;
-                        const float g4 = gam * static_cast<float>(kFourPiInv);
-#pragma unroll
-                        for (int t = 0; t < TT; ++t) {
-                            if (act[t] && nr[t]) {
-                                float ax, ay, az;
-                                ring_f32(ph, pl, dx, dy, dz, il, rc4, nocore, xh[t], yh[t], zh[t], xl[t], yl[t], zl[t],
-                                         ax, ay, az);
-                                tx[t] = fmaf(g4, ax, tx[t]);
-                                ty[t] = fmaf(g4, ay, ty[t]);
-                                tz[t] = fmaf(g4, az, tz[t]);
-                            }
-                        }
-                    } else {
-#pragma unroll
-                        for (int t = 0; t < TT; ++t) {
-                            if (act[t] && nr[t]) {
-                                d3 u = mk(0, 0, 0);
-                                d3 pp[4] = {mk(v[0], v[1], v[2]), mk(v[3], v[4], v[5]), mk(v[6], v[7], v[8]),
-                                            mk(v[9], v[10], v[11])};
-                                d3 X = mk(xh[t], yh[t], zh[t]);
-                                for (int i = 0; i < 4; ++i) u = u + line_unit_f64(pp[i], pp[(i + 1) & 3], X, v[25]);
-                                tx[t] += gam * u.x;
-                                ty[t] += gam * u.y;
-                                tz[t] += gam * u.z;
-                            }
-                        }
-                    }
-                }
-            }
-#pragma unroll
-            for (int t = 0; t < TT; ++t) {
-                if (KAHAN) {
-                    two_sum_acc(sx[t], cx[t], tx[t]);
-                    two_sum_acc(sy[t], cy[t], ty[t]);
-                    two_sum_acc(sz[t], cz[t], tz[t]);
-                } else {
+                for (int t = 0; t < TT; ++t) {
                     sx[t] += tx[t];
                     sy[t] += ty[t];
                     sz[t] += tz[t];

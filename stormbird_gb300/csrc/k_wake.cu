@@ -189,64 +189,54 @@ cudaError_t launch_wake_advect(const DevModel& m, const WakeBuffers& w, double d
 // Panel records from the new points (panel.rs:26-50, geometry_functions.rs:11-30,
 // dynamic_wake/mod.rs:82-103) and the strength shift (update_data.rs:319-328).
 // ---------------------------------------------------------------------------------------
-__global__ void k_wake_panels(DevModel m, WakeBuffers w, int shift) {
-    long long id = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
-    if (id >= m.P_pan) return;
-    const int N = m.N;
-    const long long Np = m.Np;
-    const int s = static_cast<int>(id / N), j = static_cast<int>(id % N);
-    const int wg = m.wing_of_line[j];
-    const d3* P = w.pts_new;
-    d3 p0 = P[s * Np + j + wg], p1 = P[s * Np + j + 1 + wg];
-    d3 p2 = P[(s + 1) * Np + j + 1 + wg], p3 = P[(s + 1) * Np + j + wg];
-    d3 c = 0.25 * (((p0 + p1) + p2) + p3);
-    double la = len(p1 - p0), lb = len(p2 - p1), lc = len(p3 - p2), ld = len(p0 - p3);
-    double sp = (la + lb + lc + ld) * 0.5;
-    double area = sqrt((sp - la) * (sp - lb) * (sp - lc) * (sp - ld));
-    d3 n = normalize(cross(p2 - p0, p3 - p1));
-    double rep = fmax(la, lb);
-    double t = rep * m.far_field_ratio;
-    double ff2 = t * t;
-    double rc = m.panel_core[id];
-    double g;
-    if (shift) g = (s == 0) ? w.str_old[j] : w.str_old[id - N];
-    else g = w.str_old[id];
-    w.str_new[id] = g;
+// Panel::new (panel.rs:26-50, geometry_functions.rs:11-30) for corners p[0..3], written as
+// the FP32 sweep record (float-float positions) and, when r64 is not null, the FP64 record.
+__device__ void write_panel_records(const d3 (&pp)[4], double rc, double g, double far_field_ratio, int wing,
+                                    PanelRec<float>* r32, PanelRec<double>* r64) {
+    const d3 c = 0.25 * (((pp[0] + pp[1]) + pp[2]) + pp[3]);
+    const double la = len(pp[1] - pp[0]), lb = len(pp[2] - pp[1]), lc = len(pp[3] - pp[2]), ld = len(pp[0] - pp[3]);
+    const double sp = (la + lb + lc + ld) * 0.5;
+    const double area = sqrt((sp - la) * (sp - lb) * (sp - lc) * (sp - ld));
+    const d3 n = normalize(cross(pp[2] - pp[0], pp[3] - pp[1]));
+    const double t = fmax(la, lb) * far_field_ratio;
+    const double ff2 = t * t;
 
-    // FP32 record with float-float positions (layout in sb_device.cuh)
     PanelRec<float> r;
     auto split = [](double x, float* hi, float* lo) {
         float h = static_cast<float>(x);
         *hi = h;
         *lo = static_cast<float>(x - static_cast<double>(h));
     };
-    const d3 pp[4] = {p0, p1, p2, p3};
     for (int k = 0; k < 4; ++k) {
         split(pp[k].x, &r.v[3 * k], &r.v[12 + 3 * k]);
         split(pp[k].y, &r.v[3 * k + 1], &r.v[12 + 3 * k + 1]);
         split(pp[k].z, &r.v[3 * k + 2], &r.v[12 + 3 * k + 2]);
-        double l2 = len2(pp[(k + 1) & 3] - pp[k]);
+        const d3 dk = pp[(k + 1) & 3] - pp[k];
+        r.v[24 + 3 * k] = static_cast<float>(dk.x);
+        r.v[24 + 3 * k + 1] = static_cast<float>(dk.y);
+        r.v[24 + 3 * k + 2] = static_cast<float>(dk.z);
+        const double l2 = len2(dk);
         r.v[36 + k] = l2 > 0.0 ? static_cast<float>(1.0 / l2) : 0.f;
     }
-    split(c.x, &r.v[24], &r.v[28]);
-    split(c.y, &r.v[25], &r.v[29]);
-    split(c.z, &r.v[26], &r.v[30]);
-    r.v[27] = static_cast<float>(ff2);
-    r.v[31] = static_cast<float>(area * kFourPiInv);
-    r.v[32] = static_cast<float>(n.x);
-    r.v[33] = static_cast<float>(n.y);
-    r.v[34] = static_cast<float>(n.z);
+    split(c.x, &r.v[40], &r.v[44]);
+    split(c.y, &r.v[41], &r.v[45]);
+    split(c.z, &r.v[42], &r.v[46]);
+    r.v[43] = static_cast<float>(ff2);
+    r.v[47] = static_cast<float>(area * kFourPiInv);
+    r.v[48] = static_cast<float>(n.x);
+    r.v[49] = static_cast<float>(n.y);
+    r.v[50] = static_cast<float>(n.z);
     r.v[kRec32Gamma] = static_cast<float>(g);
-    double rc2 = rc * rc;
-    r.v[40] = static_cast<float>(rc2 * rc2);
-    r.v[41] = static_cast<float>(wg);
-    r.v[42] = rc == 0.0 ? 1.f : 0.f;
-    for (int k = 43; k < 48; ++k) r.v[k] = 0.f;
-    w.rec32[id] = r;
-
-    if (s == 0 || w.rec64) {
+    // core length^4; a zero core (reference: factor 1) only occurs in the horseshoe path, which
+    // runs in FP64, so the FP32 sweep always evaluates d^2 / sqrt(d^4 + rc^4)
+    const double rc2 = rc * rc;
+    r.v[52] = static_cast<float>(rc2 * rc2);
+    r.v[53] = static_cast<float>(wing);
+    r.v[54] = 0.f;
+    r.v[55] = 0.f;
+    *r32 = r;
+    if (r64) {
         PanelRec<double> q;
-        d3 pp[4] = {p0, p1, p2, p3};
         for (int k = 0; k < 4; ++k) {
             q.v[3 * k] = pp[k].x;
             q.v[3 * k + 1] = pp[k].y;
@@ -261,13 +251,52 @@ __global__ void k_wake_panels(DevModel m, WakeBuffers w, int shift) {
         q.v[21] = n.y;
         q.v[22] = n.z;
         q.v[23] = area * kFourPiInv;
-        q.v[24] = g;
+        q.v[kRec64Gamma] = g;
         q.v[25] = rc;
-        q.v[26] = static_cast<double>(wg);
+        q.v[26] = static_cast<double>(wing);
         q.v[27] = 0.0;
-        if (s == 0) w.row0_64[j] = q;
-        if (w.rec64) w.rec64[id] = q;
+        *r64 = q;
     }
+}
+
+__global__ void k_wake_panels(DevModel m, WakeBuffers w, int shift) {
+    long long id = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+    if (id >= m.P_pan) return;
+    const int N = m.N;
+    const long long Np = m.Np;
+    const int s = static_cast<int>(id / N), j = static_cast<int>(id % N);
+    const int wg = m.wing_of_line[j];
+    const d3* P = w.pts_new;
+    const d3 pp[4] = {P[s * Np + j + wg], P[s * Np + j + 1 + wg], P[(s + 1) * Np + j + 1 + wg], P[(s + 1) * Np + j + wg]};
+    double g;
+    if (shift) g = (s == 0) ? w.str_old[j] : w.str_old[id - N];
+    else g = w.str_old[id];
+    w.str_new[id] = g;
+    PanelRec<double> q;
+    const bool need64 = (s == 0) || w.rec64;
+    write_panel_records(pp, m.panel_core[id], g, m.far_field_ratio, wg, &w.rec32[id], need64 ? &q : nullptr);
+    if (s == 0) w.row0_64[j] = q;
+    if (w.rec64) w.rec64[id] = q;
+}
+
+// Records of caller-given panels (corners [P][4][3], strengths, core lengths) for the
+// standalone sweep sb_panel_sweep.
+__global__ void k_panels_from_corners(const double* corners, const double* strengths, const double* cores, long long P,
+                                      double far_field_ratio, PanelRec<float>* r32, PanelRec<double>* r64) {
+    long long id = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+    if (id >= P) return;
+    const double* c = corners + id * 12;
+    const d3 pp[4] = {mk(c[0], c[1], c[2]), mk(c[3], c[4], c[5]), mk(c[6], c[7], c[8]), mk(c[9], c[10], c[11])};
+    write_panel_records(pp, cores[id], strengths[id], far_field_ratio, 0, &r32[id], r64 ? &r64[id] : nullptr);
+}
+
+cudaError_t launch_panels_from_corners(const double* corners, const double* strengths, const double* cores, long long P,
+                                       double far_field_ratio, PanelRec<float>* r32, PanelRec<double>* r64,
+                                       cudaStream_t s) {
+    if (P <= 0) return cudaSuccess;
+    k_panels_from_corners<<<static_cast<unsigned>((P + 127) / 128), 128, 0, s>>>(corners, strengths, cores, P,
+                                                                                 far_field_ratio, r32, r64);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_wake_panels(const DevModel& m, const WakeBuffers& w, int shift, cudaStream_t s) {

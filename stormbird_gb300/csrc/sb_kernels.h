@@ -70,6 +70,11 @@ cudaError_t launch_wake_advect(const DevModel& m, const WakeBuffers& w, double d
 // `shift_strengths` = 0 rebuilds the panels without moving strengths (initialisation).
 cudaError_t launch_wake_panels(const DevModel& m, const WakeBuffers& w, int shift_strengths, cudaStream_t s);
 
+// Records of caller-given panels for the standalone sweep (corners [P][4][3] in ring order).
+cudaError_t launch_panels_from_corners(const double* corners, const double* strengths, const double* cores, long long P,
+                                       double far_field_ratio, PanelRec<float>* r32, PanelRec<double>* r64,
+                                       cudaStream_t s);
+
 // ---- solver and forces (k_solve.cu) ----------------------------------------------------
 struct SolveSettings {
     int max_iterations = 40;

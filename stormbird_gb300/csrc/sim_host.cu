@@ -6,6 +6,7 @@
 // and every per-step computation runs as CUDA kernels on the handle's stream. The host
 // only enqueues work, copies the freestream in and the output block out (one copy each
 // way per step), and keeps the step counters that select which kernels run.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -113,6 +114,108 @@ int num_sms(int device) {
     int v = 0;
     cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device);
     return v > 0 ? v : 1;
+}
+
+
+// Work decomposition of one sweep: target tiles x source chunks, with enough work items
+// for ~4 waves of the persistent grid (sweep kernels in k_biot_savart.cu).
+struct SweepPlan {
+    int grid = 1, n_chunks = 1, chunk = 0;
+    long long n_ttiles = 0;
+};
+
+SweepPlan make_sweep_plan(long long M, long long P, int precision, int sym, int neglect, int sms) {
+    SweepPlan sp;
+    int T = bs_targets_per_thread(sym);
+    long long TM = static_cast<long long>(kBsThreads) * T;
+    sp.n_ttiles = (M + TM - 1) / TM;
+    int tile = bs_tile_panels(precision);
+    int occ = bs_occupancy_blocks_per_sm(precision, sym, neglect);
+    long long slots = static_cast<long long>(sms) * occ;
+    long long want = 4 * slots;
+    long long max_chunks = std::max<long long>(1, (P + tile - 1) / tile);
+    long long nc = (want + sp.n_ttiles - 1) / std::max<long long>(1, sp.n_ttiles);
+    nc = std::min(std::max<long long>(nc, 1), max_chunks);
+    long long chunk = (P + nc - 1) / nc;
+    chunk = ((chunk + tile - 1) / tile) * tile;
+    sp.chunk = static_cast<int>(std::max<long long>(chunk, tile));
+    sp.n_chunks = static_cast<int>((P + sp.chunk - 1) / sp.chunk);
+    if (sp.n_chunks < 1) sp.n_chunks = 1;
+    sp.grid = static_cast<int>(std::min<long long>(slots, sp.n_ttiles * sp.n_chunks));
+    if (sp.grid < 1) sp.grid = 1;
+    return sp;
+}
+
+// Device work space of one standalone call: stream-ordered allocations freed on exit.
+struct StreamBufs {
+    cudaStream_t s = nullptr;
+    std::vector<void*> ptrs;
+    explicit StreamBufs(cudaStream_t st) : s(st) {}
+    ~StreamBufs() {
+        for (void* p : ptrs) cudaFreeAsync(p, s);
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+    }
+    template <class T>
+    T* get(size_t count) {
+        void* p = nullptr;
+        ck(cudaMallocAsync(&p, std::max<size_t>(count, 1) * sizeof(T), s), "cudaMallocAsync");
+        ptrs.push_back(p);
+        return static_cast<T*>(p);
+    }
+};
+
+void panel_sweep_impl(int device, const double* corners, const double* strengths, const double* core_lengths,
+                      long long P, double far_field_ratio, int symmetry, const double* targets, long long M,
+                      int precision, double* velocities) {
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    cudaStream_t st;
+    ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+    StreamBufs B(st);
+    double* dc = B.get<double>(static_cast<size_t>(P) * 12);
+    double* ds = B.get<double>(static_cast<size_t>(P));
+    double* dr = B.get<double>(static_cast<size_t>(P));
+    PanelRec<float>* r32 = B.get<PanelRec<float>>(static_cast<size_t>(P));
+    PanelRec<double>* r64 = precision == 2 ? B.get<PanelRec<double>>(static_cast<size_t>(P)) : nullptr;
+    d3* dt = B.get<d3>(static_cast<size_t>(M));
+    d3* dout = B.get<d3>(static_cast<size_t>(M));
+    unsigned long long* ctr = B.get<unsigned long long>(1);
+    int* derr = B.get<int>(1);
+    ck(cudaMemsetAsync(derr, 0, sizeof(int), st), "memset");
+    if (P > 0) {
+        ck(cudaMemcpyAsync(dc, corners, P * 12 * sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
+        ck(cudaMemcpyAsync(ds, strengths, P * sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
+        ck(cudaMemcpyAsync(dr, core_lengths, P * sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
+    }
+    ck(cudaMemcpyAsync(dt, targets, M * sizeof(d3), cudaMemcpyHostToDevice, st), "H2D");
+    ck(launch_panels_from_corners(dc, ds, dr, P, far_field_ratio, r32, r64, st), "panel records");
+    if (P > 0) {
+        SweepPlan sp = make_sweep_plan(M, P, precision, symmetry, 0, num_sms(device));
+        double* partial = B.get<double>(static_cast<size_t>(sp.n_chunks) * static_cast<size_t>(M) * 3);
+        BsArgs a;
+        a.panels = precision == 2 ? static_cast<const void*>(r64) : static_cast<const void*>(r32);
+        a.p_begin = 0;
+        a.p_end = P;
+        a.targets = dt;
+        a.M = M;
+        a.chunk_panels = sp.chunk;
+        a.n_chunks = sp.n_chunks;
+        a.n_ttiles = sp.n_ttiles;
+        a.partial = partial;
+        a.work_counter = ctr;
+        a.err = derr;
+        a.symmetry = symmetry;
+        ck(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st), "memset");
+        ck(launch_bs_sweep(a, precision, sp.grid, st), "Biot-Savart sweep");
+        ck(launch_bs_reduce(partial, sp.n_chunks, M, M, nullptr, dout, st), "sweep reduce");
+    } else {
+        ck(launch_bs_reduce(nullptr, 0, 0, M, nullptr, dout, st), "sweep reduce");
+    }
+    int herr = 0;
+    ck(cudaMemcpyAsync(velocities, dout, M * sizeof(d3), cudaMemcpyDeviceToHost, st), "D2H");
+    ck(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H");
+    ck(cudaStreamSynchronize(st), "panel sweep");
+    if (herr == kDevTimeout) raise(SB_ERR_TIMEOUT, "a bounded device-side wait ran out");
 }
 
 }  // namespace
@@ -413,31 +516,8 @@ struct sb_sim {
         }
     }
 
-    struct SweepPlan {
-        int grid = 1, n_chunks = 1, chunk = 0;
-        long long n_ttiles = 0;
-    };
-
     SweepPlan plan_sweep(long long M, long long P, int sym, int neglect) {
-        SweepPlan sp;
-        int T = bs_targets_per_thread(sym);
-        long long TM = static_cast<long long>(kBsThreads) * T;
-        sp.n_ttiles = (M + TM - 1) / TM;
-        int tile = bs_tile_panels(precision);
-        int occ = bs_occupancy_blocks_per_sm(precision, sym, neglect);
-        long long slots = static_cast<long long>(sms) * occ;
-        long long want = 4 * slots;
-        long long max_chunks = std::max<long long>(1, (P + tile - 1) / tile);
-        long long nc = (want + sp.n_ttiles - 1) / std::max<long long>(1, sp.n_ttiles);
-        nc = std::min(std::max<long long>(nc, 1), max_chunks);
-        long long chunk = (P + nc - 1) / nc;
-        chunk = ((chunk + tile - 1) / tile) * tile;
-        sp.chunk = static_cast<int>(std::max<long long>(chunk, tile));
-        sp.n_chunks = static_cast<int>((P + sp.chunk - 1) / sp.chunk);
-        if (sp.n_chunks < 1) sp.n_chunks = 1;
-        sp.grid = static_cast<int>(std::min<long long>(slots, sp.n_ttiles * sp.n_chunks));
-        if (sp.grid < 1) sp.grid = 1;
-        return sp;
+        return make_sweep_plan(M, P, precision, sym, neglect, sms);
     }
 
     // Biot-Savart sweep into out[0..M) (+ base), base only for [M, M_total).
@@ -902,6 +982,27 @@ int sb_sim_last_step_counters(const sb_sim* sim, double* c, size_t n) {
     if (!sim || !c) { g_last_error = "null argument"; return SB_ERR_NULL_ARG; }
     for (size_t i = 0; i < n && i < 6; ++i) c[i] = sim->last_counters[i];
     return SB_OK;
+}
+
+// Standalone sweep over caller-given panels (see include/stormbird_gb300.h).
+int sb_panel_sweep(int device, const double* corners, const double* strengths, const double* core_lengths,
+                   size_t n_panels, double far_field_ratio, int symmetry, const double* targets, size_t n_targets,
+                   int precision, double* velocities) {
+    if ((n_panels && (!corners || !strengths || !core_lengths)) || (n_targets && (!targets || !velocities))) {
+        g_last_error = "null argument";
+        g_last_status = SB_ERR_NULL_ARG;
+        return SB_ERR_NULL_ARG;
+    }
+    if (symmetry < 0 || symmetry > 3 || precision < 0 || precision > 2) {
+        g_last_error = "symmetry must be 0..3 and precision 0..2";
+        g_last_status = SB_ERR_SIZE;
+        return SB_ERR_SIZE;
+    }
+    if (n_targets == 0) return SB_OK;
+    return guard([&] {
+        panel_sweep_impl(device, corners, strengths, core_lengths, static_cast<long long>(n_panels), far_field_ratio,
+                         symmetry, targets, static_cast<long long>(n_targets), precision, velocities);
+    });
 }
 
 int sb_measure_fp32_peak(int device, int reps, double* tflops) {

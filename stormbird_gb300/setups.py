@@ -182,3 +182,47 @@ class GustyWind:
 
     def freestream(self, t: float, nr_points: int) -> np.ndarray:
         return np.tile(self.velocity(t), (nr_points, 1))
+
+
+def synthetic_sail_row_wake(nr_sails=4, panels_per_sail=64, wake_rows=300, time_step=0.05, wind_speed=12.0,
+                            apparent_wind_angle_deg=45.0, angle_of_attack_deg=8.0, spacing=40.0, seed=0):
+    """A shed-wake-shaped panel set without running the solver: for sail row geometry of
+    `wing_sail_row`, rows of wake points leave the trailing edge along the wind with a
+    growing sinusoidal roll-up displacement, and every panel carries an elliptic-like
+    circulation with seeded +-10 % variation. Returns (corners [P, 4, 3], strengths [P],
+    core lengths [P], wake points [(W+1) * Np, 3]) in the reference's panel indexing
+    (stormbird/src/lifting_line/wake/dynamic_wake/mod.rs:82-103)."""
+    rng = np.random.default_rng(seed)
+    npts = panels_per_sail + 1
+    th = math.radians(apparent_wind_angle_deg)
+    wind = np.array([math.cos(th), math.sin(th), 0.0])
+    ch = math.radians(apparent_wind_angle_deg - angle_of_attack_deg)
+    chord_dir = np.array([math.cos(ch), math.sin(ch), 0.0])
+    z = np.linspace(0.0, SPAN, npts)
+    rows = []
+    for s in range(wake_rows + 1):
+        row = []
+        for i in range(nr_sails):
+            base = np.stack([np.full(npts, spacing * i), np.zeros(npts), z], axis=1)
+            if s == 0:
+                p = base
+            else:
+                p = base + chord_dir * (time_step * wind_speed) + wind * (time_step * wind_speed * (s - 1))
+                roll = 0.02 * s * np.sin(np.pi * z / SPAN + 0.1 * s)
+                p = p + np.outer(roll, [0.0, 0.0, 1.0]) + np.outer(0.01 * s * np.cos(np.pi * z / SPAN), [-wind[1], wind[0], 0])
+            row.append(p)
+        rows.append(np.concatenate(row))
+    pts = np.stack(rows)  # [W+1, Np, 3]
+    corners, gam = [], []
+    zc = 0.5 * (z[:-1] + z[1:])
+    g_span = -30.0 * np.sqrt(np.clip(1.0 - (2 * zc / SPAN - 1.0) ** 2, 0.0, 1.0)) - 1.0
+    for s in range(wake_rows):
+        for i in range(nr_sails):
+            for j in range(panels_per_sail):
+                a = i * npts + j
+                corners.append([pts[s, a], pts[s, a + 1], pts[s + 1, a + 1], pts[s + 1, a]])
+                gam.append(g_span[j] * rng.uniform(0.9, 1.1))
+    corners = np.array(corners)
+    strengths = np.array(gam)
+    cores = np.full(len(strengths), 0.1 * CHORD)
+    return corners, strengths, cores, pts.reshape(-1, 3)

@@ -159,3 +159,17 @@ def measure_fp32_peak(device: int = 0, reps: int = 5) -> float:
     v = ctypes.c_double()
     _check(lib().sb_measure_fp32_peak(int(device), int(reps), ctypes.byref(v)))
     return v.value
+
+
+def panel_sweep(corners, strengths, core_lengths, targets, far_field_ratio: float = 5.0, symmetry: int = 0,
+                precision: str | int = "kahan", device: int = 0) -> np.ndarray:
+    """Standalone Biot-Savart sweep over caller-given vortex-ring panels (sb_panel_sweep)."""
+    c = _d(corners).reshape(-1, 12)
+    s = _d(strengths).reshape(-1)
+    r = _d(core_lengths).reshape(-1)
+    t = vec3_array(targets)
+    out = np.zeros_like(t)
+    m = {"kahan": 0, "fp32": 1, "fp64": 2}.get(precision, precision)
+    _check(lib().sb_panel_sweep(int(device), as_ptr(c), as_ptr(s), as_ptr(r), c.shape[0], float(far_field_ratio),
+                                int(symmetry), as_ptr(t), t.shape[0], int(m), as_ptr(out)))
+    return out

@@ -245,3 +245,22 @@ def test_error_codes(gpu_lib):
     with pytest.raises(SbError) as e:
         q.induced_velocities([[0.0, 0.0, 0.0]])
     assert e.value.code == -8
+
+
+@pytest.mark.parametrize("symmetry", [0, 2])
+@pytest.mark.parametrize("ffr", [5.0, 1e30])
+def test_standalone_panel_sweep_matches_oracle(gpu_lib, oracle_mod, symmetry, ffr):
+    """sb_panel_sweep against the oracle's sweep over the same caller-given panels."""
+    from stormbird_gb300.simulation import panel_sweep
+
+    corners, strengths, cores, pts = S.synthetic_sail_row_wake(2, 12, 20, seed=3)
+    rng = np.random.default_rng(2)
+    targets = np.concatenate([pts[::5], rng.uniform([-10, -10, 1], [80, 60, 29], (100, 3))])
+    if symmetry:
+        targets[:, 1] += 5.0
+    uo = oracle_mod.bs_sweep(corners, cores, strengths, ffr, targets, nthreads=4) if symmetry == 0 else None
+    ug = panel_sweep(corners, strengths, cores, targets, far_field_ratio=ffr, symmetry=symmetry)
+    u64 = panel_sweep(corners, strengths, cores, targets, far_field_ratio=ffr, symmetry=symmetry, precision="fp64")
+    if uo is not None:
+        assert rel_inf(u64, uo) < 1e-12
+    assert rel_inf(ug, u64) < 1e-6
