@@ -20,6 +20,7 @@
 // points (frozen_wake.rs:198-249), in FP64: the control point lies on its own bound
 // vortex, where the reference's 1e-10 closeness cut-off must fire exactly as in f64.
 #include <cstdio>
+#include <math_constants.h>
 
 #include "sb_device.cuh"
 #include "sb_kernels.h"
@@ -165,8 +166,8 @@ __device__ __forceinline__ void ring2(const float* v, float2 xh, float2 yh, floa
         ry[k] = add2(sub2s(yh, v[3 * k + 1]), sub2s(yl, v[12 + 3 * k + 1]));
         rz[k] = add2(sub2s(zh, v[3 * k + 2]), sub2s(zl, v[12 + 3 * k + 2]));
         rs[k] = fma2(rx[k], rx[k], fma2(ry[k], ry[k], mul2(rz[k], rz[k])));
-        float2 t = add2(rs[k], bc(1e-30f));  // r = 0 (target on a corner) gives l = 0
-        rl[k] = mul2(rs[k], make_float2(rsqrtf(t.x), rsqrtf(t.y)));
+        // r = 0 (target on a corner) gives l = 0; the clamp runs on the ALU pipe
+        rl[k] = mul2(rs[k], make_float2(rsqrtf(fmaxf(rs[k].x, 1e-30f)), rsqrtf(fmaxf(rs[k].y, 1e-30f))));
     }
     const float rc4 = v[52];
     ax = ay = az = bc(0.f);
@@ -175,7 +176,9 @@ __device__ __forceinline__ void ring2(const float* v, float2 xh, float2 yh, floa
         const int k1 = (k + 1) & 3;
         const float dx = v[24 + 3 * k], dy = v[24 + 3 * k + 1], dz = v[24 + 3 * k + 2], il = v[36 + k];
         const float2 p = mul2(rl[k], rl[k1]);
-        const float2 q = fma2(rx[k], rx[k1], fma2(ry[k], ry[k1], mul2(rz[k], rz[k1])));
+        // projection on the segment, and r1.r2 = |r1|^2 - r1.d (r2 = r1 - d)
+        const float2 tp = fma2(rx[k], bc(dx), fma2(ry[k], bc(dy), mul2(rz[k], bc(dz))));
+        const float2 q = add2(rs[k], make_float2(-tp.x, -tp.y));
         const float2 cx = fma2(bc(dy), rz[k], mul2(bc(-dz), ry[k]));
         const float2 cy = fma2(bc(dz), rx[k], mul2(bc(-dx), rz[k]));
         const float2 cz = fma2(bc(dx), ry[k], mul2(bc(-dy), rx[k]));
@@ -185,15 +188,17 @@ __device__ __forceinline__ void ring2(const float* v, float2 xh, float2 yh, floa
         const float2 ppq = add2(p, q);
         const float2 Ax = make_float2(n0 ? pmq.x : 1.f, n1 ? pmq.y : 1.f);
         const float2 Bx = mul2(p, make_float2(n0 ? c2.x : ppq.x, n1 ? c2.y : ppq.y));
-        const float2 tp = fma2(rx[k], bc(dx), fma2(ry[k], bc(dy), mul2(rz[k], bc(dz))));
         const float2 tpl = mul2(tp, bc(il));
         float2 d2 = mul2(c2, bc(il));
         d2.x = tpl.x > 1.f ? rs[k1].x : d2.x;
         d2.y = tpl.y > 1.f ? rs[k1].y : d2.y;
         d2.x = tp.x < 0.f ? rs[k].x : d2.x;
         d2.y = tp.y < 0.f ? rs[k].y : d2.y;
-        const float2 X = add2(mul2(mul2(Bx, Bx), fma2(d2, d2, bc(rc4))), bc(1e-37f));
-        const float2 s0 = mul2(mul2(mul2(d2, add2(rl[k], rl[k1])), Ax), make_float2(rsqrtf(X.x), rsqrtf(X.y)));
+        // X = 0 only where B = 0 too (target on the segment or a corner); the select below
+        // then discards the lane, so the clamp only keeps rsqrt finite
+        const float2 X = mul2(mul2(Bx, Bx), fma2(d2, d2, bc(rc4)));
+        const float2 s0 = mul2(mul2(mul2(d2, add2(rl[k], rl[k1])), Ax),
+                               make_float2(rsqrtf(fmaxf(X.x, 1e-37f)), rsqrtf(fmaxf(X.y, 1e-37f))));
         const float2 lim = mul2(Ax, bc(1.0e-10f));
         const float2 s = make_float2(Bx.x > lim.x ? s0.x : 0.f, Bx.y > lim.y ? s0.y : 0.f);
         ax = fma2(s, cx, ax);
@@ -299,12 +304,17 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
                     const float* v = reinterpret_cast<const float*>(tile[buf][p].v);
                     const float gam = v[kRec32Gamma];
                     if (gam == 0.f) continue;  // uniform across the CTA
-                    const float2 ex = add2(sub2s(X2h, v[40]), sub2s(X2l, v[44]));
-                    const float2 ey = add2(sub2s(Y2h, v[41]), sub2s(Y2l, v[45]));
-                    const float2 ez = add2(sub2s(Z2h, v[42]), sub2s(Z2l, v[46]));
-                    const float2 e2 = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
                     const float ff2 = v[43];
-                    const bool n0 = e2.x <= ff2, n1 = e2.y <= ff2;
+                    float2 ex = bc(0.f), ey = bc(0.f), ez = bc(0.f), e2 = bc(0.f);
+                    bool n0 = true, n1 = true;
+                    if (ff2 != CUDART_INF_F) {  // panel.rs:53-57; uniform per panel
+                        ex = add2(sub2s(X2h, v[40]), sub2s(X2l, v[44]));
+                        ey = add2(sub2s(Y2h, v[41]), sub2s(Y2l, v[45]));
+                        ez = add2(sub2s(Z2h, v[42]), sub2s(Z2l, v[46]));
+                        e2 = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
+                        n0 = e2.x <= ff2;
+                        n1 = e2.y <= ff2;
+                    }
                     bool a0 = valid[0], a1 = valid[1];
                     if (NEGLECT) {
                         const int pw = static_cast<int>(v[53]);

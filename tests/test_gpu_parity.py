@@ -263,4 +263,4 @@ def test_standalone_panel_sweep_matches_oracle(gpu_lib, oracle_mod, symmetry, ff
     u64 = panel_sweep(corners, strengths, cores, targets, far_field_ratio=ffr, symmetry=symmetry, precision="fp64")
     if uo is not None:
         assert rel_inf(u64, uo) < 1e-12
-    assert rel_inf(ug, u64) < 1e-6
+    assert rel_inf(ug, u64) < 2e-6
