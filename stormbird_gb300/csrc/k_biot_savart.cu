@@ -149,32 +149,33 @@ __device__ __forceinline__ float2 sel2(bool cx, float2 a, bool cy, float2 b) {
     return make_float2(cx ? a.x : b.x, cy ? a.y : b.y);
 }
 
-// Vortex ring of one FP32 panel record at two targets (the two lanes of the float2s).
-// r_k = (x_hi - p_hi_k) + (x_lo - p_lo_k). Per segment, with c = d x r1 = r1 x r2:
+// Vortex ring of one FP32 panel record at two targets (the two lanes of the float2s), given
+// e = x - centre (float-float difference). r_k = e - o_k. Per segment, with c = d x r1 = r1 x r2:
+//   r1.r2 = |r1|^2 - r1.d,
 //   den = l1 l2 (l1 l2 + r1.r2) = B / A without cancellation
 //        (A, B) = (l1 l2 - r1.r2, l1 l2 |c|^2) if r1.r2 < 0, else (1, l1 l2 (l1 l2 + r1.r2)),
 //   distance^2 to the segment = |c|^2 / |d|^2 inside it, the end-point distance outside,
 //   core * k = d2 (l1 + l2) A / (B sqrt(d2^2 + rc^4)) with a single rsqrt,
 // which is the reference's (vortex_line.rs:18-106) value, evaluated without the FP32
 // cancellations of its literal form. Returns sum_k core_k k_k c_k (times Gamma/4pi = velocity).
-__device__ __forceinline__ void ring2(const float* v, float2 xh, float2 yh, float2 zh, float2 xl, float2 yl, float2 zl,
-                                      float2& ax, float2& ay, float2& az) {
+__device__ __forceinline__ void ring2(const float* v, float2 ex, float2 ey, float2 ez, float2& ax, float2& ay,
+                                      float2& az) {
     float2 rx[4], ry[4], rz[4], rs[4], rl[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        rx[k] = add2(sub2s(xh, v[3 * k]), sub2s(xl, v[12 + 3 * k]));
-        ry[k] = add2(sub2s(yh, v[3 * k + 1]), sub2s(yl, v[12 + 3 * k + 1]));
-        rz[k] = add2(sub2s(zh, v[3 * k + 2]), sub2s(zl, v[12 + 3 * k + 2]));
+        rx[k] = sub2s(ex, v[3 * k]);
+        ry[k] = sub2s(ey, v[3 * k + 1]);
+        rz[k] = sub2s(ez, v[3 * k + 2]);
         rs[k] = fma2(rx[k], rx[k], fma2(ry[k], ry[k], mul2(rz[k], rz[k])));
         // r = 0 (target on a corner) gives l = 0; the clamp runs on the ALU pipe
         rl[k] = mul2(rs[k], make_float2(rsqrtf(fmaxf(rs[k].x, 1e-30f)), rsqrtf(fmaxf(rs[k].y, 1e-30f))));
     }
-    const float rc4 = v[52];
+    const float rc4 = v[40];
     ax = ay = az = bc(0.f);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const int k1 = (k + 1) & 3;
-        const float dx = v[24 + 3 * k], dy = v[24 + 3 * k + 1], dz = v[24 + 3 * k + 2], il = v[36 + k];
+        const float dx = v[12 + 3 * k], dy = v[12 + 3 * k + 1], dz = v[12 + 3 * k + 2], il = v[24 + k];
         const float2 p = mul2(rl[k], rl[k1]);
         // projection on the segment, and r1.r2 = |r1|^2 - r1.d (r2 = r1 - d)
         const float2 tp = fma2(rx[k], bc(dx), fma2(ry[k], bc(dy), mul2(rz[k], bc(dz))));
@@ -304,20 +305,20 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
                     const float* v = reinterpret_cast<const float*>(tile[buf][p].v);
                     const float gam = v[kRec32Gamma];
                     if (gam == 0.f) continue;  // uniform across the CTA
-                    const float ff2 = v[43];
-                    float2 ex = bc(0.f), ey = bc(0.f), ez = bc(0.f), e2 = bc(0.f);
+                    const float ff2 = v[31];
+                    const float2 ex = add2(sub2s(X2h, v[28]), sub2s(X2l, v[32]));
+                    const float2 ey = add2(sub2s(Y2h, v[29]), sub2s(Y2l, v[33]));
+                    const float2 ez = add2(sub2s(Z2h, v[30]), sub2s(Z2l, v[34]));
+                    float2 e2 = bc(0.f);
                     bool n0 = true, n1 = true;
                     if (ff2 != CUDART_INF_F) {  // panel.rs:53-57; uniform per panel
-                        ex = add2(sub2s(X2h, v[40]), sub2s(X2l, v[44]));
-                        ey = add2(sub2s(Y2h, v[41]), sub2s(Y2l, v[45]));
-                        ez = add2(sub2s(Z2h, v[42]), sub2s(Z2l, v[46]));
                         e2 = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
                         n0 = e2.x <= ff2;
                         n1 = e2.y <= ff2;
                     }
                     bool a0 = valid[0], a1 = valid[1];
                     if (NEGLECT) {
-                        const int pw = static_cast<int>(v[53]);
+                        const int pw = static_cast<int>(v[41]);
                         a0 = a0 && tw[0] != pw;
                         a1 = a1 && tw[1] != pw;
                     }
@@ -327,10 +328,10 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
                         const float2 e2s = make_float2(n0 ? 1.f : e2.x, n1 ? 1.f : e2.y);
                         const float2 ir = make_float2(rsqrtf(e2s.x), rsqrtf(e2s.y));
                         const float2 ir2 = mul2(ir, ir);
-                        const float at = v[47] * gam;
+                        const float at = v[35] * gam;
                         const float2 sm = make_float2((a0 && !n0) ? at : 0.f, (a1 && !n1) ? at : 0.f);
                         const float2 s = mul2(sm, mul2(mul2(ir2, ir2), ir));
-                        const float nx = v[48], ny = v[49], nz = v[50];
+                        const float nx = v[36], ny = v[37], nz = v[38];
                         const float2 h3 = mul2(bc(3.f), fma2(ex, bc(nx), fma2(ey, bc(ny), mul2(ez, bc(nz)))));
                         TX = fma2(s, fma2(h3, ex, mul2(e2s, bc(-nx))), TX);
                         TY = fma2(s, fma2(h3, ey, mul2(e2s, bc(-ny))), TY);
@@ -338,7 +339,7 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
                     }
                     if (any_near) {  // vortex ring (panel.rs:99-118)
                         float2 ax, ay, az;
-                        ring2(v, X2h, Y2h, Z2h, X2l, Y2l, Z2l, ax, ay, az);
+                        ring2(v, ex, ey, ez, ax, ay, az);
                         const float g4 = gam * static_cast<float>(kFourPiInv);
                         const float2 gm = make_float2((a0 && n0) ? g4 : 0.f, (a1 && n1) ? g4 : 0.f);
                         TX = fma2(gm, ax, TX);

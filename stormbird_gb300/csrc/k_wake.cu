@@ -208,32 +208,32 @@ __device__ void write_panel_records(const d3 (&pp)[4], double rc, double g, doub
         *lo = static_cast<float>(x - static_cast<double>(h));
     };
     for (int k = 0; k < 4; ++k) {
-        split(pp[k].x, &r.v[3 * k], &r.v[12 + 3 * k]);
-        split(pp[k].y, &r.v[3 * k + 1], &r.v[12 + 3 * k + 1]);
-        split(pp[k].z, &r.v[3 * k + 2], &r.v[12 + 3 * k + 2]);
+        const d3 ok = pp[k] - c;
+        r.v[3 * k] = static_cast<float>(ok.x);
+        r.v[3 * k + 1] = static_cast<float>(ok.y);
+        r.v[3 * k + 2] = static_cast<float>(ok.z);
         const d3 dk = pp[(k + 1) & 3] - pp[k];
-        r.v[24 + 3 * k] = static_cast<float>(dk.x);
-        r.v[24 + 3 * k + 1] = static_cast<float>(dk.y);
-        r.v[24 + 3 * k + 2] = static_cast<float>(dk.z);
+        r.v[12 + 3 * k] = static_cast<float>(dk.x);
+        r.v[12 + 3 * k + 1] = static_cast<float>(dk.y);
+        r.v[12 + 3 * k + 2] = static_cast<float>(dk.z);
         const double l2 = len2(dk);
-        r.v[36 + k] = l2 > 0.0 ? static_cast<float>(1.0 / l2) : 0.f;
+        r.v[24 + k] = l2 > 0.0 ? static_cast<float>(1.0 / l2) : 0.f;
     }
-    split(c.x, &r.v[40], &r.v[44]);
-    split(c.y, &r.v[41], &r.v[45]);
-    split(c.z, &r.v[42], &r.v[46]);
-    r.v[43] = static_cast<float>(ff2);
-    r.v[47] = static_cast<float>(area * kFourPiInv);
-    r.v[48] = static_cast<float>(n.x);
-    r.v[49] = static_cast<float>(n.y);
-    r.v[50] = static_cast<float>(n.z);
+    split(c.x, &r.v[28], &r.v[32]);
+    split(c.y, &r.v[29], &r.v[33]);
+    split(c.z, &r.v[30], &r.v[34]);
+    r.v[31] = static_cast<float>(ff2);
+    r.v[35] = static_cast<float>(area * kFourPiInv);
+    r.v[36] = static_cast<float>(n.x);
+    r.v[37] = static_cast<float>(n.y);
+    r.v[38] = static_cast<float>(n.z);
     r.v[kRec32Gamma] = static_cast<float>(g);
     // core length^4; a zero core (reference: factor 1) only occurs in the horseshoe path, which
     // runs in FP64, so the FP32 sweep always evaluates d^2 / sqrt(d^4 + rc^4)
     const double rc2 = rc * rc;
-    r.v[52] = static_cast<float>(rc2 * rc2);
-    r.v[53] = static_cast<float>(wing);
-    r.v[54] = 0.f;
-    r.v[55] = 0.f;
+    r.v[40] = static_cast<float>(rc2 * rc2);
+    r.v[41] = static_cast<float>(wing);
+    for (int k = 42; k < 48; ++k) r.v[k] = 0.f;
     *r32 = r;
     if (r64) {
         PanelRec<double> q;

@@ -8,7 +8,7 @@
 //   * wake points, two buffers (old/new) of [W+1][Np] double3, streamwise-major, and the
 //     velocity at the points [W+1][Np] double3                   (f64: position integration)
 //   * wake strengths, two buffers of [W][N] f64
-//   * wake panel records [W][N], 56 floats each (224 B, 16-B aligned) for the FP32
+//   * wake panel records [W][N], 48 floats each (192 B, 16-B aligned) for the FP32
 //     Biot-Savart sweep, plus f64 records for the first row (unit-strength matrix) and,
 //     in the FP64 precision mode, for every panel
 //   * frozen wake: fixed velocities [N] double3, unit matrix [N][N] double3
@@ -174,24 +174,25 @@ __device__ inline double foil_cd(const FoilP& f, double a) {
 // ---------------------------------------------------------------------------------------
 // Records of one vortex-ring panel for the Biot-Savart sweeps.
 //
-// FP32 record (PanelRec<float>, 56 floats = 224 B). Positions are float-float pairs
-// (hi = fl32(x), lo = fl32(x - hi)), so that a sweep forms r = (x_hi - p_hi) + (x_lo - p_lo):
-// for nearby points the hi difference is exact (Sterbenz), which makes the FP32 sweep
-// independent of where the geometry sits in space.
-//   [0..11]  corners p0..p3 hi (x, y, z)     [12..23] corners lo
-//   [24..35] segment vectors d_k = p_{k+1} - p_k (rounded from f64)
-//   [36..39] 1/|d_k|^2 per ring segment k (0 for a degenerate segment)
-//   [40..42] centre hi, [43] far-field length squared
-//   [44..46] centre lo, [47] area / (4 pi)
-//   [48..50] unit normal, [51] strength Gamma
-//   [52] core length^4, [53] wing index, [54..55] 0
+// FP32 record (PanelRec<float>, 48 floats = 192 B). The centre is a float-float pair
+// (hi = fl32(c), lo = fl32(c - hi)) and the corners are FP32 offsets from it, so a sweep
+// forms e = x - c = (x_hi - c_hi) + (x_lo - c_lo) once per panel (the hi difference is exact
+// for nearby points, Sterbenz) and r_k = e - o_k per corner: accurate to ~ulp(|r|) + ulp(|o|)
+// wherever the geometry sits in space.
+//   [0..11]  corner offsets o_k = p_k - centre (rounded from f64)
+//   [12..23] segment vectors d_k = p_{k+1} - p_k (rounded from f64)
+//   [24..27] 1/|d_k|^2 per ring segment k (0 for a degenerate segment)
+//   [28..30] centre hi, [31] far-field length squared
+//   [32..34] centre lo, [35] area / (4 pi)
+//   [36..38] unit normal, [39] strength Gamma
+//   [40] core length^4, [41] wing index, [42..47] 0
 // FP64 record (PanelRec<double>, 28 doubles = 224 B):
 //   [0..11] corners, [16..18] centre, [19] far-field length squared, [20..22] normal,
 //   [23] area / (4 pi), [24] Gamma, [25] core length, [26] wing index.
 template <class R>
 struct PanelRecSize;
 template <>
-struct PanelRecSize<float> { static constexpr int value = 56; };
+struct PanelRecSize<float> { static constexpr int value = 48; };
 template <>
 struct PanelRecSize<double> { static constexpr int value = 28; };
 
@@ -199,10 +200,10 @@ template <class R>
 struct __align__(16) PanelRec {
     R v[PanelRecSize<R>::value];
 };
-static_assert(sizeof(PanelRec<float>) == 224, "FP32 panel record is 224 bytes");
+static_assert(sizeof(PanelRec<float>) == 192, "FP32 panel record is 192 bytes");
 static_assert(sizeof(PanelRec<double>) == 224, "FP64 panel record is 224 bytes");
 
-constexpr int kRec32Gamma = 51;  // strength slot of the FP32 record
+constexpr int kRec32Gamma = 39;  // strength slot of the FP32 record
 constexpr int kRec64Gamma = 24;  // strength slot of the FP64 record
 
 // ---------------------------------------------------------------------------------------
