@@ -188,6 +188,28 @@ int sb_panel_sweep(int device, const double* corners, const double* strengths, c
                    int precision, double* velocities);
 
 /*
+ * The standalone sweep without any device allocation, for callers that may not allocate
+ * device memory while they run: a co-simulation master stepping the lifting line in real
+ * time (as the FMU's do_step is called), where allocating after initialisation is
+ * forbidden, or a host framework whose memory pool owns the whole GPU. Not a counterpart
+ * of any reference function: it is sb_panel_sweep (FP32, compensated) with every pointer
+ * in device memory the caller owns — corners [n_panels*12], strengths and core lengths
+ * [n_panels], targets and velocities [n_targets*3], f64 — and the sweep's scratch (panel
+ * records, partial sums, work counter, error word: 7 MiB + 256 B) in one fixed device array
+ * that each GPU loading the library holds until the process exits. At most
+ * SB_NO_ALLOC_MAX_PANELS panels and SB_NO_ALLOC_MAX_TARGETS targets per call (larger
+ * sizes: SB_ERR_SIZE). Work is enqueued on `stream` (a cudaStream_t, NULL = the legacy
+ * default stream) and the call returns when it has finished. The first call on a device
+ * resolves the array's device address; make that first call before any stream capture.
+ * Every call shares the array: calls that overlap on the GPU race and must be serialised.
+ */
+#define SB_NO_ALLOC_MAX_PANELS 16384
+#define SB_NO_ALLOC_MAX_TARGETS 65536
+int sb_panel_sweep_no_alloc(int device, const double* corners, const double* strengths, const double* core_lengths,
+                            size_t n_panels, double far_field_ratio, int symmetry, const double* targets,
+                            size_t n_targets, double* velocities, void* stream);
+
+/*
  * Measured FP32 FMA throughput of a device in TFLOP/s (best of `reps` timed launches of
  * an FMA-chain kernel): the denominator of the Biot-Savart sweep's roofline. Diagnostic
  * entry point with no counterpart in the reference.

@@ -4,6 +4,8 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "sb_device.cuh"
 
 namespace sbgpu {
@@ -143,6 +145,9 @@ struct OutLayout {
         return o;
     }
 };
+
+// Sets the calling thread's sb_last_error / sb_last_status (sim_host.cu).
+void report_error(int code, const std::string& message);
 
 // FP32 FMA throughput of `device` in TFLOP/s (k_probe.cu); negative on error.
 double measure_fp32_peak(int device, int reps);

@@ -776,6 +776,13 @@ struct sb_sim {
     }
 };
 
+namespace sbgpu {
+void report_error(int code, const std::string& message) {
+    g_last_status = code;
+    g_last_error = message;
+}
+}  // namespace sbgpu
+
 // =======================================================================================
 // C ABI
 // =======================================================================================
