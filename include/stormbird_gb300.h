@@ -216,6 +216,60 @@ int sb_panel_sweep_no_alloc(int device, const double* corners, const double* str
  */
 int sb_measure_fp32_peak(int device, int reps, double* tflops);
 
+/* ===================================================================================
+ * Batched cases. The reference runs independent cases (apparent-wind sweeps, differing
+ * sail counts and wake lengths) as separate `Simulation`s, one `do_step` each
+ * (simulation.rs:107-203; CompleteSailModel loops over them,
+ * complete_sail_model/mod.rs:187-191). A batch steps many such cases together: each case
+ * is built from its own setup JSON exactly as by sb_sim_new and computes what its own
+ * Simulation::do_step would, but the Biot-Savart sweeps of all cases run as one persistent
+ * launch per sweep kind and the steady step is replayed as a CUDA graph.
+ * =================================================================================== */
+typedef struct sb_batch sb_batch;
+
+/* Per-case summary after a step: force sum [3], moment sum [3], residual, iterations,
+ * converged (0/1), device status word (0 = ok). */
+#define SB_BATCH_SUMMARY 10
+/* sb_batch_info fields: last step ms, panel-target pairs swept in the last step, tuning
+ * waves, tuning CTAs per SM (0 = occupancy limit), roll-up grid, roll-up work items,
+ * tuned (0/1), candidates timed, best tuned roll-up ms, graph in use (0/1), steps done. */
+#define SB_BATCH_INFO 11
+
+/* n_cases setup JSON strings (as sb_sim_new). NULL on error (sb_last_error names the case). */
+sb_batch* sb_batch_new(const char* const* setup_jsons, size_t n_cases, int device);
+void sb_batch_free(sb_batch* batch);
+/* Number of cases, total span lines (sum of N) and total freestream points (sum of nfs). */
+int sb_batch_sizes(const sb_batch* batch, size_t* n_cases, size_t* total_lines, size_t* total_freestream);
+/* Sizes of case i and the offsets of its lines / freestream points in the batch's arrays. */
+int sb_batch_case_sizes(const sb_batch* batch, size_t i, size_t* n_lines, size_t* n_wings, size_t* n_freestream,
+                        size_t* line_offset, size_t* freestream_offset);
+/* Freestream points of all cases, case after case (each as sb_sim_get_freestream_points). */
+int sb_batch_get_freestream_points(sb_batch* batch, double* points_xyz, size_t n_total);
+/* One step of every case: freestream [total_freestream*3], case after case. */
+int sb_batch_do_step(sb_batch* batch, double time, double time_step, const double* freestream_xyz, size_t n_total);
+int sb_batch_do_step_device(sb_batch* batch, double time, double time_step, const double* freestream_dev,
+                            size_t n_total);
+/* Results of the last step: circulation [total_lines] and summaries [n_cases*SB_BATCH_SUMMARY]. */
+int sb_batch_get_circulation(const sb_batch* batch, double* circulation, size_t n_total);
+int sb_batch_get_summary(const sb_batch* batch, double* summary, size_t n);
+/* Full output block of case i for the last step (as sb_sim_read_output). */
+int sb_batch_read_case_output(sb_batch* batch, size_t i, sb_step_output* out);
+/* Initial solution of the next step's solve for every case (the reference's
+ * previous_circulation_strength, simulation.rs:165,189): the warm-start hook. */
+int sb_batch_set_initial_circulation(sb_batch* batch, const double* circulation, size_t n_total);
+int sb_batch_set_initial_circulation_device(sb_batch* batch, const double* circulation_dev, size_t n_total);
+/* Device address of the batch's previous-circulation array [total_lines] (read/write). */
+int sb_batch_previous_circulation_device(sb_batch* batch, double** circulation_dev);
+/* Sweep precision of every case: 0 FP32 compensated (default), 1 FP32, 2 FP64. */
+int sb_batch_set_precision(sb_batch* batch, int mode);
+/* CUDA-graph replay of the steady step (default on). */
+int sb_batch_use_graph(sb_batch* batch, int enable);
+/* Times the roll-up sweep of the current state for each work-decomposition candidate within
+ * about budget_seconds and keeps the fastest for this batch and for later batches of the
+ * same workload bucket in this process. Needs a batch whose roll-up has started. */
+int sb_batch_autotune(sb_batch* batch, double budget_seconds);
+int sb_batch_info(const sb_batch* batch, double* info, size_t n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,788 @@
+// Batched execution of independent lifting-line cases: the sb_batch_* functions of the C ABI.
+//
+// A batch owns one simulation handle per case (each built from its own setup JSON, with any
+// sail count, panel count and wake length) and steps them all together. Per step:
+//   1. one host->device copy of every case's freestream (one contiguous buffer) and of the
+//      step's sweep work lists;
+//   2. the per-case kernels before solving (geometry, wake advection, panels), spread over a
+//      pool of forked streams so that small cases run side by side;
+//   3. ONE persistent sweep launch for the frozen-wake sweeps of all cases and ONE for all
+//      roll-up sweeps: every (case, source chunk, target tile) item sits in one work list,
+//      costliest items first, taken from one atomic counter (k_bs_sweep with a job list);
+//   4. the per-case solves and force kernels on the pool streams, then one gather kernel
+//      that packs every case's circulation and force summary for one device->host copy.
+// After three steps (when the step's kernel arguments stop changing except for the wake
+// buffer parity) the whole step is captured into a CUDA graph per parity and replayed; the
+// work lists are refreshed through the graph's copy node from pinned host memory.
+//
+// Work decomposition: each sweep's source chunk size is fixed per case by a target item
+// size (total steady-state pairs / (persistent grid x waves)), so items are of similar
+// cost across cases; `waves` and the CTAs per SM of the persistent grid come from the
+// autotuner (sb_batch_autotune), which times the batch's own roll-up sweep for each
+// candidate and keeps the best per workload bucket for the life of the process.
+#include <chrono>
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <numeric>
+#include <tuple>
+
+#include "sim_core.hpp"
+
+namespace {
+
+constexpr int kPoolStreams = 16;
+constexpr int kMaxChunksPerJob = 64;
+
+// summary record of one case after a step
+struct GatherJob {
+    const double* out = nullptr;  // the case's output block
+    long long fsum = 0, msum = 0, residual = 0, iterations = 0, converged = 0;
+    int N = 0;
+    const int* err = nullptr;
+    double* gamma_dst = nullptr;
+    double* summary_dst = nullptr;
+};
+
+// One CTA per case: circulation and SB_BATCH_SUMMARY summary values into the compact buffer.
+__global__ void k_gather(const GatherJob* jobs) {
+    const GatherJob& g = jobs[blockIdx.x];
+    for (int i = threadIdx.x; i < g.N; i += blockDim.x) g.gamma_dst[i] = g.out[i];
+    if (threadIdx.x == 0) {
+        double* s = g.summary_dst;
+        for (int k = 0; k < 3; ++k) {
+            s[k] = g.out[g.fsum + k];
+            s[3 + k] = g.out[g.msum + k];
+        }
+        s[6] = g.out[g.residual];
+        s[7] = g.out[g.iterations];
+        s[8] = g.out[g.converged];
+        s[9] = static_cast<double>(*g.err);
+    }
+}
+
+// Tuned parameters of the batched sweeps.
+struct Tuning {
+    int waves = 8;          // items per persistent CTA the item size aims at
+    int blocks_per_sm = 0;  // persistent CTAs per SM (0: the occupancy limit)
+};
+
+// Process-wide tuning results per workload bucket.
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int>, Tuning> g_tune_cache;
+
+}  // namespace
+
+struct sb_batch {
+    int device = 0;
+    int sms = 1;
+    int precision = 0;
+    std::vector<std::unique_ptr<sb_sim>> cases;
+    std::vector<long long> line_off, fs_off;
+    long long N_total = 0, nfs_total = 0;
+    bool any_dynamic = false;
+
+    cudaStream_t main = nullptr;
+    cudaStream_t pool[kPoolStreams] = {nullptr};
+    cudaEvent_t ev_fork[3] = {nullptr}, ev_join[3][kPoolStreams] = {{nullptr}};
+    cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
+
+    DevBuf<d3> fs_all;
+    PinnedBuf<double> h_fs_all;
+    DevBuf<double> gamma_all;
+    DevBuf<double> compact;  // [N_total] circulation, then [cases][SB_BATCH_SUMMARY]
+    PinnedBuf<double> h_compact;
+    DevBuf<GatherJob> gather_jobs;
+
+    // Sweep work lists: group = (sweep kind, symmetry, neglect); one launch each.
+    struct Group {
+        int kind = 0;  // 0 frozen-wake sweep, 1 roll-up sweep
+        int sym = 0, neglect = 0;
+        std::vector<int> cases;           // case of each job, costliest items first
+        std::vector<int> chunk;           // panels per source chunk of each job
+        std::vector<long long> part_off;  // offset of each job's partial sums
+        std::vector<long long> block_off; // first reduce block of each job
+        long long reduce_blocks = 0;
+        long long job_off = 0;            // first entry in the job staging buffer
+        int grid = 1;
+        long long items = 0;              // items in the current step
+    };
+    std::vector<Group> groups;
+    Tuning tuning;
+    bool tuned = false;
+    double tune_best_ms = 0.0;
+    int tune_candidates = 0;
+    long long job_entries = 0;
+    PinnedBuf<BsJob> h_jobs;
+    DevBuf<BsJob> d_jobs;
+    DevBuf<double> partial;
+    DevBuf<unsigned long long> counters;
+    DevBuf<int> err;
+    PinnedBuf<int> h_err;
+
+    bool use_graph = true;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    double graph_dt = 0.0;
+    int graph_precision = -1;
+    int steps = 0;
+    double last_ms = 0.0;
+    long long last_pairs = 0;  // panel-target pairs of the last step's sweeps
+
+    ~sb_batch() {
+        cudaSetDevice(device);
+        if (main) cudaStreamSynchronize(main);
+        drop_graphs();
+        cases.clear();
+        for (auto& e : ev_fork) if (e) cudaEventDestroy(e);
+        for (auto& r : ev_join) for (auto& e : r) if (e) cudaEventDestroy(e);
+        if (ev_t0) cudaEventDestroy(ev_t0);
+        if (ev_t1) cudaEventDestroy(ev_t1);
+        for (auto& s : pool) if (s) cudaStreamDestroy(s);
+        if (main) cudaStreamDestroy(main);
+    }
+
+    void drop_graphs() {
+        for (auto& g : graph) {
+            if (g) cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    }
+
+    // ------------------------------------------------------------------ construction
+    void build(const char* const* jsons, size_t n, int dev) {
+        device = dev;
+        if (n == 0) raise(SB_ERR_SIZE, "a batch needs at least one case");
+        for (size_t i = 0; i < n; ++i) {
+            if (!jsons[i]) raise(SB_ERR_NULL_ARG, "setup JSON of case " + std::to_string(i) + " is NULL");
+            std::unique_ptr<sb_sim> s(new sb_sim());
+            try {
+                s->build(jsons[i], dev);
+            } catch (const SbFail& e) {
+                raise(e.code, "case " + std::to_string(i) + ": " + e.msg);
+            }
+            cases.push_back(std::move(s));
+        }
+        ck(cudaSetDevice(device), "cudaSetDevice");
+        sms = num_sms(device);
+        ck(cudaStreamCreateWithFlags(&main, cudaStreamNonBlocking), "cudaStreamCreate");
+        for (auto& s : pool) ck(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
+        for (auto& e : ev_fork) ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+        for (auto& r : ev_join) for (auto& e : r) ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+        ck(cudaEventCreate(&ev_t0), "cudaEventCreate");
+        ck(cudaEventCreate(&ev_t1), "cudaEventCreate");
+
+        // contiguous freestream and circulation; every case works on its slice
+        for (auto& c : cases) {
+            line_off.push_back(N_total);
+            fs_off.push_back(nfs_total);
+            N_total += c->N;
+            nfs_total += c->nfs;
+            any_dynamic = any_dynamic || c->dynamic;
+        }
+        fs_all.alloc(nfs_total);
+        h_fs_all.alloc(static_cast<size_t>(nfs_total) * 3);
+        gamma_all.alloc(N_total);
+        ck(cudaMemset(gamma_all.p, 0, N_total * sizeof(double)), "memset");
+        const size_t ncomp = static_cast<size_t>(N_total) + cases.size() * SB_BATCH_SUMMARY;
+        compact.alloc(ncomp);
+        ck(cudaMemset(compact.p, 0, ncomp * sizeof(double)), "memset");
+        h_compact.alloc(ncomp);
+        std::memset(h_compact.p, 0, ncomp * sizeof(double));
+        std::vector<GatherJob> gj;
+        for (size_t i = 0; i < cases.size(); ++i) {
+            sb_sim& c = *cases[i];
+            c.fs_p = fs_all.p + fs_off[i];
+            c.gamma_p = gamma_all.p + line_off[i];
+            c.stream = pool[i % kPoolStreams];
+            GatherJob g;
+            g.out = c.out.p;
+            g.fsum = c.L.fsum;
+            g.msum = c.L.msum;
+            g.residual = c.L.residual;
+            g.iterations = c.L.iterations;
+            g.converged = c.L.converged;
+            g.N = c.N;
+            g.err = c.err.p;
+            g.gamma_dst = compact.p + line_off[i];
+            g.summary_dst = compact.p + N_total + static_cast<long long>(i) * SB_BATCH_SUMMARY;
+            gj.push_back(g);
+        }
+        gather_jobs.upload(gj);
+        counters.alloc(16);
+        err.alloc(1);
+        ck(cudaMemset(err.p, 0, sizeof(int)), "memset");
+        h_err.alloc(1);
+        make_groups();
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            auto it = g_tune_cache.find(bucket());
+            if (it != g_tune_cache.end()) {
+                tuning = it->second;
+                tuned = true;
+            }
+        }
+        plan(tuning);
+        ck(cudaDeviceSynchronize(), "batch build");
+    }
+
+    // Groups of sweeps that share a kernel variant.
+    void make_groups() {
+        groups.clear();
+        std::map<std::tuple<int, int, int>, int> index;
+        for (size_t i = 0; i < cases.size(); ++i) {
+            const sb_sim& c = *cases[i];
+            if (!c.dynamic) continue;
+            for (int kind = 0; kind < 2; ++kind) {
+                const int neglect = kind == 0 ? c.dm.neglect_self : 0;
+                auto key = std::make_tuple(kind, c.dm.symmetry, neglect);
+                auto it = index.find(key);
+                if (it == index.end()) {
+                    Group g;
+                    g.kind = kind;
+                    g.sym = c.dm.symmetry;
+                    g.neglect = neglect;
+                    it = index.emplace(key, static_cast<int>(groups.size())).first;
+                    groups.push_back(g);
+                }
+                groups[it->second].cases.push_back(static_cast<int>(i));
+            }
+        }
+        if (groups.size() > 16) raise(SB_ERR_UNSUPPORTED, "too many sweep variants in one batch");
+    }
+
+    // Workload bucket of the tuning cache: precision, log2 of the steady-state roll-up pairs,
+    // log2 of the number of cases, and the number of sweep variants.
+    std::tuple<int, int, int, int> bucket() const {
+        double pairs = 0.0;
+        for (const auto& c : cases)
+            if (c->dynamic) pairs += static_cast<double>(std::min<long long>(c->dm.end_index, c->P_pts)) * c->P_pan;
+        return std::make_tuple(precision, static_cast<int>(std::lround(std::log2(std::max(pairs, 1.0)))),
+                               static_cast<int>(std::lround(std::log2(static_cast<double>(cases.size())))),
+                               static_cast<int>(groups.size()));
+    }
+
+    // Steady-state sweep sizes (all wake rows active) of case c.
+    static void full_sizes(const sb_sim& c, int kind, long long& M, long long& P, long long& M_total) {
+        if (kind == 0) {
+            M = c.N;
+            P = c.P_pan - c.N;
+            M_total = c.N;
+        } else {
+            M = c.dm.end_index > 0 ? std::min<long long>(c.dm.end_index, c.P_pts) : 0;
+            P = c.P_pan;
+            M_total = c.P_pts;
+        }
+    }
+
+    // Chunk sizes, item order, partial-sum offsets and grids for the tuning t.
+    void plan(const Tuning& t) {
+        drop_graphs();
+        const int tile = bs_tile_panels(precision);
+        long long part_total = 0;
+        job_entries = 0;
+        for (auto& g : groups) {
+            const int T = bs_targets_per_thread(g.sym);
+            const long long TM = static_cast<long long>(kBsThreads) * T;
+            const int occ = bs_occupancy_blocks_per_sm(precision, g.sym, g.neglect);
+            const int bps = t.blocks_per_sm > 0 ? std::min(t.blocks_per_sm, occ) : occ;
+            g.grid = sms * bps;
+            double total = 0.0;
+            for (int c : g.cases) {
+                long long M, P, Mt;
+                full_sizes(*cases[c], g.kind, M, P, Mt);
+                total += static_cast<double>(M) * static_cast<double>(P);
+            }
+            const double item_pairs = std::max(total / (static_cast<double>(g.grid) * t.waves),
+                                               static_cast<double>(TM) * tile);
+            const size_t n = g.cases.size();
+            g.chunk.assign(n, tile);
+            for (size_t k = 0; k < n; ++k) {
+                long long M, P, Mt;
+                full_sizes(*cases[g.cases[k]], g.kind, M, P, Mt);
+                long long ch = static_cast<long long>(std::ceil(item_pairs / static_cast<double>(TM)));
+                ch = ((ch + tile - 1) / tile) * tile;
+                const long long whole = std::max<long long>(tile, ((P + tile - 1) / tile) * tile);
+                const long long min_for_cap = (((P + kMaxChunksPerJob - 1) / kMaxChunksPerJob + tile - 1) / tile) * tile;
+                ch = std::min(std::max<long long>({ch, static_cast<long long>(tile), min_for_cap}), whole);
+                g.chunk[k] = static_cast<int>(ch);
+            }
+            // costliest items first (LPT order); the order is fixed for the batch's life
+            std::vector<size_t> order(n);
+            std::iota(order.begin(), order.end(), 0);
+            std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return g.chunk[a] > g.chunk[b]; });
+            std::vector<int> cs(n), ch(n);
+            for (size_t k = 0; k < n; ++k) {
+                cs[k] = g.cases[order[k]];
+                ch[k] = g.chunk[order[k]];
+            }
+            g.cases = cs;
+            g.chunk = ch;
+            g.part_off.assign(n, 0);
+            g.block_off.assign(n, 0);
+            long long blocks = 0;
+            for (size_t k = 0; k < n; ++k) {
+                long long M, P, Mt;
+                full_sizes(*cases[g.cases[k]], g.kind, M, P, Mt);
+                const long long nch = P > 0 ? (P + g.chunk[k] - 1) / g.chunk[k] : 0;
+                g.part_off[k] = part_total;
+                part_total += nch * M * 3;
+                g.block_off[k] = blocks;
+                blocks += (Mt + kBsReduceThreads - 1) / kBsReduceThreads;
+            }
+            g.reduce_blocks = blocks;
+            g.job_off = job_entries;
+            job_entries += static_cast<long long>(n) + 1;  // + sentinel
+        }
+        if (partial.n < static_cast<size_t>(std::max<long long>(part_total, 1))) partial.alloc(std::max<long long>(part_total, 1));
+        if (h_jobs.n < static_cast<size_t>(std::max<long long>(job_entries, 1))) {
+            h_jobs.alloc(std::max<long long>(job_entries, 1));
+            d_jobs.alloc(std::max<long long>(job_entries, 1));
+        }
+        tuning = t;
+    }
+
+    // Work lists of the current step (host), for every group.
+    void fill_jobs() {
+        last_pairs = 0;
+        for (auto& g : groups) {
+            const int T = bs_targets_per_thread(g.sym);
+            const long long TM = static_cast<long long>(kBsThreads) * T;
+            long long item = 0;
+            for (size_t k = 0; k < g.cases.size(); ++k) {
+                sb_sim& c = *cases[g.cases[k]];
+                sb_sim::SweepDesc d = g.kind == 0 ? c.fixed_desc() : c.rollup_desc();
+                BsJob J;
+                J.panels = precision == 2 ? static_cast<const void*>(c.rec64.p) : static_cast<const void*>(c.rec32.p);
+                J.p_begin = d.p0;
+                J.p_end = d.p1;
+                J.targets = d.targets;
+                J.target_wing = d.twing;
+                J.M = d.M;
+                J.chunk_panels = g.chunk[k];
+                const long long P = d.p1 - d.p0;
+                J.n_chunks = (P > 0 && d.M > 0) ? static_cast<int>((P + g.chunk[k] - 1) / g.chunk[k]) : 0;
+                J.n_ttiles = (d.M + TM - 1) / TM;
+                J.partial = partial.p + g.part_off[k];
+                J.item_begin = item;
+                J.M_total = d.M_total;
+                J.base = d.base;
+                J.out = d.dst;
+                J.block_begin = g.block_off[k];
+                item += J.n_ttiles * static_cast<long long>(J.n_chunks);
+                if (J.n_chunks > 0) last_pairs += d.M * P;
+                h_jobs.p[g.job_off + static_cast<long long>(k)] = J;
+            }
+            BsJob sentinel;
+            sentinel.item_begin = item;
+            sentinel.block_begin = g.reduce_blocks;
+            h_jobs.p[g.job_off + static_cast<long long>(g.cases.size())] = sentinel;
+            g.items = item;
+        }
+    }
+
+    // ------------------------------------------------------------------ one step
+    void fork(int slot) {
+        ck(cudaEventRecord(ev_fork[slot], main), "fork");
+        for (auto& s : pool) ck(cudaStreamWaitEvent(s, ev_fork[slot], 0), "fork");
+    }
+    void join(int slot) {
+        for (int k = 0; k < kPoolStreams; ++k) {
+            ck(cudaEventRecord(ev_join[slot][k], pool[k]), "join");
+            ck(cudaStreamWaitEvent(main, ev_join[slot][k], 0), "join");
+        }
+    }
+
+    void launch_group(Group& g) {
+        BsArgs a;
+        a.jobs = d_jobs.p + g.job_off;
+        a.n_jobs = static_cast<int>(g.cases.size());
+        a.work_counter = counters.p + (&g - groups.data());
+        a.err = err.p;
+        a.symmetry = g.sym;
+        a.neglect = g.neglect;
+        ck(cudaMemsetAsync(a.work_counter, 0, sizeof(unsigned long long), main), "memset counter");
+        ck(launch_bs_sweep(a, precision, g.grid, main), "batched Biot-Savart sweep");
+        ck(launch_bs_reduce_jobs(a.jobs, a.n_jobs, g.reduce_blocks, main), "batched sweep reduce");
+    }
+
+    void sweeps(int kind) {
+        for (auto& g : groups)
+            if (g.kind == kind) launch_group(g);
+    }
+
+    // Enqueues one step of every case on main + pool (the freestream is in fs_all and the
+    // work lists in h_jobs).
+    void enqueue(double time, double dt) {
+        if (job_entries > 0)
+            ck(cudaMemcpyAsync(d_jobs.p, h_jobs.p, job_entries * sizeof(BsJob), cudaMemcpyHostToDevice, main), "H2D jobs");
+        fork(0);
+        for (auto& c : cases) c->step_begin(time, dt);
+        join(0);
+        sweeps(0);
+        for (auto& c : cases) if (c->dynamic) c->after_fixed_sweep();
+        fork(1);
+        for (auto& c : cases) c->step_matrix_and_solve();
+        join(1);
+        sweeps(1);
+        for (auto& c : cases) if (c->dynamic) c->after_rollup_sweep();
+        fork(2);
+        for (auto& c : cases) c->step_end();
+        join(2);
+        k_gather<<<static_cast<unsigned>(cases.size()), 128, 0, main>>>(gather_jobs.p);
+        ck(cudaGetLastError(), "gather");
+        const size_t ncomp = static_cast<size_t>(N_total) + cases.size() * SB_BATCH_SUMMARY;
+        ck(cudaMemcpyAsync(h_compact.p, compact.p, ncomp * sizeof(double), cudaMemcpyDeviceToHost, main), "D2H summary");
+        ck(cudaMemcpyAsync(h_err.p, err.p, sizeof(int), cudaMemcpyDeviceToHost, main), "D2H status");
+    }
+
+    // Host state a replayed graph step leaves behind (the same as enqueue's bookkeeping).
+    void replay_bookkeeping(double time, double dt) {
+        for (auto& c : cases) {
+            c->params.time = time;
+            c->params.dt = dt;
+            if (c->dynamic) {
+                c->cur ^= 1;
+                sb_sim::SweepDesc d = c->rollup_desc();
+                c->last_counters[0] = static_cast<double>(d.M);
+                c->last_counters[1] = static_cast<double>(d.p1 - d.p0);
+                c->last_counters[2] = static_cast<double>(c->N);
+                c->last_counters[3] = static_cast<double>(c->P_pan - c->N);
+                c->steps_completed += 1;
+                c->last_counters[4] = static_cast<double>(c->steps_completed);
+            }
+            c->fd_count += 1;
+        }
+    }
+
+    bool steady() const {
+        for (const auto& c : cases) {
+            if (!c->first_step_completed || c->fd_count < 2) return false;
+            if (c->dynamic && c->steps_completed < 3) return false;
+        }
+        return true;
+    }
+
+    void step(double time, double dt) {
+        for (auto& c : cases) {
+            if (c->timing) c->timing = false;
+            c->precision = precision;
+            c->ensure_rec64();  // FP64 records (allocation) before any capture
+        }
+        if (graph_dt != dt || graph_precision != precision) drop_graphs();
+        // the parity of the wake buffers at the start of the step selects the graph
+        const int parity = any_dynamic ? first_dynamic().cur : (steps & 1);
+        ck(cudaEventRecord(ev_t0, main), "event");
+        if (use_graph && steady()) {
+            // job lists of this step, read by the graph's copy node at launch
+            fill_jobs_after_begin();
+            if (!graph[parity]) {
+                // capture: the host-side state advances as in an eager step
+                cudaGraph_t g = nullptr;
+                ck(cudaStreamBeginCapture(main, cudaStreamCaptureModeRelaxed), "begin capture");
+                try {
+                    enqueue(time, dt);
+                } catch (...) {
+                    cudaStreamEndCapture(main, &g);
+                    if (g) cudaGraphDestroy(g);
+                    throw;
+                }
+                ck(cudaStreamEndCapture(main, &g), "end capture");
+                cudaError_t e = cudaGraphInstantiate(&graph[parity], g, 0);
+                cudaGraphDestroy(g);
+                ck(e, "graph instantiate");
+                graph_dt = dt;
+                graph_precision = precision;
+            } else {
+                replay_bookkeeping(time, dt);
+            }
+            ck(cudaGraphLaunch(graph[parity], main), "graph launch");
+        } else {
+            fill_jobs_after_begin();
+            enqueue(time, dt);
+        }
+        ck(cudaEventRecord(ev_t1, main), "event");
+        ck(cudaStreamSynchronize(main), "batch step");
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev_t0, ev_t1);
+        last_ms = ms;
+        steps += 1;
+        if (h_err.p[0] != kDevOk) {
+            ck(cudaMemset(err.p, 0, sizeof(int)), "memset");
+            raise(SB_ERR_TIMEOUT, "a bounded device-side wait ran out in a batched sweep");
+        }
+        for (size_t i = 0; i < cases.size(); ++i) {
+            const double st = h_compact.p[N_total + static_cast<long long>(i) * SB_BATCH_SUMMARY + 9];
+            if (st != 0.0) {
+                sb_sim& c = *cases[i];
+                ck(cudaMemset(c.err.p, 0, sizeof(int)), "memset");
+                if (st == kDevTimeout) raise(SB_ERR_TIMEOUT, "case " + std::to_string(i) + ": a bounded device-side wait ran out");
+                if (st == kDevSingular) raise(SB_ERR_STATE, "case " + std::to_string(i) + ": Matrix is singular or nearly singular");
+                raise(SB_ERR_CUDA, "case " + std::to_string(i) + ": device error word " + std::to_string(st));
+            }
+        }
+    }
+
+    const sb_sim& first_dynamic() const {
+        for (const auto& c : cases) if (c->dynamic) return *c;
+        return *cases[0];
+    }
+
+    // The work lists describe the sweeps as they will be after step_begin (which swaps the
+    // wake buffers): compute them with the parity flipped for the duration.
+    void fill_jobs_after_begin() {
+        for (auto& c : cases) if (c->dynamic) c->cur ^= 1;
+        fill_jobs();
+        for (auto& c : cases) if (c->dynamic) c->cur ^= 1;
+    }
+
+    void do_step(double time, double dt, const double* fs_host, size_t n) {
+        if (static_cast<long long>(n) != nfs_total)
+            raise(SB_ERR_SIZE, "freestream has " + std::to_string(n) + " points, expected " + std::to_string(nfs_total));
+        const size_t cnt = n * 3;
+        for (size_t i = 0; i < cnt; ++i)
+            if (!std::isfinite(fs_host[i])) raise(SB_ERR_NONFINITE, "non-finite freestream value at index " + std::to_string(i / 3));
+        std::memcpy(h_fs_all.p, fs_host, cnt * sizeof(double));
+        ck(cudaMemcpyAsync(fs_all.p, h_fs_all.p, cnt * sizeof(double), cudaMemcpyHostToDevice, main), "H2D freestream");
+        step(time, dt);
+    }
+
+    void do_step_device(double time, double dt, const double* fs_dev, size_t n) {
+        if (static_cast<long long>(n) != nfs_total) raise(SB_ERR_SIZE, "freestream length mismatch");
+        ck(cudaMemcpyAsync(fs_all.p, fs_dev, n * sizeof(d3), cudaMemcpyDeviceToDevice, main), "D2D freestream");
+        step(time, dt);
+    }
+
+    // ------------------------------------------------------------------ autotuner
+    // Times the roll-up sweeps of the current wake state for each candidate (waves x CTAs per
+    // SM) and keeps the fastest. The sweeps only rewrite the wake-point velocities, which the
+    // last run (with the chosen plan) leaves as an eager sweep of this state would.
+    void autotune(double budget_s) {
+        bool active = false;
+        for (const auto& c : cases) active = active || (c->dynamic && c->rollup_active());
+        if (!active) raise(SB_ERR_STATE, "autotuning needs a batch whose wake roll-up has started (4 steps)");
+        ck(cudaStreamSynchronize(main), "sync");
+        int occ = 1;
+        for (const auto& g : groups) occ = std::max(occ, bs_occupancy_blocks_per_sm(precision, g.sym, g.neglect));
+        std::vector<Tuning> cand;
+        for (int w : {1, 2, 4, 8, 16, 32})
+            for (int b : {occ, occ - 1})
+                if (b >= 1) cand.push_back(Tuning{w, b});
+        Tuning best = tuning;
+        double best_ms = 1e300;
+        double spent = 0.0;
+        tune_candidates = 0;
+        for (const Tuning& t : cand) {
+            plan(t);
+            fill_jobs();
+            ck(cudaMemcpyAsync(d_jobs.p, h_jobs.p, job_entries * sizeof(BsJob), cudaMemcpyHostToDevice, main), "H2D jobs");
+            auto t0 = std::chrono::steady_clock::now();
+            double ms = 1e300;
+            for (int rep = 0; rep < 2; ++rep) {
+                ck(cudaEventRecord(ev_t0, main), "event");
+                sweeps(1);
+                ck(cudaEventRecord(ev_t1, main), "event");
+                ck(cudaStreamSynchronize(main), "tuning sweep");
+                float f = 0.f;
+                cudaEventElapsedTime(&f, ev_t0, ev_t1);
+                ms = std::min(ms, static_cast<double>(f));
+            }
+            spent += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            tune_candidates += 1;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = t;
+            }
+            if (spent > budget_s) break;
+        }
+        plan(best);
+        fill_jobs();
+        ck(cudaMemcpyAsync(d_jobs.p, h_jobs.p, job_entries * sizeof(BsJob), cudaMemcpyHostToDevice, main), "H2D jobs");
+        sweeps(1);
+        ck(cudaMemcpyAsync(h_err.p, err.p, sizeof(int), cudaMemcpyDeviceToHost, main), "D2H status");
+        ck(cudaStreamSynchronize(main), "tuning");
+        if (h_err.p[0] != kDevOk) {
+            ck(cudaMemset(err.p, 0, sizeof(int)), "memset");
+            raise(SB_ERR_TIMEOUT, "a bounded device-side wait ran out in a batched sweep");
+        }
+        tuned = true;
+        tune_best_ms = best_ms;
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[bucket()] = best;
+    }
+};
+
+// =======================================================================================
+// C ABI
+// =======================================================================================
+namespace {
+int null_arg() {
+    report_error(SB_ERR_NULL_ARG, "null argument");
+    return SB_ERR_NULL_ARG;
+}
+}  // namespace
+
+extern "C" {
+
+sb_batch* sb_batch_new(const char* const* setup_jsons, size_t n_cases, int device) {
+    if (!setup_jsons) {
+        null_arg();
+        return nullptr;
+    }
+    std::unique_ptr<sb_batch> b(new sb_batch());
+    int rc = guard([&] { b->build(setup_jsons, n_cases, device); });
+    if (rc != SB_OK) return nullptr;
+    return b.release();
+}
+
+void sb_batch_free(sb_batch* b) { delete b; }
+
+int sb_batch_sizes(const sb_batch* b, size_t* n_cases, size_t* total_lines, size_t* total_freestream) {
+    if (!b) return null_arg();
+    if (n_cases) *n_cases = b->cases.size();
+    if (total_lines) *total_lines = static_cast<size_t>(b->N_total);
+    if (total_freestream) *total_freestream = static_cast<size_t>(b->nfs_total);
+    return SB_OK;
+}
+
+int sb_batch_case_sizes(const sb_batch* b, size_t i, size_t* n, size_t* s, size_t* nfs, size_t* line_offset,
+                        size_t* freestream_offset) {
+    if (!b) return null_arg();
+    if (i >= b->cases.size()) {
+        report_error(SB_ERR_SIZE, "case index out of range");
+        return SB_ERR_SIZE;
+    }
+    const sb_sim& c = *b->cases[i];
+    if (n) *n = static_cast<size_t>(c.N);
+    if (s) *s = static_cast<size_t>(c.S);
+    if (nfs) *nfs = static_cast<size_t>(c.nfs);
+    if (line_offset) *line_offset = static_cast<size_t>(b->line_off[i]);
+    if (freestream_offset) *freestream_offset = static_cast<size_t>(b->fs_off[i]);
+    return SB_OK;
+}
+
+int sb_batch_get_freestream_points(sb_batch* b, double* points, size_t n) {
+    if (!b || !points) return null_arg();
+    return guard([&] {
+        if (static_cast<long long>(n) != b->nfs_total) raise(SB_ERR_SIZE, "points buffer length mismatch");
+        for (size_t i = 0; i < b->cases.size(); ++i) {
+            sb_sim& c = *b->cases[i];
+            c.freestream_points(points + 3 * b->fs_off[i], static_cast<size_t>(c.nfs));
+        }
+    });
+}
+
+int sb_batch_do_step(sb_batch* b, double time, double dt, const double* freestream, size_t n) {
+    if (!b || !freestream) return null_arg();
+    return guard([&] { b->do_step(time, dt, freestream, n); });
+}
+
+int sb_batch_do_step_device(sb_batch* b, double time, double dt, const double* freestream_dev, size_t n) {
+    if (!b || !freestream_dev) return null_arg();
+    return guard([&] { b->do_step_device(time, dt, freestream_dev, n); });
+}
+
+int sb_batch_get_circulation(const sb_batch* b, double* gamma, size_t n) {
+    if (!b || !gamma) return null_arg();
+    if (static_cast<long long>(n) != b->N_total) {
+        report_error(SB_ERR_SIZE, "circulation buffer length mismatch");
+        return SB_ERR_SIZE;
+    }
+    std::memcpy(gamma, b->h_compact.p, n * sizeof(double));
+    return SB_OK;
+}
+
+int sb_batch_get_summary(const sb_batch* b, double* summary, size_t n) {
+    if (!b || !summary) return null_arg();
+    if (n != b->cases.size() * SB_BATCH_SUMMARY) {
+        report_error(SB_ERR_SIZE, "summary buffer length mismatch");
+        return SB_ERR_SIZE;
+    }
+    std::memcpy(summary, b->h_compact.p + b->N_total, n * sizeof(double));
+    return SB_OK;
+}
+
+int sb_batch_read_case_output(sb_batch* b, size_t i, sb_step_output* out) {
+    if (!b || !out) return null_arg();
+    if (i >= b->cases.size()) {
+        report_error(SB_ERR_SIZE, "case index out of range");
+        return SB_ERR_SIZE;
+    }
+    return guard([&] { b->cases[i]->read_output(out); });
+}
+
+int sb_batch_set_initial_circulation(sb_batch* b, const double* gamma, size_t n) {
+    if (!b || !gamma) return null_arg();
+    return guard([&] {
+        if (static_cast<long long>(n) != b->N_total) raise(SB_ERR_SIZE, "circulation length mismatch");
+        ck(cudaMemcpyAsync(b->gamma_all.p, gamma, n * sizeof(double), cudaMemcpyHostToDevice, b->main), "H2D");
+        ck(cudaStreamSynchronize(b->main), "sync");
+    });
+}
+
+int sb_batch_set_initial_circulation_device(sb_batch* b, const double* gamma_dev, size_t n) {
+    if (!b || !gamma_dev) return null_arg();
+    return guard([&] {
+        if (static_cast<long long>(n) != b->N_total) raise(SB_ERR_SIZE, "circulation length mismatch");
+        ck(cudaMemcpyAsync(b->gamma_all.p, gamma_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, b->main), "D2D");
+        ck(cudaStreamSynchronize(b->main), "sync");
+    });
+}
+
+int sb_batch_previous_circulation_device(sb_batch* b, double** gamma_dev) {
+    if (!b || !gamma_dev) return null_arg();
+    *gamma_dev = b->gamma_all.p;
+    return SB_OK;
+}
+
+int sb_batch_set_precision(sb_batch* b, int mode) {
+    if (!b) return null_arg();
+    if (mode < 0 || mode > 2) {
+        report_error(SB_ERR_SIZE, "precision mode must be 0, 1 or 2");
+        return SB_ERR_SIZE;
+    }
+    return guard([&] {
+        if (mode != b->precision) {
+            b->precision = mode;
+            b->plan(b->tuning);
+        }
+    });
+}
+
+int sb_batch_use_graph(sb_batch* b, int enable) {
+    if (!b) return null_arg();
+    b->use_graph = enable != 0;
+    if (!b->use_graph) b->drop_graphs();
+    return SB_OK;
+}
+
+int sb_batch_autotune(sb_batch* b, double budget_seconds) {
+    if (!b) return null_arg();
+    return guard([&] { b->autotune(budget_seconds > 0.0 ? budget_seconds : 5.0); });
+}
+
+int sb_batch_info(const sb_batch* b, double* info, size_t n) {
+    if (!b || !info) return null_arg();
+    long long items = 0;
+    int grid = 0;
+    for (const auto& g : b->groups) {
+        if (g.kind == 1) {
+            items += g.items;
+            grid = std::max(grid, g.grid);
+        }
+    }
+    const double v[SB_BATCH_INFO] = {b->last_ms,
+                                     static_cast<double>(b->last_pairs),
+                                     static_cast<double>(b->tuning.waves),
+                                     static_cast<double>(b->tuning.blocks_per_sm),
+                                     static_cast<double>(grid),
+                                     static_cast<double>(items),
+                                     b->tuned ? 1.0 : 0.0,
+                                     static_cast<double>(b->tune_candidates),
+                                     b->tune_best_ms,
+                                     (b->graph[0] || b->graph[1]) ? 1.0 : 0.0,
+                                     static_cast<double>(b->steps)};
+    for (size_t i = 0; i < n && i < SB_BATCH_INFO; ++i) info[i] = v[i];
+    return SB_OK;
+}
+
+}  // extern "C"

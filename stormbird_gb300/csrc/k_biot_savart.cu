@@ -208,8 +208,20 @@ __device__ __forceinline__ void ring2(const float* v, float2 ex, float2 ey, floa
     }
 }
 
+// Job holding global item `item` of a batched launch: the last job whose first item is
+// at or before it (item_begin ascending, jobs[0].item_begin == 0).
+__device__ __forceinline__ int find_job(const BsJob* jobs, int n, long long item) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].item_begin <= item) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 template <class R, int T, bool KAHAN, int SYM, bool NEGLECT>
-__global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
+__global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
     constexpr int TILE = TileSize<R>::value;
     constexpr int TT = SYM ? 2 * T : T;  // mirrored targets ride along as extra targets
     constexpr bool F32 = sizeof(R) == 4;
@@ -217,6 +229,7 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
     __shared__ __align__(128) PanelRec<R> tile[2][TILE];
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ long long s_item;
+    __shared__ BsJob s_job;  // the current item's sweep (one copy per item, by thread 0)
 
     const int tid = threadIdx.x;
     if (tid == 0) {
@@ -226,21 +239,27 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
     }
     __syncthreads();
     uint32_t phase0 = 0, phase1 = 0;
-    const PanelRec<R>* P = reinterpret_cast<const PanelRec<R>*>(a.panels);
-    const long long n_items = a.n_ttiles * static_cast<long long>(a.n_chunks);
+    const long long n_items = a.jobs ? a.jobs[a.n_jobs].item_begin : a.job0.n_ttiles * static_cast<long long>(a.job0.n_chunks);
     constexpr int TM = kBsThreads * T;
 
     while (true) {
-        if (tid == 0) s_item = atomicAdd(a.work_counter, 1ULL);
+        __syncthreads();  // every thread is done with the previous item's s_item and s_job
+        if (tid == 0) {
+            const long long it = static_cast<long long>(atomicAdd(a.work_counter, 1ULL));
+            s_item = it;
+            if (it < n_items) s_job = a.jobs ? a.jobs[find_job(a.jobs, a.n_jobs, it)] : a.job0;
+        }
         __syncthreads();
         const long long item = s_item;
-        __syncthreads();
         if (item >= n_items) break;
+        const BsJob& J = s_job;
+        const long long local = item - J.item_begin;
+        const PanelRec<R>* P = reinterpret_cast<const PanelRec<R>*>(J.panels);
         // chunk-major order: CTAs running together share a source chunk in L2
-        const int chunk = static_cast<int>(item / a.n_ttiles);
-        const long long ttile = item % a.n_ttiles;
-        const long long pb = a.p_begin + static_cast<long long>(chunk) * a.chunk_panels;
-        const long long pe = min(pb + static_cast<long long>(a.chunk_panels), a.p_end);
+        const int chunk = static_cast<int>(local / J.n_ttiles);
+        const long long ttile = local % J.n_ttiles;
+        const long long pb = J.p_begin + static_cast<long long>(chunk) * J.chunk_panels;
+        const long long pe = min(pb + static_cast<long long>(J.chunk_panels), J.p_end);
 
         // targets: float-float pairs (FP32) or doubles (FP64 path, lo parts 0)
         R xh[TT], yh[TT], zh[TT], xl[TT], yl[TT], zl[TT];
@@ -249,9 +268,9 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
 #pragma unroll
         for (int t = 0; t < T; ++t) {
             long long idx = ttile * TM + static_cast<long long>(t) * kBsThreads + tid;
-            valid[t] = idx < a.M;
-            d3 p = valid[t] ? a.targets[idx] : mk(0, 0, 0);
-            tw[t] = (NEGLECT && valid[t]) ? a.target_wing[idx] : -1;
+            valid[t] = idx < J.M;
+            d3 p = valid[t] ? J.targets[idx] : mk(0, 0, 0);
+            tw[t] = (NEGLECT && valid[t]) ? J.target_wing[idx] : -1;
             d3 q[2] = {p, SYM ? mirror(SYM, p) : p};
 #pragma unroll
             for (int m = 0; m < (SYM ? 2 : 1); ++m) {
@@ -391,7 +410,7 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
 #pragma unroll
         for (int t = 0; t < T; ++t) {
             long long idx = ttile * TM + static_cast<long long>(t) * kBsThreads + tid;
-            if (idx < a.M) {
+            if (idx < J.M) {
                 d3 u = mk(static_cast<double>(sx[t]) + static_cast<double>(cx[t]),
                           static_cast<double>(sy[t]) + static_cast<double>(cy[t]),
                           static_cast<double>(sz[t]) + static_cast<double>(cz[t]));
@@ -401,7 +420,7 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(BsArgs a) {
                               static_cast<double>(sz[T + t]) + static_cast<double>(cz[T + t]));
                     u = sym_correct(SYM, u, m);
                 }
-                double* o = a.partial + (static_cast<long long>(chunk) * a.M + idx) * 3;
+                double* o = J.partial + (static_cast<long long>(chunk) * J.M + idx) * 3;
                 o[0] = u.x;
                 o[1] = u.y;
                 o[2] = u.z;
@@ -429,6 +448,35 @@ __global__ void k_bs_reduce(const double* partial, int n_chunks, long long M, lo
         b.z += s2;
     }
     out[i] = b;
+}
+
+// The same reduction for every job of a batched sweep: block b belongs to the last job whose
+// block_begin is at or before it.
+__global__ void __launch_bounds__(kBsReduceThreads) k_bs_reduce_jobs(const BsJob* jobs, int n_jobs) {
+    const long long b = blockIdx.x;
+    int lo = 0, hi = n_jobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].block_begin <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    const BsJob& J = jobs[lo];
+    const long long i = (b - J.block_begin) * kBsReduceThreads + threadIdx.x;
+    if (i >= J.M_total) return;
+    d3 v = J.base ? J.base[i] : mk(0, 0, 0);
+    if (i < J.M) {
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+        for (int k = 0; k < J.n_chunks; ++k) {
+            const double* p = J.partial + (static_cast<long long>(k) * J.M + i) * 3;
+            s0 += p[0];
+            s1 += p[1];
+            s2 += p[2];
+        }
+        v.x += s0;
+        v.y += s1;
+        v.z += s2;
+    }
+    J.out[i] = v;
 }
 
 // frozen_wake.rs:198-249: factors[c][p] = unit velocity of first-row panel p at control point c
@@ -557,6 +605,12 @@ cudaError_t launch_bs_reduce(const double* partial, int n_chunks, long long M, l
     int threads = 256;
     long long blocks = (M_total + threads - 1) / threads;
     k_bs_reduce<<<static_cast<unsigned>(blocks), threads, 0, s>>>(partial, n_chunks, M, M_total, base, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bs_reduce_jobs(const BsJob* jobs, int n_jobs, long long blocks, cudaStream_t s) {
+    if (n_jobs <= 0 || blocks <= 0) return cudaSuccess;
+    k_bs_reduce_jobs<<<static_cast<unsigned>(blocks), kBsReduceThreads, 0, s>>>(jobs, n_jobs);
     return cudaGetLastError();
 }
 

@@ -114,15 +114,15 @@ extern "C" int sb_panel_sweep_no_alloc(int device, const double* corners, const 
     const int n_chunks = static_cast<int>((P + chunk - 1) / chunk);
 
     BsArgs a;
-    a.panels = rec;
-    a.p_begin = 0;
-    a.p_end = P;
-    a.targets = reinterpret_cast<const d3*>(targets);
-    a.M = M;
-    a.chunk_panels = static_cast<int>(chunk);
-    a.n_chunks = n_chunks;
-    a.n_ttiles = n_ttiles;
-    a.partial = partial;
+    a.job0.panels = rec;
+    a.job0.p_begin = 0;
+    a.job0.p_end = P;
+    a.job0.targets = reinterpret_cast<const d3*>(targets);
+    a.job0.M = M;
+    a.job0.chunk_panels = static_cast<int>(chunk);
+    a.job0.n_chunks = n_chunks;
+    a.job0.n_ttiles = n_ttiles;
+    a.job0.partial = partial;
     a.work_counter = counter;
     a.err = err;
     a.symmetry = symmetry;

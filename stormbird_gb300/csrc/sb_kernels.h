@@ -13,7 +13,8 @@ namespace sbgpu {
 constexpr int kBsThreads = 128;  // threads per Biot-Savart CTA
 
 // One Biot-Savart sweep: velocities at M targets induced by panels [p_begin, p_end).
-struct BsArgs {
+// Its work items are (source chunk, target tile) pairs, chunk-major.
+struct BsJob {
     const void* panels = nullptr;      // PanelRec<float> or PanelRec<double>
     long long p_begin = 0, p_end = 0;
     const d3* targets = nullptr;       // [M] f64 positions
@@ -23,11 +24,28 @@ struct BsArgs {
     int n_chunks = 1;
     long long n_ttiles = 0;            // target tiles of kBsThreads * T targets
     double* partial = nullptr;         // [n_chunks][M][3]
+    long long item_begin = 0;          // first item of this sweep in a batched launch
+    // reduction (batched launches): out[i] = base[i] + sum over chunks, base only for i >= M
+    long long M_total = 0;
+    const d3* base = nullptr;
+    d3* out = nullptr;
+    long long block_begin = 0;         // first block of this sweep in the batched reduce
+};
+
+// A sweep launch: one job (job0, jobs == nullptr) or a list of jobs in device memory
+// whose items are handed out in list order (the batch puts the costliest items first).
+// The list ends with a sentinel entry whose item_begin is the number of items of all jobs.
+struct BsArgs {
+    BsJob job0;
+    const BsJob* jobs = nullptr;       // [n_jobs + 1] device memory
+    int n_jobs = 0;
     unsigned long long* work_counter = nullptr;  // zero before launch
     int* err = nullptr;
     int symmetry = 0;
     int neglect = 0;
 };
+
+constexpr int kBsReduceThreads = 256;
 
 int bs_targets_per_thread(int symmetry);
 int bs_tile_panels(int precision);
@@ -35,6 +53,9 @@ int bs_occupancy_blocks_per_sm(int precision, int symmetry, int neglect);
 cudaError_t launch_bs_sweep(const BsArgs& a, int precision, int grid, cudaStream_t s);
 cudaError_t launch_bs_reduce(const double* partial, int n_chunks, long long M, long long M_total, const d3* base, d3* out,
                              cudaStream_t s);
+// Reduction of every job of a batched sweep; blocks = sum over jobs of
+// ceil(M_total / kBsReduceThreads), job k starting at its block_begin.
+cudaError_t launch_bs_reduce_jobs(const BsJob* jobs, int n_jobs, long long blocks, cudaStream_t s);
 cudaError_t launch_unit_matrix(const PanelRec<double>* row0, const d3* ctrl, int N, int sym, int neglect,
                                const int* wing_of_line, d3* factors, cudaStream_t s);
 // Quasi-steady horseshoe matrix; core_kind 0 relative, 1 absolute, 2 none.

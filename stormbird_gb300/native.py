@@ -51,6 +51,23 @@ SIGNATURES = [
     ("sb_panel_sweep_no_alloc", ctypes.c_int, [ctypes.c_int, _vp, _vp, _vp, ctypes.c_size_t, ctypes.c_double,
                                                ctypes.c_int, _vp, ctypes.c_size_t, _vp, _vp]),
     ("sb_measure_fp32_peak", ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp]),
+    ("sb_batch_new", _vp, [ctypes.POINTER(ctypes.c_char_p), ctypes.c_size_t, ctypes.c_int]),
+    ("sb_batch_free", None, [_vp]),
+    ("sb_batch_sizes", ctypes.c_int, [_vp, _szp, _szp, _szp]),
+    ("sb_batch_case_sizes", ctypes.c_int, [_vp, ctypes.c_size_t, _szp, _szp, _szp, _szp, _szp]),
+    ("sb_batch_get_freestream_points", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
+    ("sb_batch_do_step", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double, _dp, ctypes.c_size_t]),
+    ("sb_batch_do_step_device", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double, _vp, ctypes.c_size_t]),
+    ("sb_batch_get_circulation", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
+    ("sb_batch_get_summary", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
+    ("sb_batch_read_case_output", ctypes.c_int, [_vp, ctypes.c_size_t, ctypes.POINTER(StepOutput)]),
+    ("sb_batch_set_initial_circulation", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
+    ("sb_batch_set_initial_circulation_device", ctypes.c_int, [_vp, _vp, ctypes.c_size_t]),
+    ("sb_batch_previous_circulation_device", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_void_p)]),
+    ("sb_batch_set_precision", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("sb_batch_use_graph", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("sb_batch_autotune", ctypes.c_int, [_vp, ctypes.c_double]),
+    ("sb_batch_info", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
 ]
 
 _LIB = None

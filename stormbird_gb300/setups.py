@@ -226,3 +226,30 @@ def synthetic_sail_row_wake(nr_sails=4, panels_per_sail=64, wake_rows=300, time_
     strengths = np.array(gam)
     cores = np.full(len(strengths), 0.1 * CHORD)
     return corners, strengths, cores, pts.reshape(-1, 3)
+
+
+def uneven_cases(n_cases, seed=0, sails=(1, 6), panels=(16, 96), wake_rows=(50, 400), awa_deg=(20.0, 180.0),
+                 wind_speed=(5.0, 20.0), time_step=0.05, gust_amplitude=1.5, **kw):
+    """Independent dynamic cases drawn uniformly (seeded): apparent wind angle, wind speed,
+    sail count, panels per sail and wake length, each sail row otherwise as wing_sail_row.
+
+    Returns [(setup_json, GustyWind)], one per case; integer ranges are inclusive.
+    """
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_cases):
+        awa = float(rng.uniform(*awa_deg))
+        u = float(rng.uniform(*wind_speed))
+        s = int(rng.integers(sails[0], sails[1] + 1))
+        p = int(rng.integers(panels[0], panels[1] + 1))
+        w = int(rng.integers(wake_rows[0], wake_rows[1] + 1))
+        js = wing_sail_row(nr_sails=s, panels_per_sail=p, wake_rows=w, time_step=time_step, wind_speed=u,
+                           apparent_wind_angle_deg=awa, **kw)
+        out.append((js, GustyWind(wind_speed=u, apparent_wind_angle_deg=awa, gust_amplitude=gust_amplitude,
+                                  seed=int(rng.integers(0, 2**31)))))
+    return out
+
+
+def batch_freestream(batch, winds, t: float) -> np.ndarray:
+    """Freestream of every case of a Batch at time t, case after case."""
+    return np.concatenate([w.freestream(t, c["freestream_points"]) for w, c in zip(winds, batch.cases)])
