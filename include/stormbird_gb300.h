@@ -228,8 +228,9 @@ int sb_measure_fp32_peak(int device, int reps, double* tflops);
 typedef struct sb_batch sb_batch;
 
 /* Per-case summary after a step: force sum [3], moment sum [3], residual, iterations,
- * converged (0/1), device status word (0 = ok). */
-#define SB_BATCH_SUMMARY 10
+ * converged (0/1), device status word (0 = ok), warm start (1 = the network's candidate
+ * was the initial solution, 0 = the plain start had the lower residual, -1 = no candidate). */
+#define SB_BATCH_SUMMARY 11
 /* sb_batch_info fields: last step ms, panel-target pairs swept in the last step, tuning
  * waves, tuning CTAs per SM (0 = occupancy limit), roll-up grid, roll-up work items,
  * tuned (0/1), candidates timed, best tuned roll-up ms, graph in use (0/1), steps done. */
@@ -269,6 +270,42 @@ int sb_batch_use_graph(sb_batch* batch, int enable);
  * same workload bucket in this process. Needs a batch whose roll-up has started. */
 int sb_batch_autotune(sb_batch* batch, double budget_seconds);
 int sb_batch_info(const sb_batch* batch, double* info, size_t n);
+
+/* ===================================================================================
+ * Learned warm start. No counterpart in the reference, which starts every solve from the
+ * previous step's circulation (simulation.rs:165,189; simple_iterative.rs:86-101). A network
+ * (4 hidden layers of 256, GELU, BF16 weights on the tensor cores with FP32 accumulation)
+ * predicts, per panel, the change of the step's solution from per-panel features the batch
+ * builds on the GPU. The SimpleIterative solve then evaluates the residual of the plain
+ * start and of the prediction and starts from the lower one, so the solver stays the judge
+ * of the result; the batch reports per case which start was taken.
+ * =================================================================================== */
+typedef struct sb_mlp sb_mlp;
+/* Number of per-panel features the batch builds (the network's input size for mode 1). */
+#define SB_WARM_START_FEATURES 16
+/* A network with n_inputs (1..64) inputs, He-uniform weights from `seed`. */
+sb_mlp* sb_mlp_new(int device, int n_inputs, unsigned long long seed);
+void sb_mlp_free(sb_mlp* network);
+int sb_mlp_num_params(const sb_mlp* network, size_t* n);
+/* Parameters (FP32 master copy) in the order W1 [256][64], b1, W2 [256][256], b2, W3, b3,
+ * W4, b4, w_out [256], b_out. */
+int sb_mlp_get_params(sb_mlp* network, float* params, size_t n);
+int sb_mlp_set_params(sb_mlp* network, const float* params, size_t n);
+/* y [rows] = network(x [rows][n_inputs]); device pointers. */
+int sb_mlp_forward(sb_mlp* network, const float* x_dev, size_t rows, float* y_dev);
+/* Mean-squared-error loss and its gradient (host buffer [num_params]) on device data. */
+int sb_mlp_gradients(sb_mlp* network, const float* x_dev, const float* target_dev, size_t rows, float* grads,
+                     double* loss);
+/* One Adam step (beta 0.9 / 0.999) on device data; `loss` (may be NULL) gets the batch's
+ * loss before the update. */
+int sb_mlp_train_step(sb_mlp* network, const float* x_dev, const float* target_dev, size_t rows, float learning_rate,
+                      double* loss);
+/* Warm start of a batch: mode 0 off, 1 the network's candidates (SimpleIterative cases),
+ * 2 features and targets recorded each step without a candidate (training data). */
+int sb_batch_set_warm_start(sb_batch* batch, sb_mlp* network, int mode);
+/* The last step's features [total_lines][SB_WARM_START_FEATURES] and targets [total_lines]
+ * (device or host pointers; either may be NULL). */
+int sb_batch_copy_warm_start_data(sb_batch* batch, float* features, float* targets, size_t rows);
 
 #ifdef __cplusplus
 }

@@ -15,7 +15,7 @@ import numpy as np
 from ._abi import SB_ERR_BAD_JSON, OutputBuffers, SbError, as_ptr, vec3_array
 from .native import lib
 
-SUMMARY = 10  # SB_BATCH_SUMMARY
+SUMMARY = 11  # SB_BATCH_SUMMARY
 INFO_KEYS = ("last_step_ms", "pairs", "waves", "blocks_per_sm", "rollup_grid", "rollup_items", "tuned",
              "tune_candidates", "tune_best_ms", "graph", "steps")
 
@@ -84,7 +84,8 @@ class Batch:
         return out
 
     def summary(self) -> np.ndarray:
-        """[n_cases, 10]: force sum (3), moment sum (3), residual, iterations, converged, status."""
+        """[n_cases, 11]: force sum (3), moment sum (3), residual, iterations, converged, status,
+        warm start taken (1 candidate, 0 plain start, -1 no candidate)."""
         out = np.zeros((self.n_cases, SUMMARY))
         _check(lib().sb_batch_get_summary(self._h, as_ptr(out), out.size))
         return out

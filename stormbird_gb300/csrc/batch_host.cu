@@ -11,6 +11,10 @@
 //      costliest items first, taken from one atomic counter (k_bs_sweep with a job list);
 //   4. the per-case solves and force kernels on the pool streams, then one gather kernel
 //      that packs every case's circulation and force summary for one device->host copy.
+// With a warm-start network attached, the per-panel features of every case, the network's
+// forward pass and the candidate initial solutions run on the main stream between 2 and 4;
+// each case's solve starts from the candidate or from the plain start, whichever has the
+// lower residual (k_solve_si), and the change of the solution is kept as a training target.
 // After three steps (when the step's kernel arguments stop changing except for the wake
 // buffer parity) the whole step is captured into a CUDA graph per parity and replayed; the
 // work lists are refreshed through the graph's copy node from pinned host memory.
@@ -27,6 +31,7 @@
 #include <numeric>
 #include <tuple>
 
+#include "sb_mlp.h"
 #include "sim_core.hpp"
 
 namespace {
@@ -40,6 +45,7 @@ struct GatherJob {
     long long fsum = 0, msum = 0, residual = 0, iterations = 0, converged = 0;
     int N = 0;
     const int* err = nullptr;
+    const double* scalars = nullptr;  // solver scalars ([4]: start taken)
     double* gamma_dst = nullptr;
     double* summary_dst = nullptr;
 };
@@ -58,6 +64,7 @@ __global__ void k_gather(const GatherJob* jobs) {
         s[7] = g.out[g.iterations];
         s[8] = g.out[g.converged];
         s[9] = static_cast<double>(*g.err);
+        s[10] = g.scalars[4];
     }
 }
 
@@ -119,6 +126,15 @@ struct sb_batch {
     DevBuf<unsigned long long> counters;
     DevBuf<int> err;
     PinnedBuf<int> h_err;
+
+    // warm start: 0 off, 1 network candidates, 2 features and targets only (training data)
+    sb_mlp* mlp = nullptr;
+    int warm_mode = 0;
+    DevBuf<float> w_feat, w_y, w_target;
+    DevBuf<double> w_q, w_g0, w_cand, w_gamma_old;
+    DevBuf<d3> w_fs_old;
+    PinnedBuf<FeatJob> h_feat;
+    DevBuf<FeatJob> d_feat;
 
     bool use_graph = true;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -203,6 +219,7 @@ struct sb_batch {
             g.converged = c.L.converged;
             g.N = c.N;
             g.err = c.err.p;
+            g.scalars = c.scalars.p;
             g.gamma_dst = compact.p + line_off[i];
             g.summary_dst = compact.p + N_total + static_cast<long long>(i) * SB_BATCH_SUMMARY;
             gj.push_back(g);
@@ -418,11 +435,14 @@ struct sb_batch {
         fork(0);
         for (auto& c : cases) c->step_begin(time, dt);
         join(0);
+        if (warm_mode != 0) warm_start_before_solve();
         sweeps(0);
         for (auto& c : cases) if (c->dynamic) c->after_fixed_sweep();
         fork(1);
         for (auto& c : cases) c->step_matrix_and_solve();
         join(1);
+        if (warm_mode != 0)
+            ck(launch_batch_targets(gamma_all.p, w_q.p, w_g0.p, N_total, w_target.p, main), "warm-start targets");
         sweeps(1);
         for (auto& c : cases) if (c->dynamic) c->after_rollup_sweep();
         fork(2);
@@ -433,6 +453,81 @@ struct sb_batch {
         const size_t ncomp = static_cast<size_t>(N_total) + cases.size() * SB_BATCH_SUMMARY;
         ck(cudaMemcpyAsync(h_compact.p, compact.p, ncomp * sizeof(double), cudaMemcpyDeviceToHost, main), "D2H summary");
         ck(cudaMemcpyAsync(h_err.p, err.p, sizeof(int), cudaMemcpyDeviceToHost, main), "D2H status");
+    }
+
+    // ------------------------------------------------------------------ warm start
+    void set_warm_start(sb_mlp* m, int mode) {
+        if (mode < 0 || mode > 2) raise(SB_ERR_SIZE, "warm-start mode must be 0, 1 or 2");
+        if (mode == 1 && !m) raise(SB_ERR_NULL_ARG, "warm-start mode 1 needs a network");
+        if (mode == 1 && mlp_inputs(m) != kMlpFeatures)
+            raise(SB_ERR_SIZE, "the warm-start network must take " + std::to_string(kMlpFeatures) + " inputs");
+        for (const auto& c : cases)
+            if (mode != 0 && c->solver_kind != 0) raise(SB_ERR_UNSUPPORTED, "the warm start needs SimpleIterative solvers");
+        ck(cudaStreamSynchronize(main), "sync");
+        drop_graphs();
+        if (mode != 0 && w_feat.n == 0) {
+            w_feat.alloc(static_cast<size_t>(N_total) * kMlpFeatures);
+            w_y.alloc(N_total);
+            w_target.alloc(N_total);
+            w_q.alloc(N_total);
+            w_g0.alloc(N_total);
+            w_cand.alloc(N_total);
+            w_gamma_old.alloc(N_total);
+            w_fs_old.alloc(N_total);
+            ck(cudaMemset(w_target.p, 0, N_total * sizeof(float)), "memset");
+            h_feat.alloc(cases.size());
+            d_feat.alloc(cases.size());
+        }
+        if (mode == 1) mlp_reserve(m, N_total);
+        mlp = mode == 1 ? m : nullptr;
+        warm_mode = mode;
+        for (size_t i = 0; i < cases.size(); ++i)
+            cases[i]->candidate_p = mode == 1 ? w_cand.p + line_off[i] : nullptr;
+    }
+
+    // Feature jobs of this step (host; steps completed before the step).
+    void fill_feature_jobs() {
+        for (size_t i = 0; i < cases.size(); ++i) {
+            const sb_sim& c = *cases[i];
+            FeatJob f;
+            f.fs = c.fs_p;
+            f.gamma = c.gamma_p;
+            f.gamma_old = w_gamma_old.p + line_off[i];
+            f.fs_old = w_fs_old.p + line_off[i];
+            f.chord = c.chord_global.p;
+            f.span_s = c.span_s.p;
+            f.span_e = c.span_e.p;
+            f.chord_len = c.chord_len.p;
+            f.wing_of_line = c.wing_of_line.p;
+            f.wing_start = c.wing_start.p;
+            f.wing_end = c.wing_end.p;
+            f.N = c.N;
+            f.S = c.S;
+            f.W = c.W;
+            f.steps = c.dynamic ? c.steps_completed : c.fd_count;
+            f.row0 = line_off[i];
+            h_feat.p[i] = f;
+        }
+    }
+
+    void warm_start_before_solve() {
+        ck(cudaMemcpyAsync(d_feat.p, h_feat.p, cases.size() * sizeof(FeatJob), cudaMemcpyHostToDevice, main),
+           "H2D feature jobs");
+        ck(launch_batch_features(d_feat.p, static_cast<int>(cases.size()), N_total, w_feat.p, w_q.p, w_g0.p, main),
+           "warm-start features");
+        if (warm_mode == 1) {
+            mlp_forward_async(mlp, w_feat.p, N_total, w_y.p, main);
+            ck(launch_batch_candidate(w_y.p, w_q.p, w_g0.p, N_total, w_cand.p, main), "warm-start candidate");
+        }
+    }
+
+    void copy_warm_start_data(float* feat, float* target, size_t rows) {
+        if (warm_mode == 0) raise(SB_ERR_STATE, "the batch records no warm-start data (mode 0)");
+        if (static_cast<long long>(rows) != N_total) raise(SB_ERR_SIZE, "rows must equal the batch's span lines");
+        if (feat)
+            ck(cudaMemcpyAsync(feat, w_feat.p, rows * kMlpFeatures * sizeof(float), cudaMemcpyDefault, main), "copy");
+        if (target) ck(cudaMemcpyAsync(target, w_target.p, rows * sizeof(float), cudaMemcpyDefault, main), "copy");
+        ck(cudaStreamSynchronize(main), "copy");
     }
 
     // Host state a replayed graph step leaves behind (the same as enqueue's bookkeeping).
@@ -469,6 +564,7 @@ struct sb_batch {
             c->ensure_rec64();  // FP64 records (allocation) before any capture
         }
         if (graph_dt != dt || graph_precision != precision) drop_graphs();
+        if (warm_mode != 0) fill_feature_jobs();
         // the parity of the wake buffers at the start of the step selects the graph
         const int parity = any_dynamic ? first_dynamic().cur : (steps & 1);
         ck(cudaEventRecord(ev_t0, main), "event");
@@ -506,6 +602,7 @@ struct sb_batch {
         cudaEventElapsedTime(&ms, ev_t0, ev_t1);
         last_ms = ms;
         steps += 1;
+        if (mlp) mlp_check(mlp);
         if (h_err.p[0] != kDevOk) {
             ck(cudaMemset(err.p, 0, sizeof(int)), "memset");
             raise(SB_ERR_TIMEOUT, "a bounded device-side wait ran out in a batched sweep");
@@ -758,6 +855,16 @@ int sb_batch_use_graph(sb_batch* b, int enable) {
 int sb_batch_autotune(sb_batch* b, double budget_seconds) {
     if (!b) return null_arg();
     return guard([&] { b->autotune(budget_seconds > 0.0 ? budget_seconds : 5.0); });
+}
+
+int sb_batch_set_warm_start(sb_batch* b, sb_mlp* network, int mode) {
+    if (!b) return null_arg();
+    return guard([&] { b->set_warm_start(network, mode); });
+}
+
+int sb_batch_copy_warm_start_data(sb_batch* b, float* features, float* targets, size_t rows) {
+    if (!b) return null_arg();
+    return guard([&] { b->copy_warm_start_data(features, targets, rows); });
 }
 
 int sb_batch_info(const sb_batch* b, double* info, size_t n) {

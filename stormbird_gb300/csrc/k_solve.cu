@@ -138,12 +138,8 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve_si(DevModel m, SolveSet
     }
     cl.sync();
 
-    int it = 0, cur = 0;
-    bool conv = false;
-    while (it < st.max_iterations && !conv) {
-        it += 1;
-        const double* Gc = G[cur];
-        // 1. induced velocity of own rows
+    // induced velocity of own rows for the circulation Gc: fixed + M * Gc
+    auto induced_rows = [&](const double* Gc) {
         for (int row = r0 + warp; row < r1; row += nwarps) {
             const d3* fr = b.factors + static_cast<long long>(row) * N;
             double sx = 0.0, sy = 0.0, sz = 0.0;
@@ -166,6 +162,52 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve_si(DevModel m, SolveSet
             }
         }
         __syncthreads();
+    };
+
+    // Guarded warm start: residual (simple_iterative.rs:160-176) of the plain start G[0]
+    // and of the candidate, the lower one (finite) becomes the initial solution.
+    if (b.candidate) {
+        for (int i = tid; i < N; i += kSolveThreads) G[1][i] = b.candidate[i];
+        __syncthreads();
+        double rs[2];
+        for (int v = 0; v < 2; ++v) {
+            induced_rows(G[v]);
+            for (int k = 0; k < nrows; ++k) {
+                int i = r0 + tid + k * kSolveThreads;
+                const RowGeom& g = rg[k];
+                const FoilP f = m.foils[g.wing];
+                d3 u = total_velocity(st, g.felt, uind[i - r0]);
+                u = u - project(u, g.span_rel);
+                double aoa = len(u) > kMinPositive ? signed_angle_between(g.chord, u, g.span_dir) : 0.0;
+                double r = residual_term(m, g, f, G[v][i], u, aoa);
+                for (int q = 0; q < CS; ++q) cl.map_shared_rank(RR[0], q)[i] = r;
+            }
+            cl.sync();
+            if (tid == 0) {
+                double s = 0.0;
+                for (int i = 0; i < N; ++i) s += RR[0][i];
+                s_res = s;
+            }
+            __syncthreads();
+            rs[v] = s_res;
+            cl.sync();  // RR[0] is written again by the next pass or the first iteration
+        }
+        const bool take = isfinite(rs[1]) && rs[1] < rs[0];
+        if (take)
+            for (int i = tid; i < N; i += kSolveThreads) G[0][i] = G[1][i];
+        if (rank == 0 && tid == 0) b.scalars[4] = take ? 1.0 : 0.0;
+        cl.sync();  // G[1] is written through distributed shared memory by the first iteration
+    } else if (rank == 0 && tid == 0) {
+        b.scalars[4] = -1.0;
+    }
+
+    int it = 0, cur = 0;
+    bool conv = false;
+    while (it < st.max_iterations && !conv) {
+        it += 1;
+        const double* Gc = G[cur];
+        // 1. induced velocity of own rows
+        induced_rows(Gc);
         // 2. row updates
         double lmax = 0.0;
         for (int k = 0; k < nrows; ++k) {

@@ -118,11 +118,16 @@ struct SolveBuffers {
     const d3* factors = nullptr;    // [N][N]
     double* gamma_prev = nullptr;   // [N] in: initial solution, out: solution
     d3* vel_out = nullptr;          // [N] output control-point velocity
-    double* scalars = nullptr;      // [4]: residual, iterations, converged, status
+    double* scalars = nullptr;      // [8]: residual, iterations, converged, singular, start (below)
     double* lin_work = nullptr;     // [N*(N+1)] Gaussian elimination scratch (linearized)
     double* wake_str_row0 = nullptr;        // strengths row 0 (dynamic) or nullptr
     PanelRec<float>* rec32_row0 = nullptr;  // FP32 record row 0 (dynamic) or nullptr
     PanelRec<double>* rec64_row0 = nullptr; // FP64 record row 0 in the FP64 sweep mode
+    // Optional second initial solution (a predicted warm start). The solve evaluates the
+    // residual of the plain start and of the candidate and starts from the lower one;
+    // scalars[4] = 1 when the candidate was taken, 0 when the plain start was (fallback),
+    // -1 without a candidate.
+    const double* candidate = nullptr;      // [N] or nullptr
     int* err = nullptr;
 };
 

@@ -294,6 +294,8 @@ struct sb_sim {
     // batch's contiguous buffers.
     d3* fs_p = nullptr;
     double* gamma_p = nullptr;
+    // Predicted initial solution [N] offered to the SimpleIterative solve, or nullptr.
+    const double* candidate_p = nullptr;
 
     ~sb_sim() {
         for (auto& e : ev) if (e) cudaEventDestroy(e);
@@ -464,10 +466,10 @@ struct sb_sim {
         ck(cudaMemset(fixed.p, 0, N * sizeof(d3)), "memset");
         counters.alloc(4); err.alloc(4);
         ck(cudaMemset(err.p, 0, 4 * sizeof(int)), "memset");
-        gamma_prev.alloc(N); gamma_tmp.alloc(N); scalars.alloc(4);
+        gamma_prev.alloc(N); gamma_tmp.alloc(N); scalars.alloc(8);
         ck(cudaMemset(gamma_prev.p, 0, N * sizeof(double)), "memset");
         gamma_p = gamma_prev.p;
-        ck(cudaMemset(scalars.p, 0, 4 * sizeof(double)), "memset");
+        ck(cudaMemset(scalars.p, 0, 8 * sizeof(double)), "memset");
         if (solver_kind == 1 || solve.start_with_linearized) lin_work.alloc(static_cast<size_t>(N) * (N + 1));
         vel_out.alloc(N); hist0.alloc(N); hist1.alloc(N);
         ck(cudaMemset(hist0.p, 0, N * sizeof(d3)), "memset");
@@ -717,6 +719,7 @@ struct sb_sim {
         sb.scalars = scalars.p;
         sb.lin_work = lin_work.p;
         sb.err = err.p;
+        sb.candidate = candidate_p;
         if (dynamic) {
             sb.wake_str_row0 = str[cur].p;
             sb.rec32_row0 = rec32.p;

@@ -16,6 +16,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libstormbird_gb300.so")
 
 # Every entry point of include/stormbird_gb300.h: (name, restype, argtypes)
 _dp = ctypes.POINTER(ctypes.c_double)
+_fp = ctypes.POINTER(ctypes.c_float)
 _szp = ctypes.POINTER(ctypes.c_size_t)
 _vp = ctypes.c_void_p
 SIGNATURES = [
@@ -68,6 +69,16 @@ SIGNATURES = [
     ("sb_batch_use_graph", ctypes.c_int, [_vp, ctypes.c_int]),
     ("sb_batch_autotune", ctypes.c_int, [_vp, ctypes.c_double]),
     ("sb_batch_info", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
+    ("sb_mlp_new", _vp, [ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong]),
+    ("sb_mlp_free", None, [_vp]),
+    ("sb_mlp_num_params", ctypes.c_int, [_vp, _szp]),
+    ("sb_mlp_get_params", ctypes.c_int, [_vp, _fp, ctypes.c_size_t]),
+    ("sb_mlp_set_params", ctypes.c_int, [_vp, _fp, ctypes.c_size_t]),
+    ("sb_mlp_forward", ctypes.c_int, [_vp, _vp, ctypes.c_size_t, _vp]),
+    ("sb_mlp_gradients", ctypes.c_int, [_vp, _vp, _vp, ctypes.c_size_t, _fp, _dp]),
+    ("sb_mlp_train_step", ctypes.c_int, [_vp, _vp, _vp, ctypes.c_size_t, ctypes.c_float, _dp]),
+    ("sb_batch_set_warm_start", ctypes.c_int, [_vp, _vp, ctypes.c_int]),
+    ("sb_batch_copy_warm_start_data", ctypes.c_int, [_vp, _vp, _vp, ctypes.c_size_t]),
 ]
 
 _LIB = None

@@ -1,0 +1,92 @@
+"""Warm-start network on the GPU (sb_mlp_*, tcgen05 BF16 GEMMs) and its use in a batch.
+
+  * forward pass and mean-squared-error gradients through the C ABI against the f64
+    restatement tests/mlp_ref.py with the GPU's BF16 roundings emulated (tolerances below:
+    FP32 tensor-core accumulation against f64, plus rare BF16 rounding flips);
+  * training with the library's Adam lowers the loss of a smooth regression;
+  * a network trained on data the batch itself records warm-starts held-out cases: the
+    results agree with the plain solves to within the solver tolerance, and the iteration
+    counts with and without the network are reported (the gain the network brings).
+"""
+import numpy as np
+import pytest
+
+from tests import mlp_ref as R
+
+pytestmark = pytest.mark.gpu
+
+TOL_Y = 5e-3      # relative infinity norm of the outputs
+TOL_GRAD = 1e-2   # relative L2 norm per parameter block
+
+
+def _net(seed=3):
+    from stormbird_gb300.warm_start import WarmStartNet
+
+    return WarmStartNet(16, seed=seed)
+
+
+def test_forward_matches_reference(gpu_lib):
+    torch = pytest.importorskip("torch")
+    net = _net()
+    p = net.get_params()
+    rng = np.random.default_rng(1)
+    x = rng.normal(size=(300, 16)).astype(np.float32)
+    y = net.forward(torch.from_numpy(x).cuda()).cpu().numpy()
+    yr, _, _ = R.forward(p.astype(np.float64), x.astype(np.float64), emulate=True)
+    err = np.max(np.abs(y - yr)) / np.max(np.abs(yr))
+    assert err <= TOL_Y, err
+
+
+def test_gradients_match_reference(gpu_lib):
+    torch = pytest.importorskip("torch")
+    net = _net(seed=5)
+    p = net.get_params().astype(np.float64)
+    rng = np.random.default_rng(2)
+    x = rng.normal(size=(1000, 16)).astype(np.float32)
+    t = rng.normal(size=1000).astype(np.float32)
+    g, loss = net.gradients(torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda())
+    loss_r, g_r = R.loss_and_grad(p, x.astype(np.float64), t.astype(np.float64), emulate=True)
+    assert abs(loss - loss_r) <= 1e-3 * loss_r
+    for name, sl in R.blocks():
+        a, b = g[sl].astype(np.float64), g_r[sl]
+        err = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+        assert err <= TOL_GRAD, (name, err)
+
+
+def test_training_lowers_the_loss(gpu_lib):
+    torch = pytest.importorskip("torch")
+    net = _net(seed=7)
+    rng = np.random.default_rng(3)
+    x = rng.uniform(-1, 1, size=(16384, 16)).astype(np.float32)
+    t = (np.sin(2 * x[:, 0]) + x[:, 1] * x[:, 2] - 0.5 * x[:, 3] ** 2).astype(np.float32)
+    X, T = torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda()
+    first = None
+    for epoch in range(40):
+        perm = torch.randperm(X.shape[0], device=X.device)
+        for s0 in range(0, X.shape[0], 4096):
+            idx = perm[s0:s0 + 4096]
+            loss = net.train_step(X[idx].contiguous(), T[idx].contiguous(), 2e-3)
+            if first is None:
+                first = loss
+    _, final = net.gradients(X, T)
+    assert final < 0.05 * first, (first, final)
+
+
+def test_warm_start_on_held_out_cases(gpu_lib):
+    pytest.importorskip("torch")
+    from stormbird_gb300 import setups as S
+    from stormbird_gb300 import warm_start as WS
+
+    def cases(n, seed):
+        cs = S.uneven_cases(n, seed, sails=(1, 3), panels=(6, 16), wake_rows=(8, 24), wind_speed=(6.0, 14.0))
+        return [(WS.tight_solver(js), w) for js, w in cs]
+
+    X, T = WS.collect(cases(24, seed=100), steps=24)
+    net = _net(seed=11)
+    losses = WS.train(net, X, T, epochs=30, batch_rows=2048, lr=1e-3)
+    assert losses[-1] < losses[0]
+    rep = WS.evaluate(net, cases(6, seed=200), steps=16)
+    print("warm start on held-out cases:", rep)
+    assert rep["max_rel_circulation_diff"] <= 1e-4
+    assert rep["iterations_warm"] <= 1.05 * rep["iterations_plain"]
+    assert 0.0 <= rep["fallback_rate"] <= 1.0
