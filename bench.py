@@ -327,12 +327,203 @@ def run_gb300(args):
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cb, _ = cpu_baseline_sweep(pts, strengths)
         line["cpu_baseline"] = cb
+    if args.batch_cases > 0:
+        del sim
+        torch.cuda.empty_cache()
+        line["batched"] = batched_solves(args, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+# --------------------------------------------------------------------------------------
+# batched uneven cases (solves/s): plain per-case loop vs batched, with and without warm start
+# --------------------------------------------------------------------------------------
+def batched_solves(args, device):
+    """Solves/s of uneven cases, one solve = one case advanced by one step.
+
+    Cases: seeded uniformly over apparent wind angle 20-180 deg, wind 5-20 m/s, 1-6 sails,
+    16-96 panels per sail and 50-400 wake rows, otherwise the sail-row case (reference
+    default far_field_ratio 5), SimpleIterative solved to a residual of 1e-7. Every arm runs
+    the same cases with the same freestream from a cold start, untimed for the first
+    `warm` steps, then times `steps` steps on the host clock through the public call,
+    host freestream in and results out:
+      plain   — one Simulation per case, sb_sim_do_step per case and step;
+      batched — one Batch, sb_batch_do_step (CUDA graph replay after 3 steps);
+      extrapolation — the Batch with candidate starts from linear extrapolation in time;
+      warm    — the Batch with the learned warm start (extrapolation + network correction),
+                the network trained first on data the batched solver records for other
+                seeds of the same distribution.
+    """
+    import torch
+
+    from stormbird_gb300 import Batch, Simulation
+    from stormbird_gb300 import setups as S
+    from stormbird_gb300 import warm_start as WS
+
+    n, warm, steps = args.batch_cases, 5, args.batch_steps
+    cases = [(WS.tight_solver(js), w) for js, w in S.uneven_cases(n, seed=2024)]
+    winds = [w for _, w in cases]
+    out = {"workload": f"{n} uneven dynamic cases (AWA 20-180 deg, 5-20 m/s, 1-6 sails, 16-96 panels, "
+                       f"50-400 wake rows, far_field_ratio 5, SimpleIterative to residual 1e-7), "
+                       f"steps {warm}-{warm + steps - 1} from a cold start",
+           "cases": n, "timed_steps": steps}
+
+    # train the network on other seeds
+    t0 = time.perf_counter()
+    X, T = WS.collect([(WS.tight_solver(js), w) for js, w in S.uneven_cases(args.train_cases, seed=77)],
+                      steps=warm + steps, device=device)
+    t_collect = time.perf_counter() - t0
+    net = WS.WarmStartNet(WS.FEATURES, seed=1, device=device)
+    t0 = time.perf_counter()
+    losses = WS.train(net, X, T, epochs=args.train_epochs, batch_rows=4096)
+    torch.cuda.synchronize()
+    out["training"] = {"rows": int(X.shape[0]), "cases": args.train_cases, "epochs": args.train_epochs,
+                       "collect_s": t_collect, "train_s": time.perf_counter() - t0,
+                       "loss_first_epoch": losses[0] if losses else None,
+                       "loss_last_epoch": losses[-1] if losses else None}
+    del X, T
+
+    results = {}
+    # plain: one simulation per case
+    sims = [Simulation(js, device=device) for js, _ in cases]
+    its, t_run = [], 0.0
+    for k in range(warm + steps):
+        fss = [w.freestream(k * DT, s.nr_freestream_points) for s, w in zip(sims, winds)]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rs = [s.do_step(time=k * DT, time_step=DT, freestream_velocity=f) for s, f in zip(sims, fss)]
+        dt_ = time.perf_counter() - t0
+        if k >= warm:
+            t_run += dt_
+            its.append([r.iterations for r in rs])
+    results["plain"] = {"seconds": t_run, "gamma": [r.circulation_strength.copy() for r in rs],
+                        "iterations": float(np.mean(its))}
+    for s in sims:
+        s.close()
+    del sims
+
+    ex_net = WS.extrapolation_only(device)
+    for mode, mnet in (("batched", None), ("extrapolation", ex_net), ("warm", net)):
+        r = WS.run_batch(cases, warm + steps, mnet, DT, device, timed_from=warm)
+        results[mode] = {"seconds": r["seconds"], "gamma": r["gamma"][-1],
+                         "iterations": float(np.mean(r["iterations"][warm:])), "start": r["start"][warm:]}
+    ex_net.close()
+
+    def worst(a, ref):
+        return max(float(np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1e-300)) for x, y in zip(a, ref))
+
+    arms = ("batched", "extrapolation", "warm")
+    solves = n * steps
+    out["solves_per_s"] = {m: solves / results[m]["seconds"] for m in ("plain",) + arms}
+    out["speedup_vs_plain"] = {m: results["plain"]["seconds"] / results[m]["seconds"] for m in arms}
+    out["iterations_per_solve"] = {m: results[m]["iterations"] for m in ("plain",) + arms}
+    out["start_taken_fraction"] = {m: {"plain": float(np.mean(results[m]["start"] == 0.0)),
+                                       "extrapolation": float(np.mean(results[m]["start"] == 1.0)),
+                                       "network": float(np.mean(results[m]["start"] == 2.0))}
+                                   for m in ("extrapolation", "warm")}
+    out["max_rel_circulation_diff_vs_plain"] = {m: worst(results[m]["gamma"], results["plain"]["gamma"]) for m in arms}
+    out["arms"] = {"plain": "one Simulation per case, sb_sim_do_step each (previous-step start)",
+                   "batched": "one Batch, graph replay, previous-step start",
+                   "extrapolation": "batched, candidate = linear extrapolation in time (network output zero)",
+                   "warm": "batched, candidates = extrapolation and extrapolation + trained network correction; "
+                           "the solve starts from the lowest-residual of plain / extrapolation / network"}
+    out["timing"] = "host clock around each public call, host freestream in, circulation and force summary out"
+    return out
+
+
+# --------------------------------------------------------------------------------------
+# precision study: 8 sails x 128 panels, 1000 wake rows (1,024,000 rings, 1,033,032 points)
+# --------------------------------------------------------------------------------------
+def run_precision_study(args):
+    """FP32 (plain), FP32 compensated and FP64 Biot-Savart sweeps of the large single case.
+
+    1. Sweep error: a shed-wake-shaped panel set of the case's size (seeded), all-near-field;
+       induced velocity at a seeded sample of wake points and of points one chord behind the
+       sails, each precision against the f64 oracle (C++ restatement of the reference's
+       sweep) over the same panels; rates of every precision over all wake points (FP32) or a
+       target subset (FP64), device time of the standalone sweep call, against the measured
+       FP32 / FP64 FMA rates.
+    2. Circulation and force error: three identical simulations of the case shed 999 steps
+       (frozen wake: ratio_of_wake_affected 0, so a step costs the control-point sweep
+       only), then the 1000th step in each precision; the FP32 results against the FP64 one.
+    """
+    import torch
+
+    from oracle.binding import bs_sweep
+    from stormbird_gb300 import Simulation
+    from stormbird_gb300 import setups as S
+    from stormbird_gb300.simulation import measure_fp32_peak, measure_fp64_peak, panel_sweep
+
+    sails, panels, rows = 8, 128, 1000
+    corners, strengths, cores, pts = S.synthetic_sail_row_wake(sails, panels, rows, seed=5)
+    P = len(strengths)
+    rng = np.random.default_rng(11)
+    npts = sails * (panels + 1)
+    near = pts[npts:2 * npts] + np.array([0.0, 0.0, 0.05])  # one chord behind the sails
+    sample = np.concatenate([pts[rng.choice(len(pts), 768, replace=False)], near[rng.choice(npts, 256, replace=False)]])
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ref = bs_sweep(corners, cores, strengths, 1e30, sample, nthreads=threads)
+    t_oracle = time.perf_counter() - t0
+    out = {"mode": "precision-study", "case": f"{sails} sails x {panels} panels, {rows} wake rows",
+           "panels": P, "wake_points": len(pts), "far_field_ratio": 1e30,
+           "error_sample": len(sample), "oracle_seconds": t_oracle, "oracle_threads": threads}
+    fp32_peak, fp64_peak = measure_fp32_peak(0, 5), measure_fp64_peak(0, 3)
+    out["peaks_tflops"] = {"fp32": fp32_peak, "fp64": fp64_peak, "source": "measured FMA probes"}
+    sweep = {}
+    for mode in ("fp32", "kahan", "fp64"):
+        got = panel_sweep(corners, strengths, cores, sample, far_field_ratio=1e30, precision=mode)
+        err = float(np.max(np.linalg.norm(got - ref, axis=1)) / np.max(np.linalg.norm(ref, axis=1)))
+        targets = pts if mode != "fp64" else pts[rng.choice(len(pts), 16384, replace=False)]
+        panel_sweep(corners[:1024], strengths[:1024], cores[:1024], targets[:256], 1e30, precision=mode)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        panel_sweep(corners, strengths, cores, targets, far_field_ratio=1e30, precision=mode)
+        sec = time.perf_counter() - t0
+        inter = len(targets) * 4.0 * P
+        peak = fp64_peak if mode == "fp64" else fp32_peak
+        sweep[mode] = {"rel_velocity_error_vs_oracle": err, "targets_timed": len(targets), "seconds": sec,
+                       "interactions_per_s": inter / sec,
+                       "frac_of_peak": inter * FLOPS_PER_SEGMENT / sec / 1e12 / peak if peak > 0 else None,
+                       "peak": "fp64" if mode == "fp64" else "fp32"}
+    out["sweep"] = sweep
+    out["sweep_timing"] = "host clock around sb_panel_sweep (includes the H2D of corners and targets and the record build)"
+
+    # circulation and forces: identical states, last step in each precision
+    js = S.wing_sail_row(nr_sails=sails, panels_per_sail=panels, wake_rows=rows, ratio_of_wake_affected=0.0)
+    wind = S.GustyWind(seed=3)
+    sims = {m: Simulation(js) for m in ("kahan", "fp32", "fp64")}
+    n = sims["kahan"].nr_freestream_points
+    fs_dev = torch.empty((n, 3), dtype=torch.float64, device="cuda:0")  # the gust is uniform in space
+    t0 = time.perf_counter()
+    for k in range(rows - 1):
+        fs_dev.copy_(torch.from_numpy(wind.velocity(k * DT)).expand(n, 3))
+        torch.cuda.synchronize()
+        for s in sims.values():
+            s.do_step_device(time=k * DT, time_step=DT, freestream_device_ptr=fs_dev.data_ptr())
+    t_spin = time.perf_counter() - t0
+    fs_dev.copy_(torch.from_numpy(wind.velocity((rows - 1) * DT)).expand(n, 3))
+    torch.cuda.synchronize()
+    res = {}
+    for m, s in sims.items():
+        s.set_precision(m)
+        s.do_step_device(time=(rows - 1) * DT, time_step=DT, freestream_device_ptr=fs_dev.data_ptr())
+        res[m] = s.read_output()
+    g64, f64 = res["fp64"].circulation_strength, res["fp64"].integrated_forces_sum()
+    out["solution"] = {m: {"rel_circulation_error_vs_fp64": float(np.max(np.abs(res[m].circulation_strength - g64))
+                                                                  / np.max(np.abs(g64))),
+                           "rel_force_error_vs_fp64": float(np.linalg.norm(res[m].integrated_forces_sum() - f64)
+                                                            / np.linalg.norm(f64))}
+                       for m in ("kahan", "fp32")}
+    out["solution_setup"] = ("1000-step frozen-wake runs (ratio_of_wake_affected 0), identical through step 999, "
+                             f"last step in each precision; spin-up {t_spin:.1f} s for the three runs")
+    for s in sims.values():
+        s.close()
+    print(json.dumps(out), flush=True)
 
 
 # --------------------------------------------------------------------------------------
@@ -414,7 +605,13 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel-only", action="store_true", help="standalone sweep on a synthetic wake (profiling)")
+    ap.add_argument("--precision-study", action="store_true",
+                    help="FP32 / compensated FP32 / FP64 sweeps of the 8 x 128 panel, 1000-row case")
     ap.add_argument("--rows", type=int, default=0, help="wake rows of the --kernel-only wake (default 300)")
+    ap.add_argument("--batch-cases", type=int, default=512, help="uneven cases of the batched solves/s part (0: skip)")
+    ap.add_argument("--batch-steps", type=int, default=5, help="timed steps of the batched part")
+    ap.add_argument("--train-cases", type=int, default=128, help="cases whose solves train the warm-start network")
+    ap.add_argument("--train-epochs", type=int, default=40)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -423,6 +620,8 @@ def main():
     __graft_entry__.build()
     if args.kernel_only:
         run_kernel_only(args)
+    elif args.precision_study:
+        run_precision_study(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -215,6 +215,8 @@ int sb_panel_sweep_no_alloc(int device, const double* corners, const double* str
  * entry point with no counterpart in the reference.
  */
 int sb_measure_fp32_peak(int device, int reps, double* tflops);
+/* The same for FP64 FMAs (the denominator of the FP64 sweep of the precision study). */
+int sb_measure_fp64_peak(int device, int reps, double* tflops);
 
 /* ===================================================================================
  * Batched cases. The reference runs independent cases (apparent-wind sweeps, differing
@@ -228,8 +230,9 @@ int sb_measure_fp32_peak(int device, int reps, double* tflops);
 typedef struct sb_batch sb_batch;
 
 /* Per-case summary after a step: force sum [3], moment sum [3], residual, iterations,
- * converged (0/1), device status word (0 = ok), warm start (1 = the network's candidate
- * was the initial solution, 0 = the plain start had the lower residual, -1 = no candidate). */
+ * converged (0/1), device status word (0 = ok), start of the solve (0 = the plain start,
+ * 1 = the solution extrapolated in time, 2 = extrapolation plus the network's correction:
+ * the one with the lowest residual; -1 = no warm start). */
 #define SB_BATCH_SUMMARY 11
 /* sb_batch_info fields: last step ms, panel-target pairs swept in the last step, tuning
  * waves, tuning CTAs per SM (0 = occupancy limit), roll-up grid, roll-up work items,
@@ -275,10 +278,11 @@ int sb_batch_info(const sb_batch* batch, double* info, size_t n);
  * Learned warm start. No counterpart in the reference, which starts every solve from the
  * previous step's circulation (simulation.rs:165,189; simple_iterative.rs:86-101). A network
  * (4 hidden layers of 256, GELU, BF16 weights on the tensor cores with FP32 accumulation)
- * predicts, per panel, the change of the step's solution from per-panel features the batch
- * builds on the GPU. The SimpleIterative solve then evaluates the residual of the plain
- * start and of the prediction and starts from the lower one, so the solver stays the judge
- * of the result; the batch reports per case which start was taken.
+ * predicts, per panel, a correction to the solution extrapolated linearly in time, from
+ * per-panel features the batch builds on the GPU. The SimpleIterative solve evaluates the
+ * residual of the plain start, of the extrapolation and of extrapolation plus correction
+ * and starts from the lowest, so the solver stays the judge of the result; the batch
+ * reports per case which start was taken.
  * =================================================================================== */
 typedef struct sb_mlp sb_mlp;
 /* Number of per-panel features the batch builds (the network's input size for mode 1). */

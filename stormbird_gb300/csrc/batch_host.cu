@@ -12,9 +12,11 @@
 //   4. the per-case solves and force kernels on the pool streams, then one gather kernel
 //      that packs every case's circulation and force summary for one device->host copy.
 // With a warm-start network attached, the per-panel features of every case, the network's
-// forward pass and the candidate initial solutions run on the main stream between 2 and 4;
-// each case's solve starts from the candidate or from the plain start, whichever has the
-// lower residual (k_solve_si), and the change of the solution is kept as a training target.
+// forward pass and the candidate initial solutions (linear extrapolation of the solution in
+// time plus the network's correction) run on the main stream between 2 and 4;
+// each case's solve starts from the plain start, the extrapolation or the network's
+// candidate, whichever has the lowest residual (k_solve_si), and the change of the
+// solution beyond the extrapolation is kept as a training target.
 // After three steps (when the step's kernel arguments stop changing except for the wake
 // buffer parity) the whole step is captured into a CUDA graph per parity and replayed; the
 // work lists are refreshed through the graph's copy node from pinned host memory.
@@ -131,7 +133,7 @@ struct sb_batch {
     sb_mlp* mlp = nullptr;
     int warm_mode = 0;
     DevBuf<float> w_feat, w_y, w_target;
-    DevBuf<double> w_q, w_g0, w_cand, w_gamma_old;
+    DevBuf<double> w_q, w_g0, w_tr, w_cand_ex, w_cand, w_gamma_old;
     DevBuf<d3> w_fs_old;
     PinnedBuf<FeatJob> h_feat;
     DevBuf<FeatJob> d_feat;
@@ -442,7 +444,7 @@ struct sb_batch {
         for (auto& c : cases) c->step_matrix_and_solve();
         join(1);
         if (warm_mode != 0)
-            ck(launch_batch_targets(gamma_all.p, w_q.p, w_g0.p, N_total, w_target.p, main), "warm-start targets");
+            ck(launch_batch_targets(gamma_all.p, w_q.p, w_g0.p, w_tr.p, N_total, w_target.p, main), "warm-start targets");
         sweeps(1);
         for (auto& c : cases) if (c->dynamic) c->after_rollup_sweep();
         fork(2);
@@ -471,7 +473,9 @@ struct sb_batch {
             w_target.alloc(N_total);
             w_q.alloc(N_total);
             w_g0.alloc(N_total);
+            w_tr.alloc(N_total);
             w_cand.alloc(N_total);
+            w_cand_ex.alloc(N_total);
             w_gamma_old.alloc(N_total);
             w_fs_old.alloc(N_total);
             ck(cudaMemset(w_target.p, 0, N_total * sizeof(float)), "memset");
@@ -481,8 +485,10 @@ struct sb_batch {
         if (mode == 1) mlp_reserve(m, N_total);
         mlp = mode == 1 ? m : nullptr;
         warm_mode = mode;
-        for (size_t i = 0; i < cases.size(); ++i)
-            cases[i]->candidate_p = mode == 1 ? w_cand.p + line_off[i] : nullptr;
+        for (size_t i = 0; i < cases.size(); ++i) {
+            cases[i]->candidate_p[0] = mode == 1 ? w_cand_ex.p + line_off[i] : nullptr;
+            cases[i]->candidate_p[1] = mode == 1 ? w_cand.p + line_off[i] : nullptr;
+        }
     }
 
     // Feature jobs of this step (host; steps completed before the step).
@@ -513,11 +519,13 @@ struct sb_batch {
     void warm_start_before_solve() {
         ck(cudaMemcpyAsync(d_feat.p, h_feat.p, cases.size() * sizeof(FeatJob), cudaMemcpyHostToDevice, main),
            "H2D feature jobs");
-        ck(launch_batch_features(d_feat.p, static_cast<int>(cases.size()), N_total, w_feat.p, w_q.p, w_g0.p, main),
+        ck(launch_batch_features(d_feat.p, static_cast<int>(cases.size()), N_total, w_feat.p, w_q.p, w_g0.p, w_tr.p,
+                                 main),
            "warm-start features");
         if (warm_mode == 1) {
             mlp_forward_async(mlp, w_feat.p, N_total, w_y.p, main);
-            ck(launch_batch_candidate(w_y.p, w_q.p, w_g0.p, N_total, w_cand.p, main), "warm-start candidate");
+            ck(launch_batch_candidate(w_y.p, w_q.p, w_g0.p, w_tr.p, N_total, w_cand_ex.p, w_cand.p, main),
+               "warm-start candidates");
         }
     }
 

@@ -338,7 +338,7 @@ __device__ inline double geometric_aoa(d3 chord, d3 span_rel, d3 u) {
 }
 
 __global__ void k_batch_features(const FeatJob* jobs, int n_jobs, long long rows, float* feat, double* q_out,
-                                 double* g0_out) {
+                                 double* g0_out, double* tr_out) {
     const long long r = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
     if (r >= rows) return;
     int lo = 0, hi = n_jobs - 1;
@@ -394,21 +394,26 @@ __global__ void k_batch_features(const FeatJob* jobs, int n_jobs, long long rows
     f[15] = static_cast<float>(1.0 / (1.0 + k));
     q_out[r] = q;
     g0_out[r] = g0;
+    tr_out[r] = trend;
     // history for the next step (only this thread touches row i of these two arrays)
     J.gamma_old[i] = J.gamma[i];
     J.fs_old[i] = fs;
 }
 
-__global__ void k_batch_candidate(const float* y, const double* q, const double* g0, long long rows, double* cand) {
+__global__ void k_batch_candidate(const float* y, const double* q, const double* g0, const double* tr, long long rows,
+                                  double* cand_ex, double* cand_net) {
     const long long r = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
     if (r >= rows) return;
-    cand[r] = -(g0[r] + static_cast<double>(y[r])) * q[r];
+    const double e = g0[r] + tr[r];
+    cand_ex[r] = -e * q[r];
+    cand_net[r] = -(e + static_cast<double>(y[r])) * q[r];
 }
 
-__global__ void k_batch_targets(const double* gamma_new, const double* q, const double* g0, long long rows, float* t) {
+__global__ void k_batch_targets(const double* gamma_new, const double* q, const double* g0, const double* tr,
+                                long long rows, float* t) {
     const long long r = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
     if (r >= rows) return;
-    t[r] = q[r] > 0.0 ? static_cast<float>(-gamma_new[r] / q[r] - g0[r]) : 0.f;
+    t[r] = q[r] > 0.0 ? static_cast<float>(-gamma_new[r] / q[r] - g0[r] - tr[r]) : 0.f;
 }
 
 unsigned blocks_for(long long n, int t) { return static_cast<unsigned>((n + t - 1) / t); }
@@ -466,23 +471,23 @@ cudaError_t launch_mlp_cast(const float* W, int out, int in, bf16* Wb, bf16* WbT
 }
 
 cudaError_t launch_batch_features(const FeatJob* jobs, int n_jobs, long long rows, float* feat, double* q, double* g0,
-                                  cudaStream_t s) {
+                                  double* tr, cudaStream_t s) {
     if (rows <= 0 || n_jobs <= 0) return cudaSuccess;
-    k_batch_features<<<blocks_for(rows, 128), 128, 0, s>>>(jobs, n_jobs, rows, feat, q, g0);
+    k_batch_features<<<blocks_for(rows, 128), 128, 0, s>>>(jobs, n_jobs, rows, feat, q, g0, tr);
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_candidate(const float* y, const double* q, const double* g0, long long rows, double* cand,
-                                   cudaStream_t s) {
+cudaError_t launch_batch_candidate(const float* y, const double* q, const double* g0, const double* tr, long long rows,
+                                   double* cand_ex, double* cand_net, cudaStream_t s) {
     if (rows <= 0) return cudaSuccess;
-    k_batch_candidate<<<blocks_for(rows, 256), 256, 0, s>>>(y, q, g0, rows, cand);
+    k_batch_candidate<<<blocks_for(rows, 256), 256, 0, s>>>(y, q, g0, tr, rows, cand_ex, cand_net);
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_targets(const double* gamma_new, const double* q, const double* g0, long long rows,
-                                 float* target, cudaStream_t s) {
+cudaError_t launch_batch_targets(const double* gamma_new, const double* q, const double* g0, const double* tr,
+                                 long long rows, float* target, cudaStream_t s) {
     if (rows <= 0) return cudaSuccess;
-    k_batch_targets<<<blocks_for(rows, 256), 256, 0, s>>>(gamma_new, q, g0, rows, target);
+    k_batch_targets<<<blocks_for(rows, 256), 256, 0, s>>>(gamma_new, q, g0, tr, rows, target);
     return cudaGetLastError();
 }
 

@@ -1,44 +1,47 @@
-// FP32 throughput probe: the denominator for the Biot-Savart roofline.
+// FP32 / FP64 throughput probes: the denominators for the Biot-Savart roofline.
 //
 // The sweep kernels run on the FP32 pipes (not tensor cores), so their roofline is the
-// FP32 FMA rate of this GPU at its current clocks. Each thread advances 8 independent FMA
-// chains; the grid covers every SM with several CTAs. FLOPs = 2 per FMA.
+// FP32 FMA rate of this GPU at its current clocks; the FP64 sweep of the precision study is
+// set against the FP64 FMA rate. Each thread advances 8 independent FMA chains; the grid
+// covers every SM with several CTAs. FLOPs = 2 per FMA.
 #include <cuda_runtime.h>
 
 #include "sb_kernels.h"
 
 namespace sbgpu {
 
-__global__ void __launch_bounds__(256) k_fma_probe(float* out, int iters, float a, float b) {
-    float x0 = threadIdx.x * 1e-7f, x1 = x0 + 1e-3f, x2 = x0 + 2e-3f, x3 = x0 + 3e-3f;
-    float x4 = x0 + 4e-3f, x5 = x0 + 5e-3f, x6 = x0 + 6e-3f, x7 = x0 + 7e-3f;
+template <class T>
+__global__ void __launch_bounds__(256) k_fma_probe(T* out, int iters, T a, T b) {
+    T x0 = threadIdx.x * T(1e-7), x1 = x0 + T(1e-3), x2 = x0 + T(2e-3), x3 = x0 + T(3e-3);
+    T x4 = x0 + T(4e-3), x5 = x0 + T(5e-3), x6 = x0 + T(6e-3), x7 = x0 + T(7e-3);
     for (int i = 0; i < iters; ++i) {
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
-            x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
-            x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+            x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+            x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
         }
     }
-    float s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
-    if (s == 12345.678f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;  // keeps the chains live
+    T s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+    if (s == T(12345.678)) out[blockIdx.x * blockDim.x + threadIdx.x] = s;  // keeps the chains live
 }
 
-// Returns FP32 TFLOP/s (best of `reps` launches) or a negative value on error.
-double measure_fp32_peak(int device, int reps) {
+// Returns TFLOP/s of type T (best of `reps` launches) or a negative value on error.
+template <class T>
+static double measure_peak(int device, int reps, int iters) {
     if (cudaSetDevice(device) != cudaSuccess) return -1.0;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    const int blocks = sms * 8, threads = 256, iters = 4096;
-    float* out = nullptr;
-    if (cudaMalloc(&out, static_cast<size_t>(blocks) * threads * sizeof(float)) != cudaSuccess) return -1.0;
+    const int blocks = sms * 8, threads = 256;
+    T* out = nullptr;
+    if (cudaMalloc(&out, static_cast<size_t>(blocks) * threads * sizeof(T)) != cudaSuccess) return -1.0;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     double best = 0.0;
-    k_fma_probe<<<blocks, threads>>>(out, iters / 8, 0.9999f, 1e-4f);  // warm-up
+    k_fma_probe<T><<<blocks, threads>>>(out, iters / 8, T(0.9999), T(1e-4));  // warm-up
     for (int r = 0; r < reps; ++r) {
         cudaEventRecord(e0);
-        k_fma_probe<<<blocks, threads>>>(out, iters, 0.9999f, 1e-4f);
+        k_fma_probe<T><<<blocks, threads>>>(out, iters, T(0.9999), T(1e-4));
         cudaEventRecord(e1);
         cudaEventSynchronize(e1);
         float ms = 0.f;
@@ -52,5 +55,8 @@ double measure_fp32_peak(int device, int reps) {
     cudaFree(out);
     return err == cudaSuccess ? best : -1.0;
 }
+
+double measure_fp32_peak(int device, int reps) { return measure_peak<float>(device, reps, 4096); }
+double measure_fp64_peak(int device, int reps) { return measure_peak<double>(device, reps, 256); }
 
 }  // namespace sbgpu

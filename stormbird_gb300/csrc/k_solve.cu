@@ -165,13 +165,20 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve_si(DevModel m, SolveSet
     };
 
     // Guarded warm start: residual (simple_iterative.rs:160-176) of the plain start G[0]
-    // and of the candidate, the lower one (finite) becomes the initial solution.
-    if (b.candidate) {
-        for (int i = tid; i < N; i += kSolveThreads) G[1][i] = b.candidate[i];
-        __syncthreads();
-        double rs[2];
-        for (int v = 0; v < 2; ++v) {
-            induced_rows(G[v]);
+    // and of each candidate (staged in G[1]); the lowest finite one becomes the initial
+    // solution (the plain start wins ties).
+    if (b.candidate[0] || b.candidate[1]) {
+        double best = 0.0;
+        int taken = 0;
+        for (int v = 0; v < 3; ++v) {
+            const double* src = v == 0 ? nullptr : b.candidate[v - 1];
+            if (v > 0 && !src) continue;
+            double* Gv = v == 0 ? G[0] : G[1];
+            if (v > 0) {
+                for (int i = tid; i < N; i += kSolveThreads) G[1][i] = src[i];
+                __syncthreads();
+            }
+            induced_rows(Gv);
             for (int k = 0; k < nrows; ++k) {
                 int i = r0 + tid + k * kSolveThreads;
                 const RowGeom& g = rg[k];
@@ -179,7 +186,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve_si(DevModel m, SolveSet
                 d3 u = total_velocity(st, g.felt, uind[i - r0]);
                 u = u - project(u, g.span_rel);
                 double aoa = len(u) > kMinPositive ? signed_angle_between(g.chord, u, g.span_dir) : 0.0;
-                double r = residual_term(m, g, f, G[v][i], u, aoa);
+                double r = residual_term(m, g, f, Gv[i], u, aoa);
                 for (int q = 0; q < CS; ++q) cl.map_shared_rank(RR[0], q)[i] = r;
             }
             cl.sync();
@@ -189,14 +196,17 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve_si(DevModel m, SolveSet
                 s_res = s;
             }
             __syncthreads();
-            rs[v] = s_res;
-            cl.sync();  // RR[0] is written again by the next pass or the first iteration
+            const double rv = s_res;
+            if (v == 0) {
+                best = rv;
+            } else if (isfinite(rv) && rv < best) {  // same decision in every CTA
+                best = rv;
+                taken = v;
+                for (int i = tid; i < N; i += kSolveThreads) G[0][i] = G[1][i];
+            }
+            cl.sync();  // RR[0] and G[1] are written again by the next pass or the first iteration
         }
-        const bool take = isfinite(rs[1]) && rs[1] < rs[0];
-        if (take)
-            for (int i = tid; i < N; i += kSolveThreads) G[0][i] = G[1][i];
-        if (rank == 0 && tid == 0) b.scalars[4] = take ? 1.0 : 0.0;
-        cl.sync();  // G[1] is written through distributed shared memory by the first iteration
+        if (rank == 0 && tid == 0) b.scalars[4] = static_cast<double>(taken);
     } else if (rank == 0 && tid == 0) {
         b.scalars[4] = -1.0;
     }

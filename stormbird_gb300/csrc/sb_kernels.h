@@ -123,11 +123,11 @@ struct SolveBuffers {
     double* wake_str_row0 = nullptr;        // strengths row 0 (dynamic) or nullptr
     PanelRec<float>* rec32_row0 = nullptr;  // FP32 record row 0 (dynamic) or nullptr
     PanelRec<double>* rec64_row0 = nullptr; // FP64 record row 0 in the FP64 sweep mode
-    // Optional second initial solution (a predicted warm start). The solve evaluates the
-    // residual of the plain start and of the candidate and starts from the lower one;
-    // scalars[4] = 1 when the candidate was taken, 0 when the plain start was (fallback),
-    // -1 without a candidate.
-    const double* candidate = nullptr;      // [N] or nullptr
+    // Optional further initial solutions (predicted warm starts). The solve evaluates the
+    // residual of the plain start and of each candidate and starts from the lowest one;
+    // scalars[4] = k + 1 when candidate k was taken, 0 when the plain start was (fallback),
+    // -1 without candidates.
+    const double* candidate[2] = {nullptr, nullptr};  // [N] each, or nullptr
     int* err = nullptr;
 };
 
@@ -175,8 +175,9 @@ struct OutLayout {
 // Sets the calling thread's sb_last_error / sb_last_status (sim_host.cu).
 void report_error(int code, const std::string& message);
 
-// FP32 FMA throughput of `device` in TFLOP/s (k_probe.cu); negative on error.
+// FP32 / FP64 FMA throughput of `device` in TFLOP/s (k_probe.cu); negative on error.
 double measure_fp32_peak(int device, int reps);
+double measure_fp64_peak(int device, int reps);
 
 // Sectional and integrated forces (force_calculations.rs:322-452, 669-698;
 // forces_and_moments.rs:163-245; flow_derivatives.rs:31-63).

@@ -96,15 +96,18 @@ struct FeatJob {
     int N = 0, S = 0, W = 0, steps = 0;
     long long row0 = 0;              // first row of the case in the batch arrays
 };
-// feat [rows][kMlpFeatures], q (= chord * |U| / 2) and g0 (= -Gamma_prev / q) per panel.
+// Per panel, with q = chord |U| / 2 and the lift-coefficient-like variable g = -Gamma / q:
+// feat [rows][kMlpFeatures], q, g0 = g of the previous solution and tr = its change over
+// the previous step (zero before two solutions exist), the linear-extrapolation baseline.
 cudaError_t launch_batch_features(const FeatJob* jobs, int n_jobs, long long rows, float* feat, double* q, double* g0,
-                                  cudaStream_t s);
-// cand = -(g0 + y) q
-cudaError_t launch_batch_candidate(const float* y, const double* q, const double* g0, long long rows, double* cand,
-                                   cudaStream_t s);
-// target = -gamma_new / q - g0 (the change of the lift-coefficient-like variable)
-cudaError_t launch_batch_targets(const double* gamma_new, const double* q, const double* g0, long long rows,
-                                 float* target, cudaStream_t s);
+                                  double* tr, cudaStream_t s);
+// cand_ex = -(g0 + tr) q: extrapolation in time; cand_net = -(g0 + tr + y) q: plus the
+// network's correction y
+cudaError_t launch_batch_candidate(const float* y, const double* q, const double* g0, const double* tr, long long rows,
+                                   double* cand_ex, double* cand_net, cudaStream_t s);
+// target = -gamma_new / q - g0 - tr: the correction the network is trained to predict
+cudaError_t launch_batch_targets(const double* gamma_new, const double* q, const double* g0, const double* tr,
+                                 long long rows, float* target, cudaStream_t s);
 
 }  // namespace sbgpu
 

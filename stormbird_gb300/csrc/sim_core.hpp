@@ -294,8 +294,8 @@ struct sb_sim {
     // batch's contiguous buffers.
     d3* fs_p = nullptr;
     double* gamma_p = nullptr;
-    // Predicted initial solution [N] offered to the SimpleIterative solve, or nullptr.
-    const double* candidate_p = nullptr;
+    // Predicted initial solutions [N] offered to the SimpleIterative solve, or nullptr.
+    const double* candidate_p[2] = {nullptr, nullptr};
 
     ~sb_sim() {
         for (auto& e : ev) if (e) cudaEventDestroy(e);
@@ -719,7 +719,8 @@ struct sb_sim {
         sb.scalars = scalars.p;
         sb.lin_work = lin_work.p;
         sb.err = err.p;
-        sb.candidate = candidate_p;
+        sb.candidate[0] = candidate_p[0];
+        sb.candidate[1] = candidate_p[1];
         if (dynamic) {
             sb.wake_str_row0 = str[cur].p;
             sb.rec32_row0 = rec32.p;

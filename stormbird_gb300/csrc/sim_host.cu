@@ -237,4 +237,12 @@ int sb_measure_fp32_peak(int device, int reps, double* tflops) {
     return SB_OK;
 }
 
+int sb_measure_fp64_peak(int device, int reps, double* tflops) {
+    if (!tflops) { g_last_error = "null argument"; return SB_ERR_NULL_ARG; }
+    double v = measure_fp64_peak(device, reps < 1 ? 1 : reps);
+    if (v < 0.0) { g_last_error = "FP64 probe failed"; return SB_ERR_CUDA; }
+    *tflops = v;
+    return SB_OK;
+}
+
 }  // extern "C"

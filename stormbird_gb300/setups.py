@@ -213,17 +213,12 @@ def synthetic_sail_row_wake(nr_sails=4, panels_per_sail=64, wake_rows=300, time_
             row.append(p)
         rows.append(np.concatenate(row))
     pts = np.stack(rows)  # [W+1, Np, 3]
-    corners, gam = [], []
     zc = 0.5 * (z[:-1] + z[1:])
     g_span = -30.0 * np.sqrt(np.clip(1.0 - (2 * zc / SPAN - 1.0) ** 2, 0.0, 1.0)) - 1.0
-    for s in range(wake_rows):
-        for i in range(nr_sails):
-            for j in range(panels_per_sail):
-                a = i * npts + j
-                corners.append([pts[s, a], pts[s, a + 1], pts[s + 1, a + 1], pts[s + 1, a]])
-                gam.append(g_span[j] * rng.uniform(0.9, 1.1))
-    corners = np.array(corners)
-    strengths = np.array(gam)
+    # panel (row s, sail i, line j) has corners a, a+1 on row s and a+1, a on row s+1, a = i*npts + j
+    a = np.array([i * npts + j for i in range(nr_sails) for j in range(panels_per_sail)])
+    corners = np.stack([pts[:-1][:, a], pts[:-1][:, a + 1], pts[1:][:, a + 1], pts[1:][:, a]], axis=2).reshape(-1, 4, 3)
+    strengths = np.tile(g_span, wake_rows * nr_sails) * rng.uniform(0.9, 1.1, wake_rows * nr_sails * panels_per_sail)
     cores = np.full(len(strengths), 0.1 * CHORD)
     return corners, strengths, cores, pts.reshape(-1, 3)
 

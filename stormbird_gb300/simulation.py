@@ -161,6 +161,13 @@ def measure_fp32_peak(device: int = 0, reps: int = 5) -> float:
     return v.value
 
 
+def measure_fp64_peak(device: int = 0, reps: int = 3) -> float:
+    """Measured FP64 FMA throughput (TFLOP/s) of a device."""
+    v = ctypes.c_double()
+    _check(lib().sb_measure_fp64_peak(int(device), int(reps), ctypes.byref(v)))
+    return v.value
+
+
 def panel_sweep(corners, strengths, core_lengths, targets, far_field_ratio: float = 5.0, symmetry: int = 0,
                 precision: str | int = "kahan", device: int = 0) -> np.ndarray:
     """Standalone Biot-Savart sweep over caller-given vortex-ring panels (sb_panel_sweep)."""

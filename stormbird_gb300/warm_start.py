@@ -2,12 +2,16 @@
 warm-start mode).
 
 The reference starts every SimpleIterative solve from the previous step's circulation
-(stormbird/src/lifting_line/simulation.rs:165,189; solvers/simple_iterative.rs:86-101). Here a
-network predicts, per panel, how the solution changes in this step, from features the batch
-builds on the GPU (previous solution and its neighbours, freestream change, geometric angle
-of attack, span position, sail index and counts, wake fill). The solve evaluates the residual
-of the plain start and of the prediction and starts from the lower one, so the fallback to
-the plain start is decided per case and step and the solver remains the judge of the result.
+(stormbird/src/lifting_line/simulation.rs:165,189; solvers/simple_iterative.rs:86-101). Here
+the candidate start is the solution extrapolated linearly in time (2 G[t-1] - G[t-2], in f64)
+plus a correction a network predicts per panel from features the batch builds on the GPU
+(previous solution and its neighbours, its last change, freestream change, geometric angle of
+attack, span position, sail index and counts, wake fill). The solve evaluates the residual of
+the plain start, of the extrapolation and of extrapolation plus correction and starts from
+the lowest, so the fallback is decided per case and step and the solver remains the judge of
+the result.
+A network whose output layer is zero gives the extrapolation alone (`extrapolation_only`),
+the ablation that separates what the trained network adds.
 
 Training runs on the GPU through the library's own kernels (tcgen05 BF16 GEMMs with FP32
 accumulation, Adam); torch only holds the device tensors and shuffles the rows.
@@ -94,6 +98,12 @@ class WarmStartNet:
                                       g.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), ctypes.byref(loss)))
         return g, loss.value
 
+    def zero_output(self):
+        """Output layer set to zero: the network predicts no correction (extrapolation only)."""
+        p = self.get_params()
+        p[-257:] = 0.0
+        self.set_params(p)
+
     def train_step(self, x, t, lr: float, want_loss: bool = True):
         loss = ctypes.c_double()
         _check(lib().sb_mlp_train_step(self._h, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(t.data_ptr()), x.shape[0],
@@ -101,7 +111,7 @@ class WarmStartNet:
         return loss.value if want_loss else None
 
 
-def tight_solver(setup_json: str, max_iterations: int = 600, residual_tolerance: float = 1e-6) -> str:
+def tight_solver(setup_json: str, max_iterations: int = 1000, residual_tolerance: float = 1e-7) -> str:
     """The setup with a SimpleIterative solve run to a tight residual (no strength-change exit)."""
     d = json.loads(setup_json)
     si = d["simulation_settings"]["Dynamic"].setdefault("solver", {}).setdefault("SimpleIterative", {})
@@ -111,9 +121,10 @@ def tight_solver(setup_json: str, max_iterations: int = 600, residual_tolerance:
     return json.dumps(d)
 
 
-def collect(cases, steps: int, dt: float = 0.05, skip: int = 1, device: int = 0):
+def collect(cases, steps: int, dt: float = 0.05, skip: int = 2, device: int = 0, clip: float = 0.25):
     """Runs the cases as one batch with features and targets recorded; returns CUDA tensors
-    X [rows, 16], T [rows] of steps skip..steps-1 (every case and panel)."""
+    X [rows, 16], T [rows] of steps skip..steps-1 (every case and panel), targets clipped to
+    [-clip, clip] (the start-up steps hold a few large changes the guard rejects anyway)."""
     torch = _torch()
     b = Batch([js for js, _ in cases], device=device)
     winds = [w for _, w in cases]
@@ -129,16 +140,20 @@ def collect(cases, steps: int, dt: float = 0.05, skip: int = 1, device: int = 0)
             xs.append(x)
             ts.append(t)
     b.close()
-    return torch.cat(xs), torch.cat(ts)
+    return torch.cat(xs), torch.cat(ts).clamp_(-clip, clip)
 
 
-def train(net: WarmStartNet, X, T, epochs: int = 4, batch_rows: int = 8192, lr: float = 1e-3, seed: int = 0):
-    """Mini-batch Adam over shuffled rows; returns the mean loss of each epoch."""
+def train(net: WarmStartNet, X, T, epochs: int = 4, batch_rows: int = 8192, lr: float = 5e-4, seed: int = 0):
+    """Mini-batch Adam over shuffled rows; returns the mean loss of each epoch. An epoch
+    whose loss is not finite is undone (parameters of the last good epoch) and the learning
+    rate halved."""
     torch = _torch()
     g = torch.Generator(device=X.device)
     g.manual_seed(seed)
     out = []
     n = X.shape[0]
+    batch_rows = min(batch_rows, n)
+    good = net.get_params()
     for _ in range(epochs):
         perm = torch.randperm(n, device=X.device, generator=g)
         Xs, Ts = X[perm].contiguous(), T[perm].contiguous()
@@ -147,57 +162,84 @@ def train(net: WarmStartNet, X, T, epochs: int = 4, batch_rows: int = 8192, lr: 
             loss = net.train_step(Xs[s0:s0 + batch_rows], Ts[s0:s0 + batch_rows], lr)
             tot += loss
             cnt += 1
-        out.append(tot / max(cnt, 1))
+        m = tot / max(cnt, 1)
+        if not np.isfinite(m):
+            net.set_params(good)
+            lr *= 0.5
+            continue
+        good = net.get_params()
+        out.append(m)
     return out
 
 
-def evaluate(net: WarmStartNet, cases, steps: int, dt: float = 0.05, device: int = 0) -> dict:
-    """Runs the cases twice as batches, plain and warm-started, on the same freestream.
+def extrapolation_only(device: int = 0) -> WarmStartNet:
+    """A network with a zero output layer: candidates are the linear extrapolation alone."""
+    net = WarmStartNet(FEATURES, seed=0, device=device)
+    net.zero_output()
+    return net
 
-    Returns iterations per solve (plain, warm), the fraction of solves that took the plain
-    start (fallback), the largest relative circulation difference between the two runs,
-    and the wall time of each run's steps.
+
+def run_batch(cases, steps: int, net: WarmStartNet | None = None, dt: float = 0.05, device: int = 0,
+              timed_from: int = 1) -> dict:
+    """Steps the cases as one batch (warm-started when `net` is given) on their freestream.
+
+    Returns per step the circulation, iterations and start taken of every case, and the host
+    time of steps timed_from.. (one solve = one case advanced by one step).
     """
     import time
 
     winds = [w for _, w in cases]
-    res = {}
-    gam = {}
-    for mode in ("plain", "warm"):
-        b = Batch([js for js, _ in cases], device=device)
-        if mode == "warm":
-            _check(lib().sb_batch_set_warm_start(b._h, net.handle, 1))
-        its, taken, t_run = [], [], 0.0
-        g_steps = []
-        for k in range(steps):
-            fs = S.batch_freestream(b, winds, k * dt)
-            t0 = time.perf_counter()
-            b.do_step(time=k * dt, time_step=dt, freestream_velocity=fs)
+    b = Batch([js for js, _ in cases], device=device)
+    if net is not None:
+        _check(lib().sb_batch_set_warm_start(b._h, net.handle, 1))
+    its, taken, gam, t_run = [], [], [], 0.0
+    for k in range(steps):
+        fs = S.batch_freestream(b, winds, k * dt)
+        t0 = time.perf_counter()
+        b.do_step(time=k * dt, time_step=dt, freestream_velocity=fs)
+        if k >= timed_from:
             t_run += time.perf_counter() - t0
-            s = b.summary()
-            its.append(s[:, 7].copy())
-            taken.append(s[:, 10].copy())
-            g_steps.append(b.circulation())
-        res[mode] = {"iterations": np.array(its), "start": np.array(taken), "seconds": t_run}
-        gam[mode] = (g_steps, [b.case_slice(i) for i in range(b.n_cases)])
-        b.close()
+        s = b.summary()
+        its.append(s[:, 7].copy())
+        taken.append(s[:, 10].copy())
+        g = b.circulation()
+        gam.append([g[b.case_slice(i)] for i in range(b.n_cases)])
+    b.close()
+    return {"iterations": np.array(its), "start": np.array(taken), "gamma": gam, "seconds": t_run}
+
+
+def max_rel_diff(a, ref) -> float:
+    """Largest relative (infinity-norm) difference per case and step between two runs."""
     worst = 0.0
-    for (gp, sl), (gw, _) in [(gam["plain"], gam["warm"])]:
-        for k in range(steps):
-            for s in sl:
-                den = np.max(np.abs(gp[k][s]))
-                if den > 0:
-                    worst = max(worst, float(np.max(np.abs(gw[k][s] - gp[k][s])) / den))
-    # the first step has no previous solution: the warm start is not offered there
-    ip = res["plain"]["iterations"][1:]
-    iw = res["warm"]["iterations"][1:]
-    st = res["warm"]["start"][1:]
-    return {
-        "iterations_plain": float(ip.mean()),
-        "iterations_warm": float(iw.mean()),
-        "iterations_saved_fraction": float(1.0 - iw.sum() / max(ip.sum(), 1.0)),
-        "fallback_rate": float(np.mean(st == 0.0)),
-        "max_rel_circulation_diff": worst,
-        "seconds_plain": res["plain"]["seconds"],
-        "seconds_warm": res["warm"]["seconds"],
-    }
+    for ga, gr in zip(a["gamma"], ref["gamma"]):
+        for x, y in zip(ga, gr):
+            den = np.max(np.abs(y))
+            if den > 0:
+                worst = max(worst, float(np.max(np.abs(x - y)) / den))
+    return worst
+
+
+def evaluate(net: WarmStartNet, cases, steps: int, dt: float = 0.05, device: int = 0) -> dict:
+    """Plain, extrapolation-only and network warm starts on the same cases and freestream.
+
+    Iterations per solve and the fallback rate (solves that took the plain start) count
+    steps 2.. (the extrapolation needs two previous solutions); the circulation differences
+    are against the plain run over all steps.
+    """
+    plain = run_batch(cases, steps, None, dt, device, timed_from=2)
+    ex_net = extrapolation_only(device)
+    extra = run_batch(cases, steps, ex_net, dt, device, timed_from=2)
+    ex_net.close()
+    warm = run_batch(cases, steps, net, dt, device, timed_from=2)
+    ip = plain["iterations"][2:]
+    out = {"iterations_plain": float(ip.mean())}
+    for name, r in (("extrapolation", extra), ("warm", warm)):
+        it = r["iterations"][2:]
+        out[f"iterations_{name}"] = float(it.mean())
+        out[f"iterations_saved_fraction_{name}"] = float(1.0 - it.sum() / max(ip.sum(), 1.0))
+        out[f"fallback_rate_{name}"] = float(np.mean(r["start"][2:] == 0.0))
+        out[f"network_start_rate_{name}"] = float(np.mean(r["start"][2:] == 2.0))
+        out[f"max_rel_circulation_diff_{name}"] = max_rel_diff(r, plain)
+        out[f"seconds_{name}"] = r["seconds"]
+    out["seconds_plain"] = plain["seconds"]
+    return out

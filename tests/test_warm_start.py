@@ -5,8 +5,9 @@
     FP32 tensor-core accumulation against f64, plus rare BF16 rounding flips);
   * training with the library's Adam lowers the loss of a smooth regression;
   * a network trained on data the batch itself records warm-starts held-out cases: the
-    results agree with the plain solves to within the solver tolerance, and the iteration
-    counts with and without the network are reported (the gain the network brings).
+    results agree with the plain solves to within 1e-5 (solver tolerance 1e-7 residual), and
+    the iteration counts of the plain start, the extrapolation alone and extrapolation plus
+    network are reported (the gain the network brings over the method without it).
 """
 import numpy as np
 import pytest
@@ -83,10 +84,11 @@ def test_warm_start_on_held_out_cases(gpu_lib):
 
     X, T = WS.collect(cases(24, seed=100), steps=24)
     net = _net(seed=11)
-    losses = WS.train(net, X, T, epochs=30, batch_rows=2048, lr=1e-3)
+    losses = WS.train(net, X, T, epochs=30, batch_rows=2048)
     assert losses[-1] < losses[0]
     rep = WS.evaluate(net, cases(6, seed=200), steps=16)
     print("warm start on held-out cases:", rep)
-    assert rep["max_rel_circulation_diff"] <= 1e-4
-    assert rep["iterations_warm"] <= 1.05 * rep["iterations_plain"]
-    assert 0.0 <= rep["fallback_rate"] <= 1.0
+    for arm in ("extrapolation", "warm"):
+        assert rep[f"max_rel_circulation_diff_{arm}"] <= 1e-5
+        assert rep[f"iterations_{arm}"] <= 1.05 * rep["iterations_plain"]
+        assert 0.0 <= rep[f"fallback_rate_{arm}"] <= 1.0
