@@ -299,9 +299,11 @@ def run_gb300(args):
     h2d = nfs * 3 * 8
     d2h = (35 * N + 36 * sim.nr_wings + 9) * 8 + 4
 
-    # ---- roofline of the roll-up sweep kernel
+    # ---- roofline of the roll-up sweep kernel: the segments it actually evaluates (with
+    # shared segments about half of the reference's four per panel)
     rollup_targets = ct["rollup_targets"]
-    per_launch_flops = rollup_targets * 4.0 * nz * FLOPS_PER_SEGMENT
+    segs = ct["rollup_segments"]
+    per_launch_flops = rollup_targets * segs * FLOPS_PER_SEGMENT
     mean_rollup_s = statistics.mean(rollup_ms) * 1e-3
     achieved = per_launch_flops / mean_rollup_s / 1e12
     peak = measure_fp32_peak(local, 5)
@@ -316,8 +318,13 @@ def run_gb300(args):
         "roofline": {"kernel": "k_bs_sweep (wake roll-up)", "bound": "fp32", "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak if peak > 0 else None, "traffic": traffic,
                      "peak_source": "measured FP32 FMA rate (sb_measure_fp32_peak); MEASURED_PEAKS.json has no FP32 entry",
-                     "flops_per_interaction": FLOPS_PER_SEGMENT, "interactions_per_launch": rollup_targets * 4.0 * nz,
+                     "flops_per_interaction": FLOPS_PER_SEGMENT,
+                     "segment_evaluations_per_launch": rollup_targets * segs,
+                     "reference_interactions_per_launch": rollup_targets * 4.0 * nz,
                      "mean_launch_ms": statistics.mean(rollup_ms)},
+        "shared_segments": {"active": sim.segment_sharing_active,
+                            "note": "value counts the reference's 4 segments per near panel pair; the roll-up "
+                                    "evaluates each wake segment shared by two rings once (strength difference)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": 1e3 * e2e_total / args.steps},
         "gpu_launches": launches,
@@ -433,6 +440,33 @@ def batched_solves(args, device):
                            "the solve starts from the lowest-residual of plain / extrapolation / network"}
     out["timing"] = "host clock around each public call, host freestream in, circulation and force summary out"
     return out
+
+
+# --------------------------------------------------------------------------------------
+# profiling workload: a short run whose last sweep launch is a full roll-up
+# --------------------------------------------------------------------------------------
+def run_profile_rollup(args):
+    """4 sails x 64 panels, `rows` wake rows, all-near-field, run rows + 4 steps: the last
+    k_bs_sweep launch of the process is the roll-up of a full wake (shared segments unless
+    --rings). Prints the number of k_bs_sweep launches, so an ncu capture can select the last
+    one with -k regex:k_bs_sweep -s <launches - 1> -c 1."""
+    from stormbird_gb300 import Simulation
+    from stormbird_gb300 import setups as S
+
+    rows = args.rows or 60
+    sim = Simulation(S.wing_sail_row(SAILS, PANELS, rows, time_step=DT, far_field_ratio=1e30))
+    if args.rings:
+        sim.set_segment_sharing(False)
+    wind = S.GustyWind(seed=0)
+    n = sim.nr_freestream_points
+    launches = 0
+    for k in range(rows + 4):
+        sim.do_step(time=k * DT, time_step=DT, freestream_velocity=wind.freestream(k * DT, n))
+        c = sim.last_step_counters()
+        launches += (1 if c["free_wake_panels"] > 0 else 0) + (1 if c["rollup_targets"] > 0 else 0)
+    print(json.dumps({"mode": "profile-rollup", "rows": rows, "k_bs_sweep_launches": launches,
+                      "shared_segments": sim.segment_sharing_active, "rollup_segments": c["rollup_segments"],
+                      "rollup_targets": c["rollup_targets"]}), flush=True)
 
 
 # --------------------------------------------------------------------------------------
@@ -605,6 +639,8 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel-only", action="store_true", help="standalone sweep on a synthetic wake (profiling)")
+    ap.add_argument("--profile-rollup", action="store_true", help="short all-near run ending in a full roll-up")
+    ap.add_argument("--rings", action="store_true", help="--profile-rollup without shared segments")
     ap.add_argument("--precision-study", action="store_true",
                     help="FP32 / compensated FP32 / FP64 sweeps of the 8 x 128 panel, 1000-row case")
     ap.add_argument("--rows", type=int, default=0, help="wake rows of the --kernel-only wake (default 300)")
@@ -622,6 +658,8 @@ def main():
         run_kernel_only(args)
     elif args.precision_study:
         run_precision_study(args)
+    elif args.profile_rollup:
+        run_profile_rollup(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

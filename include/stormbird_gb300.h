@@ -167,10 +167,24 @@ int sb_sim_last_step_timing(const sb_sim* sim, double* ms, size_t n);
 /*
  * Sizes of the last step's Biot-Savart sweeps: [0] roll-up target points, [1] panels
  * swept for the roll-up, [2] control points, [3] free-wake panels swept at the control
- * points, [4] steps completed, [5] kernels launched by the step. Zero-strength panels are
- * included in the panel counts (the sweeps skip them).
+ * points, [4] steps completed, [5] kernels launched by the step, [6] vortex segments
+ * evaluated per roll-up target (4 per panel, or fewer with shared segments). Zero-strength
+ * panels are included in the panel counts (the sweeps skip them).
  */
 int sb_sim_last_step_counters(const sb_sim* sim, double* counters, size_t n);
+
+/*
+ * Shared-segment roll-up (default on). In a wake where every panel pair is near-field
+ * (far_field_ratio >= 1e15) and all panels have one core length, each wake segment lies on
+ * two adjacent vortex rings with opposite directions; as the segment velocity of
+ * vortex_line.rs:18-106 is antisymmetric in its end points, the roll-up sweep evaluates each
+ * segment once with the difference of the two strengths (about half the evaluations of
+ * four segments per ring). The sum is the reference's, rounded differently. Active only in
+ * the FP32 modes; the control-point sweep and sb_sim_induced_velocities keep the rings.
+ */
+int sb_sim_set_segment_sharing(sb_sim* sim, int enable);
+/* 1 if the roll-up sweep of this simulation uses shared segments in its current mode. */
+int sb_sim_segment_sharing_active(const sb_sim* sim, int* active);
 
 /*
  * Standalone Biot-Savart sweep over caller-given vortex-ring panels: the velocity that

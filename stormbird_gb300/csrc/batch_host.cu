@@ -107,6 +107,7 @@ struct sb_batch {
     struct Group {
         int kind = 0;  // 0 frozen-wake sweep, 1 roll-up sweep
         int sym = 0, neglect = 0;
+        int chain = 0;  // sources are chain records (shared-segment roll-up)
         std::vector<int> cases;           // case of each job, costliest items first
         std::vector<int> chunk;           // panels per source chunk of each job
         std::vector<long long> part_off;  // offset of each job's partial sums
@@ -247,19 +248,22 @@ struct sb_batch {
     // Groups of sweeps that share a kernel variant.
     void make_groups() {
         groups.clear();
-        std::map<std::tuple<int, int, int>, int> index;
+        std::map<std::tuple<int, int, int, int>, int> index;
         for (size_t i = 0; i < cases.size(); ++i) {
-            const sb_sim& c = *cases[i];
+            sb_sim& c = *cases[i];
             if (!c.dynamic) continue;
+            c.precision = precision;
             for (int kind = 0; kind < 2; ++kind) {
                 const int neglect = kind == 0 ? c.dm.neglect_self : 0;
-                auto key = std::make_tuple(kind, c.dm.symmetry, neglect);
+                const int chain = kind == 1 && c.use_chains() ? 1 : 0;
+                auto key = std::make_tuple(kind, c.dm.symmetry, neglect, chain);
                 auto it = index.find(key);
                 if (it == index.end()) {
                     Group g;
                     g.kind = kind;
                     g.sym = c.dm.symmetry;
                     g.neglect = neglect;
+                    g.chain = chain;
                     it = index.emplace(key, static_cast<int>(groups.size())).first;
                     groups.push_back(g);
                 }
@@ -288,7 +292,7 @@ struct sb_batch {
             M_total = c.N;
         } else {
             M = c.dm.end_index > 0 ? std::min<long long>(c.dm.end_index, c.P_pts) : 0;
-            P = c.P_pan;
+            P = c.use_chains() ? c.chain_Q * c.chain_Bq : c.P_pan;  // chain and panel records cost alike
             M_total = c.P_pts;
         }
     }
@@ -371,7 +375,8 @@ struct sb_batch {
                 sb_sim& c = *cases[g.cases[k]];
                 sb_sim::SweepDesc d = g.kind == 0 ? c.fixed_desc() : c.rollup_desc();
                 BsJob J;
-                J.panels = precision == 2 ? static_cast<const void*>(c.rec64.p) : static_cast<const void*>(c.rec32.p);
+                J.panels = d.src ? d.src
+                                 : precision == 2 ? static_cast<const void*>(c.rec64.p) : static_cast<const void*>(c.rec32.p);
                 J.p_begin = d.p0;
                 J.p_end = d.p1;
                 J.targets = d.targets;
@@ -419,6 +424,7 @@ struct sb_batch {
         a.err = err.p;
         a.symmetry = g.sym;
         a.neglect = g.neglect;
+        a.chain = g.chain;
         ck(cudaMemsetAsync(a.work_counter, 0, sizeof(unsigned long long), main), "memset counter");
         ck(launch_bs_sweep(a, precision, g.grid, main), "batched Biot-Savart sweep");
         ck(launch_bs_reduce_jobs(a.jobs, a.n_jobs, g.reduce_blocks, main), "batched sweep reduce");
@@ -545,13 +551,8 @@ struct sb_batch {
             c->params.dt = dt;
             if (c->dynamic) {
                 c->cur ^= 1;
-                sb_sim::SweepDesc d = c->rollup_desc();
-                c->last_counters[0] = static_cast<double>(d.M);
-                c->last_counters[1] = static_cast<double>(d.p1 - d.p0);
-                c->last_counters[2] = static_cast<double>(c->N);
-                c->last_counters[3] = static_cast<double>(c->P_pan - c->N);
-                c->steps_completed += 1;
-                c->last_counters[4] = static_cast<double>(c->steps_completed);
+                c->after_fixed_sweep();
+                c->after_rollup_sweep();
             }
             c->fd_count += 1;
         }
@@ -848,6 +849,7 @@ int sb_batch_set_precision(sb_batch* b, int mode) {
     return guard([&] {
         if (mode != b->precision) {
             b->precision = mode;
+            b->make_groups();  // chain records are FP32 only
             b->plan(b->tuning);
         }
     });

@@ -124,53 +124,91 @@ __device__ __forceinline__ float2 sel2(bool cx, float2 a, bool cy, float2 b) {
 //   core * k = d2 (l1 + l2) A / (B sqrt(d2^2 + rc^4)) with a single rsqrt,
 // which is the reference's (vortex_line.rs:18-106) value, evaluated without the FP32
 // cancellations of its literal form. Returns sum_k core_k k_k c_k (times Gamma/4pi = velocity).
+// Corner vector r = e - o (o: FP32 offset of the corner from the record's anchor), |r|^2, |r|.
+__device__ __forceinline__ void corner2(float2 ex, float2 ey, float2 ez, const float* o, float2& rx, float2& ry,
+                                        float2& rz, float2& rs, float2& rl) {
+    rx = sub2s(ex, o[0]);
+    ry = sub2s(ey, o[1]);
+    rz = sub2s(ez, o[2]);
+    rs = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
+    // r = 0 (target on a corner) gives l = 0; the clamp runs on the ALU pipe
+    rl = mul2(rs, make_float2(rsqrtf(fmaxf(rs.x, 1e-30f)), rsqrtf(fmaxf(rs.y, 1e-30f))));
+}
+
+// One segment from corner 1 (r1) to corner 2 (r2 = r1 - d): s * c with c = d x r1, i.e.
+// core * k * (r1 x r2) of vortex_line.rs:18-106 (see above), added to (ax, ay, az), times the
+// weight g when WEIGHTED.
+template <bool WEIGHTED>
+__device__ __forceinline__ void segment2(float2 rx, float2 ry, float2 rz, float2 rs1, float2 rl1, float2 rs2,
+                                         float2 rl2, float dx, float dy, float dz, float il, float rc4, float g,
+                                         float2& ax, float2& ay, float2& az) {
+    const float2 p = mul2(rl1, rl2);
+    // projection on the segment, and r1.r2 = |r1|^2 - r1.d (r2 = r1 - d)
+    const float2 tp = fma2(rx, bc(dx), fma2(ry, bc(dy), mul2(rz, bc(dz))));
+    const float2 q = add2(rs1, make_float2(-tp.x, -tp.y));
+    const float2 cx = fma2(bc(dy), rz, mul2(bc(-dz), ry));
+    const float2 cy = fma2(bc(dz), rx, mul2(bc(-dx), rz));
+    const float2 cz = fma2(bc(dx), ry, mul2(bc(-dy), rx));
+    const float2 c2 = fma2(cx, cx, fma2(cy, cy, mul2(cz, cz)));
+    const bool n0 = q.x < 0.f, n1 = q.y < 0.f;
+    const float2 pmq = add2(p, make_float2(-q.x, -q.y));
+    const float2 ppq = add2(p, q);
+    const float2 Ax = make_float2(n0 ? pmq.x : 1.f, n1 ? pmq.y : 1.f);
+    const float2 Bx = mul2(p, make_float2(n0 ? c2.x : ppq.x, n1 ? c2.y : ppq.y));
+    const float2 tpl = mul2(tp, bc(il));
+    float2 d2 = mul2(c2, bc(il));
+    d2.x = tpl.x > 1.f ? rs2.x : d2.x;
+    d2.y = tpl.y > 1.f ? rs2.y : d2.y;
+    d2.x = tp.x < 0.f ? rs1.x : d2.x;
+    d2.y = tp.y < 0.f ? rs1.y : d2.y;
+    // X = 0 only where B = 0 too (target on the segment or a corner); the select below
+    // then discards the lane, so the clamp only keeps rsqrt finite
+    const float2 X = mul2(mul2(Bx, Bx), fma2(d2, d2, bc(rc4)));
+    const float2 Aw = WEIGHTED ? mul2(Ax, bc(g)) : Ax;
+    const float2 s0 = mul2(mul2(mul2(d2, add2(rl1, rl2)), Aw),
+                           make_float2(rsqrtf(fmaxf(X.x, 1e-37f)), rsqrtf(fmaxf(X.y, 1e-37f))));
+    const float2 lim = mul2(Ax, bc(1.0e-10f));
+    const float2 sg = make_float2(Bx.x > lim.x ? s0.x : 0.f, Bx.y > lim.y ? s0.y : 0.f);
+    ax = fma2(sg, cx, ax);
+    ay = fma2(sg, cy, ay);
+    az = fma2(sg, cz, az);
+}
+
 __device__ __forceinline__ void ring2(const float* v, float2 ex, float2 ey, float2 ez, float2& ax, float2& ay,
                                       float2& az) {
     float2 rx[4], ry[4], rz[4], rs[4], rl[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        rx[k] = sub2s(ex, v[3 * k]);
-        ry[k] = sub2s(ey, v[3 * k + 1]);
-        rz[k] = sub2s(ez, v[3 * k + 2]);
-        rs[k] = fma2(rx[k], rx[k], fma2(ry[k], ry[k], mul2(rz[k], rz[k])));
-        // r = 0 (target on a corner) gives l = 0; the clamp runs on the ALU pipe
-        rl[k] = mul2(rs[k], make_float2(rsqrtf(fmaxf(rs[k].x, 1e-30f)), rsqrtf(fmaxf(rs[k].y, 1e-30f))));
-    }
+    for (int k = 0; k < 4; ++k) corner2(ex, ey, ez, v + 3 * k, rx[k], ry[k], rz[k], rs[k], rl[k]);
     const float rc4 = v[40];
     ax = ay = az = bc(0.f);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const int k1 = (k + 1) & 3;
-        const float dx = v[12 + 3 * k], dy = v[12 + 3 * k + 1], dz = v[12 + 3 * k + 2], il = v[24 + k];
-        const float2 p = mul2(rl[k], rl[k1]);
-        // projection on the segment, and r1.r2 = |r1|^2 - r1.d (r2 = r1 - d)
-        const float2 tp = fma2(rx[k], bc(dx), fma2(ry[k], bc(dy), mul2(rz[k], bc(dz))));
-        const float2 q = add2(rs[k], make_float2(-tp.x, -tp.y));
-        const float2 cx = fma2(bc(dy), rz[k], mul2(bc(-dz), ry[k]));
-        const float2 cy = fma2(bc(dz), rx[k], mul2(bc(-dx), rz[k]));
-        const float2 cz = fma2(bc(dx), ry[k], mul2(bc(-dy), rx[k]));
-        const float2 c2 = fma2(cx, cx, fma2(cy, cy, mul2(cz, cz)));
-        const bool n0 = q.x < 0.f, n1 = q.y < 0.f;
-        const float2 pmq = add2(p, make_float2(-q.x, -q.y));
-        const float2 ppq = add2(p, q);
-        const float2 Ax = make_float2(n0 ? pmq.x : 1.f, n1 ? pmq.y : 1.f);
-        const float2 Bx = mul2(p, make_float2(n0 ? c2.x : ppq.x, n1 ? c2.y : ppq.y));
-        const float2 tpl = mul2(tp, bc(il));
-        float2 d2 = mul2(c2, bc(il));
-        d2.x = tpl.x > 1.f ? rs[k1].x : d2.x;
-        d2.y = tpl.y > 1.f ? rs[k1].y : d2.y;
-        d2.x = tp.x < 0.f ? rs[k].x : d2.x;
-        d2.y = tp.y < 0.f ? rs[k].y : d2.y;
-        // X = 0 only where B = 0 too (target on the segment or a corner); the select below
-        // then discards the lane, so the clamp only keeps rsqrt finite
-        const float2 X = mul2(mul2(Bx, Bx), fma2(d2, d2, bc(rc4)));
-        const float2 s0 = mul2(mul2(mul2(d2, add2(rl[k], rl[k1])), Ax),
-                               make_float2(rsqrtf(fmaxf(X.x, 1e-37f)), rsqrtf(fmaxf(X.y, 1e-37f))));
-        const float2 lim = mul2(Ax, bc(1.0e-10f));
-        const float2 s = make_float2(Bx.x > lim.x ? s0.x : 0.f, Bx.y > lim.y ? s0.y : 0.f);
-        ax = fma2(s, cx, ax);
-        ay = fma2(s, cy, ay);
-        az = fma2(s, cz, az);
+        segment2<false>(rx[k], ry[k], rz[k], rs[k], rl[k], rs[k1], rl[k1], v[12 + 3 * k], v[12 + 3 * k + 1],
+                        v[12 + 3 * k + 2], v[24 + k], rc4, 1.f, ax, ay, az);
+    }
+}
+
+// Open chain of a chain record (kChain* layout) at two targets: five corners shared by four
+// segments, each weighted by its strength difference / 4 pi. Corners are computed as the
+// chain advances (two live at a time).
+__device__ __forceinline__ void chain2(const float* v, float2 ex, float2 ey, float2 ez, float2& ax, float2& ay,
+                                       float2& az) {
+    float2 rxa, rya, rza, rsa, rla;
+    corner2(ex, ey, ez, v + kChainOff, rxa, rya, rza, rsa, rla);
+    const float rc4 = v[kChainRc4];
+    ax = ay = az = bc(0.f);
+#pragma unroll
+    for (int k = 0; k < kChainSegs; ++k) {
+        float2 rxb, ryb, rzb, rsb, rlb;
+        corner2(ex, ey, ez, v + kChainOff + 3 * (k + 1), rxb, ryb, rzb, rsb, rlb);
+        segment2<true>(rxa, rya, rza, rsa, rla, rsb, rlb, v[kChainD + 3 * k], v[kChainD + 3 * k + 1],
+                       v[kChainD + 3 * k + 2], v[kChainIl + k], rc4, v[kChainG + k], ax, ay, az);
+        rxa = rxb;
+        rya = ryb;
+        rza = rzb;
+        rsa = rsb;
+        rla = rlb;
     }
 }
 
@@ -186,12 +224,13 @@ __device__ __forceinline__ int find_job(const BsJob* jobs, int n, long long item
     return lo;
 }
 
-template <class R, int T, bool KAHAN, int SYM, bool NEGLECT>
+template <class R, int T, bool KAHAN, int SYM, bool NEGLECT, bool CHAIN>
 __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
     constexpr int TILE = TileSize<R>::value;
     constexpr int TT = SYM ? 2 * T : T;  // mirrored targets ride along as extra targets
     constexpr bool F32 = sizeof(R) == 4;
     static_assert(!F32 || TT == 2, "the packed FP32 path holds exactly two targets per thread");
+    static_assert(!CHAIN || (F32 && !NEGLECT), "chain records: FP32 sweeps without neglect-self only");
     __shared__ __align__(128) PanelRec<R> tile[2][TILE];
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ long long s_item;
@@ -288,6 +327,18 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
                 float2 TX = bc(0.f), TY = bc(0.f), TZ = bc(0.f);
                 for (int p = 0; p < np; ++p) {
                     const float* v = reinterpret_cast<const float*>(tile[buf][p].v);
+                    if constexpr (CHAIN) {  // every pair near-field: the chain's segments
+                        if (v[kChainAny] == 0.f) continue;  // uniform across the CTA
+                        const float2 ex = add2(sub2s(X2h, v[0]), sub2s(X2l, v[3]));
+                        const float2 ey = add2(sub2s(Y2h, v[1]), sub2s(Y2l, v[4]));
+                        const float2 ez = add2(sub2s(Z2h, v[2]), sub2s(Z2l, v[5]));
+                        float2 ax, ay, az;
+                        chain2(v, ex, ey, ez, ax, ay, az);
+                        TX = add2(TX, ax);
+                        TY = add2(TY, ay);
+                        TZ = add2(TZ, az);
+                        continue;
+                    }
                     const float gam = v[kRec32Gamma];
                     if (gam == 0.f) continue;  // uniform across the CTA
                     const float ff2 = v[31];
@@ -513,10 +564,20 @@ cudaError_t launch_horseshoe_matrix(const DevModel& m, int core_kind, double cor
 // ---------------------------------------------------------------------------------------
 // Host launchers
 // ---------------------------------------------------------------------------------------
-template <class R, int T, bool KAHAN, int SYM, bool NEGLECT>
+template <class R, int T, bool KAHAN, int SYM, bool NEGLECT, bool CHAIN = false>
 static cudaError_t launch_t(const BsArgs& a, int grid, cudaStream_t s) {
-    k_bs_sweep<R, T, KAHAN, SYM, NEGLECT><<<grid, kBsThreads, 0, s>>>(a);
+    k_bs_sweep<R, T, KAHAN, SYM, NEGLECT, CHAIN><<<grid, kBsThreads, 0, s>>>(a);
     return cudaGetLastError();
+}
+
+template <bool KAHAN>
+static cudaError_t launch_chain(const BsArgs& a, int grid, cudaStream_t s) {
+    switch (a.symmetry) {
+        case 0: return launch_t<float, 2, KAHAN, 0, false, true>(a, grid, s);
+        case 1: return launch_t<float, 1, KAHAN, 1, false, true>(a, grid, s);
+        case 2: return launch_t<float, 1, KAHAN, 2, false, true>(a, grid, s);
+        default: return launch_t<float, 1, KAHAN, 3, false, true>(a, grid, s);
+    }
 }
 
 template <class R, bool KAHAN>
@@ -541,6 +602,10 @@ int bs_targets_per_thread(int symmetry) { return symmetry == 0 ? 2 : 1; }
 int bs_tile_panels(int precision) { return precision == 2 ? TileSize<double>::value : TileSize<float>::value; }
 
 cudaError_t launch_bs_sweep(const BsArgs& a, int precision, int grid, cudaStream_t s) {
+    if (a.chain) {
+        if (precision == 2 || a.neglect) return cudaErrorInvalidValue;
+        return precision == 1 ? launch_chain<false>(a, grid, s) : launch_chain<true>(a, grid, s);
+    }
     if (precision == 2) return launch_sym<double, false>(a, grid, s);
     if (precision == 1) return launch_sym<float, false>(a, grid, s);
     return launch_sym<float, true>(a, grid, s);
@@ -549,7 +614,8 @@ cudaError_t launch_bs_sweep(const BsArgs& a, int precision, int grid, cudaStream
 int bs_occupancy_blocks_per_sm(int precision, int symmetry, int neglect) {
     int nb = 0;
     cudaError_t e;
-#define SB_OCC(R, T, K, S, NG) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bs_sweep<R, T, K, S, NG>, kBsThreads, 0)
+#define SB_OCC(R, T, K, S, NG) \
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bs_sweep<R, T, K, S, NG, false>, kBsThreads, 0)
     if (precision == 2) {
         if (symmetry == 0) { if (neglect) SB_OCC(double, 2, false, 0, true); else SB_OCC(double, 2, false, 0, false); }
         else { if (neglect) SB_OCC(double, 1, false, 1, true); else SB_OCC(double, 1, false, 1, false); }

@@ -279,6 +279,100 @@ __global__ void k_wake_panels(DevModel m, WakeBuffers w, int shift) {
     if (w.rec64) w.rec64[id] = q;
 }
 
+// ---------------------------------------------------------------------------------------
+// Chain records. Panel (s, j) of wing w has corners p0 = P[s][j+w], p1 = P[s][j+1+w],
+// p2 = P[s+1][j+1+w], p3 = P[s+1][j+w] and segments p0->p1, p1->p2, p2->p3, p3->p0
+// (mod.rs:82-103 indexing, panel.rs:99-118 ring). The spanwise segment P[r][j+w] ->
+// P[r][j+1+w] is segment 0 of panel (r, j) and, reversed, segment 2 of panel (r-1, j);
+// the streamwise segment P[s][c] -> P[s+1][c] on column c = j + w is segment 1 of panel
+// (s, j-1) and, reversed, segment 3 of panel (s, j). The unit-strength velocity of a
+// segment changes sign with its direction (vortex_line.rs:18-106 is antisymmetric in the
+// two end points, the core factor symmetric), so with one core length for all panels the
+// two rings' contributions are one evaluation with the strength difference.
+// ---------------------------------------------------------------------------------------
+__device__ inline double chain_strength(const ChainArgs& a, int s, int j) {
+    return (s >= 0 && s < a.W) ? a.str[static_cast<long long>(s) * a.N + j] : 0.0;
+}
+
+__global__ void k_chain_records(ChainArgs a, long long n_build) {
+    const long long id = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+    if (id >= n_build) return;
+    const long long q = id / a.Bq, local = id % a.Bq;
+    const long long Np = a.Np;
+    d3 pt[kChainSegs + 1];
+    double g[kChainSegs] = {0.0, 0.0, 0.0, 0.0};
+    int npts = 0, wing = 0;
+    if (local < 4LL * a.SP) {  // spanwise chain
+        const int r = static_cast<int>(4 * q + local / a.SP);
+        const int piece = static_cast<int>(local % a.SP);
+        wing = a.span_tab[3 * piece];
+        const int j0 = a.span_tab[3 * piece + 1], n = a.span_tab[3 * piece + 2];
+        if (r <= a.W) {
+            npts = n + 1;
+            for (int k = 0; k <= n; ++k) pt[k] = a.pts[r * Np + j0 + k + wing];
+            for (int k = 0; k < n; ++k) g[k] = chain_strength(a, r, j0 + k) - chain_strength(a, r - 1, j0 + k);
+        }
+    } else {  // streamwise chain of panel rows 4q..4q+3 on one point column
+        const int col = static_cast<int>(local - 4LL * a.SP);
+        wing = a.col_tab[2 * col];
+        const int j = a.col_tab[2 * col + 1];
+        const int ws = a.wing_start[wing], we = a.wing_end[wing];
+        const int s0 = static_cast<int>(4 * q);
+        if (s0 < a.W) {
+            const int n = min(kChainSegs, a.W - s0);
+            npts = n + 1;
+            for (int k = 0; k <= n; ++k) pt[k] = a.pts[static_cast<long long>(s0 + k) * Np + col];
+            for (int k = 0; k < n; ++k) {
+                const double left = j - 1 >= ws ? chain_strength(a, s0 + k, j - 1) : 0.0;
+                const double right = j < we ? chain_strength(a, s0 + k, j) : 0.0;
+                g[k] = left - right;
+            }
+        }
+    }
+    PanelRec<float> rec;
+    for (int k = 0; k < 48; ++k) rec.v[k] = 0.f;
+    if (npts > 1) {
+        for (int k = npts; k <= kChainSegs; ++k) pt[k] = pt[npts - 1];  // empty segments
+        const d3 anchor = pt[2 < npts ? 2 : npts - 1];
+        auto split = [](double x, float* hi, float* lo) {
+            const float h = static_cast<float>(x);
+            *hi = h;
+            *lo = static_cast<float>(x - static_cast<double>(h));
+        };
+        split(anchor.x, &rec.v[0], &rec.v[3]);
+        split(anchor.y, &rec.v[1], &rec.v[4]);
+        split(anchor.z, &rec.v[2], &rec.v[5]);
+        for (int k = 0; k <= kChainSegs; ++k) {
+            const d3 o = pt[k] - anchor;
+            rec.v[kChainOff + 3 * k] = static_cast<float>(o.x);
+            rec.v[kChainOff + 3 * k + 1] = static_cast<float>(o.y);
+            rec.v[kChainOff + 3 * k + 2] = static_cast<float>(o.z);
+        }
+        double any = 0.0;
+        for (int k = 0; k < kChainSegs; ++k) {
+            const d3 dk = pt[k + 1] - pt[k];
+            rec.v[kChainD + 3 * k] = static_cast<float>(dk.x);
+            rec.v[kChainD + 3 * k + 1] = static_cast<float>(dk.y);
+            rec.v[kChainD + 3 * k + 2] = static_cast<float>(dk.z);
+            const double l2 = len2(dk);
+            rec.v[kChainIl + k] = l2 > 0.0 ? static_cast<float>(1.0 / l2) : 0.f;
+            rec.v[kChainG + k] = static_cast<float>(g[k] * kFourPiInv);
+            any += fabs(g[k]);
+        }
+        const double rc2 = a.rc * a.rc;
+        rec.v[kChainRc4] = static_cast<float>(rc2 * rc2);
+        rec.v[kChainWing] = static_cast<float>(wing);
+        rec.v[kChainAny] = static_cast<float>(any);
+    }
+    a.out[id] = rec;
+}
+
+cudaError_t launch_chain_records(const ChainArgs& a, long long n_build, cudaStream_t s) {
+    if (n_build <= 0) return cudaSuccess;
+    k_chain_records<<<static_cast<unsigned>((n_build + 127) / 128), 128, 0, s>>>(a, n_build);
+    return cudaGetLastError();
+}
+
 // Records of caller-given panels (corners [P][4][3], strengths, core lengths) for the
 // standalone sweep sb_panel_sweep.
 __global__ void k_panels_from_corners(const double* corners, const double* strengths, const double* cores, long long P,

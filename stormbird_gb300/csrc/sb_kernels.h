@@ -43,6 +43,7 @@ struct BsArgs {
     int* err = nullptr;
     int symmetry = 0;
     int neglect = 0;
+    int chain = 0;  // the sources are chain records (FP32 only, no neglect-self)
 };
 
 constexpr int kBsReduceThreads = 256;
@@ -92,6 +93,25 @@ cudaError_t launch_wake_advect(const DevModel& m, const WakeBuffers& w, double d
 // Panels of the new points and downstream strength shift (update_data.rs:102-115, 319-328).
 // `shift_strengths` = 0 rebuilds the panels without moving strengths (initialisation).
 cudaError_t launch_wake_panels(const DevModel& m, const WakeBuffers& w, int shift_strengths, cudaStream_t s);
+
+// Chain records of a wake whose panels all share one core length (kChain* layout in
+// sb_device.cuh), ordered in quads of point rows: quad q holds the spanwise chains of point
+// rows 4q..4q+3 (SP chains per row, up to 4 lines of one wing each), then the streamwise
+// chains of panel rows 4q..4q+3 (one per point column). Records past the wake's last row are
+// written empty. Only the first n_build records are written.
+struct ChainArgs {
+    const d3* pts = nullptr;        // [W+1][Np] wake points
+    const double* str = nullptr;    // [W][N] strengths (row 0: this step's solution)
+    const int* span_tab = nullptr;  // [SP][3]: wing, first line, number of lines (<= 4)
+    const int* col_tab = nullptr;   // [Np][2]: wing, point number j (column = j + wing)
+    const int* wing_start = nullptr;
+    const int* wing_end = nullptr;
+    int W = 0, N = 0, Np = 0, SP = 0;
+    long long Bq = 0;               // records per quad: 4 SP + Np
+    double rc = 0.0;                // the common core length
+    PanelRec<float>* out = nullptr;
+};
+cudaError_t launch_chain_records(const ChainArgs& a, long long n_build, cudaStream_t s);
 
 // Records of caller-given panels for the standalone sweep (corners [P][4][3] in ring order).
 cudaError_t launch_panels_from_corners(const double* corners, const double* strengths, const double* cores, long long P,

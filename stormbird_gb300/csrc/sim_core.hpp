@@ -258,7 +258,7 @@ struct sb_sim {
     std::vector<double> chord_lengths_h;
     bool timing = false;
     double last_ms[9] = {0};
-    double last_counters[6] = {0};
+    double last_counters[7] = {0};
     int launches = 0;
     bool swept[2] = {false, false};
 
@@ -296,6 +296,14 @@ struct sb_sim {
     double* gamma_p = nullptr;
     // Predicted initial solutions [N] offered to the SimpleIterative solve, or nullptr.
     const double* candidate_p[2] = {nullptr, nullptr};
+    // Shared-segment roll-up (chain records, launch_chain_records): possible when every pair
+    // is near-field and all panels share one core length; on unless switched off.
+    bool chain_ok = false, share_segments = true;
+    DevBuf<PanelRec<float>> chains;
+    DevBuf<int> chain_span_tab, chain_col_tab;
+    int chain_SP = 0;
+    long long chain_Bq = 0, chain_Q = 0;
+    double chain_rc = 0.0;
 
     ~sb_sim() {
         for (auto& e : ev) if (e) cudaEventDestroy(e);
@@ -528,6 +536,7 @@ struct sb_sim {
         }
         panel_core.upload(core);
         dm.panel_core = panel_core.p;
+        setup_chains(core);
         d3 sum = mk(0, 0, 0);
         for (const auto& c : hc) sum = sum + c;
         d3 avg = sum / static_cast<double>(Np);
@@ -535,6 +544,71 @@ struct sb_sim {
         d3 U = (wl / static_cast<double>(W)) * avg;
         ck(launch_wake_init(dm, wake(false), nullptr, U, 1.0, 1, stream), "wake init");
         ck(launch_wake_panels(dm, wake(false), 0, stream), "wake panels");
+    }
+
+    // Every pair is near-field when far_field_ratio >= 1e15: the near-field radius is then at
+    // least 1e6 m for any panel longer than 1e-9 m (panel.rs:53-57), beyond any target
+    // distance; shorter (degenerate) panels contribute nothing either way.
+    static constexpr double kAllNearRatio = 1e15;
+
+    void setup_chains(const std::vector<double>& core) {
+        chain_ok = dm.far_field_ratio >= kAllNearRatio && !core.empty() &&
+                   std::all_of(core.begin(), core.end(), [&](double c) { return c == core[0]; });
+        if (!chain_ok) return;
+        chain_rc = core[0];
+        std::vector<int> st, ct;
+        std::vector<int> ws(S), we(S);
+        ck(cudaMemcpy(ws.data(), wing_start.p, S * sizeof(int), cudaMemcpyDeviceToHost), "D2H");
+        ck(cudaMemcpy(we.data(), wing_end.p, S * sizeof(int), cudaMemcpyDeviceToHost), "D2H");
+        for (int w = 0; w < S; ++w) {
+            for (int j0 = ws[w]; j0 < we[w]; j0 += kChainSegs) {
+                st.push_back(w);
+                st.push_back(j0);
+                st.push_back(std::min(kChainSegs, we[w] - j0));
+            }
+            for (int j = ws[w]; j <= we[w]; ++j) {  // point column j + w
+                ct.push_back(w);
+                ct.push_back(j);
+            }
+        }
+        chain_SP = static_cast<int>(st.size() / 3);
+        chain_span_tab.upload(st);
+        chain_col_tab.upload(ct);
+        chain_Bq = 4LL * chain_SP + Np;
+        chain_Q = (W + 1 + 3) / 4;
+        chains.alloc(static_cast<size_t>(chain_Q * chain_Bq));
+    }
+
+    bool use_chains() const { return chain_ok && share_segments && precision != 2; }
+
+    // Panel rows that can hold a nonzero strength (see active_panels).
+    int active_rows() const { return std::min(W, steps_completed + 2); }
+
+    // Chain records covering the active rows: the quads up to the one holding point row R
+    // (its spanwise segments carry -strength of row R - 1).
+    long long active_chain_records() const {
+        return std::min<long long>(chain_Q, active_rows() / 4 + 1) * chain_Bq;
+    }
+
+    void build_chains() {
+        ChainArgs c;
+        c.pts = pts[cur].p;
+        c.str = str[cur].p;
+        c.span_tab = chain_span_tab.p;
+        c.col_tab = chain_col_tab.p;
+        c.wing_start = wing_start.p;
+        c.wing_end = wing_end.p;
+        c.W = W;
+        c.N = N;
+        c.Np = Np;
+        c.SP = chain_SP;
+        c.Bq = chain_Bq;
+        c.rc = chain_rc;
+        c.out = chains.p;
+        // all records, also the empty ones past the active rows: a captured step replays
+        // this launch with its arguments unchanged while the wake grows
+        ck(launch_chain_records(c, chain_Q * chain_Bq, stream), "chain records");
+        launches += 1;
     }
 
     // ---------------------------------------------------------------- one step
@@ -550,9 +624,27 @@ struct sb_sim {
         return make_sweep_plan(M, P, precision, sym, neglect, sms);
     }
 
+    // One Biot-Savart sweep of a step: targets [0, M) against panels [p0, p1), written to
+    // dst with `base` added; dst rows [M, M_total) get `base` only.
+    struct SweepDesc {
+        const d3* targets;
+        long long M, p0, p1;
+        const int* twing;
+        const d3* base;
+        long long M_total;
+        d3* dst;
+        const void* src = nullptr;  // chain records, or nullptr for the panel records
+        bool chain = false;
+        double segments = 0.0;      // segment evaluations per target
+    };
+
     // Biot-Savart sweep into out[0..M) (+ base), base only for [M, M_total).
-    void sweep(const d3* targets, long long M, long long p0, long long p1, const int* twing, const d3* base,
-               long long M_total, d3* dst, int counter_slot) {
+    void sweep(const SweepDesc& d, int counter_slot) {
+        const d3* targets = d.targets;
+        const long long M = d.M, p0 = d.p0, p1 = d.p1, M_total = d.M_total;
+        const int* twing = d.twing;
+        const d3* base = d.base;
+        d3* dst = d.dst;
         int sym = dm.symmetry;
         int neglect = twing ? 1 : 0;
         long long P = p1 - p0;
@@ -561,7 +653,8 @@ struct sb_sim {
             size_t need = static_cast<size_t>(sp.n_chunks) * static_cast<size_t>(M) * 3;
             if (partial.n < need) partial.alloc(need);
             BsArgs a;
-            a.job0.panels = precision == 2 ? static_cast<const void*>(rec64.p) : static_cast<const void*>(rec32.p);
+            a.job0.panels = d.src ? d.src : precision == 2 ? static_cast<const void*>(rec64.p) : static_cast<const void*>(rec32.p);
+            a.chain = d.chain ? 1 : 0;
             a.job0.p_begin = p0;
             a.job0.p_end = p1;
             a.job0.targets = targets;
@@ -597,29 +690,16 @@ struct sb_sim {
     void enqueue_step(double time, double dt) {
         step_begin(time, dt);
         if (dynamic) {
-            SweepDesc d = fixed_desc();
-            sweep(d.targets, d.M, d.p0, d.p1, d.twing, d.base, d.M_total, d.dst, 0);
+            sweep(fixed_desc(), 0);
             after_fixed_sweep();
         }
         step_matrix_and_solve();
         if (dynamic) {
-            SweepDesc d = rollup_desc();
-            sweep(d.targets, d.M, d.p0, d.p1, d.twing, d.base, d.M_total, d.dst, 1);
+            sweep(rollup_desc(), 1);
             after_rollup_sweep();
         }
         step_end();
     }
-
-    // One Biot-Savart sweep of a step: targets [0, M) against panels [p0, p1), written to
-    // dst with `base` added; dst rows [M, M_total) get `base` only.
-    struct SweepDesc {
-        const d3* targets;
-        long long M, p0, p1;
-        const int* twing;
-        const d3* base;
-        long long M_total;
-        d3* dst;
-    };
 
     // Panels that can hold a nonzero strength in this step's sweeps. Strength rows move one
     // row downstream per step and row 0 takes the new solution (update_data.rs:146-150,
@@ -634,7 +714,8 @@ struct sb_sim {
     // frozen wake (frozen_wake.rs:189-261): the free wake at the control points
     SweepDesc fixed_desc() const {
         const long long p1 = std::max<long long>(N, active_panels());
-        return {ctrl.p, N, N, p1, dm.neglect_self ? wing_of_line.p : nullptr, nullptr, N, fixed.p};
+        return {ctrl.p, N, N, p1, dm.neglect_self ? wing_of_line.p : nullptr, nullptr, N, fixed.p, nullptr, false,
+                4.0 * static_cast<double>(p1 - N)};
     }
 
     // DynamicWake::update_after_solving (update_data.rs:49-59, 125-141)
@@ -643,7 +724,14 @@ struct sb_sim {
         const d3* wake_fs = fs_p + N;
         if (!rollup_active()) return {nullptr, 0, 0, 0, nullptr, wake_fs, P_pts, vel.p};
         long long e = std::min<long long>(dm.end_index, P_pts);
-        return {pts[cur].p, e, 0, active_panels(), nullptr, wake_fs, P_pts, vel.p};
+        if (use_chains()) {
+            // segments of rows < R: spanwise on point rows 0..R, streamwise on panel rows 0..R-1
+            const double R = static_cast<double>(active_rows());
+            return {pts[cur].p, e, 0, active_chain_records(), nullptr, wake_fs, P_pts, vel.p, chains.p, true,
+                    (R + 1.0) * N + R * Np};
+        }
+        return {pts[cur].p, e, 0, active_panels(), nullptr, wake_fs, P_pts, vel.p, nullptr, false,
+                4.0 * static_cast<double>(active_panels())};
     }
 
     void after_fixed_sweep() {
@@ -655,7 +743,8 @@ struct sb_sim {
     void after_rollup_sweep() {
         SweepDesc d = rollup_desc();
         last_counters[0] = static_cast<double>(d.M);
-        last_counters[1] = static_cast<double>(d.p1 - d.p0);
+        last_counters[1] = static_cast<double>(d.chain ? active_panels() : d.p1 - d.p0);
+        last_counters[6] = d.M > 0 ? d.segments : 0.0;
         steps_completed += 1;
         last_counters[4] = static_cast<double>(steps_completed);
         record(6);
@@ -745,6 +834,8 @@ struct sb_sim {
             ck(launch_solve_linearized(dm, solve, sb, stream), "linearized solve");
         }
         launches += 1;
+        // chain records of the wake with this step's solution in row 0, for the roll-up
+        if (dynamic && use_chains() && rollup_active()) build_chains();
         record(5);
         if (!dynamic) record(6);
     }
@@ -860,7 +951,8 @@ struct sb_sim {
         ensure_rec64();
         if (aux_targets.n < n) { aux_targets.alloc(n); aux_out.alloc(n); }
         ck(cudaMemcpyAsync(aux_targets.p, p, n * sizeof(d3), cudaMemcpyHostToDevice, stream), "H2D points");
-        sweep(aux_targets.p, static_cast<long long>(n), 0, P_pan, nullptr, nullptr, static_cast<long long>(n), aux_out.p, 2);
+        sweep({aux_targets.p, static_cast<long long>(n), 0, P_pan, nullptr, nullptr, static_cast<long long>(n), aux_out.p},
+              2);
         ck(cudaMemcpyAsync(o, aux_out.p, n * sizeof(d3), cudaMemcpyDeviceToHost, stream), "D2H velocities");
         ck(cudaMemcpyAsync(h_err.p, err.p, sizeof(int), cudaMemcpyDeviceToHost, stream), "D2H status");
         ck(cudaStreamSynchronize(stream), "induced velocities");

@@ -204,7 +204,19 @@ int sb_sim_last_step_timing(const sb_sim* sim, double* ms, size_t n) {
 
 int sb_sim_last_step_counters(const sb_sim* sim, double* c, size_t n) {
     if (!sim || !c) { g_last_error = "null argument"; return SB_ERR_NULL_ARG; }
-    for (size_t i = 0; i < n && i < 6; ++i) c[i] = sim->last_counters[i];
+    for (size_t i = 0; i < n && i < 7; ++i) c[i] = sim->last_counters[i];
+    return SB_OK;
+}
+
+int sb_sim_set_segment_sharing(sb_sim* sim, int enable) {
+    if (!sim) { g_last_error = "null handle"; return SB_ERR_NULL_ARG; }
+    sim->share_segments = enable != 0;
+    return SB_OK;
+}
+
+int sb_sim_segment_sharing_active(const sb_sim* sim, int* active) {
+    if (!sim || !active) { g_last_error = "null argument"; return SB_ERR_NULL_ARG; }
+    *active = sim->use_chains() ? 1 : 0;
     return SB_OK;
 }
 

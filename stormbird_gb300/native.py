@@ -47,6 +47,8 @@ SIGNATURES = [
     ("sb_sim_enable_timing", ctypes.c_int, [_vp, ctypes.c_int]),
     ("sb_sim_last_step_timing", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
     ("sb_sim_last_step_counters", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
+    ("sb_sim_set_segment_sharing", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("sb_sim_segment_sharing_active", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int)]),
     ("sb_panel_sweep", ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp, ctypes.c_size_t, ctypes.c_double, ctypes.c_int,
                                       _dp, ctypes.c_size_t, ctypes.c_int, _dp]),
     ("sb_panel_sweep_no_alloc", ctypes.c_int, [ctypes.c_int, _vp, _vp, _vp, ctypes.c_size_t, ctypes.c_double,

@@ -147,11 +147,23 @@ class Simulation:
         return dict(zip(keys, ms.tolist()))
 
     def last_step_counters(self) -> dict:
-        c = np.zeros(6)
-        _check(lib().sb_sim_last_step_counters(self._h, as_ptr(c), 6))
+        c = np.zeros(7)
+        _check(lib().sb_sim_last_step_counters(self._h, as_ptr(c), 7))
         keys = ("rollup_targets", "rollup_panels", "ctrl_targets", "free_wake_panels", "steps_completed",
-                "kernel_launches")
+                "kernel_launches", "rollup_segments")
         return dict(zip(keys, c.tolist()))
+
+    def set_segment_sharing(self, on: bool = True):
+        """Shared-segment roll-up sweep (default on; used when every pair is near-field and all
+        panels share one core length): each wake segment evaluated once with the strength
+        difference of its two panels."""
+        _check(lib().sb_sim_set_segment_sharing(self._h, 1 if on else 0))
+
+    @property
+    def segment_sharing_active(self) -> bool:
+        v = ctypes.c_int()
+        _check(lib().sb_sim_segment_sharing_active(self._h, ctypes.byref(v)))
+        return bool(v.value)
 
 
 def measure_fp32_peak(device: int = 0, reps: int = 5) -> float:
