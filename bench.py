@@ -469,6 +469,35 @@ def run_profile_rollup(args):
                       "rollup_targets": c["rollup_targets"]}), flush=True)
 
 
+def run_profile_mlp(args):
+    """Warm-start network forward passes over 131,072 rows (1,024 GEMM tiles of 128 rows),
+    three times, then one training step on 16,384 rows: 4 tensor-core GEMMs per forward pass
+    (K = 64, 256, 256, 256), so -k regex:k_mlp_gemm -s 4 -c 4 captures the second pass.
+    Prints the forward time per pass (CUDA events) and the GEMM rate it implies."""
+    import torch
+
+    from stormbird_gb300.warm_start import FEATURES, WarmStartNet
+
+    rows = 131072
+    net = WarmStartNet(FEATURES, seed=0)
+    x = torch.randn((rows, FEATURES), dtype=torch.float32, device="cuda:0")
+    t = torch.randn(16384, dtype=torch.float32, device="cuda:0")
+    ms = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        net.forward(x)
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    net.train_step(x[:16384].contiguous(), t, 1e-3)
+    flops = 2.0 * rows * 256 * (64 + 3 * 256)
+    print(json.dumps({"mode": "profile-mlp", "rows": rows, "forward_ms": ms,
+                      "gemm_tflops_best_pass": flops / (min(ms) * 1e-3) / 1e12,
+                      "note": "host-launched forward incl. input packing and the output layer"}), flush=True)
+
+
 # --------------------------------------------------------------------------------------
 # precision study: 8 sails x 128 panels, 1000 wake rows (1,024,000 rings, 1,033,032 points)
 # --------------------------------------------------------------------------------------
@@ -641,6 +670,7 @@ def main():
     ap.add_argument("--kernel-only", action="store_true", help="standalone sweep on a synthetic wake (profiling)")
     ap.add_argument("--profile-rollup", action="store_true", help="short all-near run ending in a full roll-up")
     ap.add_argument("--rings", action="store_true", help="--profile-rollup without shared segments")
+    ap.add_argument("--profile-mlp", action="store_true", help="warm-start network forward passes (GEMM capture)")
     ap.add_argument("--precision-study", action="store_true",
                     help="FP32 / compensated FP32 / FP64 sweeps of the 8 x 128 panel, 1000-row case")
     ap.add_argument("--rows", type=int, default=0, help="wake rows of the --kernel-only wake (default 300)")
@@ -660,6 +690,8 @@ def main():
         run_precision_study(args)
     elif args.profile_rollup:
         run_profile_rollup(args)
+    elif args.profile_mlp:
+        run_profile_mlp(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

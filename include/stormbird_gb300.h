@@ -183,6 +183,19 @@ int sb_sim_last_step_counters(const sb_sim* sim, double* counters, size_t n);
  * the FP32 modes; the control-point sweep and sb_sim_induced_velocities keep the rings.
  */
 int sb_sim_set_segment_sharing(sb_sim* sim, int enable);
+
+/*
+ * Freestream from a wind model, generated on the GPU: the reference's
+ * CompleteSailModel::freestream_velocity (complete_sail_model/mod.rs:213-257) with a
+ * WindEnvironment (wind/environment.rs:21-55) and a WindCondition
+ * (wind/wind_condition/mod.rs:19-39) given as JSON, the ship moving at `ship_velocity`
+ * along the environment's zero direction. sb_sim_do_step_wind is sb_sim_do_step with that
+ * freestream, so no freestream crosses the host boundary; sb_sim_wind_freestream writes it
+ * (all freestream points, host buffer of n = nr_freestream_points) for inspection.
+ */
+int sb_sim_set_wind(sb_sim* sim, const char* environment_json, const char* condition_json);
+int sb_sim_wind_freestream(sb_sim* sim, double time, double ship_velocity, double* freestream_xyz, size_t n);
+int sb_sim_do_step_wind(sb_sim* sim, double time, double time_step, double ship_velocity, sb_step_output* out);
 /* 1 if the roll-up sweep of this simulation uses shared segments in its current mode. */
 int sb_sim_segment_sharing_active(const sb_sim* sim, int* active);
 

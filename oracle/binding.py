@@ -55,6 +55,8 @@ def lib() -> ctypes.CDLL:
         L.sbo_sigmoid.argtypes = [c_double, c_double, c_double]
         L.sbo_foil_eval.argtypes = [ctypes.c_char_p, c_double, dp]
         L.sbo_bs_sweep.argtypes = [dp, dp, dp, c_size_t, c_double, dp, c_size_t, dp, c_int]
+        L.sbo_sim_wind_freestream.argtypes = [c_void_p, ctypes.c_char_p, ctypes.c_char_p, c_double, c_double, dp,
+                                              c_size_t]
         _LIB = L
     return _LIB
 
@@ -142,6 +144,13 @@ class OracleSimulation:
     def set_previous_circulation_strength(self, g):
         a = _d(g)
         _check(lib().sbo_sim_set_previous_circulation(self._h, as_ptr(a), a.size))
+
+    def wind_freestream(self, environment_json: str, condition_json: str, time: float, ship_velocity: float):
+        """CompleteSailModel::freestream_velocity at this simulation's freestream points."""
+        out = np.zeros((self.nr_freestream_points, 3))
+        _check(lib().sbo_sim_wind_freestream(self._h, environment_json.encode(), condition_json.encode(), float(time),
+                                             float(ship_velocity), as_ptr(out), out.shape[0]))
+        return out
 
     def wake_state(self):
         npts, npan, nspan, W = (ctypes.c_size_t() for _ in range(4))

@@ -17,6 +17,8 @@ LIB = os.path.join(OUT_DIR, "libsb_oracle.so")
 SOURCES = [os.path.join(HERE, "sb_oracle_capi.cpp")]
 DEPS = SOURCES + [
     os.path.join(HERE, "sb_oracle.hpp"),
+    os.path.join(HERE, "sb_oracle_wind.hpp"),
+    os.path.join(HERE, "..", "stormbird_gb300", "csrc", "sb_wind_setup.hpp"),
     os.path.join(HERE, "..", "stormbird_gb300", "csrc", "sb_setup.hpp"),
     os.path.join(HERE, "..", "stormbird_gb300", "csrc", "json_min.hpp"),
     os.path.join(HERE, "..", "include", "stormbird_gb300.h"),

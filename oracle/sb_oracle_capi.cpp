@@ -8,6 +8,7 @@
 
 #include "../include/stormbird_gb300.h"
 #include "sb_oracle.hpp"
+#include "sb_oracle_wind.hpp"
 
 namespace {
 thread_local std::string g_err;
@@ -250,6 +251,25 @@ int sbo_foil_eval(const char* foil_json, double alpha, double* out) {
 }
 
 // Raw Biot-Savart sweep for the CPU baseline: u_i = sum_j gamma_j * unit(panel_j, x_i) over
+// Freestream of CompleteSailModel::freestream_velocity (complete_sail_model/mod.rs:213-257)
+// at the simulation's freestream points for a WindEnvironment / WindCondition JSON pair.
+int sbo_sim_wind_freestream(void* h, const char* env_json, const char* cond_json, double time, double ship_velocity,
+                            double* out, size_t n) {
+    if (!h || !env_json || !cond_json || !out) return fail(SB_ERR_NULL_ARG, "null argument");
+    try {
+        sbo::WindModel w;
+        w.env = sbsetup::parse_wind_environment(env_json);
+        w.cond = sbsetup::parse_wind_condition(cond_json);
+        const auto& sim = static_cast<OracleSim*>(h)->sim;
+        if (n != sim.nr_freestream_points()) return fail(SB_ERR_SIZE, "size mismatch");
+        const auto fs = sbo::complete_sail_freestream(sim, w, ship_velocity, time);
+        for (size_t i = 0; i < n; ++i) { out[3 * i] = fs[i].x; out[3 * i + 1] = fs[i].y; out[3 * i + 2] = fs[i].z; }
+    } catch (const std::exception& e) {
+        return fail(SB_ERR_BAD_JSON, e.what());
+    }
+    return SB_OK;
+}
+
 // panels given by corners [P*12], far-field ratio, cores [P], strengths [P]; targets [M*3].
 // Runs the reference's per-target loop (induced_velocity_calc.rs:111-126) on nthreads threads.
 int sbo_bs_sweep(const double* corners, const double* cores, const double* strengths, size_t P, double far_field_ratio,

@@ -192,6 +192,35 @@ struct OutLayout {
     }
 };
 
+// ---- freestream from a wind model (k_wind.cu) -----------------------------------------
+// A WindEnvironment + WindCondition in device form. Spectra: for gust k (parallel,
+// perpendicular, vertical) spectra[spec_off[k] ...] holds frequencies, amplitudes and
+// phases (spec_n[k] each; spec_n[k] < 0: no gust). Inflow corrections: for direction d,
+// corr[corr_off[d] ...] holds heights, magnitudes and angles (corr_len[d] each) and
+// ranges[(d * S + wing) * 2 ...] the wing's [start, end). step[0] = time, step[1] = ship
+// velocity (device memory, so a captured step reads the current values).
+struct WindDevice {
+    d3 up{0, 0, 1}, axis{0, 0, 1}, zero{1, 0, 0};
+    double water_plane_height = 0.0, direction_coming_from = 0.0;
+    int vv_kind = 0;  // 0 constant, 1 power model, 2 logarithmic model
+    double vv_constant = 0.0, reference_velocity = 0.0, reference_height = 10.0, power_factor = 1.0 / 9.0;
+    double friction_velocity = 0.0, surface_roughness = 0.0, obukhov_length = 0.0;
+    double von_karman = 0.41, stable_coefficient = 6.0, unstable_coefficient = 19.3;
+    int has_obukhov = 0;
+    const double* spectra = nullptr;
+    int spec_off[3] = {0, 0, 0}, spec_n[3] = {-1, -1, -1};
+    int n_dirs = 0, S = 0;
+    const double* dirs = nullptr;
+    const double* corr = nullptr;
+    const int* corr_off = nullptr;
+    const int* corr_len = nullptr;
+    const long long* ranges = nullptr;
+    const double* step = nullptr;
+};
+// Freestream at the control points [N] then the wake points [n_wake] into out.
+cudaError_t launch_wind_freestream(const WindDevice& w, const d3* ctrl, const int* wing_of_line, int N, const d3* wake,
+                                   long long n_wake, d3* out, cudaStream_t s);
+
 // Sets the calling thread's sb_last_error / sb_last_status (sim_host.cu).
 void report_error(int code, const std::string& message);
 

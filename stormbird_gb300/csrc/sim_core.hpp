@@ -21,6 +21,7 @@
 #include "sb_device.cuh"
 #include "sb_kernels.h"
 #include "sb_setup.hpp"
+#include "sb_wind_setup.hpp"
 
 namespace sbhost {
 
@@ -301,6 +302,14 @@ struct sb_sim {
     bool chain_ok = false, share_segments = true;
     DevBuf<PanelRec<float>> chains;
     DevBuf<int> chain_span_tab, chain_col_tab;
+    // Freestream from a wind model (set_wind): device form, its tables, and the step's
+    // time and ship velocity (device memory; a batch points `wind.step` at its own array).
+    bool has_wind = false;
+    WindDevice wind;
+    DevBuf<double> wind_data, wind_step_own;
+    DevBuf<int> wind_ints;
+    DevBuf<long long> wind_ranges;
+    PinnedBuf<double> h_wind_step;
     int chain_SP = 0;
     long long chain_Bq = 0, chain_Q = 0;
     double chain_rc = 0.0;
@@ -935,6 +944,129 @@ struct sb_sim {
         ck(cudaMemcpyAsync(h_out.p, out.p, L.total * sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H output");
         ck(cudaStreamSynchronize(stream), "read output");
         write_output(o);
+    }
+
+    // ---------------------------------------------------------------- wind model
+    void set_wind(const char* env_json, const char* cond_json) {
+        sbsetup::WindEnvironment env;
+        sbsetup::WindCondition cond;
+        try {
+            env = sbsetup::parse_wind_environment(env_json);
+            cond = sbsetup::parse_wind_condition(cond_json);
+        } catch (const sbsetup::SetupError& e) {
+            raise(SB_ERR_BAD_JSON, e.what());
+        }
+        WindDevice w;
+        auto d3of = [](const sbsetup::Vec3& v) { return mk(v.x, v.y, v.z); };
+        w.up = d3of(env.up_direction);
+        w.axis = d3of(env.wind_rotation_axis);
+        w.zero = d3of(env.zero_direction_vector);
+        w.water_plane_height = env.water_plane_height;
+        w.direction_coming_from = cond.direction_coming_from;
+        const auto& v = cond.velocity_variation;
+        w.vv_kind = static_cast<int>(v.kind);
+        w.vv_constant = v.constant;
+        w.reference_velocity = v.reference_velocity;
+        w.reference_height = v.reference_height;
+        w.power_factor = v.power_factor;
+        w.friction_velocity = v.friction_velocity;
+        w.surface_roughness = v.surface_roughness;
+        w.has_obukhov = v.has_obukhov_length ? 1 : 0;
+        w.obukhov_length = v.obukhov_length;
+        w.von_karman = v.von_karman_constant;
+        w.stable_coefficient = v.stable_coefficient;
+        w.unstable_coefficient = v.unstable_coefficient;
+        std::vector<double> data;
+        const sbsetup::Spectrum* gusts[3] = {&cond.parallel_gust, &cond.perpendicular_gust, &cond.vertical_gust};
+        for (int k = 0; k < 3; ++k) {
+            if (!gusts[k]->present) continue;
+            w.spec_off[k] = static_cast<int>(data.size());
+            w.spec_n[k] = static_cast<int>(gusts[k]->frequencies.size());
+            data.insert(data.end(), gusts[k]->frequencies.begin(), gusts[k]->frequencies.end());
+            data.insert(data.end(), gusts[k]->amplitudes.begin(), gusts[k]->amplitudes.end());
+            data.insert(data.end(), gusts[k]->phases.begin(), gusts[k]->phases.end());
+        }
+        std::vector<int> ints;
+        std::vector<long long> ranges;
+        const auto& ic = env.inflow_corrections;
+        size_t dirs_off = data.size(), corr_base = 0;
+        if (ic.present) {
+            // the reference indexes each direction's wing ranges by wing (inflow_corrections.rs:28)
+            for (const auto& c : ic.corrections)
+                if (c.wing_indices.size() < static_cast<size_t>(S))
+                    raise(SB_ERR_SIZE, "inflow corrections need one height range per wing");
+            w.n_dirs = static_cast<int>(ic.apparent_wind_directions.size());
+            w.S = S;
+            data.insert(data.end(), ic.apparent_wind_directions.begin(), ic.apparent_wind_directions.end());
+            corr_base = data.size();
+            std::vector<int> offs, lens;
+            for (const auto& c : ic.corrections) {
+                offs.push_back(static_cast<int>(data.size() - corr_base));
+                lens.push_back(static_cast<int>(c.height_values.size()));
+                data.insert(data.end(), c.height_values.begin(), c.height_values.end());
+                data.insert(data.end(), c.magnitude_corrections.begin(), c.magnitude_corrections.end());
+                data.insert(data.end(), c.angle_corrections.begin(), c.angle_corrections.end());
+                for (int wg = 0; wg < S; ++wg) {
+                    ranges.push_back(c.wing_indices[wg].first);
+                    ranges.push_back(c.wing_indices[wg].second);
+                }
+            }
+            ints = offs;
+            ints.insert(ints.end(), lens.begin(), lens.end());
+        }
+        wind_data.upload(data.empty() ? std::vector<double>{0.0} : data);
+        wind_ints.upload(ints.empty() ? std::vector<int>{0} : ints);
+        wind_ranges.upload(ranges.empty() ? std::vector<long long>{0} : ranges);
+        w.spectra = wind_data.p;
+        if (ic.present) {
+            w.dirs = wind_data.p + dirs_off;
+            w.corr = wind_data.p + corr_base;
+            w.corr_off = wind_ints.p;
+            w.corr_len = wind_ints.p + w.n_dirs;
+            w.ranges = wind_ranges.p;
+        }
+        if (wind_step_own.n == 0) {
+            wind_step_own.alloc(2);
+            h_wind_step.alloc(2);
+        }
+        w.step = has_wind && wind.step ? wind.step : wind_step_own.p;
+        wind = w;
+        has_wind = true;
+    }
+
+    void set_wind_step(double time, double ship_velocity) {
+        h_wind_step.p[0] = time;
+        h_wind_step.p[1] = ship_velocity;
+        ck(cudaMemcpyAsync(wind_step_own.p, h_wind_step.p, 2 * sizeof(double), cudaMemcpyHostToDevice, stream),
+           "H2D wind step");
+    }
+
+    // CompleteSailModel::freestream_velocity (complete_sail_model/mod.rs:213-257) into fs_p at
+    // the current freestream points (control points of the current geometry, wake points).
+    void enqueue_wind_freestream() {
+        ck(launch_prep_geometry(dm, params, nullptr, nullptr, stream), "prep geometry");
+        ck(launch_wind_freestream(wind, ctrl.p, wing_of_line.p, N, dynamic ? pts[cur].p : nullptr, dynamic ? P_pts : 0,
+                                  fs_p, stream),
+           "wind freestream");
+        launches += 2;
+    }
+
+    void do_step_wind(double time, double dt, double ship_velocity, sb_step_output* o) {
+        if (!has_wind) raise(SB_ERR_STATE, "no wind model: call sb_sim_set_wind first");
+        set_wind_step(time, ship_velocity);
+        enqueue_wind_freestream();
+        enqueue_step(time, dt);
+        finish_step();
+        if (o) write_output(o);
+    }
+
+    void wind_freestream(double time, double ship_velocity, double* outp, size_t n) {
+        if (!has_wind) raise(SB_ERR_STATE, "no wind model: call sb_sim_set_wind first");
+        if (static_cast<long long>(n) != nfs) raise(SB_ERR_SIZE, "freestream buffer length mismatch");
+        set_wind_step(time, ship_velocity);
+        enqueue_wind_freestream();
+        ck(cudaMemcpyAsync(outp, fs_p, n * sizeof(d3), cudaMemcpyDeviceToHost, stream), "D2H freestream");
+        ck(cudaStreamSynchronize(stream), "wind freestream");
     }
 
     void freestream_points(double* outp, size_t n) {

@@ -208,6 +208,21 @@ int sb_sim_last_step_counters(const sb_sim* sim, double* c, size_t n) {
     return SB_OK;
 }
 
+int sb_sim_set_wind(sb_sim* sim, const char* environment_json, const char* condition_json) {
+    if (!sim || !environment_json || !condition_json) { g_last_error = "null argument"; return SB_ERR_NULL_ARG; }
+    return guard([&] { sim->set_wind(environment_json, condition_json); });
+}
+
+int sb_sim_wind_freestream(sb_sim* sim, double time, double ship_velocity, double* freestream, size_t n) {
+    if (!sim || !freestream) { g_last_error = "null argument"; return SB_ERR_NULL_ARG; }
+    return guard([&] { sim->wind_freestream(time, ship_velocity, freestream, n); });
+}
+
+int sb_sim_do_step_wind(sb_sim* sim, double time, double time_step, double ship_velocity, sb_step_output* out) {
+    if (!sim) { g_last_error = "null handle"; return SB_ERR_NULL_ARG; }
+    return guard([&] { sim->do_step_wind(time, time_step, ship_velocity, out); });
+}
+
 int sb_sim_set_segment_sharing(sb_sim* sim, int enable) {
     if (!sim) { g_last_error = "null handle"; return SB_ERR_NULL_ARG; }
     sim->share_segments = enable != 0;

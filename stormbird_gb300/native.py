@@ -48,6 +48,10 @@ SIGNATURES = [
     ("sb_sim_last_step_timing", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
     ("sb_sim_last_step_counters", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
     ("sb_sim_set_segment_sharing", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("sb_sim_set_wind", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_char_p]),
+    ("sb_sim_wind_freestream", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double, _dp, ctypes.c_size_t]),
+    ("sb_sim_do_step_wind", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                           ctypes.POINTER(StepOutput)]),
     ("sb_sim_segment_sharing_active", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int)]),
     ("sb_panel_sweep", ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp, ctypes.c_size_t, ctypes.c_double, ctypes.c_int,
                                       _dp, ctypes.c_size_t, ctypes.c_int, _dp]),

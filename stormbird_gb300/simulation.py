@@ -153,6 +153,23 @@ class Simulation:
                 "kernel_launches", "rollup_segments")
         return dict(zip(keys, c.tolist()))
 
+    # -- freestream from a wind model (CompleteSailModel::freestream_velocity on the GPU) --
+    def set_wind(self, environment_json: str, condition_json: str):
+        """WindEnvironment and WindCondition JSON of the reference (wind/environment.rs,
+        wind/wind_condition/mod.rs)."""
+        _check(lib().sb_sim_set_wind(self._h, environment_json.encode(), condition_json.encode()))
+
+    def wind_freestream(self, *, time: float, ship_velocity: float) -> np.ndarray:
+        out = np.zeros((self.nr_freestream_points, 3))
+        _check(lib().sb_sim_wind_freestream(self._h, float(time), float(ship_velocity), as_ptr(out), out.shape[0]))
+        return out
+
+    def do_step_wind(self, *, time: float, time_step: float, ship_velocity: float):
+        """do_step with the freestream generated on the GPU from the wind model."""
+        _check(lib().sb_sim_do_step_wind(self._h, float(time), float(time_step), float(ship_velocity),
+                                         ctypes.byref(self._out.struct)))
+        return self._out.to_result(time)
+
     def set_segment_sharing(self, on: bool = True):
         """Shared-segment roll-up sweep (default on; used when every pair is near-field and all
         panels share one core length): each wake segment evaluated once with the strength
