@@ -280,6 +280,12 @@ int sb_batch_get_freestream_points(sb_batch* batch, double* points_xyz, size_t n
 int sb_batch_do_step(sb_batch* batch, double time, double time_step, const double* freestream_xyz, size_t n_total);
 int sb_batch_do_step_device(sb_batch* batch, double time, double time_step, const double* freestream_dev,
                             size_t n_total);
+/* Wind models for all cases (one environment, one WindCondition JSON per case; see
+ * sb_sim_set_wind) and a step with every case's freestream generated on the GPU: the
+ * batched form of CompleteSailModel::do_step (complete_sail_model/mod.rs:187-199) over a
+ * sweep of wind conditions, ship_velocities [n_cases]. */
+int sb_batch_set_wind(sb_batch* batch, const char* environment_json, const char* const* condition_jsons);
+int sb_batch_do_step_wind(sb_batch* batch, double time, double time_step, const double* ship_velocities);
 /* Results of the last step: circulation [total_lines] and summaries [n_cases*SB_BATCH_SUMMARY]. */
 int sb_batch_get_circulation(const sb_batch* batch, double* circulation, size_t n_total);
 int sb_batch_get_summary(const sb_batch* batch, double* summary, size_t n);

@@ -57,6 +57,7 @@ def lib() -> ctypes.CDLL:
         L.sbo_bs_sweep.argtypes = [dp, dp, dp, c_size_t, c_double, dp, c_size_t, dp, c_int]
         L.sbo_sim_wind_freestream.argtypes = [c_void_p, ctypes.c_char_p, ctypes.c_char_p, c_double, c_double, dp,
                                               c_size_t]
+        L.sbo_wind_velocity_at.argtypes = [ctypes.c_char_p, ctypes.c_char_p, dp, c_size_t, c_double, c_double, dp]
         _LIB = L
     return _LIB
 
@@ -194,6 +195,16 @@ def foil_eval(foil_json: str, alpha: float) -> dict:
     out = np.zeros(6)
     _check(lib().sbo_foil_eval(foil_json.encode(), float(alpha), as_ptr(out)))
     return dict(zip(("cl", "cl_pre_stall", "cl_post_stall", "cd", "stall", "cl_linear"), out.tolist()))
+
+
+def wind_velocity_at(environment_json: str, condition_json: str, points, time: float = 0.0,
+                     ship_velocity: float = 0.0) -> np.ndarray:
+    """Unsteady apparent wind of the reference's wind model at arbitrary points."""
+    p = vec3_array(points)
+    out = np.zeros_like(p)
+    _check(lib().sbo_wind_velocity_at(environment_json.encode(), condition_json.encode(), as_ptr(p), p.shape[0],
+                                      float(time), float(ship_velocity), as_ptr(out)))
+    return out
 
 
 def bs_sweep(corners, cores, strengths, far_field_ratio, targets, nthreads=1) -> np.ndarray:

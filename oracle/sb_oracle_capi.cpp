@@ -270,6 +270,26 @@ int sbo_sim_wind_freestream(void* h, const char* env_json, const char* cond_json
     return SB_OK;
 }
 
+// Unsteady apparent wind (environment.rs:175-188) at arbitrary locations [n*3], no
+// inflow corrections.
+int sbo_wind_velocity_at(const char* env_json, const char* cond_json, const double* points, size_t n, double time,
+                         double ship_velocity, double* out) {
+    if (!env_json || !cond_json || (n && (!points || !out))) return fail(SB_ERR_NULL_ARG, "null argument");
+    try {
+        sbo::WindModel w;
+        w.env = sbsetup::parse_wind_environment(env_json);
+        w.cond = sbsetup::parse_wind_condition(cond_json);
+        const sbo::V3 linear = ship_velocity * sbo::to_v3(w.env.zero_direction_vector);
+        for (size_t i = 0; i < n; ++i) {
+            const sbo::V3 u = w.unsteady_apparent_wind({points[3 * i], points[3 * i + 1], points[3 * i + 2]}, linear, time);
+            out[3 * i] = u.x; out[3 * i + 1] = u.y; out[3 * i + 2] = u.z;
+        }
+    } catch (const std::exception& e) {
+        return fail(SB_ERR_BAD_JSON, e.what());
+    }
+    return SB_OK;
+}
+
 // panels given by corners [P*12], far-field ratio, cores [P], strengths [P]; targets [M*3].
 // Runs the reference's per-target loop (induced_velocity_calc.rs:111-126) on nthreads threads.
 int sbo_bs_sweep(const double* corners, const double* cores, const double* strengths, size_t P, double far_field_ratio,

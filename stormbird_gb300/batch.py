@@ -78,6 +78,19 @@ class Batch:
         _check(lib().sb_batch_do_step_device(self._h, float(time), float(time_step),
                                              ctypes.c_void_p(int(freestream_device_ptr)), self.total_freestream))
 
+    def set_wind(self, environment_json: str, condition_jsons):
+        """One WindEnvironment for all cases and one WindCondition per case (reference JSON)."""
+        enc = [c.encode() for c in condition_jsons]
+        if len(enc) != self.n_cases:
+            raise SbError(-2, "one wind condition per case is needed")
+        arr = (ctypes.c_char_p * len(enc))(*enc)
+        _check(lib().sb_batch_set_wind(self._h, environment_json.encode(), arr))
+
+    def do_step_wind(self, *, time: float, time_step: float, ship_velocities):
+        """A step of every case with its freestream generated on the GPU from its wind model."""
+        v = np.ascontiguousarray(np.broadcast_to(np.asarray(ship_velocities, dtype=np.float64), (self.n_cases,)))
+        _check(lib().sb_batch_do_step_wind(self._h, float(time), float(time_step), as_ptr(v)))
+
     def circulation(self) -> np.ndarray:
         out = np.zeros(self.total_lines)
         _check(lib().sb_batch_get_circulation(self._h, as_ptr(out), out.size))

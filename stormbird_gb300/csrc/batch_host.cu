@@ -139,10 +139,16 @@ struct sb_batch {
     PinnedBuf<FeatJob> h_feat;
     DevBuf<FeatJob> d_feat;
 
+    // freestream from per-case wind models: [cases][time, ship velocity] staged per step
+    bool has_wind = false;
+    DevBuf<double> wind_steps;
+    PinnedBuf<double> h_wind_steps;
+
     bool use_graph = true;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     double graph_dt = 0.0;
     int graph_precision = -1;
+    int graph_wind = -1;
     int steps = 0;
     double last_ms = 0.0;
     long long last_pairs = 0;  // panel-target pairs of the last step's sweeps
@@ -437,11 +443,17 @@ struct sb_batch {
 
     // Enqueues one step of every case on main + pool (the freestream is in fs_all and the
     // work lists in h_jobs).
-    void enqueue(double time, double dt) {
+    void enqueue(double time, double dt, bool wind) {
         if (job_entries > 0)
             ck(cudaMemcpyAsync(d_jobs.p, h_jobs.p, job_entries * sizeof(BsJob), cudaMemcpyHostToDevice, main), "H2D jobs");
+        if (wind)
+            ck(cudaMemcpyAsync(wind_steps.p, h_wind_steps.p, cases.size() * 2 * sizeof(double), cudaMemcpyHostToDevice, main),
+               "H2D wind steps");
         fork(0);
-        for (auto& c : cases) c->step_begin(time, dt);
+        for (auto& c : cases) {
+            if (wind) c->enqueue_wind_freestream();  // complete_sail_model/mod.rs:213-257
+            c->step_begin(time, dt);
+        }
         join(0);
         if (warm_mode != 0) warm_start_before_solve();
         sweeps(0);
@@ -566,13 +578,13 @@ struct sb_batch {
         return true;
     }
 
-    void step(double time, double dt) {
+    void step(double time, double dt, bool wind = false) {
         for (auto& c : cases) {
             if (c->timing) c->timing = false;
             c->precision = precision;
             c->ensure_rec64();  // FP64 records (allocation) before any capture
         }
-        if (graph_dt != dt || graph_precision != precision) drop_graphs();
+        if (graph_dt != dt || graph_precision != precision || graph_wind != (wind ? 1 : 0)) drop_graphs();
         if (warm_mode != 0) fill_feature_jobs();
         // the parity of the wake buffers at the start of the step selects the graph
         const int parity = any_dynamic ? first_dynamic().cur : (steps & 1);
@@ -585,7 +597,7 @@ struct sb_batch {
                 cudaGraph_t g = nullptr;
                 ck(cudaStreamBeginCapture(main, cudaStreamCaptureModeRelaxed), "begin capture");
                 try {
-                    enqueue(time, dt);
+                    enqueue(time, dt, wind);
                 } catch (...) {
                     cudaStreamEndCapture(main, &g);
                     if (g) cudaGraphDestroy(g);
@@ -597,13 +609,14 @@ struct sb_batch {
                 ck(e, "graph instantiate");
                 graph_dt = dt;
                 graph_precision = precision;
+                graph_wind = wind ? 1 : 0;
             } else {
                 replay_bookkeeping(time, dt);
             }
             ck(cudaGraphLaunch(graph[parity], main), "graph launch");
         } else {
             fill_jobs_after_begin();
-            enqueue(time, dt);
+            enqueue(time, dt, wind);
         }
         ck(cudaEventRecord(ev_t1, main), "event");
         ck(cudaStreamSynchronize(main), "batch step");
@@ -650,6 +663,36 @@ struct sb_batch {
         std::memcpy(h_fs_all.p, fs_host, cnt * sizeof(double));
         ck(cudaMemcpyAsync(fs_all.p, h_fs_all.p, cnt * sizeof(double), cudaMemcpyHostToDevice, main), "H2D freestream");
         step(time, dt);
+    }
+
+    // ------------------------------------------------------------------ wind models
+    void set_wind(const char* env_json, const char* const* cond_jsons) {
+        ck(cudaStreamSynchronize(main), "sync");
+        drop_graphs();
+        if (wind_steps.n == 0) {
+            wind_steps.alloc(cases.size() * 2);
+            h_wind_steps.alloc(cases.size() * 2);
+        }
+        for (size_t i = 0; i < cases.size(); ++i) {
+            if (!cond_jsons[i]) raise(SB_ERR_NULL_ARG, "wind condition of case " + std::to_string(i) + " is NULL");
+            try {
+                cases[i]->set_wind(env_json, cond_jsons[i]);
+            } catch (const SbFail& e) {
+                raise(e.code, "case " + std::to_string(i) + ": " + e.msg);
+            }
+            cases[i]->wind.step = wind_steps.p + 2 * i;
+        }
+        has_wind = true;
+    }
+
+    void do_step_wind(double time, double dt, const double* ship_velocities) {
+        if (!has_wind) raise(SB_ERR_STATE, "no wind models: call sb_batch_set_wind first");
+        for (size_t i = 0; i < cases.size(); ++i) {
+            if (!std::isfinite(ship_velocities[i])) raise(SB_ERR_NONFINITE, "non-finite ship velocity of case " + std::to_string(i));
+            h_wind_steps.p[2 * i] = time;
+            h_wind_steps.p[2 * i + 1] = ship_velocities[i];
+        }
+        step(time, dt, true);
     }
 
     void do_step_device(double time, double dt, const double* fs_dev, size_t n) {
@@ -785,6 +828,16 @@ int sb_batch_do_step(sb_batch* b, double time, double dt, const double* freestre
 int sb_batch_do_step_device(sb_batch* b, double time, double dt, const double* freestream_dev, size_t n) {
     if (!b || !freestream_dev) return null_arg();
     return guard([&] { b->do_step_device(time, dt, freestream_dev, n); });
+}
+
+int sb_batch_set_wind(sb_batch* b, const char* environment_json, const char* const* condition_jsons) {
+    if (!b || !environment_json || !condition_jsons) return null_arg();
+    return guard([&] { b->set_wind(environment_json, condition_jsons); });
+}
+
+int sb_batch_do_step_wind(sb_batch* b, double time, double dt, const double* ship_velocities) {
+    if (!b || !ship_velocities) return null_arg();
+    return guard([&] { b->do_step_wind(time, dt, ship_velocities); });
 }
 
 int sb_batch_get_circulation(const sb_batch* b, double* gamma, size_t n) {

@@ -66,6 +66,8 @@ SIGNATURES = [
     ("sb_batch_get_freestream_points", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
     ("sb_batch_do_step", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double, _dp, ctypes.c_size_t]),
     ("sb_batch_do_step_device", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double, _vp, ctypes.c_size_t]),
+    ("sb_batch_set_wind", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_char_p)]),
+    ("sb_batch_do_step_wind", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double, _dp]),
     ("sb_batch_get_circulation", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
     ("sb_batch_get_summary", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
     ("sb_batch_read_case_output", ctypes.c_int, [_vp, ctypes.c_size_t, ctypes.POINTER(StepOutput)]),

@@ -9,7 +9,8 @@ apparent wind angle and speed drawn per case):
   * CUDA-graph replay against eager launches of the same batch: bit-identical (the same
     kernels, work lists and chunk-ordered reductions);
   * after autotuning, still within tolerance of the plain path;
-  * the warm-start hook, size checks and the error that names a bad case.
+  * the warm-start hook, size checks and the error that names a bad case;
+  * quasi-steady cases in a batch (bit-identical to their own Simulations).
 """
 import json
 
@@ -168,3 +169,26 @@ def test_batch_errors(gpu_lib):
     with pytest.raises(SbError) as e:
         b.do_step(time=0.0, time_step=DT, freestream_velocity=bad)
     assert e.value.code == -5
+
+
+def test_quasi_steady_cases_in_a_batch(gpu_lib):
+    """Quasi-steady cases (Linearized, the quasi-steady default, and SimpleIterative) in one
+    batch give what their own Simulations give: the same kernels on the same inputs."""
+    from stormbird_gb300 import Batch, Simulation
+
+    js_si, u = S.quasi_steady_single_wing(24)
+    d = json.loads(js_si)
+    del d["simulation_settings"]["QuasiSteady"]["solver"]  # Linearized default
+    js_lin = json.dumps(d)
+    cases = [js_si, js_lin, js_lin]
+    speeds = [1.0, 0.8, 1.3]
+    b = Batch(cases)
+    sims = [Simulation(js) for js in cases]
+    for k in range(6):
+        fs = np.concatenate([np.tile(u * sp, (c["freestream_points"], 1)) for sp, c in zip(speeds, b.cases)])
+        b.do_step(time=k * DT, time_step=DT, freestream_velocity=fs)
+        g, s = b.circulation(), b.summary()
+        for i, (sim, sp) in enumerate(zip(sims, speeds)):
+            r = sim.do_step(time=k * DT, time_step=DT, freestream_velocity=np.tile(u * sp, (sim.nr_freestream_points, 1)))
+            assert np.array_equal(g[b.case_slice(i)], r.circulation_strength), (k, i)
+            assert np.array_equal(s[i, :3], r.integrated_forces_sum()), (k, i)
