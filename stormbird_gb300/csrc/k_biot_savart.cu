@@ -140,7 +140,7 @@ __device__ __forceinline__ void corner2(float2 ex, float2 ey, float2 ez, const f
 // weight g when WEIGHTED.
 template <bool WEIGHTED>
 __device__ __forceinline__ void segment2(float2 rx, float2 ry, float2 rz, float2 rs1, float2 rl1, float2 rs2,
-                                         float2 rl2, float dx, float dy, float dz, float il, float rc4, float g,
+                                         float2 rl2, float dx, float dy, float dz, float il, float dd, float rc4, float g,
                                          float2& ax, float2& ay, float2& az) {
     const float2 p = mul2(rl1, rl2);
     // projection on the segment, and r1.r2 = |r1|^2 - r1.d (r2 = r1 - d)
@@ -151,14 +151,14 @@ __device__ __forceinline__ void segment2(float2 rx, float2 ry, float2 rz, float2
     const float2 cz = fma2(bc(dx), ry, mul2(bc(-dy), rx));
     const float2 c2 = fma2(cx, cx, fma2(cy, cy, mul2(cz, cz)));
     const bool n0 = q.x < 0.f, n1 = q.y < 0.f;
-    const float2 pmq = add2(p, make_float2(-q.x, -q.y));
-    const float2 ppq = add2(p, q);
-    const float2 Ax = make_float2(n0 ? pmq.x : 1.f, n1 ? pmq.y : 1.f);
-    const float2 Bx = mul2(p, make_float2(n0 ? c2.x : ppq.x, n1 ? c2.y : ppq.y));
-    const float2 tpl = mul2(tp, bc(il));
+    // both branches use l1 l2 + |r1.r2|: p - q for q < 0 (A), p + q otherwise (B)
+    const float2 pa = add2(p, make_float2(fabsf(q.x), fabsf(q.y)));
+    const float2 Ax = make_float2(n0 ? pa.x : 1.f, n1 ? pa.y : 1.f);
+    const float2 Bx = mul2(p, make_float2(n0 ? c2.x : pa.x, n1 ? c2.y : pa.y));
+    // past the segment's end (projection r1.d > |d|^2): the end-point distance
     float2 d2 = mul2(c2, bc(il));
-    d2.x = tpl.x > 1.f ? rs2.x : d2.x;
-    d2.y = tpl.y > 1.f ? rs2.y : d2.y;
+    d2.x = tp.x > dd ? rs2.x : d2.x;
+    d2.y = tp.y > dd ? rs2.y : d2.y;
     d2.x = tp.x < 0.f ? rs1.x : d2.x;
     d2.y = tp.y < 0.f ? rs1.y : d2.y;
     // X = 0 only where B = 0 too (target on the segment or a corner); the select below
@@ -185,7 +185,7 @@ __device__ __forceinline__ void ring2(const float* v, float2 ex, float2 ey, floa
     for (int k = 0; k < 4; ++k) {
         const int k1 = (k + 1) & 3;
         segment2<false>(rx[k], ry[k], rz[k], rs[k], rl[k], rs[k1], rl[k1], v[12 + 3 * k], v[12 + 3 * k + 1],
-                        v[12 + 3 * k + 2], v[24 + k], rc4, 1.f, ax, ay, az);
+                        v[12 + 3 * k + 2], v[24 + k], v[kRec32DD + k], rc4, 1.f, ax, ay, az);
     }
 }
 
@@ -203,7 +203,7 @@ __device__ __forceinline__ void chain2(const float* v, float2 ex, float2 ey, flo
         float2 rxb, ryb, rzb, rsb, rlb;
         corner2(ex, ey, ez, v + kChainOff + 3 * (k + 1), rxb, ryb, rzb, rsb, rlb);
         segment2<true>(rxa, rya, rza, rsa, rla, rsb, rlb, v[kChainD + 3 * k], v[kChainD + 3 * k + 1],
-                       v[kChainD + 3 * k + 2], v[kChainIl + k], rc4, v[kChainG + k], ax, ay, az);
+                       v[kChainD + 3 * k + 2], v[kChainIl + k], v[kChainDD + k], rc4, v[kChainG + k], ax, ay, az);
         rxa = rxb;
         rya = ryb;
         rza = rzb;

@@ -218,6 +218,7 @@ __device__ void write_panel_records(const d3 (&pp)[4], double rc, double g, doub
         r.v[12 + 3 * k + 2] = static_cast<float>(dk.z);
         const double l2 = len2(dk);
         r.v[24 + k] = l2 > 0.0 ? static_cast<float>(1.0 / l2) : 0.f;
+        r.v[kRec32DD + k] = static_cast<float>(l2);
     }
     split(c.x, &r.v[28], &r.v[32]);
     split(c.y, &r.v[29], &r.v[33]);
@@ -233,7 +234,7 @@ __device__ void write_panel_records(const d3 (&pp)[4], double rc, double g, doub
     const double rc2 = rc * rc;
     r.v[40] = static_cast<float>(rc2 * rc2);
     r.v[41] = static_cast<float>(wing);
-    for (int k = 42; k < 48; ++k) r.v[k] = 0.f;
+    for (int k = kRec32DD + 4; k < 48; ++k) r.v[k] = 0.f;
     *r32 = r;
     if (r64) {
         PanelRec<double> q;
@@ -356,6 +357,7 @@ __global__ void k_chain_records(ChainArgs a, long long n_build) {
             rec.v[kChainD + 3 * k + 2] = static_cast<float>(dk.z);
             const double l2 = len2(dk);
             rec.v[kChainIl + k] = l2 > 0.0 ? static_cast<float>(1.0 / l2) : 0.f;
+            rec.v[kChainDD + k] = static_cast<float>(l2);
             rec.v[kChainG + k] = static_cast<float>(g[k] * kFourPiInv);
             any += fabs(g[k]);
         }

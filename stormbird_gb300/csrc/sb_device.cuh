@@ -204,6 +204,7 @@ static_assert(sizeof(PanelRec<float>) == 192, "FP32 panel record is 192 bytes");
 static_assert(sizeof(PanelRec<double>) == 224, "FP64 panel record is 224 bytes");
 
 constexpr int kRec32Gamma = 39;  // strength slot of the FP32 record
+constexpr int kRec32DD = 42;     // |d_k|^2 of the FP32 record's four segments (slots 42..45)
 constexpr int kRec64Gamma = 24;  // strength slot of the FP64 record
 
 // Chain record (FP32, same 48-float size): an open chain of up to 4 wake segments that
@@ -211,8 +212,9 @@ constexpr int kRec64Gamma = 24;  // strength slot of the FP64 record
 // difference of the two rings' strengths. Slots: [0..2] anchor hi, [3..5] anchor lo
 // (float-float point 2), [6..20] offsets of points 0..4 from the anchor, [21..32] segment
 // vectors, [33..36] 1/|d|^2, [37..40] strength difference / 4 pi, [41] rc^4, [42] wing,
-// [43] sum of |strength differences| (0: nothing to evaluate).
-constexpr int kChainOff = 6, kChainD = 21, kChainIl = 33, kChainG = 37, kChainRc4 = 41, kChainWing = 42, kChainAny = 43;
+// [43] sum of |strength differences| (0: nothing to evaluate), [44..47] |d|^2.
+constexpr int kChainOff = 6, kChainD = 21, kChainIl = 33, kChainG = 37, kChainRc4 = 41, kChainWing = 42, kChainAny = 43,
+              kChainDD = 44;
 constexpr int kChainSegs = 4;
 
 // ---------------------------------------------------------------------------------------
