@@ -299,6 +299,19 @@ def run_gb300(args):
     h2d = nfs * 3 * 8
     d2h = (35 * N + 36 * sim.nr_wings + 9) * 8 + 4
 
+    # ---- e2e with the freestream generated on the GPU from the same wind (WindCondition)
+    sim.set_wind("{}", wind.condition_json())
+    wind_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = sim.do_step_wind(time=t, time_step=DT, ship_velocity=0.0)
+        wind_times.append(time.perf_counter() - t0)
+        k += 1
+        t = k * DT
+    wind_total = allreduce_max(ws, sum(wind_times), dev)
+
     # ---- roofline of the roll-up sweep kernel: the segments it actually evaluates (with
     # shared segments about half of the reference's four per panel)
     rollup_targets = ct["rollup_targets"]
@@ -327,6 +340,9 @@ def run_gb300(args):
                                     "evaluates each wake segment shared by two rings once (strength difference)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": 1e3 * e2e_total / args.steps},
+        "e2e_wind": {"value": inter_all / wind_total, "unit": UNIT, "h2d_bytes_per_step": 16, "d2h_bytes_per_step": d2h,
+                     "ms_per_step": 1e3 * wind_total / args.steps,
+                     "note": "sb_sim_do_step_wind: the freestream of the same gusty wind generated on the GPU"},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "breakdown_ms": {k2: v for k2, v in sim.last_step_timing().items()},

@@ -108,7 +108,8 @@ __device__ __forceinline__ void two_sum_acc(R& s, R& c, R t) {
 // ---------------------------------------------------------------------------------------
 __device__ __forceinline__ float2 bc(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 sub2s(float2 a, float b) { return __fadd2_rn(a, make_float2(-b, -b)); }
+// a - b as one packed FMA (b * -1 is exact, so the result is the rounded difference)
+__device__ __forceinline__ float2 sub2s(float2 a, float b) { return __ffma2_rn(make_float2(b, b), make_float2(-1.f, -1.f), a); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 sel2(bool cx, float2 a, bool cy, float2 b) {
@@ -145,7 +146,7 @@ __device__ __forceinline__ void segment2(float2 rx, float2 ry, float2 rz, float2
     const float2 p = mul2(rl1, rl2);
     // projection on the segment, and r1.r2 = |r1|^2 - r1.d (r2 = r1 - d)
     const float2 tp = fma2(rx, bc(dx), fma2(ry, bc(dy), mul2(rz, bc(dz))));
-    const float2 q = add2(rs1, make_float2(-tp.x, -tp.y));
+    const float2 q = fma2(tp, bc(-1.f), rs1);
     const float2 cx = fma2(bc(dy), rz, mul2(bc(-dz), ry));
     const float2 cy = fma2(bc(dz), rx, mul2(bc(-dx), rz));
     const float2 cz = fma2(bc(dx), ry, mul2(bc(-dy), rx));

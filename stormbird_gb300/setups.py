@@ -183,6 +183,15 @@ class GustyWind:
     def freestream(self, t: float, nr_points: int) -> np.ndarray:
         return np.tile(self.velocity(t), (nr_points, 1))
 
+    def condition_json(self) -> str:
+        """The same wind as a reference WindCondition (constant profile, parallel gust):
+        the zero direction (1, 0, 0) turned by the angle about +z gives `direction`."""
+        return json.dumps({"direction_coming_from": math.atan2(self.direction[1], self.direction[0]),
+                           "velocity_variation": {"Constant": self.speed},
+                           "parallel_gust": {"frequencies": self.frequencies.tolist(),
+                                             "amplitudes": self.amplitudes.tolist(),
+                                             "phases": self.phases.tolist()}})
+
 
 def synthetic_sail_row_wake(nr_sails=4, panels_per_sail=64, wake_rows=300, time_step=0.05, wind_speed=12.0,
                             apparent_wind_angle_deg=45.0, angle_of_attack_deg=8.0, spacing=40.0, seed=0):
