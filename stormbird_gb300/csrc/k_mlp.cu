@@ -1,23 +1,30 @@
 // Warm-start network kernels (sm_103a).
 //
 // k_mlp_gemm: C[M][N] = A[M][K] B[N][K]^T on the 5th-generation tensor cores. One CTA of
-// four warps owns a 128 x N output tile whose FP32 accumulator lives in tensor memory
-// (256 columns allocated with tcgen05.alloc). Per 64-wide K step all threads copy the A and
-// B tiles (BF16, 16-byte vectors) into shared memory in the canonical no-swizzle K-major
-// layout — 8 x 16-byte core matrices, core matrices 128 B apart along K (LBO) and 8-row
-// groups 1024 B apart (SBO) — double-buffered; one thread issues four
-// tcgen05.mma.cta_group::1.kind::f16 (K = 16 each) and tcgen05.commit to the buffer's
-// mbarrier, which frees the buffer for the copy two steps later. The epilogue reads the
-// accumulator with tcgen05.ld (32 lanes x 32 columns per warp and instruction; warp w owns
-// tensor-memory lanes 32w..32w+31 = rows) and applies the layer's bias and GELU (forward),
-// the GELU derivative (backward), or stores split-K partial sums (weight gradients).
-// Waits are bounded: a wait that runs out records kDevTimeout, skips the epilogue, waits
-// (bounded) for the MMAs in flight and frees the tensor memory.
+// eight warps owns a 128 x N output tile whose FP32 accumulator lives in tensor memory
+// (256 columns allocated with tcgen05.alloc). The operands arrive by TMA: per 64-wide K
+// step one thread issues two cp.async.bulk.tensor.2d copies (A: 64 x 128, B: 64 x N BF16)
+// into a stage of shared memory in the 128-byte-swizzled K-major layout (one 128-byte row
+// per matrix row, 16-byte chunks XOR-ed with the row index mod 8, 8-row atoms 1024 B
+// apart), completing on the stage's `full` mbarrier. Two stages run ahead of the tensor
+// cores; the same thread waits for a stage, issues four tcgen05.mma.cta_group::1.kind::f16
+// (K = 16 each: the descriptor start advances 32 B inside the swizzle atom) and commits to
+// the stage's `empty` mbarrier, and refills the stage of the previous step once its MMAs
+// have completed, so one step of MMAs is always queued behind the running one. Two CTAs
+// fit on an SM (shared memory), so one CTA's epilogue overlaps the other's MMAs. The
+// epilogue reads the accumulator with tcgen05.ld (32 lanes x 32 columns per warp and
+// instruction; warps w and w + 4 own tensor-memory lanes 32 (w mod 4) .. + 31 = rows and
+// half of the columns each) and applies the layer's bias and GELU (forward), the GELU
+// derivative (backward), or stores split-K partial sums (weight gradients). Waits are
+// bounded: a wait that runs out records kDevTimeout, skips the epilogue, waits (bounded)
+// for the copies and MMAs in flight and frees the tensor memory.
 //
 // The rest are CUDA-core kernels: the width->1 output layer with the MSE loss, input
 // packing, deterministic fixed-order reductions, Adam, weight casts, and the batch-side
 // feature / candidate / target kernels of the warm start.
+#include <cuda.h>
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 
 #include "sb_mlp.h"
 #include "sb_ptx.cuh"
@@ -26,25 +33,32 @@ namespace sbgpu {
 
 namespace {
 
-constexpr int kGemmThreads = 128;
-constexpr int kKStep = 64;
-constexpr uint32_t kLBO = 128;   // bytes between core matrices along K
-constexpr uint32_t kSBO = 1024;  // bytes between 8-row groups of a 64-wide K tile
+constexpr int kGemmThreads = 256;  // 8 warps: warps w and w + 4 drain one lane quadrant
+constexpr int kKStep = 64;       // one 128-byte swizzle row of BF16
+constexpr int kStages = 2;
+constexpr uint32_t kSBO = 1024;  // bytes between 8-row atoms
 constexpr uint32_t kStageA = kMlpRowTile * kKStep * 2;
 constexpr uint32_t kStageB = kMlpWidth * kKStep * 2;
 constexpr uint32_t kStage = kStageA + kStageB;
 constexpr uint32_t kTmemCols = 256;
+static_assert(kStageA % 1024 == 0 && kStage % 1024 == 0, "stages keep the 1024-byte swizzle alignment");
 
-// byte offset of the 16-byte chunk (row r, k chunk kc) of a K-major 64-wide tile
-__device__ __forceinline__ uint32_t core_off(int r, int kc) {
-    return static_cast<uint32_t>(r >> 3) * kSBO + static_cast<uint32_t>(kc) * kLBO + static_cast<uint32_t>(r & 7) * 16u;
+// tcgen05 shared-memory matrix descriptor of a K-major 128-byte-swizzled tile: start
+// address (>> 4), leading offset 16 B (unused by this layout), SBO 1024 B (>> 4), version
+// 1, layout type 2 (128-byte swizzle), base offset 0 (atoms are 1024-byte aligned).
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+    return static_cast<uint64_t>((addr >> 4) & 0x3FFFu) | (1ull << 16) |
+           (static_cast<uint64_t>((kSBO >> 4) & 0x3FFFu) << 32) | (1ull << 46) | (2ull << 61);
 }
 
-// tcgen05 shared-memory matrix descriptor: start address, LBO and SBO (>> 4), version 1,
-// no swizzle.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
-    return static_cast<uint64_t>((addr >> 4) & 0x3FFFu) | (static_cast<uint64_t>((kLBO >> 4) & 0x3FFFu) << 16) |
-           (static_cast<uint64_t>((kSBO >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+// 2-D tiled TMA copy of the box at (x, y) (x in elements along the contiguous dimension)
+// into shared memory, completing on `bar`.
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+            "r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
 }
 
 // Instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major, M x N.
@@ -55,7 +69,6 @@ __device__ __forceinline__ uint32_t idesc_bf16(int M, int N) {
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 __device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t cols) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(cols)
@@ -109,10 +122,13 @@ __device__ __forceinline__ void store_bf16x32(bf16* dst, const float (&v)[32]) {
     }
 }
 
-__global__ void __launch_bounds__(kGemmThreads) k_mlp_gemm(GemmArgs g) {
+__global__ void __launch_bounds__(kGemmThreads) k_mlp_gemm(const __grid_constant__ CUtensorMap map_a,
+                                                           const __grid_constant__ CUtensorMap map_b, GemmArgs g) {
     extern __shared__ unsigned char dyn[];
-    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ __align__(8) uint64_t full[kStages];
+    __shared__ __align__(8) uint64_t empty[kStages];
     __shared__ uint32_t s_tmem;
+    __shared__ int s_issued, s_ok;
     unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(dyn) + 1023) & ~uintptr_t(1023));
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int m0 = blockIdx.x * kMlpRowTile;
@@ -123,66 +139,82 @@ __global__ void __launch_bounds__(kGemmThreads) k_mlp_gemm(GemmArgs g) {
 
     if (warp == 0) tmem_alloc(&s_tmem, kTmemCols);
     if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
         fence_mbar_init();
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = s_tmem;
-    const uint32_t idesc = idesc_bf16(kMlpRowTile, g.N);
-    uint32_t ph[2] = {0u, 0u};
-    bool ok = true;
-    int issued = 0;  // K steps whose MMAs were issued
 
-    for (int kt = 0; kt < nk; ++kt) {
-        const int s = kt & 1;
-        unsigned char* sa = base + s * kStage;
-        unsigned char* sb = sa + kStageA;
-        if (kt >= 2) {  // the MMAs of step kt - 2 read this buffer
-            ok = mbar_wait_bounded(&bar[s], ph[s], g.err);
-            ph[s] ^= 1u;
-        }
-        if (!__syncthreads_and(ok)) break;
-        const int k0 = k_begin + kt * kKStep;
-        for (int c = tid; c < kMlpRowTile * 8; c += kGemmThreads) {
-            const int r = c >> 3, kc = c & 7;
-            const uint4 v = *reinterpret_cast<const uint4*>(g.A + static_cast<long long>(m0 + r) * g.lda + k0 + kc * 8);
-            *reinterpret_cast<uint4*>(sa + core_off(r, kc)) = v;
-        }
-        for (int c = tid; c < g.N * 8; c += kGemmThreads) {
-            const int r = c >> 3, kc = c & 7;
-            const uint4 v = *reinterpret_cast<const uint4*>(g.B + static_cast<long long>(r) * g.ldb + k0 + kc * 8);
-            *reinterpret_cast<uint4*>(sb + core_off(r, kc)) = v;
-        }
-        fence_async_smem();  // make the generic-proxy stores visible to the tensor cores
-        __syncthreads();
-        if (tid == 0) {
+    if (tid == 0) {
+        const uint32_t idesc = idesc_bf16(kMlpRowTile, g.N);
+        const uint32_t tx = kStageA + static_cast<uint32_t>(g.N) * kKStep * 2;
+        auto load = [&](int kt) {
+            const int s = kt % kStages;
+            unsigned char* sa = base + s * kStage;
+            mbar_expect_tx(&full[s], tx);
+            tma_load_2d(sa, &map_a, k_begin + kt * kKStep, m0, &full[s]);
+            tma_load_2d(sa + kStageA, &map_b, k_begin + kt * kKStep, 0, &full[s]);
+        };
+        int loaded = 0;  // K steps whose copies were issued
+        for (; loaded < min(nk, kStages); ++loaded) load(loaded);
+        bool ok = true;
+        int issued = 0;  // K steps whose MMAs were issued
+        for (int kt = 0; kt < nk; ++kt) {
+            const int s = kt % kStages;
+            if (!mbar_wait_bounded(&full[s], (kt / kStages) & 1, g.err)) {
+                ok = false;
+                break;
+            }
             tc_fence_after();
-            const uint32_t a_addr = smem_u32(sa), b_addr = smem_u32(sb);
+            const uint32_t a_addr = smem_u32(base + s * kStage), b_addr = a_addr + kStageA;
 #pragma unroll
             for (int j = 0; j < kKStep / 16; ++j)
-                mma_bf16(tmem, smem_desc(a_addr + j * 2 * kLBO), smem_desc(b_addr + j * 2 * kLBO), idesc,
+                mma_bf16(tmem, smem_desc_sw128(a_addr + j * 32), smem_desc_sw128(b_addr + j * 32), idesc,
                          (kt > 0 || j > 0) ? 1u : 0u);
-            mma_commit(&bar[s]);
+            mma_commit(&empty[s]);
+            issued = kt + 1;
+            // refill the stage of step kt - 1 once its MMAs are done (those of step kt stay queued)
+            if (kt >= 1 && loaded < nk) {
+                const int p = kt - 1;
+                if (!mbar_wait_bounded(&empty[p % kStages], (p / kStages) & 1, g.err)) {
+                    ok = false;
+                    break;
+                }
+                load(loaded);
+                ++loaded;
+            }
         }
-        issued = kt + 1;
+        // copies issued but never consumed still write shared memory: wait for them
+        if (!ok)
+            for (int kt = issued; kt < loaded; ++kt) mbar_wait_bounded(&full[kt % kStages], (kt / kStages) & 1, g.err);
+        s_issued = issued;
+        s_ok = ok ? 1 : 0;
     }
+    __syncthreads();
+    const int issued = s_issued;
     // the last commit arrives when every MMA issued before it has completed
-    bool done = ok && issued == nk && nk > 0;
+    bool done = s_ok && issued == nk && nk > 0;
     if (issued > 0) {
-        const int sl = (issued - 1) & 1;
-        const bool w = mbar_wait_bounded(&bar[sl], ph[sl], g.err);
+        const int p = issued - 1;
+        const bool w = mbar_wait_bounded(&empty[p % kStages], (p / kStages) & 1, g.err);
         done = done && w;
     }
     done = __syncthreads_and(done);
     tc_fence_after();
 
     if (done) {
-        const int row = m0 + warp * 32 + lane;
-        const uint32_t lane_addr = tmem + (static_cast<uint32_t>(warp * 32) << 16);
-        for (int c0 = 0; c0 < g.N; c0 += 32) {
+        // a warp reads the tensor-memory lanes of its quadrant (warp mod 4); the two warps of
+        // a quadrant take half of the columns each
+        const int quad = warp & 3, half = warp >> 2;
+        const int row = m0 + quad * 32 + lane;
+        const uint32_t lane_addr = tmem + (static_cast<uint32_t>(quad * 32) << 16);
+        const int c_end = (half + 1) * (g.N / 2);
+        for (int c0 = half * (g.N / 2); c0 < c_end; c0 += 32) {
             float v[32];
             tmem_ld32(lane_addr + static_cast<uint32_t>(c0), v);
             if (g.mode == kGemmPartial) {
@@ -420,19 +452,56 @@ unsigned blocks_for(long long n, int t) { return static_cast<unsigned>((n + t - 
 
 }  // namespace
 
-size_t mlp_gemm_smem_bytes() { return 2 * static_cast<size_t>(kStage) + 1024; }
+size_t mlp_gemm_smem_bytes() { return kStages * static_cast<size_t>(kStage) + 1024; }
 
 cudaError_t configure_mlp_gemm() {
     return cudaFuncSetAttribute(k_mlp_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 static_cast<int>(mlp_gemm_smem_bytes()));
 }
 
+namespace {
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link to the driver
+// library); null when the driver does not provide it.
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// Row-major BF16 matrix [rows][cols] with leading dimension ld, copied in boxes of 64
+// columns x box_rows rows into 128-byte-swizzled shared memory.
+bool encode_bf16_map(CUtensorMap* map, const bf16* ptr, long long rows, long long cols, long long ld, int box_rows) {
+    const auto encode = tensor_map_encoder();
+    if (!encode) return false;
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(cols), static_cast<cuuint64_t>(rows)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(ld) * sizeof(bf16)};
+    const cuuint32_t box[2] = {static_cast<cuuint32_t>(kKStep), static_cast<cuuint32_t>(box_rows)};
+    const cuuint32_t elem[2] = {1, 1};
+    return encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16*>(ptr), dims, strides, box, elem,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
 cudaError_t launch_mlp_gemm(const GemmArgs& g, cudaStream_t s) {
+    // TMA: 16-byte aligned bases and row strides; every box lies inside its matrix
     if (g.M <= 0 || g.M % kMlpRowTile || g.K <= 0 || g.K % kKStep || g.k_split <= 0 || g.k_split % kKStep ||
-        (g.N != 64 && g.N != 128 && g.N != 256) || g.lda % 8 || g.ldb % 8)
+        (g.N != 64 && g.N != 128 && g.N != 256) || g.lda % 8 || g.ldb % 8 || g.lda < g.K || g.ldb < g.K ||
+        reinterpret_cast<uintptr_t>(g.A) % 16 || reinterpret_cast<uintptr_t>(g.B) % 16)
+        return cudaErrorInvalidValue;
+    CUtensorMap ma, mb;
+    if (!encode_bf16_map(&ma, g.A, g.M, g.K, g.lda, kMlpRowTile) || !encode_bf16_map(&mb, g.B, g.N, g.K, g.ldb, g.N))
         return cudaErrorInvalidValue;
     const int splits = (g.K + g.k_split - 1) / g.k_split;
-    k_mlp_gemm<<<dim3(g.M / kMlpRowTile, splits), kGemmThreads, mlp_gemm_smem_bytes(), s>>>(g);
+    k_mlp_gemm<<<dim3(g.M / kMlpRowTile, splits), kGemmThreads, mlp_gemm_smem_bytes(), s>>>(ma, mb, g);
     return cudaGetLastError();
 }
 
