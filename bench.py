@@ -354,6 +354,8 @@ def run_gb300(args):
         del sim
         torch.cuda.empty_cache()
         line["batched"] = batched_solves(args, local)
+    if args.qs_cases > 0:
+        line["qs_sweep"] = qs_sweep(args, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -456,6 +458,56 @@ def batched_solves(args, device):
                            "the solve starts from the lowest-residual of plain / extrapolation / network"}
     out["timing"] = "host clock around each public call, host freestream in, circulation and force summary out"
     return out
+
+
+def qs_sweep(args, device):
+    """Solves/s of a quasi-steady sweep (the shape of CompleteSailModel wind-angle sweeps):
+    seeded cases of 1-6 sails x 16-96 panels at AWA 20-180 deg, 5-20 m/s, quasi-steady
+    defaults (Linearized solver, horseshoe wake). plain = one Simulation per case; batched =
+    one Batch (horseshoe matrices per case on the pool streams, all Linearized solves in one
+    k_solve_lin_jobs launch, graph replay). Host clock around the public calls, host
+    freestream in, results out; steps 0-3 untimed, then `steps` timed."""
+    import torch
+
+    from stormbird_gb300 import Batch, Simulation
+    from stormbird_gb300 import setups as S
+
+    n, warm, steps = args.qs_cases, 4, 5
+    cases = S.quasi_steady_cases(n, seed=4242)
+    scale = [1.0 + 0.02 * k for k in range(warm + steps)]
+    sims = [Simulation(js, device=device) for js, _ in cases]
+    t_plain = 0.0
+    for k in range(warm + steps):
+        fss = [np.tile(u * scale[k], (s.nr_freestream_points, 1)) for s, (_, u) in zip(sims, cases)]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rs = [s.do_step(time=k * 0.1, time_step=0.1, freestream_velocity=f) for s, f in zip(sims, fss)]
+        if k >= warm:
+            t_plain += time.perf_counter() - t0
+    g_plain = np.concatenate([r.circulation_strength for r in rs])
+    for s in sims:
+        s.close()
+    del sims
+    b = Batch([js for js, _ in cases], device=device)
+    t_batch = 0.0
+    for k in range(warm + steps):
+        fs = np.concatenate([np.tile(u * scale[k], (c["freestream_points"], 1)) for (_, u), c in zip(cases, b.cases)])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.do_step(time=k * 0.1, time_step=0.1, freestream_velocity=fs)
+        g = b.circulation()
+        if k >= warm:
+            t_batch += time.perf_counter() - t0
+    info = b.info()
+    b.close()
+    return {"workload": f"{n} quasi-steady sail rows (AWA 20-180 deg, 5-20 m/s, 1-6 sails, 16-96 panels), "
+                        "Linearized solver, horseshoe wake",
+            "cases": n, "timed_steps": steps, "span_lines": int(g.size),
+            "solves_per_s": {"plain": n * steps / t_plain, "batched": n * steps / t_batch},
+            "speedup_vs_plain": t_plain / t_batch,
+            "bit_identical_to_plain": bool(np.array_equal(g, g_plain)),
+            "graph": info.get("graph"),
+            "timing": "host clock around each public call, host freestream in, circulation and force summary out"}
 
 
 # --------------------------------------------------------------------------------------
@@ -694,6 +746,8 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=5, help="timed steps of the batched part")
     ap.add_argument("--train-cases", type=int, default=128, help="cases whose solves train the warm-start network")
     ap.add_argument("--train-epochs", type=int, default=40)
+    ap.add_argument("--qs-cases", type=int, default=512, help="cases of the quasi-steady sweep part (0: skip)")
+    ap.add_argument("--qs-only", action="store_true", help="only the quasi-steady sweep part")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -710,6 +764,8 @@ def main():
         run_profile_mlp(args)
     elif args.impl == "reference":
         run_reference(args)
+    elif args.qs_only:
+        print(json.dumps({"mode": "qs-sweep", **qs_sweep(args, 0)}), flush=True)
     else:
         run_gb300(args)
 

@@ -102,6 +102,10 @@ struct sb_batch {
     DevBuf<double> compact;  // [N_total] circulation, then [cases][SB_BATCH_SUMMARY]
     PinnedBuf<double> h_compact;
     DevBuf<GatherJob> gather_jobs;
+    // quasi-steady cases with the Linearized solver: one k_solve_lin_jobs launch per step
+    std::vector<int> lin_cases;
+    DevBuf<LinJob> lin_jobs;
+    size_t lin_smem = 0;
 
     // Sweep work lists: group = (sweep kind, symmetry, neglect); one launch each.
     struct Group {
@@ -234,6 +238,14 @@ struct sb_batch {
             gj.push_back(g);
         }
         gather_jobs.upload(gj);
+        std::vector<LinJob> lj;
+        for (size_t i = 0; i < cases.size(); ++i)
+            if (cases[i]->linearized_quasi_steady()) {
+                lin_cases.push_back(static_cast<int>(i));
+                lj.push_back(cases[i]->linearized_job());
+                lin_smem = std::max(lin_smem, linearized_smem_bytes(cases[i]->N));
+            }
+        if (!lj.empty()) lin_jobs.upload(lj);
         counters.alloc(16);
         err.alloc(1);
         ck(cudaMemset(err.p, 0, sizeof(int)), "memset");
@@ -459,8 +471,13 @@ struct sb_batch {
         sweeps(0);
         for (auto& c : cases) if (c->dynamic) c->after_fixed_sweep();
         fork(1);
-        for (auto& c : cases) c->step_matrix_and_solve();
+        for (auto& c : cases) {
+            if (c->linearized_quasi_steady()) c->step_matrix();
+            else c->step_matrix_and_solve();
+        }
         join(1);
+        ck(launch_solve_linearized_jobs(lin_jobs.p, static_cast<int>(lin_cases.size()), lin_smem, main),
+           "batched linearized solve");
         if (warm_mode != 0)
             ck(launch_batch_targets(gamma_all.p, w_q.p, w_g0.p, w_tr.p, N_total, w_target.p, main), "warm-start targets");
         sweeps(1);

@@ -16,8 +16,10 @@
 //      so the convergence test takes the same branch) and takes the max.
 // All waits are hardware cluster barriers; no spin loops.
 //
-// k_solve_lin: Linearized::solve (solvers/linearized.rs:54-222) with the Gaussian
-// elimination with partial pivoting of stormath/src/matrix/linalg.rs:41-103, one CTA.
+// k_solve_lin / k_solve_lin_jobs: Linearized::solve (solvers/linearized.rs:54-222) with
+// the Gaussian elimination with partial pivoting of stormath/src/matrix/linalg.rs:41-103,
+// one CTA per case: one case, or all linearized quasi-steady cases of a batch in one
+// launch.
 //
 // k_forces: SimulationResult of one step (force_calculations.rs:322-452, 669-698;
 // common_utils/forces_and_moments.rs:163-245; flow_derivatives.rs:31-63).
@@ -312,36 +314,36 @@ cudaError_t launch_solve_simple_iterative(const DevModel& m, const SolveSettings
 }
 
 // ---------------------------------------------------------------------------------------
-// Linearized solver, one CTA
+// Linearized solver: one CTA per case (one case, or every case of a batch in one launch)
 // ---------------------------------------------------------------------------------------
 constexpr int kLinThreads = 512;
 
-__device__ inline double block_sum(double v, double* red) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    __syncthreads();
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    double t = 0.0;
-    if (threadIdx.x == 0) {
-        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) t += red[w];
-        red[32] = t;
-    }
-    __syncthreads();
-    return red[32];
+// Per case in shared memory: control-point velocities, induced velocities and the
+// circulation, then the augmented matrix [N][N+1] when it fits in what the launch gave.
+__host__ __device__ inline size_t lin_vec_bytes(int N) {
+    return static_cast<size_t>(N) * (2 * sizeof(d3) + sizeof(double));
+}
+__host__ __device__ inline size_t lin_mat_bytes(int N) { return static_cast<size_t>(N) * (N + 1) * sizeof(double); }
+
+size_t linearized_smem_bytes(int N) {
+    const size_t v = lin_vec_bytes(N), a = lin_mat_bytes(N);
+    return v + a <= kLinSmemLimit ? v + a : v;
 }
 
-__global__ void __launch_bounds__(kLinThreads) k_solve_lin(DevModel m, SolveSettings st, SolveBuffers b) {
-    const int N = m.N, tid = threadIdx.x, nt = blockDim.x;
+// Linearized::solve (linearized.rs:54-222) for one case on the calling CTA. The Gaussian
+// elimination (linalg.rs:41-103) keeps the reference's arithmetic per element: the pivot is
+// the first row of largest |A[i][k]| (warp 0: per-lane scan, then a butterfly on (value,
+// lowest index)); row i -= (A[i][k] / pivot) * row k over columns k..N (a warp per row);
+// back substitution by warp 0, one row at a time. Where the matrix lives (shared memory or
+// the case's global scratch) does not change any result.
+__device__ void lin_solve_case(const DevModel& m, const SolveSettings& st, const SolveBuffers& b, unsigned char* dyn,
+                               size_t dyn_bytes) {
+    const int N = m.N, tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
     const int W1 = N + 1;
-    double* A = b.lin_work;  // [N][N+1]
-    extern __shared__ double smem[];
-    d3* vel = reinterpret_cast<d3*>(smem);               // [N]
+    d3* vel = reinterpret_cast<d3*>(dyn);                 // [N]
     d3* ind = vel + N;                                    // [N]
     double* gam = reinterpret_cast<double*>(ind + N);     // [N]
-    double* fac = gam + N;                                // [N]
-    __shared__ double red[33];
+    double* A = lin_vec_bytes(N) + lin_mat_bytes(N) <= dyn_bytes ? gam + N : b.lin_work;  // [N][N+1]
     __shared__ int s_piv;
 
     // velocities with the fixed part, span removed, and the equation system (linearized.rs:61-136)
@@ -368,46 +370,68 @@ __global__ void __launch_bounds__(kLinThreads) k_solve_lin(DevModel m, SolveSett
     __syncthreads();
     // forward elimination with partial pivoting
     for (int k = 0; k < N; ++k) {
-        if (tid == 0) {
-            int mr = k;
-            for (int i = k + 1; i < N; ++i)
-                if (fabs(A[static_cast<long long>(i) * W1 + k]) > fabs(A[static_cast<long long>(mr) * W1 + k])) mr = i;
-            s_piv = mr;
+        double* Ak = A + static_cast<long long>(k) * W1;
+        if (warp == 0) {
+            double bv = -1.0;
+            int bi = N;
+            for (int i = k + lane; i < N; i += 32) {
+                const double v = fabs(A[static_cast<long long>(i) * W1 + k]);
+                if (v > bv) {
+                    bv = v;
+                    bi = i;
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ov > bv || (ov == bv && oi < bi)) {
+                    bv = ov;
+                    bi = oi;
+                }
+            }
+            if (lane == 0) s_piv = bi < N ? bi : k;
         }
         __syncthreads();
-        int mr = s_piv;
-        if (mr != k)
+        const int mr = s_piv;
+        if (mr != k) {
+            double* Am = A + static_cast<long long>(mr) * W1;
             for (int j = tid; j <= N; j += nt) {
-                double t = A[static_cast<long long>(k) * W1 + j];
-                A[static_cast<long long>(k) * W1 + j] = A[static_cast<long long>(mr) * W1 + j];
-                A[static_cast<long long>(mr) * W1 + j] = t;
+                const double t = Ak[j];
+                Ak[j] = Am[j];
+                Am[j] = t;
             }
+        }
         __syncthreads();
-        double piv = A[static_cast<long long>(k) * W1 + k];
-        if (fabs(piv) < 1e-12) {
+        const double piv = Ak[k];
+        if (fabs(piv) < 1e-12) {  // the same value in every thread: the whole CTA leaves
             if (tid == 0) {
                 atomicExch(b.err, kDevSingular);
                 b.scalars[3] = 1.0;
             }
             return;
         }
-        for (int i = k + 1 + tid; i < N; i += nt) fac[i] = A[static_cast<long long>(i) * W1 + k] / piv;
-        __syncthreads();
-        const long long rows = N - k - 1, cols = N + 1 - k;
-        for (long long q = tid; q < rows * cols; q += nt) {
-            int i = k + 1 + static_cast<int>(q / cols), j = k + static_cast<int>(q % cols);
-            A[static_cast<long long>(i) * W1 + j] -= fac[i] * A[static_cast<long long>(k) * W1 + j];
+        for (int i = k + 1 + warp; i < N; i += nw) {
+            double* Ai = A + static_cast<long long>(i) * W1;
+            const double f = Ai[k] / piv;
+            __syncwarp();  // every lane has read A[i][k] before lane 0 overwrites it
+            for (int j = k + lane; j <= N; j += 32) Ai[j] -= f * Ak[j];
         }
         __syncthreads();
     }
     // back substitution
-    for (int i = N - 1; i >= 0; --i) {
-        double part = 0.0;
-        for (int j = i + 1 + tid; j < N; j += nt) part += A[static_cast<long long>(i) * W1 + j] * gam[j];
-        double sum = block_sum(part, red);
-        if (tid == 0) gam[i] = (A[static_cast<long long>(i) * W1 + N] - sum) / A[static_cast<long long>(i) * W1 + i];
-        __syncthreads();
+    if (warp == 0) {
+        for (int i = N - 1; i >= 0; --i) {
+            const double* Ai = A + static_cast<long long>(i) * W1;
+            double part = 0.0;
+            for (int j = i + 1 + lane; j < N; j += 32) part += Ai[j] * gam[j];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+            if (lane == 0) gam[i] = (Ai[N] - part) / Ai[i];
+            __syncwarp();
+        }
     }
+    __syncthreads();
     // induced velocity and the total velocity (linearized.rs:141-156)
     auto update_induced = [&]() {
         for (int i = tid; i < N; i += nt) {
@@ -463,13 +487,37 @@ __global__ void __launch_bounds__(kLinThreads) k_solve_lin(DevModel m, SolveSett
     }
 }
 
+__global__ void __launch_bounds__(kLinThreads) k_solve_lin(DevModel m, SolveSettings st, SolveBuffers b, unsigned smem) {
+    extern __shared__ __align__(16) unsigned char lin_dyn[];
+    lin_solve_case(m, st, b, lin_dyn, smem);
+}
+
+// Every case of a batch in one launch: CTA i solves jobs[i].
+__global__ void __launch_bounds__(kLinThreads) k_solve_lin_jobs(const LinJob* jobs, unsigned smem) {
+    extern __shared__ __align__(16) unsigned char lin_dyn[];
+    const LinJob& j = jobs[blockIdx.x];
+    lin_solve_case(j.m, j.st, j.b, lin_dyn, smem);
+}
+
 cudaError_t launch_solve_linearized(const DevModel& m, const SolveSettings& st, const SolveBuffers& b, cudaStream_t s) {
-    size_t smem = static_cast<size_t>(m.N) * (2 * sizeof(d3) + 2 * sizeof(double));
+    const size_t smem = linearized_smem_bytes(m.N);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k_solve_lin, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e != cudaSuccess) return e;
     }
-    k_solve_lin<<<1, kLinThreads, smem, s>>>(m, st, b);
+    k_solve_lin<<<1, kLinThreads, smem, s>>>(m, st, b, static_cast<unsigned>(smem));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_solve_linearized_jobs(const LinJob* jobs, int n, size_t smem, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    if (smem > kLinSmemLimit) return cudaErrorInvalidValue;
+    if (smem > 48 * 1024) {
+        cudaError_t e =
+            cudaFuncSetAttribute(k_solve_lin_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+    }
+    k_solve_lin_jobs<<<n, kLinThreads, smem, s>>>(jobs, static_cast<unsigned>(smem));
     return cudaGetLastError();
 }
 

@@ -155,6 +155,19 @@ int solve_cluster_size(int N);
 cudaError_t launch_solve_simple_iterative(const DevModel& m, const SolveSettings& st, const SolveBuffers& b, cudaStream_t s);
 cudaError_t launch_solve_linearized(const DevModel& m, const SolveSettings& st, const SolveBuffers& b, cudaStream_t s);
 
+// One linearized solve of a batch (CTA blockIdx.x of k_solve_lin_jobs).
+struct LinJob {
+    DevModel m;
+    SolveSettings st;
+    SolveBuffers b;
+};
+// Dynamic shared memory one linearized solve of N span lines uses: its vectors, plus its
+// matrix when that fits under kLinSmemLimit (else the matrix stays in SolveBuffers::lin_work).
+constexpr size_t kLinSmemLimit = 227 * 1024 - 1024;
+size_t linearized_smem_bytes(int N);
+// n solves in one launch, each with `smem` bytes (the largest linearized_smem_bytes of the jobs).
+cudaError_t launch_solve_linearized_jobs(const LinJob* jobs, int n, size_t smem, cudaStream_t s);
+
 struct ForceArgs {
     const double* gamma = nullptr;  // [N]
     const d3* vel = nullptr;        // [N] solver output velocity

@@ -794,7 +794,8 @@ struct sb_sim {
     }
 
     // Influence matrix (unit matrix of the first wake row, or horseshoes) and the solve.
-    void step_matrix_and_solve() {
+    // The frozen wake's matrix: unit first-row panels (dynamic) or horseshoes (quasi-steady).
+    void step_matrix() {
         if (dynamic) {
             ck(launch_unit_matrix(row0_64.p, ctrl.p, N, dm.symmetry, dm.neglect_self, wing_of_line.p, factors.p, stream),
                "unit matrix");
@@ -809,6 +810,9 @@ struct sb_sim {
             record(3);
         }
         record(4);
+    }
+
+    SolveBuffers solve_buffers() const {
         SolveBuffers sb;
         sb.fixed = fixed.p;
         sb.factors = factors.p;
@@ -824,6 +828,23 @@ struct sb_sim {
             sb.rec32_row0 = rec32.p;
             sb.rec64_row0 = precision == 2 ? rec64.p : nullptr;
         }
+        return sb;
+    }
+
+    // A quasi-steady case with the Linearized solver: its solve depends on nothing that
+    // changes between steps (device pointers and settings), so a batch solves all such
+    // cases in one launch of k_solve_lin_jobs.
+    bool linearized_quasi_steady() const { return !dynamic && solver_kind == 1; }
+    LinJob linearized_job() const {
+        LinJob j;
+        j.m = dm;
+        j.st = solve;
+        j.b = solve_buffers();
+        return j;
+    }
+
+    void step_solve() {
+        const SolveBuffers sb = solve_buffers();
         if (solver_kind == 0) {
             SolveSettings st = solve;
             if (solve.start_with_linearized) {
@@ -843,10 +864,19 @@ struct sb_sim {
             ck(launch_solve_linearized(dm, solve, sb, stream), "linearized solve");
         }
         launches += 1;
+    }
+
+    void step_after_solve() {
         // chain records of the wake with this step's solution in row 0, for the roll-up
         if (dynamic && use_chains() && rollup_active()) build_chains();
         record(5);
         if (!dynamic) record(6);
+    }
+
+    void step_matrix_and_solve() {
+        step_matrix();
+        step_solve();
+        step_after_solve();
     }
 
     // Forces and the output block (force_calculations.rs:669-698).

@@ -254,6 +254,29 @@ def uneven_cases(n_cases, seed=0, sails=(1, 6), panels=(16, 96), wake_rows=(50, 
     return out
 
 
+def quasi_steady_cases(n_cases, seed=0, sails=(1, 6), panels=(16, 96), awa_deg=(20.0, 180.0),
+                       wind_speed=(5.0, 20.0), angle_of_attack_deg=8.0, spacing=40.0):
+    """Independent quasi-steady sail rows drawn uniformly (seeded), the shape of a
+    CompleteSailModel wind-angle sweep: sail count, panels per sail, apparent wind angle and
+    speed per case; local wing angle = AWA - AoA; the quasi-steady defaults (Linearized
+    solver, horseshoe wake). Returns [(setup_json, freestream vector)]."""
+    rng = np.random.default_rng(seed)
+    f = foil(cl_initial_slope=2 * math.pi, mean_positive_stall_angle=math.radians(15.0),
+             mean_negative_stall_angle=math.radians(15.0), cd_min=0.01, cdi_correction_factor=0.05)
+    out = []
+    for _ in range(n_cases):
+        awa = float(rng.uniform(*awa_deg))
+        u = float(rng.uniform(*wind_speed))
+        s = int(rng.integers(sails[0], sails[1] + 1))
+        p = int(rng.integers(panels[0], panels[1] + 1))
+        wings = [wing_builder([(spacing * i, 0, 0), (spacing * i, 0, SPAN)], [(CHORD, 0, 0), (CHORD, 0, 0)], f)
+                 for i in range(s)]
+        lfm = line_force_model(wings, p, local_wing_angles=[math.radians(awa - angle_of_attack_deg)] * s)
+        th = math.radians(awa)
+        out.append((simulation(lfm, dynamic=False), u * np.array([math.cos(th), math.sin(th), 0.0])))
+    return out
+
+
 def batch_freestream(batch, winds, t: float) -> np.ndarray:
     """Freestream of every case of a Batch at time t, case after case."""
     return np.concatenate([w.freestream(t, c["freestream_points"]) for w, c in zip(winds, batch.cases)])

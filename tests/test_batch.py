@@ -192,3 +192,37 @@ def test_quasi_steady_cases_in_a_batch(gpu_lib):
             r = sim.do_step(time=k * DT, time_step=DT, freestream_velocity=np.tile(u * sp, (sim.nr_freestream_points, 1)))
             assert np.array_equal(g[b.case_slice(i)], r.circulation_strength), (k, i)
             assert np.array_equal(s[i, :3], r.integrated_forces_sum()), (k, i)
+
+
+def test_batched_linearized_quasi_steady_sweep(gpu_lib, oracle_mod):
+    """An angle sweep of quasi-steady cases with the Linearized solver: the batch solves them
+    in one launch (a CTA per case) and every case gives what its own Simulation gives
+    (bit-identical: the same device function) and what the oracle gives (1e-9, the tolerance
+    of the single-case Linearized test). Sizes 8 to 180 span lines: the largest system keeps
+    its matrix in global memory, the others in shared memory."""
+    import math
+
+    from stormbird_gb300 import Batch, Simulation
+
+    sizes = [8, 24, 64, 180, 31, 100]
+    cases, winds = [], []
+    for k, n in enumerate(sizes):
+        cases.append(S.simulation(S.rectangular_wing(5.0, 1.2, math.radians(2.0 + k), n), dynamic=False))
+        a = math.radians(1.5 * k)
+        winds.append(np.array([1.2 * math.cos(a), 1.2 * math.sin(a), 0.0]))
+    b = Batch(cases)
+    sims = [Simulation(js) for js in cases]
+    oracles = [oracle_mod.OracleSimulation(js) for js in cases]
+    for step in range(3):
+        scale = 1.0 + 0.1 * step
+        fs = np.concatenate([np.tile(w * scale, (c["freestream_points"], 1)) for w, c in zip(winds, b.cases)])
+        b.do_step(time=0.2 * step, time_step=0.2, freestream_velocity=fs)
+        g, s = b.circulation(), b.summary()
+        for i, (sim, o, w) in enumerate(zip(sims, oracles, winds)):
+            fi = np.tile(w * scale, (sim.nr_freestream_points, 1))
+            r = sim.do_step(time=0.2 * step, time_step=0.2, freestream_velocity=fi)
+            assert np.array_equal(g[b.case_slice(i)], r.circulation_strength), (step, i)
+            assert np.array_equal(s[i, :3], r.integrated_forces_sum()), (step, i)
+            ro = o.do_step(time=0.2 * step, time_step=0.2, freestream_velocity=fi)
+            assert rel_inf(g[b.case_slice(i)], ro.circulation_strength) <= 1e-9, (step, i)
+            assert rel_vec(s[i, :3], ro.integrated_forces_sum()) <= 1e-9, (step, i)
