@@ -132,6 +132,8 @@ int sb_sim_set_rotation_only(sb_sim* sim, const double rotation[3]);
 int sb_sim_set_velocity_linear(sb_sim* sim, const double velocity[3]);
 int sb_sim_set_velocity_angular(sb_sim* sim, const double velocity[3]);
 int sb_sim_set_local_wing_angles(sb_sim* sim, const double* angles, size_t nr_wings);
+/* LineForceModel::local_wing_angles (line_force_model/mod.rs), read back. */
+int sb_sim_get_local_wing_angles(const sb_sim* sim, double* angles, size_t nr_wings);
 
 /* previous_circulation_strength (simulation.rs:26): reset to zero, set (warm start) or read. */
 int sb_sim_reset_previous_circulation(sb_sim* sim);
@@ -343,6 +345,65 @@ int sb_batch_set_warm_start(sb_batch* batch, sb_mlp* network, int mode);
 /* The last step's features [total_lines][SB_WARM_START_FEATURES] and targets [total_lines]
  * (device or host pointers; either may be NULL). */
 int sb_batch_copy_warm_start_data(sb_batch* batch, float* features, float* targets, size_t rows);
+
+/* ---------------------------------------------------------------------------------------
+ * CompleteSailModel: a lifting-line simulation with a wind environment and a sail
+ * controller (stormbird/src/lifting_line/complete_sail_model/mod.rs), JSON schema
+ * CompleteSailModelBuilder {lifting_line_simulation, wind_environment, controller}
+ * (complete_sail_model/builder.rs:19-24). The C functions replace cstormbird's
+ * complete_sail_model_* (interfaces/cstormbird/src/lifting_line/complete_sail_model.rs).
+ * ------------------------------------------------------------------------------------- */
+typedef struct sb_csm sb_csm;
+
+/* cstormbird WindCondition (interfaces/cstormbird/src/wind.rs:9-13): a power-law profile
+ * with this velocity at 10 m and factor 1/9, coming from this direction (radians). */
+typedef struct sb_wind_condition {
+    double velocity;
+    double direction_coming_from;
+} sb_wind_condition;
+
+/* cstormbird SingleSailResult (interfaces/cstormbird/src/results.rs:5-10): per sail the
+ * total integrated force and moment and the input power. */
+typedef struct sb_single_sail_result {
+    double force[3];
+    double moment[3];
+    double input_power;
+} sb_single_sail_result;
+
+/* complete_sail_model_new (complete_sail_model.rs:26-43): NULL on error (sb_last_error). */
+sb_csm* sb_csm_new(const char* setup_json, int device);
+/* complete_sail_model_drop (complete_sail_model.rs:61-67) */
+void sb_csm_free(sb_csm* model);
+/* complete_sail_model_get_number_of_sails (complete_sail_model.rs:46-58): -1 on NULL. */
+int sb_csm_get_number_of_sails(const sb_csm* model);
+/* complete_sail_model_simulate_steady_state_condition (complete_sail_model.rs:69-110): the
+ * controller applied for the condition, then one step at time 0 with time step 1; writes
+ * min(sails, results_out_length) results and returns that count; -1 NULL, -2 zero length. */
+int sb_csm_simulate_steady_state_condition(sb_csm* model, sb_wind_condition wind_condition, double ship_velocity,
+                                           double controller_loading, sb_single_sail_result* results_out,
+                                           size_t results_out_length);
+/* CompleteSailModel::apply_controller_based_on_wind_condition (mod.rs:190-212) and ::do_step
+ * (mod.rs:170-188) with a WindCondition JSON document (wind_condition/mod.rs:19-39). */
+int sb_csm_apply_controller(sb_csm* model, double time, double time_step, const char* condition_json,
+                            double ship_velocity, double controller_loading);
+int sb_csm_do_step(sb_csm* model, double time, double time_step, const char* condition_json, double ship_velocity,
+                   sb_step_output* out);
+/* The model's lifting-line simulation (owned by the model): wing angles, motion, sizes. */
+int sb_csm_sim(sb_csm* model, sb_sim** sim);
+/* n steady-state conditions in one batched pass, each on its own replica of the model that
+ * starts from the model's current wing angles and motion (the model itself is unchanged);
+ * results_out [n_conditions][sails], results_out_length = n_conditions x sails. A replica
+ * keeps its own previous solution and velocity history between sweeps of the same size. */
+int sb_csm_sweep_steady_state(sb_csm* model, const sb_wind_condition* wind_conditions, const double* ship_velocities,
+                              const double* controller_loadings, size_t n_conditions, sb_single_sail_result* results_out,
+                              size_t results_out_length);
+/* CompleteSailModel::simulate_condition_optimal_controller_loading (mod.rs:60-101): the
+ * loadings linspace(0.1, 1, n) as one sweep; the sails' results of the loading with the
+ * largest -F_x * ship_velocity - input power (first maximum), and that loading. */
+int sb_csm_simulate_condition_optimal_controller_loading(sb_csm* model, sb_wind_condition wind_condition,
+                                                         double ship_velocity, size_t nr_loadings_to_test,
+                                                         sb_single_sail_result* results_out, size_t results_out_length,
+                                                         double* best_loading);
 
 #ifdef __cplusplus
 }

@@ -58,6 +58,12 @@ def lib() -> ctypes.CDLL:
         L.sbo_sim_wind_freestream.argtypes = [c_void_p, ctypes.c_char_p, ctypes.c_char_p, c_double, c_double, dp,
                                               c_size_t]
         L.sbo_wind_velocity_at.argtypes = [ctypes.c_char_p, ctypes.c_char_p, dp, c_size_t, c_double, c_double, dp]
+        L.sbo_csm_new.restype = c_void_p
+        L.sbo_csm_new.argtypes = [ctypes.c_char_p]
+        L.sbo_csm_free.argtypes = [c_void_p]
+        L.sbo_csm_steady_state.argtypes = [c_void_p, c_double, c_double, c_double, c_double, dp, c_size_t]
+        L.sbo_csm_local_wing_angles.argtypes = [c_void_p, dp, c_size_t]
+        L.sbo_csm_set_local_wing_angles.argtypes = [c_void_p, dp, c_size_t]
         _LIB = L
     return _LIB
 
@@ -214,3 +220,42 @@ def bs_sweep(corners, cores, strengths, far_field_ratio, targets, nthreads=1) ->
     _check(lib().sbo_bs_sweep(as_ptr(c), as_ptr(_d(cores)), as_ptr(_d(strengths)), c.shape[0], float(far_field_ratio),
                               as_ptr(t), t.shape[0], as_ptr(out), int(nthreads)))
     return out
+
+
+class OracleCompleteSailModel:
+    """f64 restatement of CompleteSailModel's steady-state conditions (controller + wind + step)."""
+
+    def __init__(self, setup_string: str, nr_sails: int):
+        h = lib().sbo_csm_new(setup_string.encode())
+        if not h:
+            raise SbError(-3, lib().sbo_last_error().decode())
+        self._h = ctypes.c_void_p(h)
+        self.nr_sails = nr_sails
+
+    def close(self):
+        if self._h:
+            lib().sbo_csm_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def simulate_steady_state_condition(self, velocity: float, direction: float, ship_velocity: float,
+                                        loading: float) -> np.ndarray:
+        """Per sail [force (3), moment (3), input power]."""
+        out = np.zeros((self.nr_sails, 7))
+        _check(lib().sbo_csm_steady_state(self._h, float(velocity), float(direction), float(ship_velocity),
+                                          float(loading), as_ptr(out), self.nr_sails))
+        return out
+
+    def local_wing_angles(self) -> np.ndarray:
+        out = np.zeros(self.nr_sails)
+        _check(lib().sbo_csm_local_wing_angles(self._h, as_ptr(out), self.nr_sails))
+        return out
+
+    def set_local_wing_angles(self, angles):
+        a = _d(angles)
+        _check(lib().sbo_csm_set_local_wing_angles(self._h, as_ptr(a), a.size))

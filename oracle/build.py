@@ -18,6 +18,8 @@ SOURCES = [os.path.join(HERE, "sb_oracle_capi.cpp")]
 DEPS = SOURCES + [
     os.path.join(HERE, "sb_oracle.hpp"),
     os.path.join(HERE, "sb_oracle_wind.hpp"),
+    os.path.join(HERE, "sb_oracle_controller.hpp"),
+    os.path.join(HERE, "..", "stormbird_gb300", "csrc", "sb_controller_setup.hpp"),
     os.path.join(HERE, "..", "stormbird_gb300", "csrc", "sb_wind_setup.hpp"),
     os.path.join(HERE, "..", "stormbird_gb300", "csrc", "sb_setup.hpp"),
     os.path.join(HERE, "..", "stormbird_gb300", "csrc", "json_min.hpp"),

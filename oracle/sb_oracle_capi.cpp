@@ -9,6 +9,7 @@
 #include "../include/stormbird_gb300.h"
 #include "sb_oracle.hpp"
 #include "sb_oracle_wind.hpp"
+#include "sb_oracle_controller.hpp"
 
 namespace {
 thread_local std::string g_err;
@@ -311,6 +312,55 @@ int sbo_bs_sweep(const double* corners, const double* cores, const double* stren
         }
         out[3 * i] = acc.x; out[3 * i + 1] = acc.y; out[3 * i + 2] = acc.z;
     }
+    return SB_OK;
+}
+
+// CompleteSailModel steady-state conditions (sb_oracle_controller.hpp)
+void* sbo_csm_new(const char* json) {
+    if (!json) { fail(SB_ERR_NULL_ARG, "setup_json is NULL"); return nullptr; }
+    try {
+        return new sbo::CompleteSailModel(json);
+    } catch (const std::exception& e) {
+        fail(SB_ERR_BAD_JSON, e.what());
+        return nullptr;
+    }
+}
+
+void sbo_csm_free(void* h) { delete static_cast<sbo::CompleteSailModel*>(h); }
+
+// per sail: total force [3], total moment [3], input power (0: NoPower) -> out [sails][7]
+int sbo_csm_steady_state(void* h, double velocity, double direction, double ship_velocity, double loading, double* out,
+                         size_t n_sails) {
+    if (!h || !out) return fail(SB_ERR_NULL_ARG, "null argument");
+    auto* m = static_cast<sbo::CompleteSailModel*>(h);
+    if (n_sails != m->sim.lfm.nr_wings()) return fail(SB_ERR_SIZE, "size mismatch");
+    try {
+        const sbo::StepResult r = m->steady_state(sbo::power_model_condition(velocity, direction), ship_velocity, loading);
+        for (size_t w = 0; w < n_sails; ++w) {
+            const sbo::V3 f = r.integrated_forces[w * 6 + 5], mo = r.integrated_moments[w * 6 + 5];
+            double* o = out + 7 * w;
+            o[0] = f.x; o[1] = f.y; o[2] = f.z; o[3] = mo.x; o[4] = mo.y; o[5] = mo.z; o[6] = 0.0;
+        }
+    } catch (const std::exception& e) {
+        return fail(SB_ERR_STATE, e.what());
+    }
+    return SB_OK;
+}
+
+int sbo_csm_local_wing_angles(void* h, double* out, size_t n) {
+    if (!h || !out) return fail(SB_ERR_NULL_ARG, "null argument");
+    const auto& lfm = static_cast<sbo::CompleteSailModel*>(h)->sim.lfm;
+    if (n != lfm.nr_wings()) return fail(SB_ERR_SIZE, "size mismatch");
+    for (size_t i = 0; i < n; ++i) out[i] = lfm.local_wing_angles[i];
+    return SB_OK;
+}
+
+int sbo_csm_set_local_wing_angles(void* h, const double* a, size_t n) {
+    if (!h || !a) return fail(SB_ERR_NULL_ARG, "null argument");
+    auto& lfm = static_cast<sbo::CompleteSailModel*>(h)->sim.lfm;
+    if (n != lfm.nr_wings()) return fail(SB_ERR_SIZE, "size mismatch");
+    for (size_t i = 0; i < n; ++i) lfm.local_wing_angles[i] = a[i];
+    lfm.update_global_data_representations();
     return SB_OK;
 }
 

@@ -60,6 +60,16 @@ class StepOutput(ctypes.Structure):
     ]
 
 
+class WindConditionC(ctypes.Structure):
+    """sb_wind_condition (cstormbird WindCondition)."""
+    _fields_ = [("velocity", ctypes.c_double), ("direction_coming_from", ctypes.c_double)]
+
+
+class SingleSailResultC(ctypes.Structure):
+    """sb_single_sail_result (cstormbird SingleSailResult)."""
+    _fields_ = [("force", ctypes.c_double * 3), ("moment", ctypes.c_double * 3), ("input_power", ctypes.c_double)]
+
+
 class SbError(RuntimeError):
     """An SB_ERR_* status from the C ABI."""
 

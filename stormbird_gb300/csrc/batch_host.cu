@@ -33,6 +33,7 @@
 #include <numeric>
 #include <tuple>
 
+#include "batch_access.hpp"
 #include "sb_mlp.h"
 #include "sim_core.hpp"
 
@@ -147,6 +148,10 @@ struct sb_batch {
     bool has_wind = false;
     DevBuf<double> wind_steps;
     PinnedBuf<double> h_wind_steps;
+    // controller measurements [3 * N_total] and per-wing force/moment totals (CompleteSailModel sweeps)
+    DevBuf<double> ctrl_in;
+    PinnedBuf<double> h_ctrl_in;
+    PinnedBuf<double> h_wing_totals;
 
     bool use_graph = true;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -712,6 +717,60 @@ struct sb_batch {
         step(time, dt, true);
     }
 
+    // The flow measurements every case's controller reads before a steady-state step
+    // (CompleteSailModel::apply_controller_based_on_freestream, complete_sail_model/mod.rs:
+    // 259-288): each case's wind freestream at its control points for (time, ship velocity),
+    // then |u|, the angle of attack and the apparent wind direction per line. Returns the
+    // host copy: case i's lines at 3 * line_off[i] (|u| [N], angle [N], direction [N]).
+    const double* controller_inputs(double time, const double* ship_velocities) {
+        if (!has_wind) raise(SB_ERR_STATE, "no wind models: call sb_batch_set_wind first");
+        for (size_t i = 0; i < cases.size(); ++i) {
+            if (!std::isfinite(ship_velocities[i])) raise(SB_ERR_NONFINITE, "non-finite ship velocity of case " + std::to_string(i));
+            h_wind_steps.p[2 * i] = time;
+            h_wind_steps.p[2 * i + 1] = ship_velocities[i];
+        }
+        if (ctrl_in.n == 0) {
+            ctrl_in.alloc(static_cast<size_t>(N_total) * 3);
+            h_ctrl_in.alloc(static_cast<size_t>(N_total) * 3);
+        }
+        ck(cudaMemcpyAsync(wind_steps.p, h_wind_steps.p, cases.size() * 2 * sizeof(double), cudaMemcpyHostToDevice, main),
+           "H2D wind steps");
+        fork(0);
+        for (size_t i = 0; i < cases.size(); ++i) {
+            sb_sim& c = *cases[i];
+            c.enqueue_wind_freestream();
+            double* d = ctrl_in.p + 3 * line_off[i];
+            ck(launch_controller_input(c.dm, c.params, c.fs_p, d, c.stream), "controller input");
+            ck(cudaMemcpyAsync(h_ctrl_in.p + 3 * line_off[i], d, 3 * c.N * sizeof(double), cudaMemcpyDeviceToHost,
+                               c.stream),
+               "D2H controller input");
+        }
+        join(0);
+        ck(cudaStreamSynchronize(main), "controller input");
+        return h_ctrl_in.p;
+    }
+
+    // Integrated forces [S][6][3] then moments [S][6][3] of every case after the last step,
+    // case after case (what SimulationResult::as_simplified reads, results/simulation.rs:150-166).
+    const double* wing_totals() {
+        size_t total = 0;
+        for (const auto& c : cases) total += static_cast<size_t>(c->S) * 36;
+        if (h_wing_totals.n < total) h_wing_totals.alloc(total);
+        size_t off = 0;
+        for (const auto& c : cases) {
+            const size_t n = static_cast<size_t>(c->S) * 18;
+            ck(cudaMemcpyAsync(h_wing_totals.p + off, c->out.p + c->L.intf, n * sizeof(double), cudaMemcpyDeviceToHost,
+                               main),
+               "D2H wing forces");
+            ck(cudaMemcpyAsync(h_wing_totals.p + off + n, c->out.p + c->L.intm, n * sizeof(double),
+                               cudaMemcpyDeviceToHost, main),
+               "D2H wing moments");
+            off += 2 * n;
+        }
+        ck(cudaStreamSynchronize(main), "wing totals");
+        return h_wing_totals.p;
+    }
+
     void do_step_device(double time, double dt, const double* fs_dev, size_t n) {
         if (static_cast<long long>(n) != nfs_total) raise(SB_ERR_SIZE, "freestream length mismatch");
         ck(cudaMemcpyAsync(fs_all.p, fs_dev, n * sizeof(d3), cudaMemcpyDeviceToDevice, main), "D2D freestream");
@@ -780,6 +839,18 @@ struct sb_batch {
 // =======================================================================================
 // C ABI
 // =======================================================================================
+namespace sbhost {
+
+size_t batch_case_count(const sb_batch* b) { return b->cases.size(); }
+sb_sim* batch_case(sb_batch* b, size_t i) { return b->cases.at(i).get(); }
+long long batch_line_offset(const sb_batch* b, size_t i) { return b->line_off.at(i); }
+const double* batch_controller_inputs(sb_batch* b, double time, const double* ship_velocities) {
+    return b->controller_inputs(time, ship_velocities);
+}
+const double* batch_wing_totals(sb_batch* b) { return b->wing_totals(); }
+
+}  // namespace sbhost
+
 namespace {
 int null_arg() {
     report_error(SB_ERR_NULL_ARG, "null argument");

@@ -9,6 +9,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstdio>
 #include <cstdlib>
 #include <map>
 #include <memory>
@@ -230,5 +231,62 @@ private:
 };
 
 inline Value parse(const std::string& text) { return Parser(text).parse_document(); }
+
+// Serialises a value back to JSON text: numbers with 17 significant digits (they parse back
+// to the same double), strings with the escapes the parser reads.
+inline void dump_to(const Value& v, std::string& out) {
+    switch (v.kind) {
+        case Value::Null: out += "null"; return;
+        case Value::Bool: out += v.b ? "true" : "false"; return;
+        case Value::Number: {
+            char buf[40];
+            std::snprintf(buf, sizeof(buf), "%.17g", v.num);
+            out += buf;
+            return;
+        }
+        case Value::String: {
+            out += '"';
+            for (unsigned char c : v.str) {
+                if (c == '"') out += "\\\"";
+                else if (c == '\\') out += "\\\\";
+                else if (c < 0x20) {
+                    char buf[8];
+                    std::snprintf(buf, sizeof(buf), "\\u%04x", c);
+                    out += buf;
+                } else out += static_cast<char>(c);
+            }
+            out += '"';
+            return;
+        }
+        case Value::Arr: {
+            out += '[';
+            for (size_t i = 0; i < v.arr->size(); ++i) {
+                if (i) out += ',';
+                dump_to((*v.arr)[i], out);
+            }
+            out += ']';
+            return;
+        }
+        case Value::Obj: {
+            out += '{';
+            for (size_t i = 0; i < v.obj->size(); ++i) {
+                if (i) out += ',';
+                Value key;
+                key.kind = Value::String;
+                key.str = (*v.obj)[i].first;
+                dump_to(key, out);
+                out += ':';
+                dump_to((*v.obj)[i].second, out);
+            }
+            out += '}';
+            return;
+        }
+    }
+}
+inline std::string dump(const Value& v) {
+    std::string s;
+    dump_to(v, s);
+    return s;
+}
 
 }  // namespace sbjson

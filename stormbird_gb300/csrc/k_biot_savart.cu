@@ -512,19 +512,27 @@ __global__ void k_unit_matrix(const PanelRec<double>* row0, const d3* ctrl, int 
     factors[id] = u;
 }
 
-// Quasi-steady wake: core length and wake vectors (frozen_wake.rs:74-100). One thread.
-__global__ void k_qs_prep(DevModel m, int core_kind, double core_value, double wake_length, d3* wake_vec, double* rc_out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double rc = 0.0;
-    if (core_kind == 0) {
-        double s = 0.0;
-        for (int i = 0; i < m.N; ++i) s += len(m.span_e[i] - m.span_s[i]);
-        rc = core_value * (s / static_cast<double>(m.N));
-    } else if (core_kind == 1) {
-        rc = core_value;
+// Quasi-steady wake: core length and wake vectors (frozen_wake.rs:74-100). One CTA: the
+// span line lengths and the wake vectors in parallel (FP64 square roots and divisions are
+// slow on this part, so a serial loop over them costs microseconds per line), the mean
+// length summed in line order by one thread.
+constexpr int kQsPrepThreads = 256;
+__global__ void __launch_bounds__(kQsPrepThreads) k_qs_prep(DevModel m, int core_kind, double core_value,
+                                                            double wake_length, d3* wake_vec, double* rc_out) {
+    const int tid = threadIdx.x;
+    for (int k = tid; k < m.Np; k += kQsPrepThreads) wake_vec[k] = normalize(m.felt_span[k]) * wake_length;
+    if (core_kind != 0) {
+        if (tid == 0) *rc_out = core_kind == 1 ? core_value : 0.0;
+        return;
     }
-    *rc_out = rc;
-    for (int k = 0; k < m.Np; ++k) wake_vec[k] = normalize(m.felt_span[k]) * wake_length;
+    extern __shared__ double lens[];  // [N]
+    for (int i = tid; i < m.N; i += kQsPrepThreads) lens[i] = len(m.span_e[i] - m.span_s[i]);
+    __syncthreads();
+    if (tid == 0) {
+        double s = 0.0;
+        for (int i = 0; i < m.N; ++i) s += lens[i];
+        *rc_out = core_value * (s / static_cast<double>(m.N));
+    }
 }
 
 // Horseshoe influence matrix (frozen_wake.rs:102-128, horseshoe_vortex.rs:23-103):
@@ -554,7 +562,12 @@ __global__ void k_horseshoe_matrix(DevModel m, const d3* wake_vec, const double*
 
 cudaError_t launch_horseshoe_matrix(const DevModel& m, int core_kind, double core_value, double wake_length, d3* wake_vec,
                                     double* rc_dev, int sym, d3* factors, cudaStream_t s) {
-    k_qs_prep<<<1, 32, 0, s>>>(m, core_kind, core_value, wake_length, wake_vec, rc_dev);
+    const size_t smem = static_cast<size_t>(m.N) * sizeof(double);
+    if (smem > 48 * 1024) {
+        cudaError_t a = cudaFuncSetAttribute(k_qs_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (a != cudaSuccess) return a;
+    }
+    k_qs_prep<<<1, kQsPrepThreads, smem, s>>>(m, core_kind, core_value, wake_length, wake_vec, rc_dev);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     long long tot = static_cast<long long>(m.N) * m.N;

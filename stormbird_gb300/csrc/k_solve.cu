@@ -581,28 +581,25 @@ __global__ void k_forces(DevModel m, StepParams p, ForceArgs f) {
         }
     }
     __syncthreads();
-    for (int w = tid; w < S; w += nt) {
-        d3 fs[6], ms[6];
-        for (int c = 0; c < 6; ++c) fs[c] = ms[c] = mk(0, 0, 0);
+    // integrated force and moment of each (wing, component), summed in line order
+    for (int t = tid; t < S * 6; t += nt) {
+        const int w = t / 6, c = t % 6;
+        d3 fs = mk(0, 0, 0), ms = mk(0, 0, 0);
         for (int i = m.wing_start[w]; i < m.wing_end[w]; ++i) {
             if (m.is_virtual[i]) continue;
             d3 cp = body ? 0.5 * (m.span_s_local[i] + m.span_e_local[i]) : 0.5 * (m.span_s[i] + m.span_e[i]);
-            for (int c = 0; c < 6; ++c) {
-                long long base = L.sect + (static_cast<long long>(c) * N + i) * 3;
-                d3 sf = mk(o[base], o[base + 1], o[base + 2]);
-                fs[c] = fs[c] + sf;
-                ms[c] = ms[c] + cross(cp, sf);
-            }
+            long long base = L.sect + (static_cast<long long>(c) * N + i) * 3;
+            d3 sf = mk(o[base], o[base + 1], o[base + 2]);
+            fs = fs + sf;
+            ms = ms + cross(cp, sf);
         }
-        for (int c = 0; c < 6; ++c) {
-            long long bf = L.intf + (static_cast<long long>(w) * 6 + c) * 3, bm = L.intm + (static_cast<long long>(w) * 6 + c) * 3;
-            o[bf] = fs[c].x;
-            o[bf + 1] = fs[c].y;
-            o[bf + 2] = fs[c].z;
-            o[bm] = ms[c].x;
-            o[bm + 1] = ms[c].y;
-            o[bm + 2] = ms[c].z;
-        }
+        long long bf = L.intf + (static_cast<long long>(w) * 6 + c) * 3, bm = L.intm + (static_cast<long long>(w) * 6 + c) * 3;
+        o[bf] = fs.x;
+        o[bf + 1] = fs.y;
+        o[bf + 2] = fs.z;
+        o[bm] = ms.x;
+        o[bm + 1] = ms.y;
+        o[bm + 2] = ms.z;
     }
     __syncthreads();
     if (tid == 0) {

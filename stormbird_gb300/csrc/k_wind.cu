@@ -10,6 +10,9 @@
 // along the zero direction. Control points then get the inflow corrections
 // (environment.rs:242-271, inflow_corrections.rs:21-95) at the apparent wind direction of
 // the steady wind at 10 m (environment.rs:273-292). f64 throughout.
+//
+// k_controller_input: the flow measurements a CompleteSailModel's controller reads from
+// that freestream before each steady-state step.
 #include "sb_kernels.h"
 
 namespace sbgpu {
@@ -109,7 +112,34 @@ __global__ void k_wind_freestream(WindDevice w, const d3* ctrl, const int* wing_
     out[i] = u;
 }
 
+// ControllerInput::new_from_velocity (controller/input.rs:99-157) per line, on the geometry
+// k_prep_geometry left for the current wing angles and motion: out[i] = |v_i|,
+// out[N + i] = the angle of attack (force_calculations.rs:79-107: signed angle from the global
+// chord to v about the span line's direction, 0 when |v| <= MIN_POSITIVE), out[2N + i] = the
+// apparent wind direction (environment.rs:315-345: signed angle from the unrotated chord of
+// the wing's first strip, moved by the rigid body's rotation, to v about that strip's global
+// span direction).
+__global__ void k_controller_input(DevModel m, StepParams p, const d3* v, double* out) {
+    const int N = m.N;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        const d3 u = v[i];
+        const d3 span_dir = normalize(m.span_e[i] - m.span_s[i]);
+        out[i] = len(u);
+        out[N + i] = len(u) > kMinPositive ? signed_angle_between(m.chord_global[i], u, span_dir) : 0.0;
+        const int ws = m.wing_start[m.wing_of_line[i]];
+        const d3 axis = normalize(m.span_e[ws] - m.span_s[ws]);
+        const d3 chord_first = rotate_xyz(m.chord_not_rotated[ws], p.rotation);
+        out[2 * N + i] = signed_angle_between(chord_first, u, axis);
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_controller_input(const DevModel& m, const StepParams& p, const d3* v, double* out, cudaStream_t s) {
+    if (m.N <= 0) return cudaSuccess;
+    k_controller_input<<<(m.N + 127) / 128, 128, 0, s>>>(m, p, v, out);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_wind_freestream(const WindDevice& w, const d3* ctrl, const int* wing_of_line, int N, const d3* wake,
                                    long long n_wake, d3* out, cudaStream_t s) {

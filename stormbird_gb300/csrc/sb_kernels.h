@@ -233,6 +233,9 @@ struct WindDevice {
 // Freestream at the control points [N] then the wake points [n_wake] into out.
 cudaError_t launch_wind_freestream(const WindDevice& w, const d3* ctrl, const int* wing_of_line, int N, const d3* wake,
                                    long long n_wake, d3* out, cudaStream_t s);
+// Controller flow measurements per line from the control-point velocities v [N]:
+// out [3][N] = |v|, angle of attack, apparent wind direction (geometry from k_prep_geometry).
+cudaError_t launch_controller_input(const DevModel& m, const StepParams& p, const d3* v, double* out, cudaStream_t s);
 
 // Sets the calling thread's sb_last_error / sb_last_status (sim_host.cu).
 void report_error(int code, const std::string& message);

@@ -135,6 +135,16 @@ int sb_sim_set_local_wing_angles(sb_sim* sim, const double* a, size_t n) {
     return SB_OK;
 }
 
+int sb_sim_get_local_wing_angles(const sb_sim* sim, double* a, size_t n) {
+    if (!sim || !a) { g_last_error = "null argument"; return SB_ERR_NULL_ARG; }
+    if (n != static_cast<size_t>(sim->S)) {
+        g_last_error = "The number of wing angles must match the number of wings in the simulation.";
+        return SB_ERR_SIZE;
+    }
+    for (size_t i = 0; i < n; ++i) a[i] = sim->params.local_wing_angles[i];
+    return SB_OK;
+}
+
 int sb_sim_reset_previous_circulation(sb_sim* sim) {
     if (!sim) { g_last_error = "null handle"; return SB_ERR_NULL_ARG; }
     return guard([&] {

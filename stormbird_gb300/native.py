@@ -9,7 +9,7 @@ from __future__ import annotations
 import ctypes
 import os
 
-from ._abi import StepOutput
+from ._abi import SingleSailResultC, StepOutput, WindConditionC
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libstormbird_gb300.so")
@@ -38,6 +38,7 @@ SIGNATURES = [
     ("sb_sim_set_velocity_linear", ctypes.c_int, [_vp, _dp]),
     ("sb_sim_set_velocity_angular", ctypes.c_int, [_vp, _dp]),
     ("sb_sim_set_local_wing_angles", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
+    ("sb_sim_get_local_wing_angles", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
     ("sb_sim_reset_previous_circulation", ctypes.c_int, [_vp]),
     ("sb_sim_set_previous_circulation", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
     ("sb_sim_get_previous_circulation", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
@@ -88,6 +89,21 @@ SIGNATURES = [
     ("sb_mlp_train_step", ctypes.c_int, [_vp, _vp, _vp, ctypes.c_size_t, ctypes.c_float, _dp]),
     ("sb_batch_set_warm_start", ctypes.c_int, [_vp, _vp, ctypes.c_int]),
     ("sb_batch_copy_warm_start_data", ctypes.c_int, [_vp, _vp, _vp, ctypes.c_size_t]),
+    ("sb_csm_new", _vp, [ctypes.c_char_p, ctypes.c_int]),
+    ("sb_csm_free", None, [_vp]),
+    ("sb_csm_get_number_of_sails", ctypes.c_int, [_vp]),
+    ("sb_csm_simulate_steady_state_condition", ctypes.c_int, [_vp, WindConditionC, ctypes.c_double, ctypes.c_double,
+                                                              ctypes.POINTER(SingleSailResultC), ctypes.c_size_t]),
+    ("sb_csm_apply_controller", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double, ctypes.c_char_p,
+                                               ctypes.c_double, ctypes.c_double]),
+    ("sb_csm_do_step", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double, ctypes.c_char_p, ctypes.c_double,
+                                      ctypes.POINTER(StepOutput)]),
+    ("sb_csm_sim", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_void_p)]),
+    ("sb_csm_sweep_steady_state", ctypes.c_int, [_vp, ctypes.POINTER(WindConditionC), _dp, _dp, ctypes.c_size_t,
+                                                 ctypes.POINTER(SingleSailResultC), ctypes.c_size_t]),
+    ("sb_csm_simulate_condition_optimal_controller_loading", ctypes.c_int,
+     [_vp, WindConditionC, ctypes.c_double, ctypes.c_size_t, ctypes.POINTER(SingleSailResultC), ctypes.c_size_t,
+      _dp]),
 ]
 
 _LIB = None

@@ -277,6 +277,36 @@ def quasi_steady_cases(n_cases, seed=0, sails=(1, 6), panels=(16, 96), awa_deg=(
     return out
 
 
+def wing_sail_set_points(max_angle_deg: float = 15.0, **extra) -> dict:
+    """Set points of a single-element wing sail: angle-of-attack set point 0 for apparent wind
+    within 10 deg of the bow, ramping to +/- max_angle at 15 deg and held to 180 deg (the
+    reference's default, stormbird_setup/controller.py new_default_wing_sail_single_element)."""
+    d = {"apparent_wind_directions_data": [math.radians(a) for a in (-180, -15, -10, 10, 15, 180)],
+         "angle_of_attack_data": [math.radians(a) for a in
+                                  (-max_angle_deg, -max_angle_deg, 0.0, 0.0, max_angle_deg, max_angle_deg)]}
+    d.update(extra)
+    return d
+
+
+def complete_sail_model(nr_sails=2, panels_per_sail=24, spacing=40.0, set_points=None, flow_measurement=None,
+                        wind_environment=None, solver=None, **controller_extra) -> str:
+    """CompleteSailModelBuilder JSON (complete_sail_model/builder.rs:19-24): a quasi-steady row
+    of wing sails (span 30 m, chord 10 m), the default wind environment, a controller with
+    one set point table per sail."""
+    f = foil(cl_initial_slope=2 * math.pi, mean_positive_stall_angle=math.radians(15.0),
+             mean_negative_stall_angle=math.radians(15.0), cd_min=0.01, cdi_correction_factor=0.05)
+    wings = [wing_builder([(spacing * i, 0, 0), (spacing * i, 0, SPAN)], [(CHORD, 0, 0), (CHORD, 0, 0)], f)
+             for i in range(nr_sails)]
+    lls = json.loads(simulation(line_force_model(wings, panels_per_sail), dynamic=False, solver=solver))
+    controller = {"set_points": set_points if set_points is not None else [wing_sail_set_points()] * nr_sails}
+    if flow_measurement is not None:
+        controller["flow_measurement_settings"] = flow_measurement
+    controller.update(controller_extra)
+    return json.dumps({"lifting_line_simulation": lls,
+                       "wind_environment": wind_environment if wind_environment is not None else {},
+                       "controller": controller})
+
+
 def batch_freestream(batch, winds, t: float) -> np.ndarray:
     """Freestream of every case of a Batch at time t, case after case."""
     return np.concatenate([w.freestream(t, c["freestream_points"]) for w, c in zip(winds, batch.cases)])

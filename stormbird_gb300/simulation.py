@@ -89,6 +89,11 @@ class Simulation:
         a = _d(local_wing_angles)
         _check(lib().sb_sim_set_local_wing_angles(self._h, as_ptr(a), a.size))
 
+    def local_wing_angles(self) -> np.ndarray:
+        out = np.zeros(self.nr_wings)
+        _check(lib().sb_sim_get_local_wing_angles(self._h, as_ptr(out), self.nr_wings))
+        return out
+
     def reset_previous_circulation_strength(self):
         _check(lib().sb_sim_reset_previous_circulation(self._h))
 
