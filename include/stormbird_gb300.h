@@ -198,6 +198,29 @@ int sb_sim_set_segment_sharing(sb_sim* sim, int enable);
 int sb_sim_set_wind(sb_sim* sim, const char* environment_json, const char* condition_json);
 int sb_sim_wind_freestream(sb_sim* sim, double time, double ship_velocity, double* freestream_xyz, size_t n);
 int sb_sim_do_step_wind(sb_sim* sim, double time, double time_step, double ship_velocity, sb_step_output* out);
+
+/*
+ * Result output in the reference's formats (stormbird/src/common_utils/results/simulation.rs).
+ * sb_sim_result_json: the last step's SimulationResult as serde writes it (write_to_file,
+ * simulation.rs:91-98); *length = bytes needed including the terminating NUL (SB_ERR_SIZE
+ * when capacity is smaller). sb_sim_result_csv: the reduced flattened header and data row
+ * (as_reduced_flatten_csv_string, simulation.rs:168-205). "Last step" = the last
+ * sb_sim_do_step / sb_sim_do_step_wind, or the step sb_sim_read_output copied.
+ * sb_sim_set_result_file: from the next step on, every sb_sim_do_step / sb_sim_do_step_wind
+ * result goes to `path`, formatted and written on a background thread from a host copy:
+ * SB_RESULTS_JSON_HISTORY writes a JSON array of SimulationResult (the file
+ * result_history_from_file reads, simulation.rs:37-45), closed when the writer is replaced
+ * or the handle freed; SB_RESULTS_CSV appends one reduced row per step, with the header first
+ * when the file is new (io_utils/csv_data.rs:11-33). NULL or SB_RESULTS_OFF stops writing.
+ * sb_sim_flush_results waits until every queued step is written.
+ */
+#define SB_RESULTS_OFF 0
+#define SB_RESULTS_JSON_HISTORY 1
+#define SB_RESULTS_CSV 2
+int sb_sim_result_json(const sb_sim* sim, char* buffer, size_t capacity, size_t* length);
+int sb_sim_result_csv(const sb_sim* sim, char* header, size_t header_capacity, char* data, size_t data_capacity);
+int sb_sim_set_result_file(sb_sim* sim, const char* path, int format);
+int sb_sim_flush_results(sb_sim* sim);
 /* 1 if the roll-up sweep of this simulation uses shared segments in its current mode. */
 int sb_sim_segment_sharing_active(const sb_sim* sim, int* active);
 

@@ -17,9 +17,10 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libstormbird_gb300.so")
 UNITS = ["k_biot_savart.cu", "k_wake.cu", "k_solve.cu", "k_probe.cu", "sim_host.cu", "batch_host.cu", "noalloc_sweep.cu", "k_mlp.cu",
-         "mlp_host.cu", "k_wind.cu", "csm_host.cu"]
+         "mlp_host.cu", "k_wind.cu", "csm_host.cu",
+         "result_io.cu"]
 HEADERS = ["sb_device.cuh", "sb_kernels.h", "sb_setup.hpp", "json_min.hpp", "sim_core.hpp", "sb_ptx.cuh", "sb_mlp.h", "sb_wind_setup.hpp",
-           "sb_controller_setup.hpp", "batch_access.hpp"]
+           "sb_controller_setup.hpp", "batch_access.hpp", "result_io.hpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -85,7 +85,7 @@ __device__ inline d3 rotate_around_axis(d3 v, double angle, d3 axis) {
 // Euler XYZ rotation (transformations.rs:182-207). The line force model's rigid-body
 // motion always uses this form: the builder never copies its rotation_type into the
 // motion (line_force_model/builder/mod.rs:107-108).
-__device__ inline d3 rotate_xyz(d3 v, d3 r) {
+__host__ __device__ inline d3 rotate_xyz(d3 v, d3 r) {
     d3 n = v;
     if (r.x != 0.0) {
         double ty = n.y, tz = n.z, c = cos(r.x), s = sin(r.x);
@@ -106,7 +106,7 @@ __device__ inline d3 rotate_xyz(d3 v, d3 r) {
 }
 
 // Vector expressed in the body frame (transformations.rs:233-265, XYZ).
-__device__ inline d3 to_body(d3 v, d3 r) {
+__host__ __device__ inline d3 to_body(d3 v, d3 r) {
     d3 ax = rotate_xyz(mk(1, 0, 0), r), ay = rotate_xyz(mk(0, 1, 0), r), az = rotate_xyz(mk(0, 0, 1), r);
     return {dot(v, ax), dot(v, ay), dot(v, az)};
 }

@@ -22,6 +22,7 @@
 #include "sb_kernels.h"
 #include "sb_setup.hpp"
 #include "sb_wind_setup.hpp"
+#include "result_io.hpp"
 
 namespace sbhost {
 
@@ -914,6 +915,40 @@ struct sb_sim {
             if (swept[0]) { cudaEventElapsedTime(&ms, ev[8], ev[9]); last_ms[8] = ms; }
         }
         check_device_status();
+        if (writer) writer->push(result_record());
+    }
+
+    // ---------------------------------------------------------------- result output
+    std::unique_ptr<sbhost::ResultWriter> writer;
+    mutable std::vector<std::pair<int, int>> wing_ranges_h;  // line range of each wing (filled once)
+
+    // The last step's SimulationResult from the host copy of the output block.
+    sbhost::ResultRecord result_record() const {
+        if (wing_ranges_h.empty()) {
+            std::vector<int> ws(S), we(S);
+            ck(cudaMemcpy(ws.data(), wing_start.p, S * sizeof(int), cudaMemcpyDeviceToHost), "D2H");
+            ck(cudaMemcpy(we.data(), wing_end.p, S * sizeof(int), cudaMemcpyDeviceToHost), "D2H");
+            for (int w = 0; w < S; ++w) wing_ranges_h.emplace_back(ws[w], we[w]);
+        }
+        sbhost::ResultRecord r;
+        r.time = params.time;
+        r.N = N;
+        r.S = S;
+        r.body = dm.output_body != 0;
+        r.motion = params;
+        r.wings = wing_ranges_h;
+        r.out.assign(h_out.p, h_out.p + L.total);
+        return r;
+    }
+
+    void set_result_file(const char* path, int format) {
+        writer.reset();
+        if (!path || format == sbhost::kResultsOff) return;
+        try {
+            writer.reset(new sbhost::ResultWriter(path, format));
+        } catch (const std::exception& e) {
+            raise(SB_ERR_STATE, e.what());
+        }
     }
 
     void check_device_status() {

@@ -233,6 +233,40 @@ int sb_sim_do_step_wind(sb_sim* sim, double time, double time_step, double ship_
     return guard([&] { sim->do_step_wind(time, time_step, ship_velocity, out); });
 }
 
+int sb_sim_set_result_file(sb_sim* sim, const char* path, int format) {
+    if (!sim) { g_last_error = "null handle"; return SB_ERR_NULL_ARG; }
+    if (format < SB_RESULTS_OFF || format > SB_RESULTS_CSV) { g_last_error = "unknown result format"; return SB_ERR_SIZE; }
+    return guard([&] { sim->set_result_file(path, format); });
+}
+
+int sb_sim_flush_results(sb_sim* sim) {
+    if (!sim) { g_last_error = "null handle"; return SB_ERR_NULL_ARG; }
+    return guard([&] {
+        if (sim->writer && !sim->writer->flush()) raise(SB_ERR_STATE, "writing the result file failed");
+    });
+}
+
+int sb_sim_result_json(const sb_sim* sim, char* buf, size_t capacity, size_t* length) {
+    if (!sim || !length) { g_last_error = "null argument"; return SB_ERR_NULL_ARG; }
+    return guard([&] {
+        const std::string s = sbhost::result_json(sim->result_record());
+        *length = s.size() + 1;
+        if (!buf || capacity < s.size() + 1) raise(SB_ERR_SIZE, "buffer too small: " + std::to_string(s.size() + 1) + " bytes needed");
+        std::memcpy(buf, s.c_str(), s.size() + 1);
+    });
+}
+
+int sb_sim_result_csv(const sb_sim* sim, char* header, size_t header_capacity, char* data, size_t data_capacity) {
+    if (!sim || !header || !data) { g_last_error = "null argument"; return SB_ERR_NULL_ARG; }
+    return guard([&] {
+        std::string h, d;
+        sbhost::result_csv(sim->result_record(), h, d);
+        if (header_capacity < h.size() + 1 || data_capacity < d.size() + 1) raise(SB_ERR_SIZE, "buffer too small");
+        std::memcpy(header, h.c_str(), h.size() + 1);
+        std::memcpy(data, d.c_str(), d.size() + 1);
+    });
+}
+
 int sb_sim_set_segment_sharing(sb_sim* sim, int enable) {
     if (!sim) { g_last_error = "null handle"; return SB_ERR_NULL_ARG; }
     sim->share_segments = enable != 0;

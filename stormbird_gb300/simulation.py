@@ -175,6 +175,31 @@ class Simulation:
                                          ctypes.byref(self._out.struct)))
         return self._out.to_result(time)
 
+    # -- result output (common_utils/results/simulation.rs) ------------------------------
+    def result_json(self) -> str:
+        """The last step's SimulationResult as the reference serialises it (write_to_file)."""
+        n = ctypes.c_size_t()
+        lib().sb_sim_result_json(self._h, None, 0, ctypes.byref(n))
+        buf = ctypes.create_string_buffer(n.value)
+        _check(lib().sb_sim_result_json(self._h, buf, n.value, ctypes.byref(n)))
+        return buf.value.decode()
+
+    def as_reduced_flatten_csv_string(self) -> tuple[str, str]:
+        """(header, data) of the last step: time and each wing's total force and moment."""
+        cap = 64 * (self.nr_wings + 1) * 8
+        h, d = ctypes.create_string_buffer(cap), ctypes.create_string_buffer(cap * 4)
+        _check(lib().sb_sim_result_csv(self._h, h, cap, d, cap * 4))
+        return h.value.decode(), d.value.decode()
+
+    def write_results_to(self, path: str | None, fmt: str = "json"):
+        """Every following do_step / do_step_wind result is written to `path` on a background
+        thread: "json" a JSON array of SimulationResult, "csv" reduced rows (None stops)."""
+        code = {"json": 1, "csv": 2}[fmt] if path else 0
+        _check(lib().sb_sim_set_result_file(self._h, path.encode() if path else None, code))
+
+    def flush_results(self):
+        _check(lib().sb_sim_flush_results(self._h))
+
     def set_segment_sharing(self, on: bool = True):
         """Shared-segment roll-up sweep (default on; used when every pair is near-field and all
         panels share one core length): each wake segment evaluated once with the strength
