@@ -103,10 +103,15 @@ struct sb_batch {
     DevBuf<double> compact;  // [N_total] circulation, then [cases][SB_BATCH_SUMMARY]
     PinnedBuf<double> h_compact;
     DevBuf<GatherJob> gather_jobs;
-    // quasi-steady cases with the Linearized solver: one k_solve_lin_jobs launch per step
-    std::vector<int> lin_cases;
-    DevBuf<LinJob> lin_jobs;
-    size_t lin_smem = 0;
+    // quasi-steady cases with the Linearized solver: one launch per plan shape and step
+    // (group g: clusters of 2^g CTAs; g = 0 one CTA per case)
+    struct LinGroup {
+        LinPlan plan;
+        int n = 0;
+        DevBuf<LinJob> jobs;
+    };
+    static constexpr int kLinGroups = 5;
+    LinGroup lin_groups[kLinGroups];
 
     // Sweep work lists: group = (sweep kind, symmetry, neglect); one launch each.
     struct Group {
@@ -243,14 +248,20 @@ struct sb_batch {
             gj.push_back(g);
         }
         gather_jobs.upload(gj);
-        std::vector<LinJob> lj;
+        std::vector<LinJob> lj[kLinGroups];
         for (size_t i = 0; i < cases.size(); ++i)
             if (cases[i]->linearized_quasi_steady()) {
-                lin_cases.push_back(static_cast<int>(i));
-                lj.push_back(cases[i]->linearized_job());
-                lin_smem = std::max(lin_smem, linearized_smem_bytes(cases[i]->N));
+                const LinPlan p = linearized_plan(cases[i]->N);
+                int g = 0;
+                while ((1 << g) < p.cluster) ++g;
+                lin_groups[g].plan.cluster = p.cluster;
+                lin_groups[g].plan.smem = std::max(lin_groups[g].plan.smem, p.smem);
+                lj[g].push_back(cases[i]->linearized_job());
             }
-        if (!lj.empty()) lin_jobs.upload(lj);
+        for (int g = 0; g < kLinGroups; ++g) {
+            lin_groups[g].n = static_cast<int>(lj[g].size());
+            if (!lj[g].empty()) lin_groups[g].jobs.upload(lj[g]);
+        }
         counters.alloc(16);
         err.alloc(1);
         ck(cudaMemset(err.p, 0, sizeof(int)), "memset");
@@ -481,8 +492,20 @@ struct sb_batch {
             else c->step_matrix_and_solve();
         }
         join(1);
-        ck(launch_solve_linearized_jobs(lin_jobs.p, static_cast<int>(lin_cases.size()), lin_smem, main),
-           "batched linearized solve");
+        // the plan groups run side by side on the pool streams
+        int lin_used = 0;
+        for (const auto& g : lin_groups) lin_used += g.n > 0 ? 1 : 0;
+        if (lin_used == 1) {
+            for (const auto& g : lin_groups)
+                if (g.n > 0) ck(launch_solve_linearized_jobs(g.jobs.p, g.n, g.plan, main), "batched linearized solve");
+        } else if (lin_used > 1) {
+            fork(1);
+            for (int gi = 0; gi < kLinGroups; ++gi)
+                if (lin_groups[gi].n > 0)
+                    ck(launch_solve_linearized_jobs(lin_groups[gi].jobs.p, lin_groups[gi].n, lin_groups[gi].plan, pool[gi]),
+                       "batched linearized solve");
+            join(1);
+        }
         if (warm_mode != 0)
             ck(launch_batch_targets(gamma_all.p, w_q.p, w_g0.p, w_tr.p, N_total, w_target.p, main), "warm-start targets");
         sweeps(1);

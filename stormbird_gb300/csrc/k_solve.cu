@@ -25,6 +25,10 @@
 // common_utils/forces_and_moments.rs:163-245; flow_derivatives.rs:31-63).
 #include <cooperative_groups.h>
 
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "sb_device.cuh"
 #include "sb_kernels.h"
 
@@ -317,6 +321,7 @@ cudaError_t launch_solve_simple_iterative(const DevModel& m, const SolveSettings
 // Linearized solver: one CTA per case (one case, or every case of a batch in one launch)
 // ---------------------------------------------------------------------------------------
 constexpr int kLinThreads = 512;
+constexpr int kLinMaxCluster = 16;  // non-portable cluster size (16 SMs of one GPC)
 
 // Per case in shared memory: control-point velocities, induced velocities and the
 // circulation, then the augmented matrix [N][N+1] when it fits in what the launch gave.
@@ -325,9 +330,96 @@ __host__ __device__ inline size_t lin_vec_bytes(int N) {
 }
 __host__ __device__ inline size_t lin_mat_bytes(int N) { return static_cast<size_t>(N) * (N + 1) * sizeof(double); }
 
-size_t linearized_smem_bytes(int N) {
-    const size_t v = lin_vec_bytes(N), a = lin_mat_bytes(N);
-    return v + a <= kLinSmemLimit ? v + a : v;
+// Cluster of C CTAs: the vectors, the pivot row, the row permutation and its inverse, and
+// the CTA's share of rows ((N + C - 1) / C rows of N + 1 values).
+__host__ __device__ inline size_t lin_cluster_bytes(int N, int C) {
+    const size_t W1 = static_cast<size_t>(N) + 1;
+    return lin_vec_bytes(N) + W1 * sizeof(double) + 2 * static_cast<size_t>(N) * sizeof(int) +
+           static_cast<size_t>((N + C - 1) / C) * W1 * sizeof(double);
+}
+
+// One row of the linearized system (linearized.rs:61-136): the velocity with the fixed part
+// and the span component removed, the coefficients row[0..N-1] and the right-hand side row[N].
+__device__ inline void lin_build_row(const DevModel& m, const SolveBuffers& b, int i, double* row) {
+    const int N = m.N;
+    RowGeom g = row_geom(m, i);
+    d3 v = g.felt + b.fixed[i];
+    v = v - project(v, g.span_rel);
+    d3 un = normalize(v);
+    d3 sd = normalize(g.span_rel);
+    d3 nd = cross(un, sd);
+    double aoa = len(v) > kMinPositive ? signed_angle_between(g.chord, v, g.span_dir) : 0.0;
+    const FoilP f = m.foils[g.wing];
+    double cll = foil_cl_linear(f, aoa);
+    double ut = dot(v, un);
+    double dcl = f.cl_initial_slope;
+    for (int c = 0; c < N; ++c) {
+        double uin = dot(b.factors[static_cast<long long>(i) * N + c], nd);
+        double a = -dcl * uin / ut;
+        if (i == c) a += 2.0 / (g.chord_len * ut);
+        row[c] = a;
+    }
+    row[N] = -cll;
+}
+
+// After the solve, on one CTA: induced and total velocities, the viscous correction, the
+// residual and the outputs (linearized.rs:141-213).
+__device__ void lin_finish(const DevModel& m, const SolveSettings& st, const SolveBuffers& b, d3* vel, d3* ind,
+                           double* gam) {
+    const int N = m.N, tid = threadIdx.x, nt = blockDim.x;
+    // induced velocity and the total velocity (linearized.rs:141-156)
+    auto update_induced = [&]() {
+        for (int i = tid; i < N; i += nt) {
+            double sx = 0.0, sy = 0.0, sz = 0.0;
+            for (int c = 0; c < N; ++c) {
+                d3 f = b.factors[static_cast<long long>(i) * N + c];
+                sx += f.x * gam[c];
+                sy += f.y * gam[c];
+                sz += f.z * gam[c];
+            }
+            d3 fx = b.fixed[i];
+            ind[i] = mk(fx.x + sx, fx.y + sy, fx.z + sz);
+        }
+        __syncthreads();
+    };
+    update_induced();
+    for (int i = tid; i < N; i += nt) vel[i] = total_velocity(st, m.felt_ctrl[i], ind[i]);
+    __syncthreads();
+    // viscous correction (linearized.rs:158-202)
+    if (!st.disable_viscous_corrections) {
+        for (int i = tid; i < N; i += nt) {
+            RowGeom g = row_geom(m, i);
+            const FoilP f = m.foils[g.wing];
+            double aoa = len(vel[i]) > kMinPositive ? signed_angle_between(g.chord, vel[i], g.span_dir) : 0.0;
+            double cll = foil_cl_linear(f, aoa);
+            double clf = foil_cl_pre_stall(f, aoa);
+            if (fabs(cll) > kMinPositive) gam[i] *= clf / cll;
+        }
+        __syncthreads();
+        if (st.full_induced_correction) update_induced();
+        for (int i = tid; i < N; i += nt) vel[i] = total_velocity(st, m.felt_ctrl[i], ind[i]);
+        __syncthreads();
+    }
+    // residual (linearized.rs:204-213), summed in control-point order
+    if (tid == 0) {
+        double s = 0.0;
+        for (int i = 0; i < N; ++i) {
+            RowGeom g = row_geom(m, i);
+            const FoilP f = m.foils[g.wing];
+            double aoa = len(vel[i]) > kMinPositive ? signed_angle_between(g.chord, vel[i], g.span_dir) : 0.0;
+            s += residual_term(m, g, f, gam[i], vel[i], aoa);
+        }
+        b.scalars[0] = s / static_cast<double>(N);
+        b.scalars[1] = 1.0;
+        b.scalars[2] = 1.0;
+    }
+    for (int i = tid; i < N; i += nt) {
+        b.gamma_prev[i] = gam[i];
+        b.vel_out[i] = vel[i];
+        if (b.wake_str_row0) b.wake_str_row0[i] = gam[i];
+        if (b.rec32_row0) b.rec32_row0[i].v[kRec32Gamma] = static_cast<float>(gam[i]);
+        if (b.rec64_row0) b.rec64_row0[i].v[kRec64Gamma] = gam[i];
+    }
 }
 
 // Linearized::solve (linearized.rs:54-222) for one case on the calling CTA. The Gaussian
@@ -346,27 +438,7 @@ __device__ void lin_solve_case(const DevModel& m, const SolveSettings& st, const
     double* A = lin_vec_bytes(N) + lin_mat_bytes(N) <= dyn_bytes ? gam + N : b.lin_work;  // [N][N+1]
     __shared__ int s_piv;
 
-    // velocities with the fixed part, span removed, and the equation system (linearized.rs:61-136)
-    for (int i = tid; i < N; i += nt) {
-        RowGeom g = row_geom(m, i);
-        d3 v = g.felt + b.fixed[i];
-        v = v - project(v, g.span_rel);
-        d3 un = normalize(v);
-        d3 sd = normalize(g.span_rel);
-        d3 nd = cross(un, sd);
-        double aoa = len(v) > kMinPositive ? signed_angle_between(g.chord, v, g.span_dir) : 0.0;
-        const FoilP f = m.foils[g.wing];
-        double cll = foil_cl_linear(f, aoa);
-        double ut = dot(v, un);
-        double dcl = f.cl_initial_slope;
-        for (int c = 0; c < N; ++c) {
-            double uin = dot(b.factors[static_cast<long long>(i) * N + c], nd);
-            double a = -dcl * uin / ut;
-            if (i == c) a += 2.0 / (g.chord_len * ut);
-            A[static_cast<long long>(i) * W1 + c] = a;
-        }
-        A[static_cast<long long>(i) * W1 + N] = -cll;
-    }
+    for (int i = tid; i < N; i += nt) lin_build_row(m, b, i, A + static_cast<long long>(i) * W1);
     __syncthreads();
     // forward elimination with partial pivoting
     for (int k = 0; k < N; ++k) {
@@ -432,59 +504,7 @@ __device__ void lin_solve_case(const DevModel& m, const SolveSettings& st, const
         }
     }
     __syncthreads();
-    // induced velocity and the total velocity (linearized.rs:141-156)
-    auto update_induced = [&]() {
-        for (int i = tid; i < N; i += nt) {
-            double sx = 0.0, sy = 0.0, sz = 0.0;
-            for (int c = 0; c < N; ++c) {
-                d3 f = b.factors[static_cast<long long>(i) * N + c];
-                sx += f.x * gam[c];
-                sy += f.y * gam[c];
-                sz += f.z * gam[c];
-            }
-            d3 fx = b.fixed[i];
-            ind[i] = mk(fx.x + sx, fx.y + sy, fx.z + sz);
-        }
-        __syncthreads();
-    };
-    update_induced();
-    for (int i = tid; i < N; i += nt) vel[i] = total_velocity(st, m.felt_ctrl[i], ind[i]);
-    __syncthreads();
-    // viscous correction (linearized.rs:158-202)
-    if (!st.disable_viscous_corrections) {
-        for (int i = tid; i < N; i += nt) {
-            RowGeom g = row_geom(m, i);
-            const FoilP f = m.foils[g.wing];
-            double aoa = len(vel[i]) > kMinPositive ? signed_angle_between(g.chord, vel[i], g.span_dir) : 0.0;
-            double cll = foil_cl_linear(f, aoa);
-            double clf = foil_cl_pre_stall(f, aoa);
-            if (fabs(cll) > kMinPositive) gam[i] *= clf / cll;
-        }
-        __syncthreads();
-        if (st.full_induced_correction) update_induced();
-        for (int i = tid; i < N; i += nt) vel[i] = total_velocity(st, m.felt_ctrl[i], ind[i]);
-        __syncthreads();
-    }
-    // residual (linearized.rs:204-213), summed in control-point order
-    if (tid == 0) {
-        double s = 0.0;
-        for (int i = 0; i < N; ++i) {
-            RowGeom g = row_geom(m, i);
-            const FoilP f = m.foils[g.wing];
-            double aoa = len(vel[i]) > kMinPositive ? signed_angle_between(g.chord, vel[i], g.span_dir) : 0.0;
-            s += residual_term(m, g, f, gam[i], vel[i], aoa);
-        }
-        b.scalars[0] = s / static_cast<double>(N);
-        b.scalars[1] = 1.0;
-        b.scalars[2] = 1.0;
-    }
-    for (int i = tid; i < N; i += nt) {
-        b.gamma_prev[i] = gam[i];
-        b.vel_out[i] = vel[i];
-        if (b.wake_str_row0) b.wake_str_row0[i] = gam[i];
-        if (b.rec32_row0) b.rec32_row0[i].v[kRec32Gamma] = static_cast<float>(gam[i]);
-        if (b.rec64_row0) b.rec64_row0[i].v[kRec64Gamma] = gam[i];
-    }
+    lin_finish(m, st, b, vel, ind, gam);
 }
 
 __global__ void __launch_bounds__(kLinThreads) k_solve_lin(DevModel m, SolveSettings st, SolveBuffers b, unsigned smem) {
@@ -499,26 +519,255 @@ __global__ void __launch_bounds__(kLinThreads) k_solve_lin_jobs(const LinJob* jo
     lin_solve_case(j.m, j.st, j.b, lin_dyn, smem);
 }
 
-cudaError_t launch_solve_linearized(const DevModel& m, const SolveSettings& st, const SolveBuffers& b, cudaStream_t s) {
-    const size_t smem = linearized_smem_bytes(m.N);
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_solve_lin, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        if (e != cudaSuccess) return e;
+// Linearized::solve for a system whose matrix does not fit one CTA's shared memory, on a
+// thread-block cluster of C CTAs: physical row r lives in the shared memory of CTA r mod C
+// (row r / C there). Row exchanges are kept as a permutation held by every CTA (at[k] =
+// physical row at position k, pos[r] its inverse), so rows never move. Per column k, one
+// cluster barrier: each CTA's warp 0 has put its candidate for column k (the rows at
+// positions >= k: largest |A[r][k]|, then lowest position, i.e. the reference's first
+// largest row after its swaps) into a double-buffered slot; after the barrier every CTA
+// reduces the C candidates in rank order, applies the same exchange to its permutation,
+// copies the pivot row (columns k..N; a pivot row never changes again) through distributed
+// shared memory, eliminates its own rows at positions > k with lin_solve_case's per-element
+// arithmetic, and posts its candidate for column k + 1. Back substitution runs on CTA 0,
+// reading each pivot row from its owner as lin_solve_case reads it (warp 0, lane-strided
+// sum, butterfly), while the other CTAs wait at the final barrier. CTA 0 then finishes the
+// solve. The result is bit-identical to lin_solve_case; all waits are cluster barriers.
+__device__ void lin_solve_cluster(const DevModel& m, const SolveSettings& st, const SolveBuffers& b, unsigned char* dyn) {
+    cg::cluster_group cl = cg::this_cluster();
+    const int C = static_cast<int>(cl.num_blocks()), rank = static_cast<int>(cl.block_rank());
+    const int N = m.N, W1 = N + 1, R = (N + C - 1) / C;
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    d3* vel = reinterpret_cast<d3*>(dyn);              // [N] (CTA 0)
+    d3* ind = vel + N;                                 // [N] (CTA 0)
+    double* gam = reinterpret_cast<double*>(ind + N);  // [N] (CTA 0)
+    double* prow = gam + N;                            // [N + 1] pivot row of the current column
+    int* at = reinterpret_cast<int*>(prow + W1);       // [N] physical row at each position
+    int* pos = at + N;                                 // [N] position of each physical row
+    double* A = reinterpret_cast<double*>(pos + N);    // [R][N + 1] rows rank, rank + C, ...
+    __shared__ double s_cand_v[2];
+    __shared__ int s_cand_p[2], s_piv;
+
+    // the candidate of this CTA for column k: first largest |A[r][k]| over its rows at
+    // positions >= k (lowest position among equal values), into slot k & 1
+    auto post_candidate = [&](int k) {
+        double bv = -1.0;
+        int bp = N;
+        for (int l = lane; l < R; l += 32) {
+            const int r = rank + l * C;
+            if (r >= N) break;
+            const int p = pos[r];
+            if (p < k) continue;
+            const double v = fabs(A[static_cast<long long>(l) * W1 + k]);
+            if (v > bv || (v == bv && p < bp)) {
+                bv = v;
+                bp = p;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            const int op = __shfl_xor_sync(0xffffffffu, bp, o);
+            if (ov > bv || (ov == bv && op < bp)) {
+                bv = ov;
+                bp = op;
+            }
+        }
+        if (lane == 0) {
+            s_cand_v[k & 1] = bv;
+            s_cand_p[k & 1] = bp;
+        }
+    };
+
+    for (int i = tid; i < N; i += nt) {
+        at[i] = i;
+        pos[i] = i;
     }
-    k_solve_lin<<<1, kLinThreads, smem, s>>>(m, st, b, static_cast<unsigned>(smem));
-    return cudaGetLastError();
+    for (int l = tid; l < R; l += nt) {
+        const int r = rank + l * C;
+        if (r < N) lin_build_row(m, b, r, A + static_cast<long long>(l) * W1);
+    }
+    __syncthreads();
+    if (warp == 0) post_candidate(0);
+    for (int k = 0; k < N; ++k) {
+        cl.sync();  // every CTA's candidate for column k is posted; column k of every row is final
+        if (tid == 0) {
+            double bv = -1.0;
+            int bp = N;
+            for (int q = 0; q < C; ++q) {
+                const double v = *cl.map_shared_rank(&s_cand_v[k & 1], q);
+                const int p = *cl.map_shared_rank(&s_cand_p[k & 1], q);
+                if (v > bv || (v == bv && p < bp)) {
+                    bv = v;
+                    bp = p;
+                }
+            }
+            const int mr = bp < N ? bp : k;  // position of the pivot row
+            const int rk = at[k], rm = at[mr];
+            at[k] = rm;
+            at[mr] = rk;
+            pos[rm] = k;
+            pos[rk] = mr;
+            s_piv = rm;
+        }
+        __syncthreads();
+        const int pr = s_piv;  // physical pivot row
+        {
+            const double* src = cl.map_shared_rank(A, pr % C) + static_cast<long long>(pr / C) * W1;
+            for (int j = k + tid; j <= N; j += nt) prow[j] = src[j];
+        }
+        __syncthreads();
+        const double piv = prow[k];
+        if (fabs(piv) < 1e-12) {  // the same value in every CTA: the whole cluster leaves
+            if (rank == 0 && tid == 0) {
+                atomicExch(b.err, kDevSingular);
+                b.scalars[3] = 1.0;
+            }
+            cl.sync();  // no CTA leaves while another may still read its rows
+            return;
+        }
+        for (int l = warp; l < R; l += nw) {
+            const int r = rank + l * C;
+            if (r >= N) break;
+            if (pos[r] <= k) continue;
+            double* Ai = A + static_cast<long long>(l) * W1;
+            const double f = Ai[k] / piv;
+            __syncwarp();  // every lane has read A[i][k] before lane 0 overwrites it
+            for (int j = k + lane; j <= N; j += 32) Ai[j] -= f * prow[j];
+        }
+        __syncthreads();
+        if (warp == 0 && k + 1 < N) post_candidate(k + 1);
+    }
+    cl.sync();  // every row is final
+    if (rank == 0) {
+        if (warp == 0) {
+            for (int i = N - 1; i >= 0; --i) {
+                const int r = at[i];
+                const double* Ai = cl.map_shared_rank(A, r % C) + static_cast<long long>(r / C) * W1;
+                double part = 0.0;
+                for (int j = i + 1 + lane; j < N; j += 32) part += Ai[j] * gam[j];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+                if (lane == 0) gam[i] = (Ai[N] - part) / Ai[i];
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+    }
+    cl.sync();  // CTA 0 has read every row it needs
+    if (rank == 0) lin_finish(m, st, b, vel, ind, gam);
 }
 
-cudaError_t launch_solve_linearized_jobs(const LinJob* jobs, int n, size_t smem, cudaStream_t s) {
-    if (n <= 0) return cudaSuccess;
-    if (smem > kLinSmemLimit) return cudaErrorInvalidValue;
-    if (smem > 48 * 1024) {
-        cudaError_t e =
-            cudaFuncSetAttribute(k_solve_lin_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        if (e != cudaSuccess) return e;
+__global__ void __launch_bounds__(kLinThreads) k_solve_lin_cluster(DevModel m, SolveSettings st, SolveBuffers b) {
+    extern __shared__ __align__(16) unsigned char lin_dyn[];
+    lin_solve_cluster(m, st, b, lin_dyn);
+}
+
+// Every case of a batch that needs a cluster of this launch's size: cluster i solves jobs[i].
+__global__ void __launch_bounds__(kLinThreads) k_solve_lin_cluster_jobs(const LinJob* jobs) {
+    extern __shared__ __align__(16) unsigned char lin_dyn[];
+    cg::cluster_group cl = cg::this_cluster();
+    const LinJob& j = jobs[blockIdx.x / cl.num_blocks()];
+    lin_solve_cluster(j.m, j.st, j.b, lin_dyn);
+}
+
+namespace {
+
+void cluster_config(cudaLaunchConfig_t& cfg, cudaLaunchAttribute& attr, int clusters, int C, size_t smem, cudaStream_t s) {
+    cfg = {};
+    cfg.gridDim = dim3(static_cast<unsigned>(clusters * C), 1, 1);
+    cfg.blockDim = dim3(kLinThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = static_cast<unsigned>(C);
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+}
+
+template <class K>
+cudaError_t prepare_cluster_kernel(K kernel, int C, size_t smem) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e == cudaSuccess && C > 8) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return e;
+}
+
+// Whether clusters of C CTAs with `smem` bytes of shared memory each can be resident on the
+// current device (cached per device and shape).
+bool cluster_fits(int C, size_t smem) {
+    static std::mutex mu;
+    static std::map<std::tuple<int, int, size_t>, bool> cache;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    std::lock_guard<std::mutex> lk(mu);
+    const auto key = std::make_tuple(dev, C, smem);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    bool ok = prepare_cluster_kernel(k_solve_lin_cluster, C, smem) == cudaSuccess &&
+              prepare_cluster_kernel(k_solve_lin_cluster_jobs, C, smem) == cudaSuccess;
+    if (ok) {
+        cudaLaunchConfig_t cfg;
+        cudaLaunchAttribute attr;
+        cluster_config(cfg, attr, 1, C, smem, nullptr);
+        int n = 0;
+        ok = cudaOccupancyMaxActiveClusters(&n, k_solve_lin_cluster, &cfg) == cudaSuccess && n > 0;
     }
-    k_solve_lin_jobs<<<n, kLinThreads, smem, s>>>(jobs, static_cast<unsigned>(smem));
-    return cudaGetLastError();
+    if (!ok) (void)cudaGetLastError();  // a refused shape is not an error of the caller
+    cache[key] = ok;
+    return ok;
+}
+
+}  // namespace
+
+LinPlan linearized_plan(int N) {
+    const size_t v = lin_vec_bytes(N), a = lin_mat_bytes(N);
+    if (v + a <= kLinSmemLimit) return {1, v + a};
+    for (int C = 2; C <= kLinMaxCluster; C *= 2) {
+        const size_t bytes = lin_cluster_bytes(N, C);
+        if (bytes <= kLinSmemLimit && cluster_fits(C, bytes)) return {C, bytes};
+    }
+    return {1, v};  // matrix in the case's global scratch
+}
+
+cudaError_t launch_solve_linearized(const DevModel& m, const SolveSettings& st, const SolveBuffers& b, cudaStream_t s) {
+    const LinPlan p = linearized_plan(m.N);
+    if (p.cluster == 1) {
+        if (p.smem > 48 * 1024) {
+            cudaError_t e =
+                cudaFuncSetAttribute(k_solve_lin, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(p.smem));
+            if (e != cudaSuccess) return e;
+        }
+        k_solve_lin<<<1, kLinThreads, p.smem, s>>>(m, st, b, static_cast<unsigned>(p.smem));
+        return cudaGetLastError();
+    }
+    cudaError_t e = prepare_cluster_kernel(k_solve_lin_cluster, p.cluster, p.smem);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute attr;
+    cluster_config(cfg, attr, 1, p.cluster, p.smem, s);
+    return cudaLaunchKernelEx(&cfg, k_solve_lin_cluster, m, st, b);
+}
+
+cudaError_t launch_solve_linearized_jobs(const LinJob* jobs, int n, const LinPlan& plan, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    if (plan.smem > kLinSmemLimit) return cudaErrorInvalidValue;
+    if (plan.cluster == 1) {
+        if (plan.smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(k_solve_lin_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 static_cast<int>(plan.smem));
+            if (e != cudaSuccess) return e;
+        }
+        k_solve_lin_jobs<<<n, kLinThreads, plan.smem, s>>>(jobs, static_cast<unsigned>(plan.smem));
+        return cudaGetLastError();
+    }
+    cudaError_t e = prepare_cluster_kernel(k_solve_lin_cluster_jobs, plan.cluster, plan.smem);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute attr;
+    cluster_config(cfg, attr, n, plan.cluster, plan.smem, s);
+    return cudaLaunchKernelEx(&cfg, k_solve_lin_cluster_jobs, jobs);
 }
 
 // ---------------------------------------------------------------------------------------

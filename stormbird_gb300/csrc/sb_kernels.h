@@ -161,12 +161,18 @@ struct LinJob {
     SolveSettings st;
     SolveBuffers b;
 };
-// Dynamic shared memory one linearized solve of N span lines uses: its vectors, plus its
-// matrix when that fits under kLinSmemLimit (else the matrix stays in SolveBuffers::lin_work).
+// How a linearized solve of N span lines runs. cluster == 1: one CTA, its matrix in shared
+// memory when matrix and vectors fit under kLinSmemLimit, else in SolveBuffers::lin_work;
+// cluster > 1: a thread-block cluster of that many CTAs with the rows spread over their
+// shared memory. smem = dynamic shared memory per CTA.
 constexpr size_t kLinSmemLimit = 227 * 1024 - 1024;
-size_t linearized_smem_bytes(int N);
-// n solves in one launch, each with `smem` bytes (the largest linearized_smem_bytes of the jobs).
-cudaError_t launch_solve_linearized_jobs(const LinJob* jobs, int n, size_t smem, cudaStream_t s);
+struct LinPlan {
+    int cluster = 1;
+    size_t smem = 0;
+};
+LinPlan linearized_plan(int N);
+// n solves of one plan shape in one launch (smem: the largest of the jobs' plans).
+cudaError_t launch_solve_linearized_jobs(const LinJob* jobs, int n, const LinPlan& plan, cudaStream_t s);
 
 struct ForceArgs {
     const double* gamma = nullptr;  // [N]

@@ -198,13 +198,14 @@ def test_batched_linearized_quasi_steady_sweep(gpu_lib, oracle_mod):
     """An angle sweep of quasi-steady cases with the Linearized solver: the batch solves them
     in one launch (a CTA per case) and every case gives what its own Simulation gives
     (bit-identical: the same device function) and what the oracle gives (1e-9, the tolerance
-    of the single-case Linearized test). Sizes 8 to 180 span lines: the largest system keeps
-    its matrix in global memory, the others in shared memory."""
+    of the single-case Linearized test). Sizes 8 to 600 span lines: up to 164 the matrix sits
+    in one CTA's shared memory; 180, 400 and 600 are spread over clusters of 2, 8 and 16 CTAs
+    (one launch per cluster size)."""
     import math
 
     from stormbird_gb300 import Batch, Simulation
 
-    sizes = [8, 24, 64, 180, 31, 100]
+    sizes = [8, 24, 64, 180, 31, 100, 400, 600]
     cases, winds = [], []
     for k, n in enumerate(sizes):
         cases.append(S.simulation(S.rectangular_wing(5.0, 1.2, math.radians(2.0 + k), n), dynamic=False))
