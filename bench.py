@@ -485,6 +485,25 @@ def qs_sweep(args, device):
         if k >= warm:
             t_plain += time.perf_counter() - t0
     g_plain = np.concatenate([r.circulation_strength for r in rs])
+    # the largest case alone: its Linearized solve (Gaussian elimination, 2N^3/3 FLOP in f64)
+    # timed with CUDA events on the library's stream, against the measured FP64 peak
+    from stormbird_gb300.simulation import measure_fp64_peak
+
+    ib = max(range(n), key=lambda i: sims[i].nr_span_lines)
+    big, (_, ub) = sims[ib], cases[ib]
+    big.enable_timing(True)
+    solve_ms = []
+    for k in range(5):
+        big.do_step(time=0.0, time_step=0.1, freestream_velocity=np.tile(ub * (1.0 + 0.01 * k), (big.nr_freestream_points, 1)))
+        solve_ms.append(big.last_step_timing()["solve"])
+    nb = big.nr_span_lines
+    ge_flop = 2.0 * nb ** 3 / 3.0
+    fp64 = measure_fp64_peak(device, 3)
+    largest = {"span_lines": nb, "solve_ms": min(solve_ms),
+               "elimination_gflops": ge_flop / (min(solve_ms) * 1e-3) / 1e9, "fp64_peak_tflops": fp64,
+               "frac_of_fp64_peak": ge_flop / (min(solve_ms) * 1e-3) / (fp64 * 1e12) if fp64 > 0 else None,
+               "note": "solve phase = matrix elimination, back substitution and the Linearized epilogue; "
+                       "FLOP counts the elimination only"}
     for s in sims:
         s.close()
     del sims
@@ -506,6 +525,7 @@ def qs_sweep(args, device):
             "solves_per_s": {"plain": n * steps / t_plain, "batched": n * steps / t_batch},
             "speedup_vs_plain": t_plain / t_batch,
             "bit_identical_to_plain": bool(np.array_equal(g, g_plain)),
+            "largest_case": largest,
             "graph": info.get("graph"),
             "timing": "host clock around each public call, host freestream in, circulation and force summary out"}
 

@@ -400,15 +400,19 @@ __device__ void lin_finish(const DevModel& m, const SolveSettings& st, const Sol
         for (int i = tid; i < N; i += nt) vel[i] = total_velocity(st, m.felt_ctrl[i], ind[i]);
         __syncthreads();
     }
-    // residual (linearized.rs:204-213), summed in control-point order
+    // residual (linearized.rs:204-213): the terms in parallel (into the induced-velocity
+    // storage, no longer needed), summed in control-point order by one thread
+    double* terms = reinterpret_cast<double*>(ind);
+    for (int i = tid; i < N; i += nt) {
+        RowGeom g = row_geom(m, i);
+        const FoilP f = m.foils[g.wing];
+        double aoa = len(vel[i]) > kMinPositive ? signed_angle_between(g.chord, vel[i], g.span_dir) : 0.0;
+        terms[i] = residual_term(m, g, f, gam[i], vel[i], aoa);
+    }
+    __syncthreads();
     if (tid == 0) {
         double s = 0.0;
-        for (int i = 0; i < N; ++i) {
-            RowGeom g = row_geom(m, i);
-            const FoilP f = m.foils[g.wing];
-            double aoa = len(vel[i]) > kMinPositive ? signed_angle_between(g.chord, vel[i], g.span_dir) : 0.0;
-            s += residual_term(m, g, f, gam[i], vel[i], aoa);
-        }
+        for (int i = 0; i < N; ++i) s += terms[i];
         b.scalars[0] = s / static_cast<double>(N);
         b.scalars[1] = 1.0;
         b.scalars[2] = 1.0;
@@ -526,7 +530,8 @@ __global__ void __launch_bounds__(kLinThreads) k_solve_lin_jobs(const LinJob* jo
 // cluster barrier: each CTA's warp 0 has put its candidate for column k (the rows at
 // positions >= k: largest |A[r][k]|, then lowest position, i.e. the reference's first
 // largest row after its swaps) into a double-buffered slot; after the barrier every CTA
-// reduces the C candidates in rank order, applies the same exchange to its permutation,
+// reduces the C candidates (one per lane, the same butterfly), applies the same exchange
+// to its permutation,
 // copies the pivot row (columns k..N; a pivot row never changes again) through distributed
 // shared memory, eliminates its own rows at positions > k with lin_solve_case's per-element
 // arithmetic, and posts its candidate for column k + 1. Back substitution runs on CTA 0,
@@ -591,24 +596,31 @@ __device__ void lin_solve_cluster(const DevModel& m, const SolveSettings& st, co
     if (warp == 0) post_candidate(0);
     for (int k = 0; k < N; ++k) {
         cl.sync();  // every CTA's candidate for column k is posted; column k of every row is final
-        if (tid == 0) {
+        if (warp == 0) {  // lane q reads CTA q's candidate; the same butterfly as post_candidate
             double bv = -1.0;
             int bp = N;
-            for (int q = 0; q < C; ++q) {
-                const double v = *cl.map_shared_rank(&s_cand_v[k & 1], q);
-                const int p = *cl.map_shared_rank(&s_cand_p[k & 1], q);
-                if (v > bv || (v == bv && p < bp)) {
-                    bv = v;
-                    bp = p;
+            if (lane < C) {
+                bv = *cl.map_shared_rank(&s_cand_v[k & 1], lane);
+                bp = *cl.map_shared_rank(&s_cand_p[k & 1], lane);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+                const int op = __shfl_xor_sync(0xffffffffu, bp, o);
+                if (ov > bv || (ov == bv && op < bp)) {
+                    bv = ov;
+                    bp = op;
                 }
             }
-            const int mr = bp < N ? bp : k;  // position of the pivot row
-            const int rk = at[k], rm = at[mr];
-            at[k] = rm;
-            at[mr] = rk;
-            pos[rm] = k;
-            pos[rk] = mr;
-            s_piv = rm;
+            if (lane == 0) {  // the cluster's first largest row: apply the exchange
+                const int mr = bp < N ? bp : k;  // position of the pivot row
+                const int rk = at[k], rm = at[mr];
+                at[k] = rm;
+                at[mr] = rk;
+                pos[rm] = k;
+                pos[rk] = mr;
+                s_piv = rm;
+            }
         }
         __syncthreads();
         const int pr = s_piv;  // physical pivot row
