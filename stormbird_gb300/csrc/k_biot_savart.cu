@@ -115,6 +115,14 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __
 __device__ __forceinline__ float2 sel2(bool cx, float2 a, bool cy, float2 b) {
     return make_float2(cx ? a.x : b.x, cy ? a.y : b.y);
 }
+// The hardware reciprocal square root (PTX rsqrt.approx.ftz.f32). Every argument below is
+// first clamped to a normal float, where this is the same approximation rsqrtf returns,
+// without the handling of subnormal arguments around it.
+__device__ __forceinline__ float rsqrt_n(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 
 // Vortex ring of one FP32 panel record at two targets (the two lanes of the float2s), given
 // e = x - centre (float-float difference). r_k = e - o_k. Per segment, with c = d x r1 = r1 x r2:
@@ -133,7 +141,7 @@ __device__ __forceinline__ void corner2(float2 ex, float2 ey, float2 ez, const f
     rz = sub2s(ez, o[2]);
     rs = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
     // r = 0 (target on a corner) gives l = 0; the clamp runs on the ALU pipe
-    rl = mul2(rs, make_float2(rsqrtf(fmaxf(rs.x, 1e-30f)), rsqrtf(fmaxf(rs.y, 1e-30f))));
+    rl = mul2(rs, make_float2(rsqrt_n(fmaxf(rs.x, 1e-30f)), rsqrt_n(fmaxf(rs.y, 1e-30f))));
 }
 
 // One segment from corner 1 (r1) to corner 2 (r2 = r1 - d): s * c with c = d x r1, i.e.
@@ -167,7 +175,7 @@ __device__ __forceinline__ void segment2(float2 rx, float2 ry, float2 rz, float2
     const float2 X = mul2(mul2(Bx, Bx), fma2(d2, d2, bc(rc4)));
     const float2 Aw = WEIGHTED ? mul2(Ax, bc(g)) : Ax;
     const float2 s0 = mul2(mul2(mul2(d2, add2(rl1, rl2)), Aw),
-                           make_float2(rsqrtf(fmaxf(X.x, 1e-37f)), rsqrtf(fmaxf(X.y, 1e-37f))));
+                           make_float2(rsqrt_n(fmaxf(X.x, 1e-37f)), rsqrt_n(fmaxf(X.y, 1e-37f))));
     const float2 lim = mul2(Ax, bc(1.0e-10f));
     const float2 sg = make_float2(Bx.x > lim.x ? s0.x : 0.f, Bx.y > lim.y ? s0.y : 0.f);
     ax = fma2(sg, cx, ax);
