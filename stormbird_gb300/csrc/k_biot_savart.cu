@@ -19,6 +19,7 @@
 // k_unit_matrix: the unit-strength influence of the first-row panels at the control
 // points (frozen_wake.rs:198-249), in FP64: the control point lies on its own bound
 // vortex, where the reference's 1e-10 closeness cut-off must fire exactly as in f64.
+#include <cfloat>
 #include <cstdio>
 #include <math_constants.h>
 
@@ -371,7 +372,8 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
                     const bool any_far = __any_sync(0xffffffffu, (a0 && !n0) || (a1 && !n1));
                     if (any_far) {  // point doublet (panel.rs:82-96)
                         const float2 e2s = make_float2(n0 ? 1.f : e2.x, n1 ? 1.f : e2.y);
-                        const float2 ir = make_float2(rsqrtf(e2s.x), rsqrtf(e2s.y));
+                        // a subnormal |e|^2 (a degenerate panel) overflows s to inf either way
+                        const float2 ir = make_float2(rsqrt_n(fmaxf(e2s.x, FLT_MIN)), rsqrt_n(fmaxf(e2s.y, FLT_MIN)));
                         const float2 ir2 = mul2(ir, ir);
                         const float at = v[35] * gam;
                         const float2 sm = make_float2((a0 && !n0) ? at : 0.f, (a1 && !n1) ? at : 0.f);
