@@ -212,7 +212,10 @@ int sb_sim_do_step_wind(sb_sim* sim, double time, double time_step, double ship_
  * result_history_from_file reads, simulation.rs:37-45), closed when the writer is replaced
  * or the handle freed; SB_RESULTS_CSV appends one reduced row per step, with the header first
  * when the file is new (io_utils/csv_data.rs:11-33). NULL or SB_RESULTS_OFF stops writing.
- * sb_sim_flush_results waits until every queued step is written.
+ * sb_sim_flush_results waits until every queued step is written, including the wake files
+ * a dynamic setup asks for with write_wake_data_to_file (one VTK PolyData file
+ * `{wake_files_folder_path}/wake_{time / time_step}.vtp` per step, as
+ * lifting_line/wake/dynamic_wake/export.rs:75-163 writes it, also on a background thread).
  */
 #define SB_RESULTS_OFF 0
 #define SB_RESULTS_JSON_HISTORY 1

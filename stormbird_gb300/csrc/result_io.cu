@@ -262,4 +262,117 @@ void ResultWriter::run() {
     }
 }
 
+// export.rs:75-163: the same elements, attributes, tab indentation and order; numbers in
+// Rust's Display format.
+std::string wake_vtp(const WakeRecord& w) {
+    const long long n_pts = static_cast<long long>(w.W + 1) * w.Np, n_faces = static_cast<long long>(w.W) * w.N;
+    std::string s;
+    s.reserve(static_cast<size_t>(n_pts) * 72 + static_cast<size_t>(n_faces) * 96 + 1024);
+    s += "<?xml version=\"1.0\"?>\n";
+    s += "<VTKFile type=\"PolyData\" version=\"0.1\" byte_order=\"LittleEndian\">\n";
+    s += "\t<PolyData>\n";
+    s += "\t\t<Piece NumberOfPoints=\"" + std::to_string(n_pts) +
+         "\" NumberOfVerts=\"0\" NumberOfLines=\"0\" NumberOfStrips=\"0\" NumberOfPolys=\"" + std::to_string(n_faces) +
+         "\">\n";
+    s += "\t\t\t<Points>\n";
+    s += "\t\t\t\t<DataArray type=\"Float32\" NumberOfComponents=\"3\" format=\"ascii\">\n";
+    for (long long i = 0; i < n_pts; ++i) {
+        s += "\t\t\t\t\t";
+        display_num(s, w.pts[3 * i]);
+        s += ' ';
+        display_num(s, w.pts[3 * i + 1]);
+        s += ' ';
+        display_num(s, w.pts[3 * i + 2]);
+        s += '\n';
+    }
+    s += "\t\t\t\t</DataArray>\n";
+    s += "\t\t\t</Points>\n";
+    s += "\t\t\t<Polys>\n";
+    s += "\t\t\t\t<DataArray type=\"Int32\" Name=\"connectivity\" format=\"ascii\">\n";
+    // panel_point_indices (dynamic_wake/mod.rs:82-91): point (row, j + wing) of each corner
+    for (long long f = 0; f < n_faces; ++f) {
+        const long long row = f / w.N;
+        const int j = static_cast<int>(f % w.N);
+        const long long c = j + w.wing_of_line[j];
+        const long long a = row * w.Np + c, b = (row + 1) * w.Np + c;
+        s += "\t\t\t\t\t" + std::to_string(a) + " " + std::to_string(a + 1) + " " + std::to_string(b + 1) + " " +
+             std::to_string(b) + "\n";
+    }
+    s += "\t\t\t\t</DataArray>\n";
+    s += "\t\t\t\t<DataArray type=\"Int32\" Name=\"offsets\" format=\"ascii\">\n";
+    for (long long f = 0; f < n_faces; ++f) s += "\t\t\t\t\t" + std::to_string((f + 1) * 4) + "\n";
+    s += "\t\t\t\t</DataArray>\n";
+    s += "\t\t\t</Polys>\n";
+    s += "\t\t\t<CellData Scalars=\"strength\">\n";
+    const char* names[2] = {"strength", "viscous_core_length"};
+    const std::vector<double>* vals[2] = {&w.str, &w.core};
+    for (int a = 0; a < 2; ++a) {
+        s += "\t\t\t\t<DataArray type=\"Float32\" Name=\"";
+        s += names[a];
+        s += "\" format=\"ascii\">\n";
+        for (long long f = 0; f < n_faces; ++f) {
+            s += "\t\t\t\t\t";
+            display_num(s, (*vals[a])[f]);
+            s += '\n';
+        }
+        s += "\t\t\t\t</DataArray>\n";
+    }
+    s += "\t\t\t</CellData>\n";
+    s += "\t\t</Piece>\n";
+    s += "\t</PolyData>\n";
+    s += "</VTKFile>\n";
+    return s;
+}
+
+WakeFileWriter::WakeFileWriter() { thread_ = std::thread([this] { run(); }); }
+
+WakeFileWriter::~WakeFileWriter() {
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        stop_ = true;
+    }
+    cv_.notify_all();
+    if (thread_.joinable()) thread_.join();
+}
+
+void WakeFileWriter::push(WakeRecord&& w) {
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        queue_.push_back(std::move(w));
+        ++pushed_;
+    }
+    cv_.notify_one();
+}
+
+bool WakeFileWriter::flush() {
+    std::unique_lock<std::mutex> lk(mu_);
+    done_cv_.wait(lk, [this] { return written_ == pushed_; });
+    return !failed_;
+}
+
+void WakeFileWriter::run() {
+    for (;;) {
+        WakeRecord w;
+        {
+            std::unique_lock<std::mutex> lk(mu_);
+            cv_.wait(lk, [this] { return stop_ || !queue_.empty(); });
+            if (queue_.empty()) return;
+            w = std::move(queue_.front());
+            queue_.pop_front();
+        }
+        const std::string text = wake_vtp(w);
+        bool ok = false;
+        if (std::FILE* f = std::fopen(w.path.c_str(), "wb")) {
+            ok = std::fwrite(text.data(), 1, text.size(), f) == text.size();
+            ok = std::fclose(f) == 0 && ok;
+        }
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            failed_ = failed_ || !ok;
+            ++written_;
+        }
+        done_cv_.notify_all();
+    }
+}
+
 }  // namespace sbhost

@@ -61,4 +61,35 @@ private:
     std::thread thread_;
 };
 
+// One step's dynamic wake for the VTK PolyData file the reference writes
+// (lifting_line/wake/dynamic_wake/export.rs:75-163): points (streamwise-major rows of Np),
+// quadrilateral panels (row-major, N per row) with their strength and viscous core length.
+struct WakeRecord {
+    std::string path;
+    int N = 0, Np = 0, W = 0;
+    std::vector<int> wing_of_line;  // [N]
+    std::vector<double> pts;        // [(W + 1) Np][3]
+    std::vector<double> str;        // [W N]
+    std::vector<double> core;       // [W N]
+};
+std::string wake_vtp(const WakeRecord& w);
+
+// Writes wake files on its own thread, one file per record, in push order.
+class WakeFileWriter {
+public:
+    WakeFileWriter();
+    ~WakeFileWriter();  // writes what is queued, joins the thread
+    void push(WakeRecord&& w);
+    bool flush();  // false after a write error
+
+private:
+    void run();
+    bool failed_ = false, stop_ = false;
+    size_t pushed_ = 0, written_ = 0;
+    std::deque<WakeRecord> queue_;
+    std::mutex mu_;
+    std::condition_variable cv_, done_cv_;
+    std::thread thread_;
+};
+
 }  // namespace sbhost

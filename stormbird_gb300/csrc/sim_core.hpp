@@ -414,6 +414,7 @@ struct sb_sim {
         span_s_local.upload(ss); span_e_local.upload(se); chord_nr.upload(cn);
         chord_len.upload(cl); span_len_local.upload(sl);
         wing_of_line.upload(wol); wing_start.upload(ws); wing_end.upload(we);
+        wing_of_line_h = wol;
         is_virtual.upload(virt); foils.upload(fo);
         sp_line.upload(spl); sp_end.upload(spe); sp_a.upload(spa); sp_b.upload(spb);
 
@@ -545,6 +546,7 @@ struct sb_sim {
             }
         }
         panel_core.upload(core);
+        panel_core_h = core;
         dm.panel_core = panel_core.p;
         setup_chains(core);
         d3 sum = mk(0, 0, 0);
@@ -916,6 +918,34 @@ struct sb_sim {
         }
         check_device_status();
         if (writer) writer->push(result_record());
+        if (dynamic && setup.dynamic_wake.write_wake_data_to_file) push_wake_file();
+    }
+
+    // The wake after the step as a VTK file `{wake_files_folder_path}/wake_{time / dt}.vtp`
+    // (Simulation::do_step, simulation.rs:183-185; export.rs:11-23, 75-163), written on a
+    // background thread.
+    std::unique_ptr<sbhost::WakeFileWriter> wake_writer;
+    std::vector<int> wing_of_line_h;
+    std::vector<double> panel_core_h;
+
+    void push_wake_file() {
+        if (!wake_writer) wake_writer.reset(new sbhost::WakeFileWriter());
+        sbhost::WakeRecord w;
+        const double q = params.dt != 0.0 ? params.time / params.dt : 0.0;
+        const unsigned long long index = q > 0.0 ? static_cast<unsigned long long>(q) : 0ull;  // `as usize`
+        w.path = setup.dynamic_wake.wake_files_folder_path + "/wake_" + std::to_string(index) + ".vtp";
+        w.N = N;
+        w.Np = Np;
+        w.W = W;
+        w.wing_of_line = wing_of_line_h;
+        w.pts.resize(static_cast<size_t>(P_pts) * 3);
+        w.str.resize(static_cast<size_t>(P_pan));
+        ck(cudaMemcpyAsync(w.pts.data(), pts[cur].p, P_pts * sizeof(d3), cudaMemcpyDeviceToHost, stream), "D2H wake points");
+        ck(cudaMemcpyAsync(w.str.data(), str[cur].p, P_pan * sizeof(double), cudaMemcpyDeviceToHost, stream),
+           "D2H wake strengths");
+        ck(cudaStreamSynchronize(stream), "wake file");
+        w.core = panel_core_h;
+        wake_writer->push(std::move(w));
     }
 
     // ---------------------------------------------------------------- result output

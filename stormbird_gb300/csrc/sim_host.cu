@@ -243,6 +243,7 @@ int sb_sim_flush_results(sb_sim* sim) {
     if (!sim) { g_last_error = "null handle"; return SB_ERR_NULL_ARG; }
     return guard([&] {
         if (sim->writer && !sim->writer->flush()) raise(SB_ERR_STATE, "writing the result file failed");
+        if (sim->wake_writer && !sim->wake_writer->flush()) raise(SB_ERR_STATE, "writing a wake file failed");
     });
 }
 

@@ -93,3 +93,46 @@ def test_csv_rows_and_append(gpu_lib, tmp_path):
     sim2.write_results_to(None)
     lines2 = path.read_text().splitlines()
     assert len(lines2) == len(lines) + 2 and lines2[:len(lines)] == lines
+
+
+def test_wake_vtk_files(gpu_lib, tmp_path):
+    """A dynamic setup with write_wake_data_to_file writes, per step, the VTK PolyData file of
+    lifting_line/wake/dynamic_wake/export.rs:75-163 to {folder}/wake_{time / dt as integer}.vtp:
+    the wake's points and strengths as sb_sim_get_wake_state gives them (exact: shortest
+    round-trip numbers), the panels' corner indices (dynamic_wake/mod.rs:82-91), offsets and
+    the viscous core length of every panel."""
+    import xml.etree.ElementTree as ET
+
+    from stormbird_gb300 import Simulation
+
+    sails, panels, rows, dt = 2, 6, 12, 0.05
+    d = json.loads(S.wing_sail_row(sails, panels, rows, time_step=dt))
+    wake = d["simulation_settings"]["Dynamic"]["wake"]
+    wake["write_wake_data_to_file"] = True
+    wake["wake_files_folder_path"] = str(tmp_path)
+    sim = Simulation(json.dumps(d))
+    wind = S.GustyWind(seed=9)
+    N, Np = sails * panels, sails * (panels + 1)
+    for k in range(4):
+        t = dt * k
+        sim.do_step(time=t, time_step=dt, freestream_velocity=wind.freestream(t, sim.nr_freestream_points))
+        sim.flush_results()
+        path = tmp_path / f"wake_{int(t / dt)}.vtp"
+        root = ET.parse(path).getroot()
+        piece = root.find("PolyData/Piece")
+        assert piece.get("NumberOfPoints") == str(Np * (rows + 1)) and piece.get("NumberOfPolys") == str(N * rows)
+        arrays = {a.get("Name"): a for a in root.iter("DataArray")}
+        pts_file = np.array(piece.find("Points/DataArray").text.split(), dtype=float).reshape(-1, 3)
+        pts, strengths, _ = sim.wake_state()
+        assert np.array_equal(pts_file, pts)
+        assert np.array_equal(np.array(arrays["strength"].text.split(), dtype=float), strengths)
+        assert np.all(np.array(arrays["viscous_core_length"].text.split(), dtype=float) == 0.1 * S.CHORD)
+        conn = np.array(arrays["connectivity"].text.split(), dtype=int).reshape(-1, 4)
+        want = []
+        for s_ in range(rows):
+            for j in range(N):
+                c = j + j // panels  # span index + wing index
+                want.append([s_ * Np + c, s_ * Np + c + 1, (s_ + 1) * Np + c + 1, (s_ + 1) * Np + c])
+        assert np.array_equal(conn, np.array(want))
+        offs = np.array(arrays["offsets"].text.split(), dtype=int)
+        assert np.array_equal(offs, 4 * np.arange(1, N * rows + 1))
