@@ -108,10 +108,25 @@ struct sb_batch {
     struct LinGroup {
         LinPlan plan;
         int n = 0;
-        DevBuf<LinJob> jobs;
+        DevBuf<SolveJob> jobs;
     };
     static constexpr int kLinGroups = 5;
     LinGroup lin_groups[kLinGroups];
+    // SimpleIterative solves: one launch per cluster size (1, 4, 8 CTAs, solve_cluster_size),
+    // a cluster per case; the job list is refilled every step from pinned memory, since it
+    // names the wake buffer of the step's parity
+    struct SiGroup {
+        int cluster = 0;
+        size_t smem = 0;
+        std::vector<int> cases;
+        long long off = 0;
+    };
+    static constexpr int kSiGroups = 3;
+    SiGroup si_groups[kSiGroups];
+    long long si_entries = 0;
+    std::vector<char> si_batched;  // per case: its solve runs in a k_solve_si_jobs launch
+    PinnedBuf<SolveJob> h_si_jobs;
+    DevBuf<SolveJob> d_si_jobs;
 
     // Sweep work lists: group = (sweep kind, symmetry, neglect); one launch each.
     struct Group {
@@ -248,7 +263,7 @@ struct sb_batch {
             gj.push_back(g);
         }
         gather_jobs.upload(gj);
-        std::vector<LinJob> lj[kLinGroups];
+        std::vector<SolveJob> lj[kLinGroups];
         for (size_t i = 0; i < cases.size(); ++i)
             if (cases[i]->linearized_quasi_steady()) {
                 const LinPlan p = linearized_plan(cases[i]->N);
@@ -261,6 +276,26 @@ struct sb_batch {
         for (int g = 0; g < kLinGroups; ++g) {
             lin_groups[g].n = static_cast<int>(lj[g].size());
             if (!lj[g].empty()) lin_groups[g].jobs.upload(lj[g]);
+        }
+        si_batched.assign(cases.size(), 0);
+        for (size_t i = 0; i < cases.size(); ++i) {
+            const sb_sim& c = *cases[i];
+            if (c.solver_kind != 0 || c.solve.start_with_linearized) continue;
+            const int CS = solve_cluster_size(c.N);
+            if ((c.N + CS - 1) / CS > 1024) continue;  // too many rows per CTA: the single path reports it
+            const int g = CS == 1 ? 0 : (CS == 4 ? 1 : 2);
+            si_groups[g].cluster = CS;
+            si_groups[g].smem = std::max(si_groups[g].smem, si_smem_bytes(c.N));
+            si_groups[g].cases.push_back(static_cast<int>(i));
+            si_batched[i] = 1;
+        }
+        for (auto& g : si_groups) {
+            g.off = si_entries;
+            si_entries += static_cast<long long>(g.cases.size());
+        }
+        if (si_entries > 0) {
+            h_si_jobs.alloc(si_entries);
+            d_si_jobs.alloc(si_entries);
         }
         counters.alloc(16);
         err.alloc(1);
@@ -474,6 +509,9 @@ struct sb_batch {
     void enqueue(double time, double dt, bool wind) {
         if (job_entries > 0)
             ck(cudaMemcpyAsync(d_jobs.p, h_jobs.p, job_entries * sizeof(BsJob), cudaMemcpyHostToDevice, main), "H2D jobs");
+        if (si_entries > 0)
+            ck(cudaMemcpyAsync(d_si_jobs.p, h_si_jobs.p, si_entries * sizeof(SolveJob), cudaMemcpyHostToDevice, main),
+               "H2D solve jobs");
         if (wind)
             ck(cudaMemcpyAsync(wind_steps.p, h_wind_steps.p, cases.size() * 2 * sizeof(double), cudaMemcpyHostToDevice, main),
                "H2D wind steps");
@@ -487,23 +525,38 @@ struct sb_batch {
         sweeps(0);
         for (auto& c : cases) if (c->dynamic) c->after_fixed_sweep();
         fork(1);
-        for (auto& c : cases) {
-            if (c->linearized_quasi_steady()) c->step_matrix();
-            else c->step_matrix_and_solve();
+        for (size_t i = 0; i < cases.size(); ++i) {
+            sb_sim& c = *cases[i];
+            if (c.linearized_quasi_steady() || si_batched[i]) c.step_matrix();
+            else c.step_matrix_and_solve();
         }
         join(1);
-        // the plan groups run side by side on the pool streams
-        int lin_used = 0;
-        for (const auto& g : lin_groups) lin_used += g.n > 0 ? 1 : 0;
-        if (lin_used == 1) {
+        // the batched solves: a launch per Linearized plan shape and per SimpleIterative
+        // cluster size, side by side on the pool streams
+        int n_launch = 0;
+        for (const auto& g : lin_groups) n_launch += g.n > 0 ? 1 : 0;
+        for (const auto& g : si_groups) n_launch += g.cases.empty() ? 0 : 1;
+        if (n_launch > 0) {
+            if (n_launch > 1) fork(1);
+            int k = 0;
             for (const auto& g : lin_groups)
-                if (g.n > 0) ck(launch_solve_linearized_jobs(g.jobs.p, g.n, g.plan, main), "batched linearized solve");
-        } else if (lin_used > 1) {
-            fork(1);
-            for (int gi = 0; gi < kLinGroups; ++gi)
-                if (lin_groups[gi].n > 0)
-                    ck(launch_solve_linearized_jobs(lin_groups[gi].jobs.p, lin_groups[gi].n, lin_groups[gi].plan, pool[gi]),
+                if (g.n > 0)
+                    ck(launch_solve_linearized_jobs(g.jobs.p, g.n, g.plan, n_launch > 1 ? pool[k++] : main),
                        "batched linearized solve");
+            for (const auto& g : si_groups)
+                if (!g.cases.empty())
+                    ck(launch_solve_simple_iterative_jobs(d_si_jobs.p + g.off, static_cast<int>(g.cases.size()), g.cluster,
+                                                          g.smem, n_launch > 1 ? pool[k++] : main),
+                       "batched simple iterative solve");
+            if (n_launch > 1) join(1);
+        }
+        // what follows a solve in its case (chain records of the wake), after the batched solves
+        bool after = false;
+        for (size_t i = 0; i < cases.size(); ++i) after = after || si_batched[i];
+        if (after) {
+            fork(1);
+            for (size_t i = 0; i < cases.size(); ++i)
+                if (si_batched[i]) cases[i]->step_after_solve();
             join(1);
         }
         if (warm_mode != 0)
@@ -696,7 +749,21 @@ struct sb_batch {
     void fill_jobs_after_begin() {
         for (auto& c : cases) if (c->dynamic) c->cur ^= 1;
         fill_jobs();
+        fill_si_jobs();
         for (auto& c : cases) if (c->dynamic) c->cur ^= 1;
+    }
+
+    // The SimpleIterative jobs of the step (each case's model, settings and buffers, with the
+    // wake buffer its solve writes row 0 into).
+    void fill_si_jobs() {
+        for (const auto& g : si_groups)
+            for (size_t k = 0; k < g.cases.size(); ++k) {
+                const sb_sim& c = *cases[g.cases[k]];
+                SolveJob& j = h_si_jobs.p[g.off + static_cast<long long>(k)];
+                j.m = c.dm;
+                j.st = c.solve;
+                j.b = c.solve_buffers();
+            }
     }
 
     void do_step(double time, double dt, const double* fs_host, size_t n) {

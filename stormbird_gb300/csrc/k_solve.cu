@@ -93,7 +93,9 @@ __device__ inline double residual_term(const DevModel& m, const RowGeom& g, cons
     return fabs(clg - foil_cl_pre_stall(f, aoa));
 }
 
-__global__ void __launch_bounds__(kSolveThreads) k_solve_si(DevModel m, SolveSettings st, SolveBuffers b) {
+// SimpleIterative::solve for one case on the calling thread-block cluster (see the top of
+// the file). Run by k_solve_si (one case) and k_solve_si_jobs (a cluster per case of a batch).
+__device__ void si_solve(const DevModel& m, const SolveSettings& st, const SolveBuffers& b) {
     cg::cluster_group cl = cg::this_cluster();
     const int CS = static_cast<int>(cl.num_blocks());
     const int rank = static_cast<int>(cl.block_rank());
@@ -171,10 +173,12 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve_si(DevModel m, SolveSet
     };
 
     // Guarded warm start: residual (simple_iterative.rs:160-176) of the plain start G[0]
-    // and of each candidate (staged in G[1]); the lowest finite one becomes the initial
-    // solution (the plain start wins ties).
+    // and of each candidate (staged in G[1]). A candidate replaces the current start only
+    // when both its mean residual (the solver's own measure) and its largest per-line term
+    // are lower: the solver stops on the mean, which a start with its error on a few lines
+    // could pass while those lines are still off. The plain start wins ties.
     if (b.candidate[0] || b.candidate[1]) {
-        double best = 0.0;
+        double best = 0.0, best_max = 0.0;
         int taken = 0;
         for (int v = 0; v < 3; ++v) {
             const double* src = v == 0 ? nullptr : b.candidate[v - 1];
@@ -197,16 +201,22 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve_si(DevModel m, SolveSet
             }
             cl.sync();
             if (tid == 0) {
-                double s = 0.0;
-                for (int i = 0; i < N; ++i) s += RR[0][i];
+                double s = 0.0, mx = 0.0;
+                for (int i = 0; i < N; ++i) {
+                    s += RR[0][i];
+                    mx = fmax(mx, RR[0][i]);
+                }
                 s_res = s;
+                s_red[0] = mx;
             }
             __syncthreads();
-            const double rv = s_res;
+            const double rv = s_res, rmax = s_red[0];
             if (v == 0) {
                 best = rv;
-            } else if (isfinite(rv) && rv < best) {  // same decision in every CTA
+                best_max = rmax;
+            } else if (isfinite(rv) && rv < best && rmax < best_max) {  // same decision in every CTA
                 best = rv;
+                best_max = rmax;
                 taken = v;
                 for (int i = tid; i < N; i += kSolveThreads) G[0][i] = G[1][i];
             }
@@ -293,11 +303,51 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve_si(DevModel m, SolveSet
     cl.sync();  // no CTA leaves while others may still write into its shared memory
 }
 
+__global__ void __launch_bounds__(kSolveThreads) k_solve_si(DevModel m, SolveSettings st, SolveBuffers b) {
+    si_solve(m, st, b);
+}
+
+// Every case of a batch whose cluster size is this launch's: cluster i solves jobs[i].
+__global__ void __launch_bounds__(kSolveThreads) k_solve_si_jobs(const SolveJob* jobs) {
+    cg::cluster_group cl = cg::this_cluster();
+    const SolveJob& j = jobs[blockIdx.x / cl.num_blocks()];
+    si_solve(j.m, j.st, j.b);
+}
+
+size_t si_smem_bytes(int N) {
+    const int CS = solve_cluster_size(N);
+    const int rp = (N + CS - 1) / CS;
+    return (4 * static_cast<size_t>(N) + 2 * kMaxCluster) * sizeof(double) + static_cast<size_t>(rp) * sizeof(d3);
+}
+
+cudaError_t launch_solve_simple_iterative_jobs(const SolveJob* jobs, int n, int cluster, size_t smem, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    if (cluster != 1 && cluster != 4 && cluster != 8) return cudaErrorInvalidValue;
+    if (smem > 48 * 1024) {
+        cudaError_t e =
+            cudaFuncSetAttribute(k_solve_si_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(static_cast<unsigned>(n * cluster), 1, 1);
+    cfg.blockDim = dim3(kSolveThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = static_cast<unsigned>(cluster);
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_solve_si_jobs, jobs);
+}
+
 cudaError_t launch_solve_simple_iterative(const DevModel& m, const SolveSettings& st, const SolveBuffers& b, cudaStream_t s) {
     const int CS = solve_cluster_size(m.N);
     const int rp = (m.N + CS - 1) / CS;
     if (rp > kSolveThreads * kSolveRowsPerThread) return cudaErrorInvalidValue;
-    size_t smem = (4 * static_cast<size_t>(m.N) + 2 * kMaxCluster) * sizeof(double) + static_cast<size_t>(rp) * sizeof(d3);
+    size_t smem = si_smem_bytes(m.N);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k_solve_si, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e != cudaSuccess) return e;
@@ -517,9 +567,9 @@ __global__ void __launch_bounds__(kLinThreads) k_solve_lin(DevModel m, SolveSett
 }
 
 // Every case of a batch in one launch: CTA i solves jobs[i].
-__global__ void __launch_bounds__(kLinThreads) k_solve_lin_jobs(const LinJob* jobs, unsigned smem) {
+__global__ void __launch_bounds__(kLinThreads) k_solve_lin_jobs(const SolveJob* jobs, unsigned smem) {
     extern __shared__ __align__(16) unsigned char lin_dyn[];
-    const LinJob& j = jobs[blockIdx.x];
+    const SolveJob& j = jobs[blockIdx.x];
     lin_solve_case(j.m, j.st, j.b, lin_dyn, smem);
 }
 
@@ -676,10 +726,10 @@ __global__ void __launch_bounds__(kLinThreads) k_solve_lin_cluster(DevModel m, S
 }
 
 // Every case of a batch that needs a cluster of this launch's size: cluster i solves jobs[i].
-__global__ void __launch_bounds__(kLinThreads) k_solve_lin_cluster_jobs(const LinJob* jobs) {
+__global__ void __launch_bounds__(kLinThreads) k_solve_lin_cluster_jobs(const SolveJob* jobs) {
     extern __shared__ __align__(16) unsigned char lin_dyn[];
     cg::cluster_group cl = cg::this_cluster();
-    const LinJob& j = jobs[blockIdx.x / cl.num_blocks()];
+    const SolveJob& j = jobs[blockIdx.x / cl.num_blocks()];
     lin_solve_cluster(j.m, j.st, j.b, lin_dyn);
 }
 
@@ -762,7 +812,7 @@ cudaError_t launch_solve_linearized(const DevModel& m, const SolveSettings& st, 
     return cudaLaunchKernelEx(&cfg, k_solve_lin_cluster, m, st, b);
 }
 
-cudaError_t launch_solve_linearized_jobs(const LinJob* jobs, int n, const LinPlan& plan, cudaStream_t s) {
+cudaError_t launch_solve_linearized_jobs(const SolveJob* jobs, int n, const LinPlan& plan, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     if (plan.smem > kLinSmemLimit) return cudaErrorInvalidValue;
     if (plan.cluster == 1) {

@@ -155,8 +155,8 @@ int solve_cluster_size(int N);
 cudaError_t launch_solve_simple_iterative(const DevModel& m, const SolveSettings& st, const SolveBuffers& b, cudaStream_t s);
 cudaError_t launch_solve_linearized(const DevModel& m, const SolveSettings& st, const SolveBuffers& b, cudaStream_t s);
 
-// One linearized solve of a batch (CTA blockIdx.x of k_solve_lin_jobs).
-struct LinJob {
+// One solve of a batch (k_solve_lin_jobs, k_solve_lin_cluster_jobs, k_solve_si_jobs).
+struct SolveJob {
     DevModel m;
     SolveSettings st;
     SolveBuffers b;
@@ -172,7 +172,11 @@ struct LinPlan {
 };
 LinPlan linearized_plan(int N);
 // n solves of one plan shape in one launch (smem: the largest of the jobs' plans).
-cudaError_t launch_solve_linearized_jobs(const LinJob* jobs, int n, const LinPlan& plan, cudaStream_t s);
+cudaError_t launch_solve_linearized_jobs(const SolveJob* jobs, int n, const LinPlan& plan, cudaStream_t s);
+// SimpleIterative solves of a batch: n cases of one cluster size (solve_cluster_size of
+// their N) in one launch, a cluster per case; smem = the largest si_smem_bytes of the jobs.
+size_t si_smem_bytes(int N);
+cudaError_t launch_solve_simple_iterative_jobs(const SolveJob* jobs, int n, int cluster, size_t smem, cudaStream_t s);
 
 struct ForceArgs {
     const double* gamma = nullptr;  // [N]

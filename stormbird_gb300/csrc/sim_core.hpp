@@ -838,8 +838,8 @@ struct sb_sim {
     // changes between steps (device pointers and settings), so a batch solves all such
     // cases in one launch of k_solve_lin_jobs.
     bool linearized_quasi_steady() const { return !dynamic && solver_kind == 1; }
-    LinJob linearized_job() const {
-        LinJob j;
+    SolveJob linearized_job() const {
+        SolveJob j;
         j.m = dm;
         j.st = solve;
         j.b = solve_buffers();
