@@ -770,9 +770,8 @@ struct sb_batch {
         if (static_cast<long long>(n) != nfs_total)
             raise(SB_ERR_SIZE, "freestream has " + std::to_string(n) + " points, expected " + std::to_string(nfs_total));
         const size_t cnt = n * 3;
-        for (size_t i = 0; i < cnt; ++i)
-            if (!std::isfinite(fs_host[i])) raise(SB_ERR_NONFINITE, "non-finite freestream value at index " + std::to_string(i / 3));
-        std::memcpy(h_fs_all.p, fs_host, cnt * sizeof(double));
+        const size_t bad = copy_finite(fs_host, h_fs_all.p, cnt);
+        if (bad < cnt) raise(SB_ERR_NONFINITE, "non-finite freestream value at index " + std::to_string(bad / 3));
         ck(cudaMemcpyAsync(fs_all.p, h_fs_all.p, cnt * sizeof(double), cudaMemcpyHostToDevice, main), "H2D freestream");
         step(time, dt);
     }

@@ -15,6 +15,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/stormbird_gb300.h"
@@ -126,6 +127,40 @@ inline d3 interp(double x, const std::vector<double>& xd, const std::vector<d3>&
     }
     if (lo == n - 1) return yd[lo];
     return two(x, xd[lo], xd[lo + 1], yd[lo], yd[lo + 1]);
+}
+
+// Copies n values into the staging buffer and returns the index of the first non-finite
+// one (n when all are finite; the copy is then complete). Large inputs are split over
+// host threads, each checking and copying its own contiguous part in one pass.
+inline size_t copy_finite(const double* src, double* dst, size_t n) {
+    auto part = [](const double* s, double* d, size_t b, size_t e) {
+        for (size_t i = b; i < e; ++i) {
+            if (!std::isfinite(s[i])) return i;
+            d[i] = s[i];
+        }
+        return e;
+    };
+    constexpr size_t kSerial = size_t(1) << 20;
+    const unsigned hw = std::thread::hardware_concurrency();
+    const size_t T = std::min<size_t>(hw ? hw : 1, 16);
+    if (n < kSerial || T < 2) {
+        const size_t r = part(src, dst, 0, n);
+        return r;
+    }
+    std::vector<size_t> first(T, n);
+    std::vector<std::thread> th;
+    const size_t chunk = (n + T - 1) / T;
+    for (size_t t = 0; t < T; ++t) {
+        const size_t b = std::min(n, t * chunk), e = std::min(n, b + chunk);
+        th.emplace_back([&, t, b, e] {
+            const size_t r = part(src, dst, b, e);
+            first[t] = r < e ? r : n;
+        });
+    }
+    for (auto& x : th) x.join();
+    size_t bad = n;
+    for (size_t r : first) bad = std::min(bad, r);
+    return bad;
 }
 
 inline int num_sms(int device) {
@@ -1017,9 +1052,8 @@ struct sb_sim {
     void do_step(double time, double dt, const double* fs_host, size_t n, sb_step_output* o) {
         if (static_cast<long long>(n) != nfs) raise(SB_ERR_SIZE, "freestream has " + std::to_string(n) + " points, expected " + std::to_string(nfs));
         const size_t cnt = n * 3;
-        for (size_t i = 0; i < cnt; ++i)
-            if (!std::isfinite(fs_host[i])) raise(SB_ERR_NONFINITE, "non-finite freestream value at index " + std::to_string(i / 3));
-        std::memcpy(h_fs.p, fs_host, cnt * sizeof(double));
+        const size_t bad = copy_finite(fs_host, h_fs.p, cnt);
+        if (bad < cnt) raise(SB_ERR_NONFINITE, "non-finite freestream value at index " + std::to_string(bad / 3));
         ck(cudaMemcpyAsync(fs_p, h_fs.p, cnt * sizeof(double), cudaMemcpyHostToDevice, stream), "H2D freestream");
         enqueue_step(time, dt);
         finish_step();
