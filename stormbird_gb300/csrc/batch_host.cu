@@ -116,12 +116,12 @@ struct sb_batch {
     // a cluster per case; the job list is refilled every step from pinned memory, since it
     // names the wake buffer of the step's parity
     struct SiGroup {
-        int cluster = 0;
+        int cluster = 0, rows_per_thread = 1;
         size_t smem = 0;
         std::vector<int> cases;
         long long off = 0;
     };
-    static constexpr int kSiGroups = 3;
+    static constexpr int kSiGroups = 6;  // cluster size 1, 4, 8 x rows per thread 1, 4
     SiGroup si_groups[kSiGroups];
     long long si_entries = 0;
     std::vector<char> si_batched;  // per case: its solve runs in a k_solve_si_jobs launch
@@ -283,8 +283,10 @@ struct sb_batch {
             if (c.solver_kind != 0 || c.solve.start_with_linearized) continue;
             const int CS = solve_cluster_size(c.N);
             if ((c.N + CS - 1) / CS > 1024) continue;  // too many rows per CTA: the single path reports it
-            const int g = CS == 1 ? 0 : (CS == 4 ? 1 : 2);
+            const int rpt = si_rows_per_thread(c.N);
+            const int g = (CS == 1 ? 0 : (CS == 4 ? 1 : 2)) + (rpt == 1 ? 0 : 3);
             si_groups[g].cluster = CS;
+            si_groups[g].rows_per_thread = rpt;
             si_groups[g].smem = std::max(si_groups[g].smem, si_smem_bytes(c.N));
             si_groups[g].cases.push_back(static_cast<int>(i));
             si_batched[i] = 1;
@@ -546,7 +548,7 @@ struct sb_batch {
             for (const auto& g : si_groups)
                 if (!g.cases.empty())
                     ck(launch_solve_simple_iterative_jobs(d_si_jobs.p + g.off, static_cast<int>(g.cases.size()), g.cluster,
-                                                          g.smem, n_launch > 1 ? pool[k++] : main),
+                                                          g.rows_per_thread, g.smem, n_launch > 1 ? pool[k++] : main),
                        "batched simple iterative solve");
             if (n_launch > 1) join(1);
         }

@@ -37,7 +37,7 @@ namespace cg = cooperative_groups;
 namespace sbgpu {
 
 constexpr int kSolveThreads = 256;
-constexpr int kSolveRowsPerThread = 4;
+constexpr int kSolveRowsPerThread = 4;  // most rows per thread (1024 per CTA)
 constexpr int kMaxCluster = 8;
 
 int solve_cluster_size(int N) {
@@ -95,6 +95,9 @@ __device__ inline double residual_term(const DevModel& m, const RowGeom& g, cons
 
 // SimpleIterative::solve for one case on the calling thread-block cluster (see the top of
 // the file). Run by k_solve_si (one case) and k_solve_si_jobs (a cluster per case of a batch).
+// RPT = rows per thread: 1 while a CTA owns at most kSolveThreads rows (registers for two
+// CTAs per SM), else kSolveRowsPerThread.
+template <int RPT>
 __device__ void si_solve(const DevModel& m, const SolveSettings& st, const SolveBuffers& b) {
     cg::cluster_group cl = cg::this_cluster();
     const int CS = static_cast<int>(cl.num_blocks());
@@ -118,11 +121,11 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
         G[0][i] = g;
     }
     // per-thread rows
-    RowGeom rg[kSolveRowsPerThread];
-    d3 u_last[kSolveRowsPerThread];
-    double aoa_last[kSolveRowsPerThread];
+    RowGeom rg[RPT];
+    d3 u_last[RPT];
+    double aoa_last[RPT];
     int nrows = 0;
-    for (int k = 0; k < kSolveRowsPerThread; ++k) {
+    for (int k = 0; k < RPT; ++k) {
         int i = r0 + tid + k * kSolveThreads;
         if (i < r1) {
             rg[k] = row_geom(m, i);
@@ -303,15 +306,25 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
     cl.sync();  // no CTA leaves while others may still write into its shared memory
 }
 
-__global__ void __launch_bounds__(kSolveThreads) k_solve_si(DevModel m, SolveSettings st, SolveBuffers b) {
-    si_solve(m, st, b);
+template <int RPT>
+__global__ void __launch_bounds__(kSolveThreads, RPT == 1 ? 2 : 1) k_solve_si(DevModel m, SolveSettings st, SolveBuffers b) {
+    si_solve<RPT>(m, st, b);
 }
 
-// Every case of a batch whose cluster size is this launch's: cluster i solves jobs[i].
-__global__ void __launch_bounds__(kSolveThreads) k_solve_si_jobs(const SolveJob* jobs) {
+// Every case of a batch whose cluster size (and rows per thread) is this launch's: cluster i
+// solves jobs[i].
+template <int RPT>
+__global__ void __launch_bounds__(kSolveThreads, RPT == 1 ? 2 : 1) k_solve_si_jobs(const SolveJob* jobs) {
     cg::cluster_group cl = cg::this_cluster();
     const SolveJob& j = jobs[blockIdx.x / cl.num_blocks()];
-    si_solve(j.m, j.st, j.b);
+    si_solve<RPT>(j.m, j.st, j.b);
+}
+
+// rows per thread of a solve of N span lines
+int si_rows_per_thread(int N) {
+    const int CS = solve_cluster_size(N);
+    const int rp = (N + CS - 1) / CS;
+    return rp <= kSolveThreads ? 1 : kSolveRowsPerThread;
 }
 
 size_t si_smem_bytes(int N) {
@@ -320,12 +333,14 @@ size_t si_smem_bytes(int N) {
     return (4 * static_cast<size_t>(N) + 2 * kMaxCluster) * sizeof(double) + static_cast<size_t>(rp) * sizeof(d3);
 }
 
-cudaError_t launch_solve_simple_iterative_jobs(const SolveJob* jobs, int n, int cluster, size_t smem, cudaStream_t s) {
+cudaError_t launch_solve_simple_iterative_jobs(const SolveJob* jobs, int n, int cluster, int rows_per_thread,
+                                               size_t smem, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     if (cluster != 1 && cluster != 4 && cluster != 8) return cudaErrorInvalidValue;
+    if (rows_per_thread != 1 && rows_per_thread != kSolveRowsPerThread) return cudaErrorInvalidValue;
+    auto kernel = rows_per_thread == 1 ? k_solve_si_jobs<1> : k_solve_si_jobs<kSolveRowsPerThread>;
     if (smem > 48 * 1024) {
-        cudaError_t e =
-            cudaFuncSetAttribute(k_solve_si_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e != cudaSuccess) return e;
     }
     cudaLaunchConfig_t cfg = {};
@@ -340,7 +355,7 @@ cudaError_t launch_solve_simple_iterative_jobs(const SolveJob* jobs, int n, int 
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_solve_si_jobs, jobs);
+    return cudaLaunchKernelEx(&cfg, kernel, jobs);
 }
 
 cudaError_t launch_solve_simple_iterative(const DevModel& m, const SolveSettings& st, const SolveBuffers& b, cudaStream_t s) {
@@ -348,8 +363,9 @@ cudaError_t launch_solve_simple_iterative(const DevModel& m, const SolveSettings
     const int rp = (m.N + CS - 1) / CS;
     if (rp > kSolveThreads * kSolveRowsPerThread) return cudaErrorInvalidValue;
     size_t smem = si_smem_bytes(m.N);
+    auto kernel = si_rows_per_thread(m.N) == 1 ? k_solve_si<1> : k_solve_si<kSolveRowsPerThread>;
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_solve_si, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e != cudaSuccess) return e;
     }
     cudaLaunchConfig_t cfg = {};
@@ -364,7 +380,7 @@ cudaError_t launch_solve_simple_iterative(const DevModel& m, const SolveSettings
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_solve_si, m, st, b);
+    return cudaLaunchKernelEx(&cfg, kernel, m, st, b);
 }
 
 // ---------------------------------------------------------------------------------------
