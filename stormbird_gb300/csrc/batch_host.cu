@@ -127,6 +127,9 @@ struct sb_batch {
     std::vector<char> si_batched;  // per case: its solve runs in a k_solve_si_jobs launch
     PinnedBuf<SolveJob> h_si_jobs;
     DevBuf<SolveJob> d_si_jobs;
+    // forces of every case, one launch (refilled each step: step parameters can change)
+    PinnedBuf<ForceJob> h_force_jobs;
+    DevBuf<ForceJob> d_force_jobs;
 
     // Sweep work lists: group = (sweep kind, symmetry, neglect); one launch each.
     struct Group {
@@ -299,6 +302,8 @@ struct sb_batch {
             h_si_jobs.alloc(si_entries);
             d_si_jobs.alloc(si_entries);
         }
+        h_force_jobs.alloc(cases.size());
+        d_force_jobs.alloc(cases.size());
         counters.alloc(16);
         err.alloc(1);
         ck(cudaMemset(err.p, 0, sizeof(int)), "memset");
@@ -565,9 +570,11 @@ struct sb_batch {
             ck(launch_batch_targets(gamma_all.p, w_q.p, w_g0.p, w_tr.p, N_total, w_target.p, main), "warm-start targets");
         sweeps(1);
         for (auto& c : cases) if (c->dynamic) c->after_rollup_sweep();
-        fork(2);
-        for (auto& c : cases) c->step_end();
-        join(2);
+        fill_force_jobs();
+        ck(cudaMemcpyAsync(d_force_jobs.p, h_force_jobs.p, cases.size() * sizeof(ForceJob), cudaMemcpyHostToDevice, main),
+           "H2D force jobs");
+        ck(launch_forces_jobs(d_force_jobs.p, static_cast<int>(cases.size()), main), "batched forces");
+        for (auto& c : cases) c->after_forces();
         k_gather<<<static_cast<unsigned>(cases.size()), 128, 0, main>>>(gather_jobs.p);
         ck(cudaGetLastError(), "gather");
         const size_t ncomp = static_cast<size_t>(N_total) + cases.size() * SB_BATCH_SUMMARY;
@@ -711,7 +718,11 @@ struct sb_batch {
                 graph_precision = precision;
                 graph_wind = wind ? 1 : 0;
             } else {
+                // host state of the step as an eager step leaves it before its forces
                 replay_bookkeeping(time, dt);
+                for (auto& c : cases) c->fd_count -= 1;
+                fill_force_jobs();
+                for (auto& c : cases) c->fd_count += 1;
             }
             ck(cudaGraphLaunch(graph[parity], main), "graph launch");
         } else {
@@ -753,6 +764,11 @@ struct sb_batch {
         fill_jobs();
         fill_si_jobs();
         for (auto& c : cases) if (c->dynamic) c->cur ^= 1;
+    }
+
+    // The forces job of every case (read by the graph's copy node at launch when replayed).
+    void fill_force_jobs() {
+        for (size_t i = 0; i < cases.size(); ++i) h_force_jobs.p[i] = cases[i]->force_job();
     }
 
     // The SimpleIterative jobs of the step (each case's model, settings and buffers, with the

@@ -507,9 +507,20 @@ __global__ void __launch_bounds__(kBsReduceThreads) k_bs_reduce_jobs(const BsJob
     J.out[i] = v;
 }
 
+// one matrix entry into the f64 and/or split matrix (row c, column j)
+__device__ inline void store_factor(d3* factors, float2* split, int N, long long id, int c, int j, d3 u) {
+    if (factors) factors[id] = u;
+    if (split) {
+        float2* r = split + static_cast<long long>(c) * 3 * N + j;
+        r[0] = split_f64(u.x);
+        r[N] = split_f64(u.y);
+        r[2 * N] = split_f64(u.z);
+    }
+}
+
 // frozen_wake.rs:198-249: factors[c][p] = unit velocity of first-row panel p at control point c
 __global__ void k_unit_matrix(const PanelRec<double>* row0, const d3* ctrl, int N, int sym, int neglect,
-                              const int* wing_of_line, d3* factors) {
+                              const int* wing_of_line, d3* factors, float2* split) {
     long long id = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
     if (id >= static_cast<long long>(N) * N) return;
     int c = static_cast<int>(id / N), p = static_cast<int>(id % N);
@@ -519,7 +530,7 @@ __global__ void k_unit_matrix(const PanelRec<double>* row0, const d3* ctrl, int 
         u = panel_unit_f64(row0[p].v, x);
         if (sym) u = sym_correct(sym, u, panel_unit_f64(row0[p].v, mirror(sym, x)));
     }
-    factors[id] = u;
+    store_factor(factors, split, N, id, c, p, u);
 }
 
 // Quasi-steady wake: core length and wake vectors (frozen_wake.rs:74-100). One CTA: the
@@ -548,7 +559,8 @@ __global__ void __launch_bounds__(kQsPrepThreads) k_qs_prep(DevModel m, int core
 // Horseshoe influence matrix (frozen_wake.rs:102-128, horseshoe_vortex.rs:23-103):
 // factors[c][j] = unit velocity of horseshoe j (bound + start trailing + end trailing) at
 // control point c. Horseshoe j of wing w uses wake vectors j + w and j + w + 1.
-__global__ void k_horseshoe_matrix(DevModel m, const d3* wake_vec, const double* rc_dev, int sym, d3* factors) {
+__global__ void k_horseshoe_matrix(DevModel m, const d3* wake_vec, const double* rc_dev, int sym, d3* factors,
+                                   float2* split) {
     long long id = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
     const int N = m.N;
     if (id >= static_cast<long long>(N) * N) return;
@@ -567,11 +579,11 @@ __global__ void k_horseshoe_matrix(DevModel m, const d3* wake_vec, const double*
     d3 x = m.ctrl[c];
     d3 u = hs(x);
     if (sym) u = sym_correct(sym, u, hs(mirror(sym, x)));
-    factors[id] = u;
+    store_factor(factors, split, N, id, c, j, u);
 }
 
 cudaError_t launch_horseshoe_matrix(const DevModel& m, int core_kind, double core_value, double wake_length, d3* wake_vec,
-                                    double* rc_dev, int sym, d3* factors, cudaStream_t s) {
+                                    double* rc_dev, int sym, d3* factors, float2* split, cudaStream_t s) {
     const size_t smem = static_cast<size_t>(m.N) * sizeof(double);
     if (smem > 48 * 1024) {
         cudaError_t a = cudaFuncSetAttribute(k_qs_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
@@ -581,7 +593,7 @@ cudaError_t launch_horseshoe_matrix(const DevModel& m, int core_kind, double cor
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     long long tot = static_cast<long long>(m.N) * m.N;
-    k_horseshoe_matrix<<<static_cast<unsigned>((tot + 127) / 128), 128, 0, s>>>(m, wake_vec, rc_dev, sym, factors);
+    k_horseshoe_matrix<<<static_cast<unsigned>((tot + 127) / 128), 128, 0, s>>>(m, wake_vec, rc_dev, sym, factors, split);
     return cudaGetLastError();
 }
 
@@ -671,11 +683,11 @@ cudaError_t launch_bs_reduce_jobs(const BsJob* jobs, int n_jobs, long long block
 }
 
 cudaError_t launch_unit_matrix(const PanelRec<double>* row0, const d3* ctrl, int N, int sym, int neglect,
-                               const int* wing_of_line, d3* factors, cudaStream_t s) {
+                               const int* wing_of_line, d3* factors, float2* split, cudaStream_t s) {
     long long tot = static_cast<long long>(N) * N;
     int threads = 128;
     long long blocks = (tot + threads - 1) / threads;
-    k_unit_matrix<<<static_cast<unsigned>(blocks), threads, 0, s>>>(row0, ctrl, N, sym, neglect, wing_of_line, factors);
+    k_unit_matrix<<<static_cast<unsigned>(blocks), threads, 0, s>>>(row0, ctrl, N, sym, neglect, wing_of_line, factors, split);
     return cudaGetLastError();
 }
 

@@ -5,15 +5,19 @@
 // thread-block cluster. Every CTA of the cluster keeps the full circulation vector in
 // shared memory; CTA r owns a contiguous block of control points. Per iteration:
 //   1. induced velocity of its rows: fixed + M * Gamma (frozen_wake.rs:268-301), one warp
-//      per row, matrix rows read from L2;
-//   2. per row: total velocity (velocity_corrections.rs:28-100), span component removed
-//      (line_force_model/mod.rs:235-254), angle of attack (force_calculations.rs:79-107),
-//      Foil lift, circulation estimate (force_calculations.rs:271-292), residual term
-//      (force_calculations.rs:552-627) and the damped update;
-//   3. new Gamma and residual terms are stored into every CTA's shared memory through
-//      distributed shared memory, the per-CTA max |dGamma| likewise, one cluster barrier;
-//   4. every CTA sums the residual terms in control-point order (the reference's order,
-//      so the convergence test takes the same branch) and takes the max.
+//      per row, matrix rows read from L2 as (hi, lo) float pairs and the products summed
+//      in double-float arithmetic on the FP32 pipes (~2^-44 relative per product; this
+//      part's FP64 rate is 1/64 of its FP32 rate);
+//   2. per row, in f64: total velocity (velocity_corrections.rs:28-100), span component
+//      removed (line_force_model/mod.rs:235-254), angle of attack
+//      (force_calculations.rs:79-107), Foil lift, circulation estimate
+//      (force_calculations.rs:271-292), residual term (force_calculations.rs:552-627) and
+//      the damped update; the thread's own f64 circulation stays in registers;
+//   3. new Gamma (as a float pair) and residual terms are stored into every CTA's shared
+//      memory through distributed shared memory, the per-CTA max |dGamma| likewise, one
+//      cluster barrier;
+//   4. every CTA sums the residual terms with one warp in a fixed order (the same value,
+//      hence the same stopping decision, in every CTA) and takes the max.
 // All waits are hardware cluster barriers; no spin loops.
 //
 // k_solve_lin / k_solve_lin_jobs: Linearized::solve (solvers/linearized.rs:54-222) with
@@ -47,7 +51,7 @@ int solve_cluster_size(int N) {
 }
 
 struct RowGeom {
-    d3 felt, span_rel, span_dir, chord, span_rel_out;
+    d3 felt, span_dir, chord, span_rel_out;  // span_dir = normalize(span end - span start)
     double chord_len, area;
     int wing;
 };
@@ -55,10 +59,10 @@ struct RowGeom {
 __device__ inline RowGeom row_geom(const DevModel& m, int i) {
     RowGeom g;
     g.felt = m.felt_ctrl[i];
-    g.span_rel = m.span_e[i] - m.span_s[i];
-    g.span_dir = normalize(g.span_rel);
+    const d3 span_rel = m.span_e[i] - m.span_s[i];
+    g.span_dir = normalize(span_rel);
     g.chord = m.chord_global[i];
-    g.span_rel_out = m.output_body ? (m.span_e_local[i] - m.span_s_local[i]) : g.span_rel;
+    g.span_rel_out = m.output_body ? (m.span_e_local[i] - m.span_s_local[i]) : span_rel;
     g.chord_len = m.chord_len[i];
     g.area = m.chord_len[i] * m.span_len_local[i];
     g.wing = m.wing_of_line[i];
@@ -83,14 +87,66 @@ __device__ inline double circulation_cl(const DevModel& m, const FoilP& f, doubl
     return cl;
 }
 
-// |cl_gamma - cl_direct| of force_calculations.rs:552-607
-__device__ inline double residual_term(const DevModel& m, const RowGeom& g, const FoilP& f, double gam, d3 u, double aoa) {
+// |cl_gamma - cl_direct| of force_calculations.rs:552-607, given cl_direct = the foil's
+// pre-stall lift coefficient at the line's angle of attack
+__device__ inline double residual_from_cl(const DevModel& m, const RowGeom& g, double gam, d3 u, double cl_pre) {
     double ul = len(u);
     d3 force = ul == 0.0 ? mk(0, 0, 0) : (gam * cross(u, g.span_rel_out)) * m.density;
     double sign = -1.0 * signum(gam);
     double ff = 0.5 * g.area * m.density * len2(u);
     double clg = ff == 0.0 ? 0.0 : len(force) * sign / ff;
-    return fabs(clg - foil_cl_pre_stall(f, aoa));
+    return fabs(clg - cl_pre);
+}
+__device__ inline double residual_term(const DevModel& m, const RowGeom& g, const FoilP& f, double gam, d3 u, double aoa) {
+    return residual_from_cl(m, g, gam, u, foil_cl_pre_stall(f, aoa));
+}
+
+// Double-float accumulation for the matrix-vector product: (S, C) += (xh + xl) * (gh + gl).
+// The product's head xh*gh is added to S by an error-free two-sum (Knuth); its rounding error
+// (an exact FMA) and the cross terms xh*gl + xl*gh go into C; xl*gl (~2^-48 of the product)
+// is dropped. The _rn intrinsics keep the compiler from fusing the steps.
+__device__ __forceinline__ void ff_mac(float& S, float& C, float2 x, float2 g) {
+    const float p = __fmul_rn(x.x, g.x);
+    float t = fmaf(x.x, g.x, -p);
+    t = fmaf(x.x, g.y, t);
+    t = fmaf(x.y, g.x, t);
+    const float s = __fadd_rn(S, p);
+    const float bv = __fsub_rn(s, S);
+    const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(s, bv)), __fsub_rn(p, bv));
+    S = s;
+    C = __fadd_rn(C, __fadd_rn(err, t));
+}
+// (S, C) += (h, l), another double-float partial sum
+__device__ __forceinline__ void ff_add(float& S, float& C, float h, float l) {
+    const float s = __fadd_rn(S, h);
+    const float bv = __fsub_rn(s, S);
+    const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(s, bv)), __fsub_rn(h, bv));
+    S = s;
+    C = __fadd_rn(C, __fadd_rn(err, l));
+}
+
+// Sum / max over a warp in a fixed order (lane 0 gets the result): every CTA of a cluster
+// reduces the same residual terms the same way and takes the same stopping decision.
+__device__ __forceinline__ double warp_sum_to_lane0(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+// Maxima of magnitudes on the integer pipe (this part's FP64 pipe costs a full warp
+// instruction per compare): |v| as its IEEE bit pattern, which orders like an unsigned
+// integer for non-negative values; a NaN maps to 0, as fmax(x, NaN) = x leaves it out.
+__device__ __forceinline__ unsigned long long mag_bits(double v) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v)) & 0x7FFFFFFFFFFFFFFFull;
+    return b > 0x7FF0000000000000ull ? 0ull : b;
+}
+__device__ __forceinline__ double bits_value(unsigned long long b) { return __longlong_as_double(static_cast<long long>(b)); }
+__device__ __forceinline__ unsigned long long warp_umax_to_lane0(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
 }
 
 // SimpleIterative::solve for one case on the calling thread-block cluster (see the top of
@@ -105,29 +161,41 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
     const int N = m.N;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = kSolveThreads / 32;
     extern __shared__ double smem[];
-    double* G[2] = {smem, smem + N};
+    // circulation of every line as (hi, lo) float pairs for the matrix-vector products; the
+    // f64 circulation of the thread's own rows stays in registers (gown)
+    float2* G[2] = {reinterpret_cast<float2*>(smem), reinterpret_cast<float2*>(smem + N)};
     double* RR[2] = {smem + 2 * N, smem + 3 * N};
     double* MX[2] = {smem + 4 * N, smem + 4 * N + kMaxCluster};
     const int rp = (N + CS - 1) / CS;
     const int r0 = min(N, rank * rp), r1 = min(N, r0 + rp);
-    d3* uind = reinterpret_cast<d3*>(smem + 4 * N + 2 * kMaxCluster);
-    __shared__ double s_res, s_red[kSolveThreads / 32];
+    // The thread's k-th own row (offset from r0): consecutive rows on consecutive threads, so
+    // that a CTA owning fewer than 256 rows fills as few warps as possible (this part's FP64
+    // pipe costs the same per warp instruction however few lanes are active).
+    auto own_row = [&](int k) { return tid + k * kSolveThreads; };
+    // M * Gamma of the CTA's rows as double-float pairs (x hi, x lo, y hi, y lo, z hi, z lo);
+    // the row's owner adds them to the fixed part in f64
+    float* uff = reinterpret_cast<float*>(smem + 4 * N + 2 * kMaxCluster);
+    __shared__ double s_res;
+    __shared__ unsigned long long s_umax[kSolveThreads / 32];
     __shared__ int s_conv;
 
     const bool scale0 = fabs(st.correction_factor_initial - 1.0) > kMinPositive;
     for (int i = tid; i < N; i += kSolveThreads) {
         double g = b.gamma_prev[i];
         if (scale0) g *= st.correction_factor_initial;
-        G[0][i] = g;
+        G[0][i] = split_f64(g);
     }
     // per-thread rows
     RowGeom rg[RPT];
     d3 u_last[RPT];
-    double aoa_last[RPT];
+    double aoa_last[RPT], gown[RPT];
     int nrows = 0;
     for (int k = 0; k < RPT; ++k) {
-        int i = r0 + tid + k * kSolveThreads;
+        int i = r0 + own_row(k);
         if (i < r1) {
+            double g = b.gamma_prev[i];
+            if (scale0) g *= st.correction_factor_initial;
+            gown[k] = g;
             rg[k] = row_geom(m, i);
             u_last[k] = mk(0, 0, 0);
             aoa_last[k] = 0.0;
@@ -149,30 +217,44 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
     }
     cl.sync();
 
-    // induced velocity of own rows for the circulation Gc: fixed + M * Gc
-    auto induced_rows = [&](const double* Gc) {
+    // induced velocity of own rows for the circulation Gc: fixed + M * Gc. One warp per row;
+    // double-float arithmetic on the FP32 pipes (this part's FP64 rate is 1/64 of its FP32
+    // rate): the split matrix row and the split circulation, ~2^-44 relative per product.
+    auto induced_rows = [&](const float2* Gc) {
         for (int row = r0 + warp; row < r1; row += nwarps) {
-            const d3* fr = b.factors + static_cast<long long>(row) * N;
-            double sx = 0.0, sy = 0.0, sz = 0.0;
+            const float2* fr = b.factors_split + static_cast<long long>(row) * 3 * N;
+            float sxh = 0.f, sxl = 0.f, syh = 0.f, syl = 0.f, szh = 0.f, szl = 0.f;
             for (int j = lane; j < N; j += 32) {
-                d3 f = fr[j];
-                double g = Gc[j];
-                sx += f.x * g;
-                sy += f.y * g;
-                sz += f.z * g;
+                const float2 g = Gc[j];
+                ff_mac(sxh, sxl, __ldg(fr + j), g);
+                ff_mac(syh, syl, __ldg(fr + N + j), g);
+                ff_mac(szh, szl, __ldg(fr + 2 * N + j), g);
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                sx += __shfl_down_sync(0xffffffffu, sx, o);
-                sy += __shfl_down_sync(0xffffffffu, sy, o);
-                sz += __shfl_down_sync(0xffffffffu, sz, o);
+                ff_add(sxh, sxl, __shfl_down_sync(0xffffffffu, sxh, o), __shfl_down_sync(0xffffffffu, sxl, o));
+                ff_add(syh, syl, __shfl_down_sync(0xffffffffu, syh, o), __shfl_down_sync(0xffffffffu, syl, o));
+                ff_add(szh, szl, __shfl_down_sync(0xffffffffu, szh, o), __shfl_down_sync(0xffffffffu, szl, o));
             }
             if (lane == 0) {
-                d3 fx = b.fixed[row];
-                uind[row - r0] = mk(fx.x + sx, fx.y + sy, fx.z + sz);
+                float* o = uff + 6 * (row - r0);
+                o[0] = sxh;
+                o[1] = sxl;
+                o[2] = syh;
+                o[3] = syl;
+                o[4] = szh;
+                o[5] = szl;
             }
         }
         __syncthreads();
+    };
+    // induced velocity of own row i: fixed + M * Gamma
+    auto induced_of = [&](int i) {
+        const float* o = uff + 6 * (i - r0);
+        const d3 fx = b.fixed[i];
+        return mk(fx.x + (static_cast<double>(o[0]) + static_cast<double>(o[1])),
+                  fx.y + (static_cast<double>(o[2]) + static_cast<double>(o[3])),
+                  fx.z + (static_cast<double>(o[4]) + static_cast<double>(o[5])));
     };
 
     // Guarded warm start: residual (simple_iterative.rs:160-176) of the plain start G[0]
@@ -186,34 +268,40 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
         for (int v = 0; v < 3; ++v) {
             const double* src = v == 0 ? nullptr : b.candidate[v - 1];
             if (v > 0 && !src) continue;
-            double* Gv = v == 0 ? G[0] : G[1];
+            float2* Gv = v == 0 ? G[0] : G[1];
             if (v > 0) {
-                for (int i = tid; i < N; i += kSolveThreads) G[1][i] = src[i];
+                for (int i = tid; i < N; i += kSolveThreads) G[1][i] = split_f64(src[i]);
                 __syncthreads();
             }
             induced_rows(Gv);
             for (int k = 0; k < nrows; ++k) {
-                int i = r0 + tid + k * kSolveThreads;
+                int i = r0 + own_row(k);
                 const RowGeom& g = rg[k];
                 const FoilP f = m.foils[g.wing];
-                d3 u = total_velocity(st, g.felt, uind[i - r0]);
-                u = u - project(u, g.span_rel);
+                d3 u = total_velocity(st, g.felt, induced_of(i));
+                u = u - g.span_dir * dot(u, g.span_dir);  // project(u, span_rel)
                 double aoa = len(u) > kMinPositive ? signed_angle_between(g.chord, u, g.span_dir) : 0.0;
-                double r = residual_term(m, g, f, Gv[i], u, aoa);
+                double r = residual_term(m, g, f, v == 0 ? gown[k] : src[i], u, aoa);
                 for (int q = 0; q < CS; ++q) cl.map_shared_rank(RR[0], q)[i] = r;
             }
             cl.sync();
-            if (tid == 0) {
-                double s = 0.0, mx = 0.0;
-                for (int i = 0; i < N; ++i) {
+            if (warp == 0) {
+                double s = 0.0;
+                unsigned long long mx = 0;
+                for (int i = lane; i < N; i += 32) {
                     s += RR[0][i];
-                    mx = fmax(mx, RR[0][i]);
+                    const unsigned long long bi = mag_bits(RR[0][i]);
+                    mx = bi > mx ? bi : mx;
                 }
-                s_res = s;
-                s_red[0] = mx;
+                s = warp_sum_to_lane0(s);
+                mx = warp_umax_to_lane0(mx);
+                if (lane == 0) {
+                    s_res = s;
+                    s_umax[0] = mx;
+                }
             }
             __syncthreads();
-            const double rv = s_res, rmax = s_red[0];
+            const double rv = s_res, rmax = bits_value(s_umax[0]);
             if (v == 0) {
                 best = rv;
                 best_max = rmax;
@@ -222,6 +310,7 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
                 best_max = rmax;
                 taken = v;
                 for (int i = tid; i < N; i += kSolveThreads) G[0][i] = G[1][i];
+                for (int k = 0; k < nrows; ++k) gown[k] = src[r0 + own_row(k)];
             }
             cl.sync();  // RR[0] and G[1] are written again by the next pass or the first iteration
         }
@@ -234,52 +323,64 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
     bool conv = false;
     while (it < st.max_iterations && !conv) {
         it += 1;
-        const double* Gc = G[cur];
+        const float2* Gc = G[cur];
         // 1. induced velocity of own rows
         induced_rows(Gc);
         // 2. row updates
-        double lmax = 0.0;
+        unsigned long long lmax = 0;  // max |dGamma| of the thread's rows (mag_bits)
         for (int k = 0; k < nrows; ++k) {
-            int i = r0 + tid + k * kSolveThreads;
+            int i = r0 + own_row(k);
             const RowGeom& g = rg[k];
             const FoilP f = m.foils[g.wing];
-            d3 u = total_velocity(st, g.felt, uind[i - r0]);
-            u = u - project(u, g.span_rel);
+            d3 u = total_velocity(st, g.felt, induced_of(i));
+            u = u - g.span_dir * dot(u, g.span_dir);  // project(u, span_rel)
             double aoa = len(u) > kMinPositive ? signed_angle_between(g.chord, u, g.span_dir) : 0.0;
-            double est = -0.5 * g.chord_len * len(u) * circulation_cl(m, f, aoa);
-            double gold = Gc[i];
-            double r = residual_term(m, g, f, gold, u, aoa);
+            // the pre-stall lift coefficient serves the estimate and the residual alike
+            const double clp = foil_cl_pre_stall(f, aoa);
+            const double clc = m.include_viscous_lift ? clp + foil_cl_post_stall(f, aoa) : clp;  // circulation_cl
+            double est = -0.5 * g.chord_len * len(u) * clc;
+            double gold = gown[k];
+            double r = residual_from_cl(m, g, gold, u, clp);
             double d = est - gold;
-            lmax = fmax(lmax, fabs(d));
+            const unsigned long long db = mag_bits(d);
+            lmax = db > lmax ? db : lmax;
             double gnew = gold + st.damping * d;
+            gown[k] = gnew;
             u_last[k] = u;
             aoa_last[k] = aoa;
+            const float2 gs = split_f64(gnew);
             for (int q = 0; q < CS; ++q) {
-                double* Gr = cl.map_shared_rank(G[cur ^ 1], q);
+                float2* Gr = cl.map_shared_rank(G[cur ^ 1], q);
                 double* Rr = cl.map_shared_rank(RR[cur], q);
-                Gr[i] = gnew;
+                Gr[i] = gs;
                 Rr[i] = r;
             }
         }
         // block max
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_down_sync(0xffffffffu, lmax, o));
-        if (lane == 0) s_red[warp] = lmax;
+        lmax = warp_umax_to_lane0(lmax);
+        if (lane == 0) s_umax[warp] = lmax;
         __syncthreads();
         if (tid == 0) {
-            double v = 0.0;
-            for (int w = 0; w < nwarps; ++w) v = fmax(v, s_red[w]);
-            for (int q = 0; q < CS; ++q) cl.map_shared_rank(MX[cur], q)[rank] = v;
+            unsigned long long v = 0;
+            for (int w = 0; w < nwarps; ++w) v = s_umax[w] > v ? s_umax[w] : v;
+            for (int q = 0; q < CS; ++q) cl.map_shared_rank(MX[cur], q)[rank] = bits_value(v);
         }
         cl.sync();
-        if (tid == 0) {
+        if (warp == 0) {
             double s = 0.0;
-            for (int i = 0; i < N; ++i) s += RR[cur][i];
-            double res = s / static_cast<double>(N);
-            double mx = 0.0;
-            for (int q = 0; q < CS; ++q) mx = fmax(mx, MX[cur][q]);
-            s_res = res;
-            s_conv = (res < st.residual_tolerance) || (mx < st.strength_tolerance);
+            for (int i = lane; i < N; i += 32) s += RR[cur][i];
+            s = warp_sum_to_lane0(s);
+            if (lane == 0) {
+                double res = s / static_cast<double>(N);
+                unsigned long long mb = 0;
+                for (int q = 0; q < CS; ++q) {
+                    const unsigned long long bq = static_cast<unsigned long long>(__double_as_longlong(MX[cur][q]));
+                    mb = bq > mb ? bq : mb;
+                }
+                const double mx = bits_value(mb);
+                s_res = res;
+                s_conv = (res < st.residual_tolerance) || (mx < st.strength_tolerance);
+            }
         }
         __syncthreads();
         residual = s_res;
@@ -289,7 +390,7 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
 
     // final circulation from the last velocities (simple_iterative.rs:200-203)
     for (int k = 0; k < nrows; ++k) {
-        int i = r0 + tid + k * kSolveThreads;
+        int i = r0 + own_row(k);
         const RowGeom& g = rg[k];
         double gam = -0.5 * g.chord_len * len(u_last[k]) * circulation_cl(m, m.foils[g.wing], aoa_last[k]);
         b.gamma_prev[i] = gam;
@@ -410,9 +511,9 @@ __device__ inline void lin_build_row(const DevModel& m, const SolveBuffers& b, i
     const int N = m.N;
     RowGeom g = row_geom(m, i);
     d3 v = g.felt + b.fixed[i];
-    v = v - project(v, g.span_rel);
+    v = v - g.span_dir * dot(v, g.span_dir);  // project(v, span_rel)
     d3 un = normalize(v);
-    d3 sd = normalize(g.span_rel);
+    const d3 sd = g.span_dir;
     d3 nd = cross(un, sd);
     double aoa = len(v) > kMinPositive ? signed_angle_between(g.chord, v, g.span_dir) : 0.0;
     const FoilP f = m.foils[g.wing];
@@ -851,7 +952,11 @@ cudaError_t launch_solve_linearized_jobs(const SolveJob* jobs, int n, const LinP
 // ---------------------------------------------------------------------------------------
 // Forces, one CTA
 // ---------------------------------------------------------------------------------------
-__global__ void k_forces(DevModel m, StepParams p, ForceArgs f) {
+constexpr int kForceThreads = 256;
+
+// One case's forces on the calling CTA (k_forces: one case; k_forces_jobs: a CTA per case
+// of a batch, all cases side by side instead of one SM per case on a few streams).
+__device__ void forces_case(const DevModel& m, const StepParams& p, const ForceArgs& f) {
     const int N = m.N, S = m.S, tid = threadIdx.x, nt = blockDim.x;
     const OutLayout L = OutLayout::make(N, S);
     double* o = f.out;
@@ -948,8 +1053,21 @@ __global__ void k_forces(DevModel m, StepParams p, ForceArgs f) {
     }
 }
 
+__global__ void __launch_bounds__(kForceThreads) k_forces(DevModel m, StepParams p, ForceArgs f) { forces_case(m, p, f); }
+
+__global__ void __launch_bounds__(kForceThreads) k_forces_jobs(const ForceJob* jobs) {
+    const ForceJob& j = jobs[blockIdx.x];
+    forces_case(j.m, j.p, j.f);
+}
+
 cudaError_t launch_forces(const DevModel& m, const StepParams& p, const ForceArgs& f, cudaStream_t s) {
-    k_forces<<<1, 256, 0, s>>>(m, p, f);
+    k_forces<<<1, kForceThreads, 0, s>>>(m, p, f);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_forces_jobs(const ForceJob* jobs, int n, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_forces_jobs<<<static_cast<unsigned>(n), kForceThreads, 0, s>>>(jobs);
     return cudaGetLastError();
 }
 

@@ -58,6 +58,13 @@ __host__ __device__ inline d3 project(d3 a, d3 onto) {
 }
 __host__ __device__ inline double signum(double v) { return copysign(1.0, v); }
 
+// f64 value as a pair of floats: hi = the nearest float, lo = the nearest float of v - hi
+// (hi + lo carries about 48 significant bits)
+__device__ inline float2 split_f64(double v) {
+    const float h = __double2float_rn(v);
+    return make_float2(h, __double2float_rn(v - static_cast<double>(h)));
+}
+
 // Angle between two vectors, signed by the right-hand rule about `axis`
 // (stormath/src/spatial_vector/vector_math.rs:65-95).
 __device__ inline double signed_angle_between(d3 a, d3 b, d3 axis) {
@@ -119,11 +126,13 @@ struct FoilP {
         cl_high_order_power, cl_max_after_stall, cd_min, angle_cd_min, cd_second_order_factor, cd_max_after_stall,
         cd_power_after_stall, cdi_correction_factor, mean_positive_stall_angle, mean_negative_stall_angle, stall_range,
         cd_bump_during_stall, cd_stall_angle_offset, added_mass_factor;
+    // 4.5951212 / stall_range, the stall sigmoid's slope (transition_functions.rs:20-27),
+    // divided once on the host (both sides round the f64 quotient correctly: same bits)
+    double stall_slope;
 };
 
-// stormath/src/transition_functions.rs:20-27
-__device__ inline double sigmoid_zero_to_one(double x, double x0, double range) {
-    double slope = 4.5951212 / range;
+// stormath/src/transition_functions.rs:20-27, with slope = 4.5951212 / range
+__device__ inline double sigmoid_zero_to_one_slope(double x, double x0, double slope) {
     return 1.0 / (1.0 + exp(-(slope * (x - x0))));
 }
 // foil.rs:119-129
@@ -136,7 +145,7 @@ __device__ inline double stall_angle(double a) {
 __device__ inline double foil_amount_of_stall(const FoilP& f, double a) {
     double e = a + f.angle_cd_min;
     double mean = e >= 0.0 ? fabs(f.mean_positive_stall_angle) : fabs(f.mean_negative_stall_angle);
-    return sigmoid_zero_to_one(fabs(e), mean, f.stall_range);
+    return sigmoid_zero_to_one_slope(fabs(e), mean, f.stall_slope);
 }
 // foil.rs:161-163
 __device__ inline double foil_cl_linear(const FoilP& f, double a) { return f.cl_zero_angle + f.cl_initial_slope * sin(a); }

@@ -57,11 +57,15 @@ cudaError_t launch_bs_reduce(const double* partial, int n_chunks, long long M, l
 // Reduction of every job of a batched sweep; blocks = sum over jobs of
 // ceil(M_total / kBsReduceThreads), job k starting at its block_begin.
 cudaError_t launch_bs_reduce_jobs(const BsJob* jobs, int n_jobs, long long blocks, cudaStream_t s);
+// The influence matrices are written in f64 (`factors`, [N][N] d3, for the Linearized
+// solver) and/or as f32 (hi, lo) pairs (`split`, [N][3][N] float2: row c, component, column;
+// hi = the nearest float, lo = the nearest float of the remainder, for the SimpleIterative
+// solver's matrix-vector products). Either pointer may be null.
 cudaError_t launch_unit_matrix(const PanelRec<double>* row0, const d3* ctrl, int N, int sym, int neglect,
-                               const int* wing_of_line, d3* factors, cudaStream_t s);
+                               const int* wing_of_line, d3* factors, float2* split, cudaStream_t s);
 // Quasi-steady horseshoe matrix; core_kind 0 relative, 1 absolute, 2 none.
 cudaError_t launch_horseshoe_matrix(const DevModel& m, int core_kind, double core_value, double wake_length, d3* wake_vec,
-                                    double* rc_dev, int sym, d3* factors, cudaStream_t s);
+                                    double* rc_dev, int sym, d3* factors, float2* split, cudaStream_t s);
 
 // ---- wake and geometry (k_wake.cu) ------------------------------------------------------
 struct WakeBuffers {
@@ -135,7 +139,8 @@ struct SolveSettings {
 
 struct SolveBuffers {
     const d3* fixed = nullptr;      // [N]
-    const d3* factors = nullptr;    // [N][N]
+    const d3* factors = nullptr;    // [N][N] (Linearized)
+    const float2* factors_split = nullptr;  // [N][3][N] (hi, lo) pairs (SimpleIterative)
     double* gamma_prev = nullptr;   // [N] in: initial solution, out: solution
     d3* vel_out = nullptr;          // [N] output control-point velocity
     double* scalars = nullptr;      // [8]: residual, iterations, converged, singular, start (below)
@@ -259,5 +264,12 @@ double measure_fp64_peak(int device, int reps);
 // Sectional and integrated forces (force_calculations.rs:322-452, 669-698;
 // forces_and_moments.rs:163-245; flow_derivatives.rs:31-63).
 cudaError_t launch_forces(const DevModel& m, const StepParams& p, const ForceArgs& f, cudaStream_t s);
+// The forces of every case of a batch in one launch (one CTA per case).
+struct ForceJob {
+    DevModel m;
+    StepParams p;
+    ForceArgs f;
+};
+cudaError_t launch_forces_jobs(const ForceJob* jobs, int n, cudaStream_t s);
 
 }  // namespace sbgpu

@@ -89,6 +89,7 @@ struct PinnedBuf {
 
 inline FoilP to_dev(const sbsetup::Foil& f) {
     FoilP o;
+    o.stall_slope = 4.5951212 / f.stall_range;
     o.cl_zero_angle = f.cl_zero_angle;
     o.cl_initial_slope = f.cl_initial_slope;
     o.cl_high_order_factor_positive = f.cl_high_order_factor_positive;
@@ -315,6 +316,7 @@ struct sb_sim {
     int cur = 0;
     // frozen wake and sweeps
     DevBuf<d3> fixed, factors, qs_wake_vec;
+    DevBuf<float2> factors_split;  // the SimpleIterative solver's matrix as (hi, lo) float pairs
     DevBuf<double> qs_rc, partial;
     DevBuf<unsigned long long> counters;
     DevBuf<int> err;
@@ -516,7 +518,11 @@ struct sb_sim {
         dm.chord_local = chord_local.p; dm.chord_global = chord_global.p; dm.chord_span_pts = chord_span_pts.p;
         dm.span_s = span_s.p; dm.span_e = span_e.p; dm.span_pts = span_pts.p; dm.ctrl = ctrl.p;
         dm.felt_ctrl = felt_ctrl.p; dm.felt_span = felt_span.p;
-        fixed.alloc(N); factors.alloc(static_cast<size_t>(N) * N);
+        fixed.alloc(N);
+        // f64 matrix for the Linearized solve (also the start of a SimpleIterative one),
+        // split matrix for the SimpleIterative iterations
+        if (solver_kind == 1 || solve.start_with_linearized) factors.alloc(static_cast<size_t>(N) * N);
+        if (solver_kind == 0) factors_split.alloc(static_cast<size_t>(N) * N * 3);
         ck(cudaMemset(fixed.p, 0, N * sizeof(d3)), "memset");
         counters.alloc(4); err.alloc(4);
         ck(cudaMemset(err.p, 0, 4 * sizeof(int)), "memset");
@@ -835,14 +841,16 @@ struct sb_sim {
     // The frozen wake's matrix: unit first-row panels (dynamic) or horseshoes (quasi-steady).
     void step_matrix() {
         if (dynamic) {
-            ck(launch_unit_matrix(row0_64.p, ctrl.p, N, dm.symmetry, dm.neglect_self, wing_of_line.p, factors.p, stream),
+            ck(launch_unit_matrix(row0_64.p, ctrl.p, N, dm.symmetry, dm.neglect_self, wing_of_line.p, factors.p,
+                                  factors_split.p, stream),
                "unit matrix");
             launches += 1;
         } else {
             const auto& q = setup.quasi_steady_wake;
             double wl = q.wake_length_factor * dm.rep_chord;
             ck(launch_horseshoe_matrix(dm, static_cast<int>(q.viscous_core_length.kind), q.viscous_core_length.value, wl,
-                                       qs_wake_vec.p, qs_rc.p, static_cast<int>(q.symmetry_condition), factors.p, stream),
+                                       qs_wake_vec.p, qs_rc.p, static_cast<int>(q.symmetry_condition), factors.p,
+                                       factors_split.p, stream),
                "horseshoe matrix");
             launches += 2;
             record(3);
@@ -854,6 +862,7 @@ struct sb_sim {
         SolveBuffers sb;
         sb.fixed = fixed.p;
         sb.factors = factors.p;
+        sb.factors_split = factors_split.p;
         sb.gamma_prev = gamma_p;
         sb.vel_out = vel_out.p;
         sb.scalars = scalars.p;
@@ -918,16 +927,28 @@ struct sb_sim {
     }
 
     // Forces and the output block (force_calculations.rs:669-698).
+    ForceJob force_job() const {
+        ForceJob j;
+        j.m = dm;
+        j.p = params;
+        j.f.gamma = gamma_p;
+        j.f.vel = vel_out.p;
+        j.f.hist0 = hist0.p;
+        j.f.hist1 = hist1.p;
+        j.f.fd_count = fd_count;
+        j.f.out = out.p;
+        j.f.scalars = scalars.p;
+        return j;
+    }
+
     void step_end() {
-        ForceArgs fa;
-        fa.gamma = gamma_p;
-        fa.vel = vel_out.p;
-        fa.hist0 = hist0.p;
-        fa.hist1 = hist1.p;
-        fa.fd_count = fd_count;
-        fa.out = out.p;
-        fa.scalars = scalars.p;
-        ck(launch_forces(dm, params, fa, stream), "forces");
+        const ForceJob j = force_job();
+        ck(launch_forces(j.m, j.p, j.f, stream), "forces");
+        after_forces();
+    }
+
+    // what follows the forces launch, also when a batch launches them for all its cases
+    void after_forces() {
         launches += 1;
         last_counters[5] = static_cast<double>(launches);
         fd_count += 1;
