@@ -16,6 +16,11 @@
  *
  * Threading: one handle owns one CUDA stream and its device memory. A handle is not
  * thread-safe; different handles may be driven from different host threads.
+ * Device pointers passed in: the call reads them after the work enqueued before it on the
+ * legacy default stream (stream 0, PyTorch's default stream) has finished, and is done
+ * with them (and has written device outputs) when it returns. A caller producing device
+ * inputs on another stream synchronises that stream first. (sb_panel_sweep_no_alloc takes
+ * the stream to work on and follows that stream's order instead.)
  * Errors: every entry point returns SB_OK (0) or a negative SB_ERR_* code; the
  * message of the last error on the calling thread is available from sb_last_error().
  */

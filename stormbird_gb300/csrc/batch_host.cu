@@ -657,6 +657,7 @@ struct sb_batch {
     void copy_warm_start_data(float* feat, float* target, size_t rows) {
         if (warm_mode == 0) raise(SB_ERR_STATE, "the batch records no warm-start data (mode 0)");
         if (static_cast<long long>(rows) != N_total) raise(SB_ERR_SIZE, "rows must equal the batch's span lines");
+        order_after_caller(main);  // the caller's buffers may still be in use on its stream
         if (feat)
             ck(cudaMemcpyAsync(feat, w_feat.p, rows * kMlpFeatures * sizeof(float), cudaMemcpyDefault, main), "copy");
         if (target) ck(cudaMemcpyAsync(target, w_target.p, rows * sizeof(float), cudaMemcpyDefault, main), "copy");
@@ -880,6 +881,7 @@ struct sb_batch {
 
     void do_step_device(double time, double dt, const double* fs_dev, size_t n) {
         if (static_cast<long long>(n) != nfs_total) raise(SB_ERR_SIZE, "freestream length mismatch");
+        order_after_caller(main);
         ck(cudaMemcpyAsync(fs_all.p, fs_dev, n * sizeof(d3), cudaMemcpyDeviceToDevice, main), "D2D freestream");
         step(time, dt);
     }
@@ -1077,6 +1079,7 @@ int sb_batch_set_initial_circulation_device(sb_batch* b, const double* gamma_dev
     if (!b || !gamma_dev) return null_arg();
     return guard([&] {
         if (static_cast<long long>(n) != b->N_total) raise(SB_ERR_SIZE, "circulation length mismatch");
+        order_after_caller(b->main);
         ck(cudaMemcpyAsync(b->gamma_all.p, gamma_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, b->main), "D2D");
         ck(cudaStreamSynchronize(b->main), "sync");
     });

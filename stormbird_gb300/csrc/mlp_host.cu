@@ -309,6 +309,7 @@ int sb_mlp_forward(sb_mlp* m, const float* x_dev, size_t rows, float* y_dev) {
     if (rows == 0) return SB_OK;
     return guard([&] {
         m->ensure(static_cast<long long>(rows), m->cap_train);
+        order_after_caller(m->stream);
         m->forward(x_dev, static_cast<long long>(rows), y_dev, nullptr, m->stream);
         m->check_err(m->stream);
     });
@@ -323,6 +324,7 @@ int sb_mlp_gradients(sb_mlp* m, const float* x_dev, const float* target_dev, siz
     }
     return guard([&] {
         m->ensure(static_cast<long long>(rows), true);
+        order_after_caller(m->stream);
         m->forward(x_dev, static_cast<long long>(rows), m->y_tmp.p, target_dev, m->stream);
         m->backward(static_cast<long long>(rows), m->stream);
         ck(cudaMemcpyAsync(grads_host, m->grads.p, m->n_params * sizeof(float), cudaMemcpyDeviceToHost, m->stream),
@@ -341,10 +343,13 @@ int sb_mlp_train_step(sb_mlp* m, const float* x_dev, const float* target_dev, si
     }
     return guard([&] {
         m->ensure(static_cast<long long>(rows), true);
+        order_after_caller(m->stream);
         m->forward(x_dev, static_cast<long long>(rows), m->y_tmp.p, target_dev, m->stream);
         m->backward(static_cast<long long>(rows), m->stream);
         m->adam(learning_rate, m->stream);
+        // the inputs are read by the time the call returns (the caller may reuse them)
         if (loss) *loss = m->read_loss(m->stream) / static_cast<double>(rows);
+        else m->check_err(m->stream);
     });
 }
 

@@ -75,6 +75,20 @@ struct DevBuf {
     }
 };
 
+// Device memory a caller passes in is read after the work the caller enqueued before the
+// call on the legacy default stream (where PyTorch's default stream and the runtime's
+// stream 0 both put their work): `s` waits on an event recorded there, without blocking the
+// host. Without it a handle's own (non-blocking) stream could read an input that a kernel
+// of the caller is still writing.
+inline void order_after_caller(cudaStream_t s) {
+    cudaEvent_t ev = nullptr;
+    ck(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
+    cudaError_t e = cudaEventRecord(ev, cudaStreamLegacy);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev, 0);
+    cudaEventDestroy(ev);
+    ck(e, "order after the caller's stream");
+}
+
 template <class T>
 struct PinnedBuf {
     T* p = nullptr;
@@ -1083,6 +1097,7 @@ struct sb_sim {
 
     void do_step_device(double time, double dt, const double* fs_dev, size_t n) {
         if (static_cast<long long>(n) != nfs) raise(SB_ERR_SIZE, "freestream length mismatch");
+        order_after_caller(stream);
         ck(cudaMemcpyAsync(fs_p, fs_dev, n * sizeof(d3), cudaMemcpyDeviceToDevice, stream), "D2D freestream");
         enqueue_step(time, dt);
         ck(cudaMemcpyAsync(h_err.p, err.p, sizeof(int), cudaMemcpyDeviceToHost, stream), "D2H status");
