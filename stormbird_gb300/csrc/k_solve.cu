@@ -43,6 +43,7 @@ namespace sbgpu {
 constexpr int kSolveThreads = 256;
 constexpr int kSolveRowsPerThread = 4;  // most rows per thread (1024 per CTA)
 constexpr int kMaxCluster = 8;
+constexpr double kSecondCandidateMargin = 0.5;  // warm-start guard, see si_solve
 
 int solve_cluster_size(int N) {
     if (N <= 64) return 1;
@@ -261,7 +262,11 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
     // and of each candidate (staged in G[1]). A candidate replaces the current start only
     // when both its mean residual (the solver's own measure) and its largest per-line term
     // are lower: the solver stops on the mean, which a start with its error on a few lines
-    // could pass while those lines are still off. The plain start wins ties.
+    // could pass while those lines are still off. The plain start wins ties. The second
+    // candidate (the network's) must beat the best start so far by kSecondCandidateMargin
+    // on both measures: its per-line error is noise-like, and a start that is only slightly
+    // better by the initial residual took more iterations than the extrapolation (566 of
+    // 2,560 solves of the uneven-case batch: 108 iterations against 107 from the plain start).
     if (b.candidate[0] || b.candidate[1]) {
         double best = 0.0, best_max = 0.0;
         int taken = 0;
@@ -305,7 +310,8 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
             if (v == 0) {
                 best = rv;
                 best_max = rmax;
-            } else if (isfinite(rv) && rv < best && rmax < best_max) {  // same decision in every CTA
+            } else if (isfinite(rv) && rv < (v == 2 ? kSecondCandidateMargin : 1.0) * best &&
+                       rmax < (v == 2 ? kSecondCandidateMargin : 1.0) * best_max) {  // same decision in every CTA
                 best = rv;
                 best_max = rmax;
                 taken = v;
