@@ -557,6 +557,31 @@ def run_profile_rollup(args):
                       "rollup_targets": c["rollup_targets"]}), flush=True)
 
 
+def run_profile_batch(args):
+    """The batched part's uneven cases (`--batch-cases`, default 512) stepped as one Batch
+    (graph replay, previous-step start) for 5 + `--batch-steps` steps. Prints the device time
+    of every step and the number of kernel launches of the last step, so an ncu launch list
+    can select it with -s <launches before it>."""
+    from stormbird_gb300 import Batch
+    from stormbird_gb300 import setups as S
+    from stormbird_gb300 import warm_start as WS
+
+    n, steps = args.batch_cases, 5 + args.batch_steps
+    cases = [(WS.tight_solver(js), w) for js, w in S.uneven_cases(n, seed=2024)]
+    winds = [w for _, w in cases]
+    b = Batch([js for js, _ in cases], device=0)
+    gpu_ms, host_ms = [], []
+    for k in range(steps):
+        fs = S.batch_freestream(b, winds, k * DT)
+        t0 = time.perf_counter()
+        b.do_step(time=k * DT, time_step=DT, freestream_velocity=fs)
+        host_ms.append((time.perf_counter() - t0) * 1e3)
+        gpu_ms.append(b.info()["last_step_ms"])
+    print(json.dumps({"mode": "profile-batch", "cases": n, "steps": steps, "step_gpu_ms": gpu_ms,
+                      "step_host_ms": host_ms, "pairs_last_step": b.info()["pairs"]}), flush=True)
+    b.close()
+
+
 def run_profile_mlp(args):
     """Warm-start network forward passes over 131,072 rows (1,024 GEMM tiles of 128 rows),
     three times, then one training step on 16,384 rows: 4 tensor-core GEMMs per forward pass
@@ -759,6 +784,8 @@ def main():
     ap.add_argument("--profile-rollup", action="store_true", help="short all-near run ending in a full roll-up")
     ap.add_argument("--rings", action="store_true", help="--profile-rollup without shared segments")
     ap.add_argument("--profile-mlp", action="store_true", help="warm-start network forward passes (GEMM capture)")
+    ap.add_argument("--profile-batch", action="store_true",
+                    help="the batched part's uneven cases stepped as one batch (launch-list capture)")
     ap.add_argument("--precision-study", action="store_true",
                     help="FP32 / compensated FP32 / FP64 sweeps of the 8 x 128 panel, 1000-row case")
     ap.add_argument("--rows", type=int, default=0, help="wake rows of the --kernel-only wake (default 300)")
@@ -782,6 +809,8 @@ def main():
         run_profile_rollup(args)
     elif args.profile_mlp:
         run_profile_mlp(args)
+    elif args.profile_batch:
+        run_profile_batch(args)
     elif args.impl == "reference":
         run_reference(args)
     elif args.qs_only:
