@@ -478,6 +478,41 @@ __global__ void k_bs_reduce(const double* partial, int n_chunks, long long M, lo
     out[i] = b;
 }
 
+// The same reduction when there are many chunks (a few targets against many panels, as the
+// control points against the whole wake: 1,200 chunks): one warp per target, the lanes
+// over chunks lane, lane + 32, ... in f64, then a fixed-order shuffle tree (deterministic).
+// A thread per target would walk the chunks one dependent L2 load after another.
+constexpr int kBsReduceWideChunks = 64;  // from this many chunks on
+__global__ void k_bs_reduce_wide(const double* partial, int n_chunks, long long M, long long M_total, const d3* base,
+                                 d3* out) {
+    const long long i = (blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= M_total) return;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    if (i < M) {
+#pragma unroll 4
+        for (int k = lane; k < n_chunks; k += 32) {
+            const double* p = partial + (static_cast<long long>(k) * M + i) * 3;
+            s0 += p[0];
+            s1 += p[1];
+            s2 += p[2];
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s0 += __shfl_down_sync(0xffffffffu, s0, o);
+            s1 += __shfl_down_sync(0xffffffffu, s1, o);
+            s2 += __shfl_down_sync(0xffffffffu, s2, o);
+        }
+    }
+    if (lane == 0) {
+        d3 b = base ? base[i] : mk(0, 0, 0);
+        b.x += s0;
+        b.y += s1;
+        b.z += s2;
+        out[i] = b;
+    }
+}
+
 // The same reduction for every job of a batched sweep: block b belongs to the last job whose
 // block_begin is at or before it.
 __global__ void __launch_bounds__(kBsReduceThreads) k_bs_reduce_jobs(const BsJob* jobs, int n_jobs) {
@@ -671,6 +706,11 @@ cudaError_t launch_bs_reduce(const double* partial, int n_chunks, long long M, l
                              cudaStream_t s) {
     if (M_total <= 0) return cudaSuccess;
     int threads = 256;
+    if (n_chunks >= kBsReduceWideChunks) {
+        const long long blocks = (M_total * 32 + threads - 1) / threads;
+        k_bs_reduce_wide<<<static_cast<unsigned>(blocks), threads, 0, s>>>(partial, n_chunks, M, M_total, base, out);
+        return cudaGetLastError();
+    }
     long long blocks = (M_total + threads - 1) / threads;
     k_bs_reduce<<<static_cast<unsigned>(blocks), threads, 0, s>>>(partial, n_chunks, M, M_total, base, out);
     return cudaGetLastError();
