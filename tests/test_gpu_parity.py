@@ -130,6 +130,19 @@ def test_quasi_steady_simple_iterative_single_wing(gpu_lib, oracle_mod):
     assert rg.iterations == ro.iterations
 
 
+def test_quasi_steady_simple_iterative_four_rows_per_thread(gpu_lib, oracle_mod):
+    """2,400 span lines: each CTA of the 8-CTA cluster owns 300 (> 256) lines, so the solve
+    runs the four-rows-per-thread variant; 30 fixed iterations against the oracle (the
+    double-float matrix-vector product keeps the f64 result to ~1e-13)."""
+    setup, u = S.quasi_steady_single_wing(nr_panels=2400)
+    g, o = pair(fixed_iterations(setup, 30), oracle_mod)
+    n = g.nr_freestream_points
+    rg = g.do_step(time=0.0, time_step=1.0, freestream_velocity=np.tile(u, (n, 1)))
+    ro = o.do_step(time=0.0, time_step=1.0, freestream_velocity=np.tile(u, (n, 1)))
+    check_step(0, rg, ro, tol=1e-9)
+    assert rg.iterations == ro.iterations == 30
+
+
 def test_quasi_steady_linearized_default(gpu_lib, oracle_mod):
     lfm = S.rectangular_wing(5.0, 1.2, math.radians(2.0), 64)
     setup = S.simulation(lfm, dynamic=False)
