@@ -352,9 +352,12 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
                     const float gam = v[kRec32Gamma];
                     if (gam == 0.f) continue;  // uniform across the CTA
                     const float ff2 = v[31];
-                    const float2 ex = add2(sub2s(X2h, v[28]), sub2s(X2l, v[32]));
-                    const float2 ey = add2(sub2s(Y2h, v[29]), sub2s(Y2l, v[33]));
-                    const float2 ez = add2(sub2s(Z2h, v[30]), sub2s(Z2l, v[34]));
+                    // target - centre from the hi parts alone: enough for the near/far test and
+                    // the far-field doublet (at least ff_ratio panel sizes away, where its
+                    // relative error stays near FP32 rounding); the ring below adds the lo parts
+                    float2 ex = sub2s(X2h, v[28]);
+                    float2 ey = sub2s(Y2h, v[29]);
+                    float2 ez = sub2s(Z2h, v[30]);
                     float2 e2 = bc(0.f);
                     bool n0 = true, n1 = true;
                     if (ff2 != CUDART_INF_F) {  // panel.rs:53-57; uniform per panel
@@ -385,6 +388,10 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
                         TZ = fma2(s, fma2(h3, ez, mul2(e2s, bc(-nz))), TZ);
                     }
                     if (any_near) {  // vortex ring (panel.rs:99-118)
+                        // float-float difference: (x_hi - c_hi) + (x_lo - c_lo)
+                        ex = add2(ex, sub2s(X2l, v[32]));
+                        ey = add2(ey, sub2s(Y2l, v[33]));
+                        ez = add2(ez, sub2s(Z2l, v[34]));
                         float2 ax, ay, az;
                         ring2(v, ex, ey, ez, ax, ay, az);
                         const float g4 = gam * static_cast<float>(kFourPiInv);
