@@ -390,16 +390,18 @@ def batched_solves(args, device):
     from stormbird_gb300 import warm_start as WS
 
     n, warm, steps = args.batch_cases, 5, args.batch_steps
-    cases = [(WS.tight_solver(js), w) for js, w in S.uneven_cases(n, seed=2024)]
+    tol = args.batch_tolerance
+    cases = [(WS.tight_solver(js, residual_tolerance=tol), w) for js, w in S.uneven_cases(n, seed=2024)]
     winds = [w for _, w in cases]
     out = {"workload": f"{n} uneven dynamic cases (AWA 20-180 deg, 5-20 m/s, 1-6 sails, 16-96 panels, "
-                       f"50-400 wake rows, far_field_ratio 5, SimpleIterative to residual 1e-7), "
+                       f"50-400 wake rows, far_field_ratio 5, SimpleIterative to residual {tol:g}), "
                        f"steps {warm}-{warm + steps - 1} from a cold start",
            "cases": n, "timed_steps": steps}
 
     # train the network on other seeds
     t0 = time.perf_counter()
-    X, T = WS.collect([(WS.tight_solver(js), w) for js, w in S.uneven_cases(args.train_cases, seed=77)],
+    X, T = WS.collect([(WS.tight_solver(js, residual_tolerance=tol), w)
+                       for js, w in S.uneven_cases(args.train_cases, seed=77)],
                       steps=warm + steps, device=device)
     t_collect = time.perf_counter() - t0
     net = WS.WarmStartNet(WS.FEATURES, seed=1, device=device)
@@ -567,7 +569,7 @@ def run_profile_batch(args):
     from stormbird_gb300 import warm_start as WS
 
     n, steps = args.batch_cases, 5 + args.batch_steps
-    cases = [(WS.tight_solver(js), w) for js, w in S.uneven_cases(n, seed=2024)]
+    cases = [(WS.tight_solver(js, residual_tolerance=args.batch_tolerance), w) for js, w in S.uneven_cases(n, seed=2024)]
     winds = [w for _, w in cases]
     b = Batch([js for js, _ in cases], device=0)
     gpu_ms, host_ms = [], []
@@ -791,6 +793,8 @@ def main():
     ap.add_argument("--rows", type=int, default=0, help="wake rows of the --kernel-only wake (default 300)")
     ap.add_argument("--batch-cases", type=int, default=512, help="uneven cases of the batched solves/s part (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=5, help="timed steps of the batched part")
+    ap.add_argument("--batch-tolerance", type=float, default=1e-7,
+                    help="SimpleIterative mean-residual tolerance of the batched part's cases")
     ap.add_argument("--train-cases", type=int, default=128, help="cases whose solves train the warm-start network")
     ap.add_argument("--train-epochs", type=int, default=40)
     ap.add_argument("--qs-cases", type=int, default=512, help="cases of the quasi-steady sweep part (0: skip)")

@@ -273,6 +273,14 @@ __global__ void k_wake_panels(DevModel m, WakeBuffers w, int shift) {
     if (shift) g = (s == 0) ? w.str_old[j] : w.str_old[id - N];
     else g = w.str_old[id];
     w.str_new[id] = g;
+    // A panel of zero strength is skipped by every sweep (induced_velocity_calc.rs:203): only
+    // its strength slot matters, so its record is not rebuilt. While a wake fills (the first
+    // W steps) that is every row past the newest strengths; row 0 (the frozen-wake matrix)
+    // and the FP64 records are always built.
+    if (g == 0.0 && s != 0 && !w.rec64) {
+        w.rec32[id].v[kRec32Gamma] = 0.f;
+        return;
+    }
     PanelRec<double> q;
     const bool need64 = (s == 0) || w.rec64;
     write_panel_records(pp, m.panel_core[id], g, m.far_field_ratio, wg, &w.rec32[id], need64 ? &q : nullptr);
