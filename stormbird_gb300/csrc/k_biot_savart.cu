@@ -575,6 +575,108 @@ __global__ void k_unit_matrix(const PanelRec<double>* row0, const d3* ctrl, int 
     store_factor(factors, split, N, id, c, p, u);
 }
 
+// The same matrix from the FP32 panel records of row 0, two control points per thread as the
+// lanes of the sweep's f32x2 arithmetic (the per-pair rule of panel.rs:53-57, vortex ring or
+// point doublet, exactly as k_bs_sweep evaluates it). A control point lies on the bound
+// vortex of its own panel, where the reference's 1e-10 cut-off decides a segment: that entry
+// (c == p) is evaluated in FP64 as in k_unit_matrix. The other entries carry FP32 rounding,
+// like the frozen-wake sweep over the rows behind.
+__device__ __forceinline__ void split2(double a, double b, float2& h, float2& l) {
+    const float ha = static_cast<float>(a), hb = static_cast<float>(b);
+    h = make_float2(ha, hb);
+    l = make_float2(static_cast<float>(a - static_cast<double>(ha)), static_cast<float>(b - static_cast<double>(hb)));
+}
+__device__ __forceinline__ void panel_unit2(const float* v, float2 X2h, float2 Y2h, float2 Z2h, float2 X2l, float2 Y2l,
+                                            float2 Z2l, float2& ux, float2& uy, float2& uz) {
+    float2 ex = sub2s(X2h, v[28]), ey = sub2s(Y2h, v[29]), ez = sub2s(Z2h, v[30]);
+    const float ff2 = v[31];
+    float2 e2 = bc(0.f);
+    bool n0 = true, n1 = true;
+    if (ff2 != CUDART_INF_F) {
+        e2 = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
+        n0 = e2.x <= ff2;
+        n1 = e2.y <= ff2;
+    }
+    ux = uy = uz = bc(0.f);
+    if (!n0 || !n1) {  // point doublet (panel.rs:82-96), unit strength
+        const float2 e2s = make_float2(n0 ? 1.f : e2.x, n1 ? 1.f : e2.y);
+        const float2 ir = make_float2(rsqrt_n(fmaxf(e2s.x, FLT_MIN)), rsqrt_n(fmaxf(e2s.y, FLT_MIN)));
+        const float2 ir2 = mul2(ir, ir);
+        const float2 sm = make_float2(n0 ? 0.f : v[35], n1 ? 0.f : v[35]);
+        const float2 sd = mul2(sm, mul2(mul2(ir2, ir2), ir));
+        const float nx = v[36], ny = v[37], nz = v[38];
+        const float2 h3 = mul2(bc(3.f), fma2(ex, bc(nx), fma2(ey, bc(ny), mul2(ez, bc(nz)))));
+        ux = mul2(sd, fma2(h3, ex, mul2(e2s, bc(-nx))));
+        uy = mul2(sd, fma2(h3, ey, mul2(e2s, bc(-ny))));
+        uz = mul2(sd, fma2(h3, ez, mul2(e2s, bc(-nz))));
+    }
+    if (n0 || n1) {  // vortex ring (panel.rs:99-118), unit strength
+        ex = add2(ex, sub2s(X2l, v[32]));
+        ey = add2(ey, sub2s(Y2l, v[33]));
+        ez = add2(ez, sub2s(Z2l, v[34]));
+        float2 ax, ay, az;
+        ring2(v, ex, ey, ez, ax, ay, az);
+        const float g4 = static_cast<float>(kFourPiInv);
+        const float2 gm = make_float2(n0 ? g4 : 0.f, n1 ? g4 : 0.f);
+        ux = fma2(gm, ax, ux);
+        uy = fma2(gm, ay, uy);
+        uz = fma2(gm, az, uz);
+    }
+}
+
+__global__ void k_unit_matrix_f32(const PanelRec<float>* row0_32, const PanelRec<double>* row0, const d3* ctrl, int N,
+                                  int sym, int neglect, const int* wing_of_line, d3* factors, float2* split) {
+    const long long id = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+    const int pairs = (N + 1) / 2;
+    if (id >= static_cast<long long>(pairs) * N) return;
+    const int cp = static_cast<int>(id / N), p = static_cast<int>(id % N);
+    const int c0 = 2 * cp, c1 = min(c0 + 1, N - 1);  // an odd N repeats the last control point
+    const d3 x0 = ctrl[c0], x1 = ctrl[c1];
+    float2 Xh, Yh, Zh, Xl, Yl, Zl;
+    split2(x0.x, x1.x, Xh, Xl);
+    split2(x0.y, x1.y, Yh, Yl);
+    split2(x0.z, x1.z, Zh, Zl);
+    const float* v = row0_32[p].v;
+    float2 ux, uy, uz;
+    panel_unit2(v, Xh, Yh, Zh, Xl, Yl, Zl, ux, uy, uz);
+    if (sym) {  // symmetry_condition.rs:27-43: the mirrored control points
+        float2 mx, my, mz;
+        const float2 nXh = mul2(Xh, bc(-1.f)), nXl = mul2(Xl, bc(-1.f)), nYh = mul2(Yh, bc(-1.f)),
+                     nYl = mul2(Yl, bc(-1.f)), nZh = mul2(Zh, bc(-1.f)), nZl = mul2(Zl, bc(-1.f));
+        if (sym == 1) panel_unit2(v, nXh, Yh, Zh, nXl, Yl, Zl, mx, my, mz);
+        else if (sym == 2) panel_unit2(v, Xh, nYh, Zh, Xl, nYl, Zl, mx, my, mz);
+        else panel_unit2(v, Xh, Yh, nZh, Xl, Yl, nZl, mx, my, mz);
+        if (sym == 1) {
+            ux = add2(ux, mul2(mx, bc(-1.f)));
+            uy = add2(uy, my);
+            uz = add2(uz, mz);
+        } else if (sym == 2) {
+            ux = add2(ux, mx);
+            uy = add2(uy, mul2(my, bc(-1.f)));
+            uz = add2(uz, mz);
+        } else {
+            ux = add2(ux, mx);
+            uy = add2(uy, my);
+            uz = add2(uz, mul2(mz, bc(-1.f)));
+        }
+    }
+    const float uxa[2] = {ux.x, ux.y}, uya[2] = {uy.x, uy.y}, uza[2] = {uz.x, uz.y};
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {
+        const int c = l == 0 ? c0 : c1;
+        if (l == 1 && c1 == c0) break;
+        d3 u = mk(uxa[l], uya[l], uza[l]);
+        if (neglect && wing_of_line[c] == wing_of_line[p]) {
+            u = mk(0, 0, 0);
+        } else if (c == p) {
+            const d3 x = ctrl[c];
+            u = panel_unit_f64(row0[p].v, x);
+            if (sym) u = sym_correct(sym, u, panel_unit_f64(row0[p].v, mirror(sym, x)));
+        }
+        store_factor(factors, split, N, static_cast<long long>(c) * N + p, c, p, u);
+    }
+}
+
 // Quasi-steady wake: core length and wake vectors (frozen_wake.rs:74-100). One CTA: the
 // span line lengths and the wake vectors in parallel (FP64 square roots and divisions are
 // slow on this part, so a serial loop over them costs microseconds per line), the mean
@@ -729,8 +831,16 @@ cudaError_t launch_bs_reduce_jobs(const BsJob* jobs, int n_jobs, long long block
     return cudaGetLastError();
 }
 
-cudaError_t launch_unit_matrix(const PanelRec<double>* row0, const d3* ctrl, int N, int sym, int neglect,
-                               const int* wing_of_line, d3* factors, float2* split, cudaStream_t s) {
+cudaError_t launch_unit_matrix(const PanelRec<double>* row0, const PanelRec<float>* row0_32, const d3* ctrl, int N,
+                               int sym, int neglect, const int* wing_of_line, d3* factors, float2* split, cudaStream_t s) {
+    if (row0_32) {
+        const long long tot = static_cast<long long>((N + 1) / 2) * N;
+        const int threads = 128;
+        const long long blocks = (tot + threads - 1) / threads;
+        k_unit_matrix_f32<<<static_cast<unsigned>(blocks), threads, 0, s>>>(row0_32, row0, ctrl, N, sym, neglect,
+                                                                            wing_of_line, factors, split);
+        return cudaGetLastError();
+    }
     long long tot = static_cast<long long>(N) * N;
     int threads = 128;
     long long blocks = (tot + threads - 1) / threads;

@@ -61,8 +61,10 @@ cudaError_t launch_bs_reduce_jobs(const BsJob* jobs, int n_jobs, long long block
 // solver) and/or as f32 (hi, lo) pairs (`split`, [N][3][N] float2: row c, component, column;
 // hi = the nearest float, lo = the nearest float of the remainder, for the SimpleIterative
 // solver's matrix-vector products). Either pointer may be null.
-cudaError_t launch_unit_matrix(const PanelRec<double>* row0, const d3* ctrl, int N, int sym, int neglect,
-                               const int* wing_of_line, d3* factors, float2* split, cudaStream_t s);
+// Frozen-wake unit matrix of the first wake row: from the FP32 row-0 records when row0_32 is
+// given (k_unit_matrix_f32; the control point's own panel in FP64), else all in FP64.
+cudaError_t launch_unit_matrix(const PanelRec<double>* row0, const PanelRec<float>* row0_32, const d3* ctrl, int N,
+                               int sym, int neglect, const int* wing_of_line, d3* factors, float2* split, cudaStream_t s);
 // Quasi-steady horseshoe matrix; core_kind 0 relative, 1 absolute, 2 none.
 cudaError_t launch_horseshoe_matrix(const DevModel& m, int core_kind, double core_value, double wake_length, d3* wake_vec,
                                     double* rc_dev, int sym, d3* factors, float2* split, cudaStream_t s);

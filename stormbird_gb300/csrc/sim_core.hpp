@@ -855,7 +855,9 @@ struct sb_sim {
     // The frozen wake's matrix: unit first-row panels (dynamic) or horseshoes (quasi-steady).
     void step_matrix() {
         if (dynamic) {
-            ck(launch_unit_matrix(row0_64.p, ctrl.p, N, dm.symmetry, dm.neglect_self, wing_of_line.p, factors.p,
+            // FP32 records unless the sweeps run in FP64
+            ck(launch_unit_matrix(row0_64.p, precision == 2 ? nullptr : rec32.p, ctrl.p, N, dm.symmetry, dm.neglect_self,
+                                  wing_of_line.p, factors.p,
                                   factors_split.p, stream),
                "unit matrix");
             launches += 1;
