@@ -73,6 +73,32 @@ def test_training_lowers_the_loss(gpu_lib):
     assert final < 0.05 * first, (first, final)
 
 
+def test_training_reads_rows_after_the_callers_stream(gpu_lib):
+    """A training step reads rows PyTorch has just gathered on its default stream: the call
+    orders its own stream after that work, so stepping straight after the gather gives the
+    same losses and parameters as synchronising first."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(9)
+    X = torch.from_numpy(rng.normal(size=(262144, 16)).astype(np.float32)).cuda()
+    T = torch.from_numpy(rng.normal(size=262144).astype(np.float32)).cuda()
+    g = torch.Generator(device=X.device)
+    runs = []
+    for sync in (False, True):
+        net = _net(seed=13)
+        g.manual_seed(4)
+        losses = []
+        for _ in range(3):
+            perm = torch.randperm(X.shape[0], device=X.device, generator=g)
+            Xs, Ts = X[perm].contiguous(), T[perm].contiguous()  # gathered on PyTorch's stream
+            if sync:
+                torch.cuda.synchronize()
+            losses.append(net.train_step(Xs[:8192], Ts[:8192], 1e-3))
+            del Xs, Ts
+        runs.append((losses, net.get_params()))
+    assert runs[0][0] == runs[1][0]
+    assert np.array_equal(runs[0][1], runs[1][1])
+
+
 def test_warm_start_on_held_out_cases(gpu_lib):
     pytest.importorskip("torch")
     from stormbird_gb300 import setups as S
