@@ -117,10 +117,13 @@ def test_full_size_wing_sail_row_sampled(gpu_lib, oracle_mod, ffr):
     targets = pts[idx]
     ug = g.induced_velocities(targets)
     uo = oracle_mod.bs_sweep(corners, np.full(len(strengths), 1.0), strengths, ffr, targets, nthreads=8)
-    assert rel_inf(ug, uo) < 2e-6
+    # FP32 sweep against f64: 307,200 segment evaluations per target when every pair is
+    # near-field; with the default far-field ratio most pairs are point doublets instead
+    tol = 2e-6 if ffr < 1e15 else 4e-6
+    assert rel_inf(ug, uo) < tol
     # velocity_at_points = freestream + induced (update_data.rs:125-141), last step's freestream
     u_fs = wind.velocity(0.05 * (rows + 4))
-    assert rel_inf(vel[idx], ug + u_fs) < 1e-6
+    assert rel_inf(vel[idx], ug + u_fs) < tol / 2
 
 
 def test_quasi_steady_simple_iterative_single_wing(gpu_lib, oracle_mod):
