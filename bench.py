@@ -379,7 +379,9 @@ def batched_solves(args, device):
     `warm` steps, then times `steps` steps on the host clock through the public call,
     host freestream in and results out:
       plain   — one Simulation per case, sb_sim_do_step per case and step;
-      batched — one Batch, sb_batch_do_step (CUDA graph replay after 3 steps);
+      batched — one Batch, sb_batch_do_step (CUDA graph replay after 3 steps); with
+                `--tune-seconds` > 0 every batched arm first lets sb_batch_autotune pick the
+                roll-up work decomposition (untimed) on the state before the timed steps;
       extrapolation — the Batch with candidate starts from linear extrapolation in time;
       warm    — the Batch with the learned warm start (extrapolation + network correction),
                 the network trained first on data the batched solver records for other
@@ -437,9 +439,10 @@ def batched_solves(args, device):
 
     ex_net = WS.extrapolation_only(device)
     for mode, mnet in (("batched", None), ("extrapolation", ex_net), ("warm", net)):
-        r = WS.run_batch(cases, warm + steps, mnet, DT, device, timed_from=warm)
+        r = WS.run_batch(cases, warm + steps, mnet, DT, device, timed_from=warm, tune_seconds=args.tune_seconds)
         results[mode] = {"seconds": r["seconds"], "gamma": r["gamma"][-1],
-                         "iterations": float(np.mean(r["iterations"][warm:])), "start": r["start"][warm:]}
+                         "iterations": float(np.mean(r["iterations"][warm:])), "start": r["start"][warm:],
+                         "tune_seconds": r["tune_seconds"], "tuning": r["tuning"]}
     ex_net.close()
 
     def worst(a, ref):
@@ -460,6 +463,7 @@ def batched_solves(args, device):
                    "extrapolation": "batched, candidate = linear extrapolation in time (network output zero)",
                    "warm": "batched, candidates = extrapolation and extrapolation + trained network correction; "
                            "the solve starts from the lowest-residual of plain / extrapolation / network"}
+    out["autotune"] = {m: {"seconds": results[m]["tune_seconds"], **results[m]["tuning"]} for m in arms}
     out["timing"] = "host clock around each public call, host freestream in, circulation and force summary out"
     return out
 
@@ -795,6 +799,8 @@ def main():
     ap.add_argument("--rows", type=int, default=0, help="wake rows of the --kernel-only wake (default 300)")
     ap.add_argument("--batch-cases", type=int, default=512, help="uneven cases of the batched solves/s part (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=5, help="timed steps of the batched part")
+    ap.add_argument("--tune-seconds", type=float, default=0.0,
+                    help="autotuner budget of each batched arm before its timed steps (0: default plan)")
     ap.add_argument("--batch-tolerance", type=float, default=1e-8,
                     help="SimpleIterative mean-residual tolerance of the batched part's cases")
     ap.add_argument("--train-cases", type=int, default=128, help="cases whose solves train the warm-start network")

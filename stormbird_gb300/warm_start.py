@@ -180,11 +180,13 @@ def extrapolation_only(device: int = 0) -> WarmStartNet:
 
 
 def run_batch(cases, steps: int, net: WarmStartNet | None = None, dt: float = 0.05, device: int = 0,
-              timed_from: int = 1) -> dict:
+              timed_from: int = 1, tune_seconds: float = 0.0) -> dict:
     """Steps the cases as one batch (warm-started when `net` is given) on their freestream.
 
-    Returns per step the circulation, iterations and start taken of every case, and the host
-    time of steps timed_from.. (one solve = one case advanced by one step).
+    Returns per step the circulation, iterations and start taken of every case, the host
+    time of steps timed_from.. (one solve = one case advanced by one step) and, with
+    tune_seconds > 0, the time the autotuner took before step timed_from (untimed; it
+    needs 4 steps of wake, so timed_from >= 4).
     """
     import time
 
@@ -192,8 +194,12 @@ def run_batch(cases, steps: int, net: WarmStartNet | None = None, dt: float = 0.
     b = Batch([js for js, _ in cases], device=device)
     if net is not None:
         _check(lib().sb_batch_set_warm_start(b._h, net.handle, 1))
-    its, taken, gam, t_run = [], [], [], 0.0
+    its, taken, gam, t_run, t_tune = [], [], [], 0.0, 0.0
     for k in range(steps):
+        if tune_seconds > 0.0 and k == timed_from and k >= 4:
+            t0 = time.perf_counter()
+            b.autotune(tune_seconds)
+            t_tune = time.perf_counter() - t0
         fs = S.batch_freestream(b, winds, k * dt)
         t0 = time.perf_counter()
         b.do_step(time=k * dt, time_step=dt, freestream_velocity=fs)
@@ -204,8 +210,10 @@ def run_batch(cases, steps: int, net: WarmStartNet | None = None, dt: float = 0.
         taken.append(s[:, 10].copy())
         g = b.circulation()
         gam.append([g[b.case_slice(i)] for i in range(b.n_cases)])
+    info = b.info()
     b.close()
-    return {"iterations": np.array(its), "start": np.array(taken), "gamma": gam, "seconds": t_run}
+    return {"iterations": np.array(its), "start": np.array(taken), "gamma": gam, "seconds": t_run,
+            "tune_seconds": t_tune, "tuning": {k: info[k] for k in ("waves", "blocks_per_sm", "tuned")}}
 
 
 def max_rel_diff(a, ref) -> float:
