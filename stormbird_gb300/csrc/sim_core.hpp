@@ -186,7 +186,7 @@ inline int num_sms(int device) {
 
 
 // Work decomposition of one sweep: target tiles x source chunks, with enough work items
-// for ~4 waves of the persistent grid (sweep kernels in k_biot_savart.cu).
+// for ~16 waves of the persistent grid (sweep kernels in k_biot_savart.cu).
 struct SweepPlan {
     int grid = 1, n_chunks = 1, chunk = 0;
     long long n_ttiles = 0;
@@ -200,7 +200,10 @@ inline SweepPlan make_sweep_plan(long long M, long long P, int precision, int sy
     int tile = bs_tile_panels(precision);
     int occ = bs_occupancy_blocks_per_sm(precision, sym, neglect);
     long long slots = static_cast<long long>(sms) * occ;
-    long long want = 4 * slots;
+    // ~16 items per persistent CTA: a roll-up item (256 targets x a source chunk) runs for
+    // milliseconds, and with 4 the last wave left SMs idle (4-wave plan 17.42 ms, 16 waves
+    // 16.71 ms, 32 and 64 no better for the 4 x 64 panel, 300-row roll-up)
+    long long want = 16 * slots;
     long long max_chunks = std::max<long long>(1, (P + tile - 1) / tile);
     long long nc = (want + sp.n_ttiles - 1) / std::max<long long>(1, sp.n_ttiles);
     nc = std::min(std::max<long long>(nc, 1), max_chunks);
