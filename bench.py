@@ -749,10 +749,12 @@ def run_reference(args):
         "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * float(np.mean(secs)), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic", "impl": "reference",
-        "config": workload_config({"sample": "each step: a seeded random sample of wake points, ~1.5 s of work"}),
+        "config": workload_config({"parallelism": f"{ws} independent replica(s), one per GPU"}),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": cb["sample"] + " (C++ f64 restatement of the reference algorithm; "
-                                                  "the Rust reference cannot be built here)"},
+                         "sample": "each step a seeded random sample of wake points (~1.5 s of work) against every "
+                                   "panel of the workload's 300-row wake; last step: " + cb["sample"] +
+                                   " (C++ f64 restatement of the reference algorithm, OpenMP over targets as the "
+                                   "reference's rayon loop; the Rust reference cannot be built here)"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -810,6 +812,13 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.impl == "reference":
+        # the reference arm runs the oracle alone: the CUDA library is neither built nor loaded
+        from oracle import build as oracle_build
+
+        oracle_build.build()
+        run_reference(args)
+        return
     import __graft_entry__
 
     __graft_entry__.build()
@@ -823,8 +832,6 @@ def main():
         run_profile_mlp(args)
     elif args.profile_batch:
         run_profile_batch(args)
-    elif args.impl == "reference":
-        run_reference(args)
     elif args.qs_only:
         print(json.dumps({"mode": "qs-sweep", **qs_sweep(args, 0)}), flush=True)
     else:

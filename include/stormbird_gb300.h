@@ -259,9 +259,11 @@ int sb_panel_sweep(int device, const double* corners, const double* strengths, c
  * that each GPU loading the library holds until the process exits. At most
  * SB_NO_ALLOC_MAX_PANELS panels and SB_NO_ALLOC_MAX_TARGETS targets per call (larger
  * sizes: SB_ERR_SIZE). Work is enqueued on `stream` (a cudaStream_t, NULL = the legacy
- * default stream) and the call returns when it has finished. The first call on a device
- * resolves the array's device address; make that first call before any stream capture.
- * Every call shares the array: calls that overlap on the GPU race and must be serialised.
+ * default stream) and the call returns when it has finished; the caller's current device is
+ * the same after the call as before it. The first call on a device (and the first after
+ * that device's context has been reset) resolves the array's device address; make that
+ * first call before any stream capture begins. Every call shares the array: calls that
+ * overlap on the GPU race and must be serialised.
  */
 #define SB_NO_ALLOC_MAX_PANELS 16384
 #define SB_NO_ALLOC_MAX_TARGETS 65536
@@ -277,6 +279,21 @@ int sb_panel_sweep_no_alloc(int device, const double* corners, const double* str
 int sb_measure_fp32_peak(int device, int reps, double* tflops);
 /* The same for FP64 FMAs (the denominator of the FP64 sweep of the precision study). */
 int sb_measure_fp64_peak(int device, int reps, double* tflops);
+
+/*
+ * Failure path of the bounded device-side waits (diagnostics with no counterpart in the
+ * reference, whose CPU loops have no waits). Every wait of a kernel on an asynchronous copy
+ * polls a bounded number of times; when it runs out the kernel records the timeout, waits
+ * (bounded again) for its copies still in flight, leaves, and the call returns
+ * SB_ERR_TIMEOUT with the device context still usable.
+ * sb_set_sweep_wait_polls: polls of each tile wait of the Biot-Savart sweeps launched after
+ * it, process-wide (0: every sweep's first wait runs out at once; < 0 restores the default,
+ * 2^22). sb_wait_timeout_self_test: one CTA waits, with `polls` polls, on an mbarrier armed
+ * for bytes no copy delivers; returns SB_ERR_TIMEOUT when the wait ran out and the kernel
+ * returned (the expected outcome).
+ */
+int sb_set_sweep_wait_polls(int polls);
+int sb_wait_timeout_self_test(int device, int polls);
 
 /* ===================================================================================
  * Batched cases. The reference runs independent cases (apparent-wind sweeps, differing

@@ -55,6 +55,7 @@ def lib() -> ctypes.CDLL:
         L.sbo_sigmoid.argtypes = [c_double, c_double, c_double]
         L.sbo_foil_eval.argtypes = [ctypes.c_char_p, c_double, dp]
         L.sbo_bs_sweep.argtypes = [dp, dp, dp, c_size_t, c_double, dp, c_size_t, dp, c_int]
+        L.sbo_bs_sweep_sym.argtypes = [dp, dp, dp, c_size_t, c_double, c_int, dp, c_size_t, dp, c_int]
         L.sbo_sim_wind_freestream.argtypes = [c_void_p, ctypes.c_char_p, ctypes.c_char_p, c_double, c_double, dp,
                                               c_size_t]
         L.sbo_wind_velocity_at.argtypes = [ctypes.c_char_p, ctypes.c_char_p, dp, c_size_t, c_double, c_double, dp]
@@ -213,10 +214,15 @@ def wind_velocity_at(environment_json: str, condition_json: str, points, time: f
     return out
 
 
-def bs_sweep(corners, cores, strengths, far_field_ratio, targets, nthreads=1) -> np.ndarray:
+def bs_sweep(corners, cores, strengths, far_field_ratio, targets, nthreads=1, symmetry=0) -> np.ndarray:
     c = _d(corners).reshape(-1, 12)
     t = vec3_array(targets)
     out = np.zeros_like(t)
+    if symmetry:
+        _check(lib().sbo_bs_sweep_sym(as_ptr(c), as_ptr(_d(cores)), as_ptr(_d(strengths)), c.shape[0],
+                                      float(far_field_ratio), int(symmetry), as_ptr(t), t.shape[0], as_ptr(out),
+                                      int(nthreads)))
+        return out
     _check(lib().sbo_bs_sweep(as_ptr(c), as_ptr(_d(cores)), as_ptr(_d(strengths)), c.shape[0], float(far_field_ratio),
                               as_ptr(t), t.shape[0], as_ptr(out), int(nthreads)))
     return out

@@ -315,6 +315,36 @@ int sbo_bs_sweep(const double* corners, const double* cores, const double* stren
     return SB_OK;
 }
 
+// The same sweep with a symmetry condition (0 none, 1 X, 2 Y, 3 Z): each panel's unit velocity
+// at x is corrected by its velocity at the mirrored point (induced_velocity_calc.rs:182-198,
+// symmetry_condition.rs:27-43).
+int sbo_bs_sweep_sym(const double* corners, const double* cores, const double* strengths, size_t P,
+                     double far_field_ratio, int symmetry, const double* targets, size_t M, double* out, int nthreads) {
+    if (symmetry < 0 || symmetry > 3) return fail(SB_ERR_SIZE, "symmetry must be 0..3");
+    const auto sym = static_cast<sbsetup::Symmetry>(symmetry);
+    std::vector<sbo::Panel> pans(P);
+    for (size_t j = 0; j < P; ++j) {
+        sbo::V3 p[4];
+        for (int i = 0; i < 4; ++i) p[i] = {corners[12 * j + 3 * i], corners[12 * j + 3 * i + 1], corners[12 * j + 3 * i + 2]};
+        pans[j] = sbo::Panel(p, far_field_ratio, cores[j]);
+    }
+    const long long mm = static_cast<long long>(M);
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads < 1 ? 1 : nthreads)
+    for (long long i = 0; i < mm; ++i) {
+        sbo::V3 x{targets[3 * i], targets[3 * i + 1], targets[3 * i + 2]};
+        sbo::V3 acc, m;
+        const bool mirrored = sbo::mirrored_point(sym, x, &m);
+        for (size_t j = 0; j < P; ++j) {
+            if (strengths[j] == 0.0) continue;
+            sbo::V3 u = pans[j].unit(x);
+            if (mirrored) u = sbo::corrected_velocity(sym, u, pans[j].unit(m));
+            acc = acc + strengths[j] * u;
+        }
+        out[3 * i] = acc.x; out[3 * i + 1] = acc.y; out[3 * i + 2] = acc.z;
+    }
+    return SB_OK;
+}
+
 // CompleteSailModel steady-state conditions (sb_oracle_controller.hpp)
 void* sbo_csm_new(const char* json) {
     if (!json) { fail(SB_ERR_NULL_ARG, "setup_json is NULL"); return nullptr; }

@@ -19,6 +19,7 @@
 // k_unit_matrix: the unit-strength influence of the first-row panels at the control
 // points (frozen_wake.rs:198-249), in FP64: the control point lies on its own bound
 // vortex, where the reference's 1e-10 closeness cut-off must fire exactly as in f64.
+#include <atomic>
 #include <cfloat>
 #include <cstdio>
 #include <math_constants.h>
@@ -260,7 +261,9 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
     while (true) {
         __syncthreads();  // every thread is done with the previous item's s_item and s_job
         if (tid == 0) {
-            const long long it = static_cast<long long>(atomicAdd(a.work_counter, 1ULL));
+            // once a wait of any CTA has run out the launch's results are void: take no more items
+            const bool stop = *reinterpret_cast<volatile const int*>(a.err) == kDevTimeout;
+            const long long it = stop ? n_items : static_cast<long long>(atomicAdd(a.work_counter, 1ULL));
             s_item = it;
             if (it < n_items) s_job = a.jobs ? a.jobs[find_job(a.jobs, a.n_jobs, it)] : a.job0;
         }
@@ -324,11 +327,12 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
         for (int k = 0; k < ntiles; ++k) {
             const int buf = k & 1;
             if (tid == 0 && k + 1 < ntiles) issue(k + 1);
+            bool waited;
             if (buf == 0) {
-                mbar_wait_bounded(&bar[0], phase0, a.err);
+                waited = mbar_wait_bounded(&bar[0], phase0, a.err, a.wait_polls);
                 phase0 ^= 1;
             } else {
-                mbar_wait_bounded(&bar[1], phase1, a.err);
+                waited = mbar_wait_bounded(&bar[1], phase1, a.err, a.wait_polls);
                 phase1 ^= 1;
             }
             const int np = static_cast<int>(min(static_cast<long long>(TILE), pe - (pb + static_cast<long long>(k) * TILE)));
@@ -439,7 +443,17 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
                     sz[t] += tz[t];
                 }
             }
-            __syncthreads();  // the buffer is refilled in the next-but-one tile
+            // The buffer is refilled in the next-but-one tile. If a wait of this tile ran out
+            // in any thread (its copy may still be landing; the sums above are void), thread 0
+            // waits, again bounded, for the copies of tiles k and k + 1, and the CTA leaves:
+            // no copy is in flight into its shared memory when it exits.
+            if (__syncthreads_or(!waited)) {
+                if (tid == 0) {
+                    mbar_wait_bounded(&bar[buf], (buf == 0 ? phase0 : phase1) ^ 1u, a.err);
+                    if (k + 1 < ntiles) mbar_wait_bounded(&bar[buf ^ 1], buf == 0 ? phase1 : phase0, a.err);
+                }
+                return;
+            }
         }
 
 #pragma unroll
@@ -781,7 +795,14 @@ static cudaError_t launch_sym(const BsArgs& a, int grid, cudaStream_t s) {
 int bs_targets_per_thread(int symmetry) { return symmetry == 0 ? 2 : 1; }
 int bs_tile_panels(int precision) { return precision == 2 ? TileSize<double>::value : TileSize<float>::value; }
 
-cudaError_t launch_bs_sweep(const BsArgs& a, int precision, int grid, cudaStream_t s) {
+static std::atomic<int> g_sweep_wait_polls{-1};
+
+void set_sweep_wait_polls(int polls) { g_sweep_wait_polls.store(polls < 0 ? -1 : polls); }
+
+cudaError_t launch_bs_sweep(const BsArgs& args, int precision, int grid, cudaStream_t s) {
+    BsArgs a = args;
+    const int polls = g_sweep_wait_polls.load();
+    if (polls >= 0) a.wait_polls = polls;
     if (a.chain) {
         if (precision == 2 || a.neglect) return cudaErrorInvalidValue;
         return precision == 1 ? launch_chain<false>(a, grid, s) : launch_chain<true>(a, grid, s);

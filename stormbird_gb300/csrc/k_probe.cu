@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include "sb_kernels.h"
+#include "sb_ptx.cuh"
 
 namespace sbgpu {
 
@@ -54,6 +55,26 @@ static double measure_peak(int device, int reps, int iters) {
     cudaEventDestroy(e1);
     cudaFree(out);
     return err == cudaSuccess ? best : -1.0;
+}
+
+// Failure path of the bounded waits: thread 0 arms an mbarrier for 16 bytes of a copy that is
+// never issued, so its phase cannot complete; every thread's bounded wait runs out after
+// `polls` polls and records kDevTimeout, and the kernel returns. Nothing is in flight into
+// shared memory when the CTA exits.
+__global__ void __launch_bounds__(128) k_wait_probe(int polls, int* err) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+        mbar_expect_tx(&bar, 16);  // the single arrival, with 16 bytes still expected
+    }
+    __syncthreads();
+    mbar_wait_bounded(&bar, 0, err, polls);
+}
+
+cudaError_t launch_wait_probe(int polls, int* err, cudaStream_t s) {
+    k_wait_probe<<<1, 128, 0, s>>>(polls, err);
+    return cudaGetLastError();
 }
 
 double measure_fp32_peak(int device, int reps) { return measure_peak<float>(device, reps, 4096); }

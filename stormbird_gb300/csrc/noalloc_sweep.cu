@@ -12,6 +12,15 @@
 // counter and the error word are cleared on every call, the records and partial sums are
 // fully rewritten. Calls that overlap on the GPU (two streams, or two host threads) race on
 // it and must be serialised by the caller.
+//
+// Host code cannot use the array's name as a device address, so the entry point resolves the
+// address once per device, with that device current, by cudaGetSymbolAddress (set-up on the
+// first call). A context reset (cudaDeviceReset) reloads the module and can move the array,
+// so the resolved address is kept together with the identity of the context it belongs to
+// and resolved again when the device's current context has changed.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <cstdint>
 #include <mutex>
@@ -34,14 +43,57 @@ constexpr size_t kScratchBytes = kRecordBytes + kPartialBytes + kControlBytes;
 
 static __device__ __align__(256) unsigned char g_sweep_scratch[kScratchBytes];
 
-// Device address of g_sweep_scratch per device (host code may not use the symbol itself).
+// Resolved address of g_sweep_scratch per device, and the id of the context it was resolved in.
+struct Resolved {
+    unsigned long long ctx_id = 0;
+    unsigned char* addr = nullptr;
+};
 std::mutex g_mu;
-unsigned char* g_addr[256] = {nullptr};
+Resolved g_resolved[256];
 
 int fail(int code, const std::string& m) {
     report_error(code, m);  // sb_last_error / sb_last_status
     return code;
 }
+
+int ok() {
+    report_error(SB_OK, "");
+    return SB_OK;
+}
+
+// Id of the calling thread's current context (cuCtxGetId, unique for the life of the
+// process), through the runtime's driver entry points; 0 when it cannot be read.
+unsigned long long current_context_id() {
+    static const auto fns = [] {
+        std::pair<PFN_cuCtxGetCurrent_v4000, PFN_cuCtxGetId_v12000> f{nullptr, nullptr};
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            f.first = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(p);
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            f.second = reinterpret_cast<PFN_cuCtxGetId_v12000>(p);
+        return f;
+    }();
+    if (!fns.first || !fns.second) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (fns.first(&ctx) != CUDA_SUCCESS || !ctx || fns.second(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// The caller's current device, restored when the call returns.
+struct RestoreDevice {
+    int dev = -1;
+    RestoreDevice() {
+        if (cudaGetDevice(&dev) != cudaSuccess) dev = -1;
+    }
+    ~RestoreDevice() {
+        if (dev >= 0) cudaSetDevice(dev);
+    }
+};
 
 }  // namespace
 
@@ -57,21 +109,25 @@ extern "C" int sb_panel_sweep_no_alloc(int device, const double* corners, const 
                                      " panels and " + std::to_string(kMaxTargets) + " targets per call (got " +
                                      std::to_string(n_panels) + " panels, " + std::to_string(n_targets) + " targets)");
     if (device < 0 || device >= 256) return fail(SB_ERR_SIZE, "device ordinal out of range");
-    if (n_targets == 0) return SB_OK;
+    if (n_targets == 0) return ok();
+    RestoreDevice restore;
     cudaError_t e = cudaSetDevice(device);
     if (e != cudaSuccess) return fail(SB_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
     unsigned char* base = nullptr;
     {
-        // once per device, with that device current
+        // set-up, once per device (again after a context reset), with that device current
         std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_addr[device]) {
+        Resolved& r = g_resolved[device];
+        const unsigned long long id = current_context_id();
+        if (!r.addr || id == 0 || id != r.ctx_id) {
             void* p = nullptr;
             e = cudaGetSymbolAddress(&p, g_sweep_scratch);
             if (e != cudaSuccess || !p)
                 return fail(SB_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-            g_addr[device] = static_cast<unsigned char*>(p);
+            r.addr = static_cast<unsigned char*>(p);
+            r.ctx_id = id;
         }
-        base = g_addr[device];
+        base = r.addr;
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     PanelRec<float>* rec = reinterpret_cast<PanelRec<float>*>(base);
@@ -91,7 +147,7 @@ extern "C" int sb_panel_sweep_no_alloc(int device, const double* corners, const 
     if (P == 0) {
         if (!check(launch_bs_reduce(nullptr, 0, 0, M, nullptr, reinterpret_cast<d3*>(velocities), st), "reduce"))
             return SB_ERR_CUDA;
-        return check(cudaStreamSynchronize(st), "sweep") ? SB_OK : SB_ERR_CUDA;
+        return check(cudaStreamSynchronize(st), "sweep") ? ok() : SB_ERR_CUDA;
     }
     if (!check(launch_panels_from_corners(corners, strengths, core_lengths, P, far_field_ratio, rec, nullptr, st),
                "panel records"))
@@ -135,6 +191,5 @@ extern "C" int sb_panel_sweep_no_alloc(int device, const double* corners, const 
     if (!check(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st), "read error word")) return SB_ERR_CUDA;
     if (!check(cudaStreamSynchronize(st), "sweep")) return SB_ERR_CUDA;
     if (herr == kDevTimeout) return fail(SB_ERR_TIMEOUT, "a bounded device-side wait ran out");
-    report_error(SB_OK, "");
-    return SB_OK;
+    return ok();
 }

@@ -282,4 +282,7 @@ struct StepParams {
 // Error word written by kernels whose bounded waits ran out (0 = none).
 enum DeviceError : int { kDevOk = 0, kDevTimeout = 1, kDevSingular = 2 };
 
+// Polls a bounded device-side wait makes before it gives up and records kDevTimeout.
+constexpr int kWaitPolls = 1 << 22;
+
 }  // namespace sbgpu

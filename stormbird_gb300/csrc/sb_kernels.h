@@ -44,7 +44,16 @@ struct BsArgs {
     int symmetry = 0;
     int neglect = 0;
     int chain = 0;  // the sources are chain records (FP32 only, no neglect-self)
+    int wait_polls = kWaitPolls;  // polls of each bounded wait on a tile copy
 };
+
+// Polls of the bounded tile waits of later sweep launches (launch_bs_sweep overrides
+// BsArgs::wait_polls with it when >= 0; < 0 = each launch's own value). Process-wide;
+// exists so that a test can make the waits run out.
+void set_sweep_wait_polls(int polls);
+// One CTA waiting, with `polls` polls, on an mbarrier that expects bytes no copy delivers:
+// the wait runs out, *err gets kDevTimeout and the kernel returns (k_probe.cu).
+cudaError_t launch_wait_probe(int polls, int* err, cudaStream_t s);
 
 constexpr int kBsReduceThreads = 256;
 

@@ -33,9 +33,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait: gives up after a fixed number of polls and records kDevTimeout.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err) {
-    for (int i = 0; i < (1 << 22); ++i)
+// Bounded wait: gives up after `polls` polls (kWaitPolls unless a launch passes fewer; 0
+// gives up at once) and records kDevTimeout in *err.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err, int polls = kWaitPolls) {
+    for (int i = 0; i < polls; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     atomicExch(err, kDevTimeout);
     return false;

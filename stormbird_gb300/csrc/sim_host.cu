@@ -294,7 +294,10 @@ int sb_panel_sweep(int device, const double* corners, const double* strengths, c
         g_last_status = SB_ERR_SIZE;
         return SB_ERR_SIZE;
     }
-    if (n_targets == 0) return SB_OK;
+    if (n_targets == 0) {
+        report_error(SB_OK, "");
+        return SB_OK;
+    }
     return guard([&] {
         panel_sweep_impl(device, corners, strengths, core_lengths, static_cast<long long>(n_panels), far_field_ratio,
                          symmetry, targets, static_cast<long long>(n_targets), precision, velocities);
@@ -315,6 +318,34 @@ int sb_measure_fp64_peak(int device, int reps, double* tflops) {
     if (v < 0.0) { g_last_error = "FP64 probe failed"; return SB_ERR_CUDA; }
     *tflops = v;
     return SB_OK;
+}
+
+// Bounded-wait diagnostics (see include/stormbird_gb300.h).
+int sb_set_sweep_wait_polls(int polls) {
+    set_sweep_wait_polls(polls);
+    report_error(SB_OK, "");
+    return SB_OK;
+}
+
+int sb_wait_timeout_self_test(int device, int polls) {
+    if (polls < 0) {
+        report_error(SB_ERR_SIZE, "polls must be >= 0");
+        return SB_ERR_SIZE;
+    }
+    return guard([&] {
+        ck(cudaSetDevice(device), "cudaSetDevice");
+        cudaStream_t st;
+        ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+        StreamBufs B(st);
+        int* derr = B.get<int>(1);
+        int herr = 0;
+        ck(cudaMemsetAsync(derr, 0, sizeof(int), st), "memset");
+        ck(launch_wait_probe(polls, derr, st), "wait probe");
+        ck(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H");
+        ck(cudaStreamSynchronize(st), "wait probe");
+        if (herr == kDevTimeout) raise(SB_ERR_TIMEOUT, "a bounded device-side wait ran out");
+        if (herr != kDevOk) raise(SB_ERR_CUDA, "device error word " + std::to_string(herr));
+    });
 }
 
 }  // extern "C"

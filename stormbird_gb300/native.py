@@ -60,6 +60,8 @@ SIGNATURES = [
                                                ctypes.c_int, _vp, ctypes.c_size_t, _vp, _vp]),
     ("sb_measure_fp32_peak", ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp]),
     ("sb_measure_fp64_peak", ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp]),
+    ("sb_set_sweep_wait_polls", ctypes.c_int, [ctypes.c_int]),
+    ("sb_wait_timeout_self_test", ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     ("sb_batch_new", _vp, [ctypes.POINTER(ctypes.c_char_p), ctypes.c_size_t, ctypes.c_int]),
     ("sb_batch_free", None, [_vp]),
     ("sb_batch_sizes", ctypes.c_int, [_vp, _szp, _szp, _szp]),
