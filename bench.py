@@ -203,6 +203,30 @@ def cpu_baseline_sweep(points, strengths, target_seconds=8.0, seed=0):
 
 
 # --------------------------------------------------------------------------------------
+# parity at full size: the benchmark's next step on the GPU and in the oracle, same state
+# --------------------------------------------------------------------------------------
+def full_size_parity(sim, fs, t):
+    """Loads the GPU simulation's state (sb_sim_get_state) into the oracle and takes the next
+    step in both with the same freestream; relative circulation and total-force errors of
+    that step (the oracle leaves the step's roll-up out: it does not enter the step's outputs)."""
+    from oracle.binding import OracleSimulation
+
+    t0 = time.perf_counter()
+    o = OracleSimulation(setup_json(), nthreads=os.cpu_count() or 1)
+    o.set_state(sim.state())
+    o.skip_next_rollup()
+    ro = o.do_step(time=t, time_step=DT, freestream_velocity=fs)
+    rg = sim.do_step(time=t, time_step=DT, freestream_velocity=fs)
+    g_ref, f_ref = ro.circulation_strength, ro.integrated_forces_sum()
+    return {"rel_circulation_error": float(np.max(np.abs(rg.circulation_strength - g_ref)) / np.max(np.abs(g_ref))),
+            "rel_force_error": float(np.linalg.norm(rg.integrated_forces_sum() - f_ref) / np.linalg.norm(f_ref)),
+            "iterations": {"gpu": int(rg.iterations), "oracle": int(ro.iterations)},
+            "tolerance": 1e-5,
+            "how": f"step {int(sim.state()[0])} of the benchmark's wake (76,800 rings) from the GPU's state, "
+                   f"oracle (C++ f64 restatement) from the same state; {time.perf_counter() - t0:.1f} s"}
+
+
+# --------------------------------------------------------------------------------------
 # GB300 arm
 # --------------------------------------------------------------------------------------
 def read_traffic():
@@ -282,6 +306,13 @@ def run_gb300(args):
     inter_all = allreduce_sum(ws, inter, dev)
     value = inter_all / (total_ms_max * 1e-3)
 
+    # ---- parity of the benchmark's own next step against the oracle from the same state
+    parity = None
+    if rank == 0 and not args.no_cpu_baseline:
+        parity = full_size_parity(sim, fs_host(t), t)
+        k += 1
+        t = k * DT
+
     # ---- e2e: host buffers through sb_sim_do_step
     e2e_times = []
     for _ in range(args.steps):
@@ -347,6 +378,8 @@ def run_gb300(args):
         "clocks": clk.summary(),
         "breakdown_ms": {k2: v for k2, v in sim.last_step_timing().items()},
     }
+    if parity is not None:
+        line["parity"] = parity
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cb, _ = cpu_baseline_sweep(pts, strengths)
         line["cpu_baseline"] = cb

@@ -155,6 +155,24 @@ int sb_sim_wake_sizes(const sb_sim* sim, size_t* nr_wake_points, size_t* nr_wake
 int sb_sim_get_wake_state(sb_sim* sim, double* points_xyz, double* strengths, double* velocities_xyz);
 
 /*
+ * The state a step reads from the steps before it, as one f64 array: what the public fields
+ * of the reference's Simulation (simulation.rs:20-28: previous_circulation_strength,
+ * flow_derivatives, first_time_step_completed) and DynamicWake (wake/dynamic_wake/mod.rs:41-64:
+ * points, velocity_at_points, strengths, number_of_time_steps_completed) hold, which Rust code
+ * reads and assigns directly (Simulation derives Clone). Layout: [0] wake time steps
+ * completed, [1] first time step completed (0/1), [2] flow-derivative updates, then for a
+ * dynamic wake the points [nr_wake_points*3], the velocity at the points [nr_wake_points*3]
+ * and the panel strengths [nr_wake_panels], then the previous circulation [N] and the two
+ * stored control-point velocities of the flow derivatives [2*N*3]. Rigid-body motion and wing
+ * angles are not included (their setters above set them). n must equal sb_sim_state_size.
+ * A state taken from one simulation and set on another built from the same setup makes its
+ * next step compute what the first one's next step would.
+ */
+int sb_sim_state_size(const sb_sim* sim, size_t* n);
+int sb_sim_get_state(sb_sim* sim, double* state, size_t n);
+int sb_sim_set_state(sb_sim* sim, const double* state, size_t n);
+
+/*
  * Biot-Savart precision variant used by the Biot-Savart sweeps of this handle:
  * 0 = FP32 with compensated (Kahan) accumulation (default), 1 = plain FP32,
  * 2 = FP64. Kept as a switch for the precision study.
@@ -166,7 +184,9 @@ int sb_sim_set_precision(sb_sim* sim, int precision_mode);
  * [0] whole step, [1] wake update, [2] free-wake sweep at control points (with its
  * reduction), [3] unit-strength matrix, [4] circulation solve, [5] wake roll-up sweep
  * (with its reduction), [6] forces, [7] roll-up sweep kernel alone, [8] control-point
- * sweep kernel alone. Only filled when enabled with sb_sim_enable_timing(sim, 1).
+ * sweep kernel alone, [9] wake-point advection kernel, [10] wake panel-record kernel,
+ * [11] chain-record kernel (shared-segment roll-up; 0 when the step built none); n <= 12.
+ * Only filled when enabled with sb_sim_enable_timing(sim, 1).
  */
 int sb_sim_enable_timing(sb_sim* sim, int enable);
 int sb_sim_last_step_timing(const sb_sim* sim, double* ms, size_t n);
@@ -341,6 +361,12 @@ int sb_batch_get_circulation(const sb_batch* batch, double* circulation, size_t 
 int sb_batch_get_summary(const sb_batch* batch, double* summary, size_t n);
 /* Full output block of case i for the last step (as sb_sim_read_output). */
 int sb_batch_read_case_output(sb_batch* batch, size_t i, sb_step_output* out);
+/* State of case i after the last step, in the layout of sb_sim_get_state (n = its size), and
+ * the same to load a state into case i (a batch of the same setups can so start where
+ * another stopped; the cases of a batch step together, so load every case's state). */
+int sb_batch_case_state_size(const sb_batch* batch, size_t i, size_t* n);
+int sb_batch_get_case_state(sb_batch* batch, size_t i, double* state, size_t n);
+int sb_batch_set_case_state(sb_batch* batch, size_t i, const double* state, size_t n);
 /* Initial solution of the next step's solve for every case (the reference's
  * previous_circulation_strength, simulation.rs:165,189): the warm-start hook. */
 int sb_batch_set_initial_circulation(sb_batch* batch, const double* circulation, size_t n_total);

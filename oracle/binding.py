@@ -55,6 +55,10 @@ def lib() -> ctypes.CDLL:
         L.sbo_sigmoid.argtypes = [c_double, c_double, c_double]
         L.sbo_foil_eval.argtypes = [ctypes.c_char_p, c_double, dp]
         L.sbo_bs_sweep.argtypes = [dp, dp, dp, c_size_t, c_double, dp, c_size_t, dp, c_int]
+        L.sbo_sim_state_size.argtypes = [c_void_p, ctypes.POINTER(c_size_t)]
+        L.sbo_sim_get_state.argtypes = [c_void_p, dp, c_size_t]
+        L.sbo_sim_set_state.argtypes = [c_void_p, dp, c_size_t]
+        L.sbo_sim_skip_next_rollup.argtypes = [c_void_p]
         L.sbo_bs_sweep_sym.argtypes = [dp, dp, dp, c_size_t, c_double, c_int, dp, c_size_t, dp, c_int]
         L.sbo_sim_wind_freestream.argtypes = [c_void_p, ctypes.c_char_p, ctypes.c_char_p, c_double, c_double, dp,
                                               c_size_t]
@@ -159,6 +163,23 @@ class OracleSimulation:
         _check(lib().sbo_sim_wind_freestream(self._h, environment_json.encode(), condition_json.encode(), float(time),
                                              float(ship_velocity), as_ptr(out), out.shape[0]))
         return out
+
+    def state(self) -> np.ndarray:
+        """State between steps, in the GPU library's sb_sim_get_state layout."""
+        n = ctypes.c_size_t()
+        _check(lib().sbo_sim_state_size(self._h, ctypes.byref(n)))
+        out = np.zeros(n.value)
+        _check(lib().sbo_sim_get_state(self._h, as_ptr(out), out.size))
+        return out
+
+    def set_state(self, state):
+        a = _d(state).reshape(-1)
+        _check(lib().sbo_sim_set_state(self._h, as_ptr(a), a.size))
+
+    def skip_next_rollup(self):
+        """The next step leaves the wake's induced velocity out of the velocity at the wake
+        points (harness option: that step's circulation and forces do not depend on it)."""
+        _check(lib().sbo_sim_skip_next_rollup(self._h))
 
     def wake_state(self):
         npts, npan, nspan, W = (ctypes.c_size_t() for _ in range(4))

@@ -629,6 +629,10 @@ struct DynamicWake {
     bool neglect_self = false;
     size_t steps_completed = 0;
     int nthreads = 1;
+    // Harness option, not in the reference: the next update_velocity_at_points keeps the
+    // freestream only (no induced velocity), for checks of one step's circulation and forces,
+    // which do not depend on the O(points x panels) roll-up sweep at the end of that step.
+    bool skip_induced_once = false;
 
     size_t nr_points() const { return nr_points_along_span * nr_points_per_line; }
     size_t nr_panels() const { return nr_panels_along_span * nr_panels_per_line; }
@@ -711,7 +715,9 @@ struct DynamicWake {
     void update_velocity_at_points(const V3* fs) {
         for (size_t i = 0; i < points.size(); ++i) velocity_at_points[i] = fs[i];
         size_t e = std::min(end_index, points.size());
-        if (e > 0 && steps_completed > 2) {
+        const bool skip = skip_induced_once;
+        skip_induced_once = false;
+        if (e > 0 && steps_completed > 2 && !skip) {
             std::vector<V3> u = induced_velocities(points.data(), e);
             for (size_t i = 0; i < e; ++i) velocity_at_points[i] += u[i];
         }

@@ -174,6 +174,72 @@ int sbo_sim_set_previous_circulation(void* h, const double* g, size_t n) {
     return SB_OK;
 }
 
+// State between steps, in the layout of the library's sb_sim_get_state: [0] wake steps
+// completed, [1] first step completed, [2] flow-derivative updates, then (dynamic) wake points,
+// velocity at the points, strengths, then previous circulation and the flow-derivative
+// history h0, h1 (the public fields of simulation.rs:20-28 and dynamic_wake/mod.rs:41-64).
+int sbo_sim_state_size(void* h, size_t* n) {
+    if (!h || !n) return fail(SB_ERR_NULL_ARG, "null argument");
+    const auto& sim = static_cast<OracleSim*>(h)->sim;
+    const size_t N = sim.lfm.nr_span_lines();
+    *n = 3 + (sim.dynamic ? sim.wake.points.size() * 6 + sim.wake.strengths.size() : 0) + 7 * N;
+    return SB_OK;
+}
+
+int sbo_sim_get_state(void* h, double* o, size_t n) {
+    size_t need = 0;
+    if (sbo_sim_state_size(h, &need) != SB_OK || !o) return fail(SB_ERR_NULL_ARG, "null argument");
+    if (n != need) return fail(SB_ERR_SIZE, "state size mismatch");
+    const auto& sim = static_cast<OracleSim*>(h)->sim;
+    o[0] = sim.dynamic ? static_cast<double>(sim.wake.steps_completed) : 0.0;
+    o[1] = sim.first_step_completed ? 1.0 : 0.0;
+    o[2] = static_cast<double>(sim.fd.count);
+    double* p = o + 3;
+    auto put = [&](const std::vector<sbo::V3>& v) {
+        for (const auto& x : v) { p[0] = x.x; p[1] = x.y; p[2] = x.z; p += 3; }
+    };
+    if (sim.dynamic) {
+        put(sim.wake.points);
+        put(sim.wake.velocity_at_points);
+        for (double g : sim.wake.strengths) *p++ = g;
+    }
+    for (double g : sim.previous_circulation) *p++ = g;
+    put(sim.fd.h0);
+    put(sim.fd.h1);
+    return SB_OK;
+}
+
+int sbo_sim_set_state(void* h, const double* s, size_t n) {
+    size_t need = 0;
+    if (sbo_sim_state_size(h, &need) != SB_OK || !s) return fail(SB_ERR_NULL_ARG, "null argument");
+    if (n != need) return fail(SB_ERR_SIZE, "state size mismatch");
+    auto& sim = static_cast<OracleSim*>(h)->sim;
+    const double* p = s + 3;
+    auto get = [&](std::vector<sbo::V3>& v) {
+        for (auto& x : v) { x = {p[0], p[1], p[2]}; p += 3; }
+    };
+    sim.first_step_completed = s[1] != 0.0;
+    sim.fd.count = static_cast<size_t>(s[2]);
+    if (sim.dynamic) {
+        sim.wake.steps_completed = static_cast<size_t>(s[0]);
+        get(sim.wake.points);
+        get(sim.wake.velocity_at_points);
+        for (double& g : sim.wake.strengths) g = *p++;
+        sim.wake.update_panel_data();
+    }
+    for (double& g : sim.previous_circulation) g = *p++;
+    get(sim.fd.h0);
+    get(sim.fd.h1);
+    return SB_OK;
+}
+
+// Harness option: the next step's wake-velocity update keeps the freestream only.
+int sbo_sim_skip_next_rollup(void* h) {
+    if (!h) return fail(SB_ERR_NULL_ARG, "null handle");
+    static_cast<OracleSim*>(h)->sim.wake.skip_induced_once = true;
+    return SB_OK;
+}
+
 int sbo_sim_wake_sizes(void* h, size_t* npts, size_t* npan, size_t* nspan, size_t* W) {
     if (!h) return fail(SB_ERR_NULL_ARG, "null handle");
     auto& sim = static_cast<OracleSim*>(h)->sim;

@@ -109,6 +109,18 @@ class Batch:
         _check(lib().sb_batch_read_case_output(self._h, int(i), ctypes.byref(buf.struct)))
         return buf.to_result(time)
 
+    def case_state(self, i: int) -> np.ndarray:
+        """State of case i after the last step (the layout of Simulation.state())."""
+        n = ctypes.c_size_t()
+        _check(lib().sb_batch_case_state_size(self._h, int(i), ctypes.byref(n)))
+        out = np.zeros(n.value)
+        _check(lib().sb_batch_get_case_state(self._h, int(i), as_ptr(out), out.size))
+        return out
+
+    def set_case_state(self, i: int, state):
+        a = np.ascontiguousarray(np.asarray(state, dtype=np.float64).reshape(-1))
+        _check(lib().sb_batch_set_case_state(self._h, int(i), as_ptr(a), a.size))
+
     def set_initial_circulation(self, circulation):
         a = np.ascontiguousarray(np.asarray(circulation, dtype=np.float64).reshape(-1))
         _check(lib().sb_batch_set_initial_circulation(self._h, as_ptr(a), a.size))

@@ -130,6 +130,14 @@ struct sb_batch {
     // forces of every case, one launch (refilled each step: step parameters can change)
     PinnedBuf<ForceJob> h_force_jobs;
     DevBuf<ForceJob> d_force_jobs;
+    // geometry, wake update, unit-strength matrix and chain records of the dynamic cases past
+    // their first step: one launch per kind for all of them (refilled each step: the jobs
+    // name the step's wake buffers and time step)
+    std::vector<char> case_batched;  // per case, in the current step
+    PinnedBuf<CaseStepJob> h_case_jobs;
+    DevBuf<CaseStepJob> d_case_jobs;
+    int n_case_jobs = 0;
+    long long blk_advect = 0, blk_panels = 0, blk_matrix = 0, blk_chain = 0;
 
     // Sweep work lists: group = (sweep kind, symmetry, neglect); one launch each.
     struct Group {
@@ -304,6 +312,9 @@ struct sb_batch {
         }
         h_force_jobs.alloc(cases.size());
         d_force_jobs.alloc(cases.size());
+        case_batched.assign(cases.size(), 0);
+        h_case_jobs.alloc(cases.size());
+        d_case_jobs.alloc(cases.size());
         counters.alloc(16);
         err.alloc(1);
         ck(cudaMemset(err.p, 0, sizeof(int)), "memset");
@@ -522,20 +533,36 @@ struct sb_batch {
         if (wind)
             ck(cudaMemcpyAsync(wind_steps.p, h_wind_steps.p, cases.size() * 2 * sizeof(double), cudaMemcpyHostToDevice, main),
                "H2D wind steps");
+        if (n_case_jobs > 0)
+            ck(cudaMemcpyAsync(d_case_jobs.p, h_case_jobs.p, n_case_jobs * sizeof(CaseStepJob), cudaMemcpyHostToDevice,
+                               main),
+               "H2D case jobs");
         fork(0);
-        for (auto& c : cases) {
-            if (wind) c->enqueue_wind_freestream();  // complete_sail_model/mod.rs:213-257
-            c->step_begin(time, dt);
+        for (size_t i = 0; i < cases.size(); ++i) {
+            sb_sim& c = *cases[i];
+            if (wind) c.enqueue_wind_freestream();  // complete_sail_model/mod.rs:213-257
+            if (case_batched[i]) c.step_begin_host(time, dt);
+            else c.step_begin(time, dt);
         }
         join(0);
+        if (n_case_jobs > 0) {  // geometry, then wake advection and panels, of the batched cases
+            ck(launch_prep_geometry_jobs(d_case_jobs.p, n_case_jobs, main), "batched geometry");
+            ck(launch_wake_jobs(d_case_jobs.p, n_case_jobs, blk_advect, blk_panels, main), "batched wake update");
+        }
         if (warm_mode != 0) warm_start_before_solve();
         sweeps(0);
         for (auto& c : cases) if (c->dynamic) c->after_fixed_sweep();
+        if (n_case_jobs > 0) ck(launch_unit_matrix_jobs(d_case_jobs.p, n_case_jobs, blk_matrix, main), "batched unit matrix");
         fork(1);
         for (size_t i = 0; i < cases.size(); ++i) {
             sb_sim& c = *cases[i];
-            if (c.linearized_quasi_steady() || si_batched[i]) c.step_matrix();
-            else c.step_matrix_and_solve();
+            if (case_batched[i]) {
+                if (!si_batched[i]) c.step_solve();  // matrix and chain records come from the batch
+            } else if (c.linearized_quasi_steady() || si_batched[i]) {
+                c.step_matrix();
+            } else {
+                c.step_matrix_and_solve();
+            }
         }
         join(1);
         // the batched solves: a launch per Linearized plan shape and per SimpleIterative
@@ -559,13 +586,15 @@ struct sb_batch {
         }
         // what follows a solve in its case (chain records of the wake), after the batched solves
         bool after = false;
-        for (size_t i = 0; i < cases.size(); ++i) after = after || si_batched[i];
+        for (size_t i = 0; i < cases.size(); ++i) after = after || (si_batched[i] && !case_batched[i]);
         if (after) {
             fork(1);
             for (size_t i = 0; i < cases.size(); ++i)
-                if (si_batched[i]) cases[i]->step_after_solve();
+                if (si_batched[i] && !case_batched[i]) cases[i]->step_after_solve();
             join(1);
         }
+        if (n_case_jobs > 0 && blk_chain > 0)
+            ck(launch_chain_records_jobs(d_case_jobs.p, n_case_jobs, blk_chain, main), "batched chain records");
         if (warm_mode != 0)
             ck(launch_batch_targets(gamma_all.p, w_q.p, w_g0.p, w_tr.p, N_total, w_target.p, main), "warm-start targets");
         sweeps(1);
@@ -697,6 +726,7 @@ struct sb_batch {
         // the parity of the wake buffers at the start of the step selects the graph
         const int parity = any_dynamic ? first_dynamic().cur : (steps & 1);
         ck(cudaEventRecord(ev_t0, main), "event");
+        fill_case_jobs(time, dt);
         if (use_graph && steady()) {
             // job lists of this step, read by the graph's copy node at launch
             fill_jobs_after_begin();
@@ -753,6 +783,16 @@ struct sb_batch {
         }
     }
 
+    // Loads case i's state (sb_sim_set_state layout). Every dynamic case of a batch must be
+    // at the same wake-buffer parity and step count for the batched step; a state taken from
+    // another batch's case i at the same step keeps that.
+    void set_case_state(size_t i, const double* state, size_t n) {
+        ck(cudaStreamSynchronize(main), "sync");
+        sb_sim& c = *cases[i];
+        c.set_state(state, n);
+        drop_graphs();
+    }
+
     const sb_sim& first_dynamic() const {
         for (const auto& c : cases) if (c->dynamic) return *c;
         return *cases[0];
@@ -760,6 +800,27 @@ struct sb_batch {
 
     // The work lists describe the sweeps as they will be after step_begin (which swaps the
     // wake buffers): compute them with the parity flipped for the duration.
+    // The job of every dynamic case past its first step (state before the step).
+    void fill_case_jobs(double time, double dt) {
+        n_case_jobs = 0;
+        blk_advect = blk_panels = blk_matrix = blk_chain = 0;
+        for (size_t i = 0; i < cases.size(); ++i) {
+            const sb_sim& c = *cases[i];
+            case_batched[i] = c.batch_kernels_ok() ? 1 : 0;
+            if (!case_batched[i]) continue;
+            CaseStepJob j = c.step_job(time, dt);
+            j.blk_advect = blk_advect;
+            j.blk_panels = blk_panels;
+            j.blk_matrix = blk_matrix;
+            j.blk_chain = blk_chain;
+            blk_advect += wake_advect_blocks(c.dm);
+            blk_panels += wake_panels_blocks(c.dm);
+            blk_matrix += unit_matrix_blocks(c.N, j.row0_32 != nullptr);
+            blk_chain += chain_records_blocks(j.chain_n);
+            h_case_jobs.p[n_case_jobs++] = j;
+        }
+    }
+
     void fill_jobs_after_begin() {
         for (auto& c : cases) if (c->dynamic) c->cur ^= 1;
         fill_jobs();
@@ -1064,6 +1125,34 @@ int sb_batch_read_case_output(sb_batch* b, size_t i, sb_step_output* out) {
         return SB_ERR_SIZE;
     }
     return guard([&] { b->cases[i]->read_output(out); });
+}
+
+int sb_batch_case_state_size(const sb_batch* b, size_t i, size_t* n) {
+    if (!b || !n) return null_arg();
+    if (i >= b->cases.size()) {
+        report_error(SB_ERR_SIZE, "case index out of range");
+        return SB_ERR_SIZE;
+    }
+    *n = b->cases[i]->state_size();
+    return SB_OK;
+}
+
+int sb_batch_get_case_state(sb_batch* b, size_t i, double* state, size_t n) {
+    if (!b || !state) return null_arg();
+    if (i >= b->cases.size()) {
+        report_error(SB_ERR_SIZE, "case index out of range");
+        return SB_ERR_SIZE;
+    }
+    return guard([&] { b->cases[i]->get_state(state, n); });
+}
+
+int sb_batch_set_case_state(sb_batch* b, size_t i, const double* state, size_t n) {
+    if (!b || !state) return null_arg();
+    if (i >= b->cases.size()) {
+        report_error(SB_ERR_SIZE, "case index out of range");
+        return SB_ERR_SIZE;
+    }
+    return guard([&] { b->set_case_state(i, state, n); });
 }
 
 int sb_batch_set_initial_circulation(sb_batch* b, const double* gamma, size_t n) {

@@ -245,6 +245,7 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
     __shared__ __align__(128) PanelRec<R> tile[2][TILE];
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ long long s_item;
+    __shared__ int s_timed_out;  // a tile wait of this CTA ran out
     __shared__ BsJob s_job;  // the current item's sweep (one copy per item, by thread 0)
 
     const int tid = threadIdx.x;
@@ -252,6 +253,7 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         fence_mbar_init();
+        s_timed_out = 0;
     }
     __syncthreads();
     uint32_t phase0 = 0, phase1 = 0;
@@ -324,15 +326,15 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
         };
         if (tid == 0 && ntiles > 0) issue(0);
 
-        for (int k = 0; k < ntiles; ++k) {
+        int k = 0;
+        for (; k < ntiles; ++k) {
             const int buf = k & 1;
             if (tid == 0 && k + 1 < ntiles) issue(k + 1);
-            bool waited;
             if (buf == 0) {
-                waited = mbar_wait_bounded(&bar[0], phase0, a.err, a.wait_polls);
+                if (!mbar_wait_bounded(&bar[0], phase0, a.err, a.wait_polls)) s_timed_out = 1;
                 phase0 ^= 1;
             } else {
-                waited = mbar_wait_bounded(&bar[1], phase1, a.err, a.wait_polls);
+                if (!mbar_wait_bounded(&bar[1], phase1, a.err, a.wait_polls)) s_timed_out = 1;
                 phase1 ^= 1;
             }
             const int np = static_cast<int>(min(static_cast<long long>(TILE), pe - (pb + static_cast<long long>(k) * TILE)));
@@ -443,17 +445,22 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
                     sz[t] += tz[t];
                 }
             }
-            // The buffer is refilled in the next-but-one tile. If a wait of this tile ran out
-            // in any thread (its copy may still be landing; the sums above are void), thread 0
-            // waits, again bounded, for the copies of tiles k and k + 1, and the CTA leaves:
-            // no copy is in flight into its shared memory when it exits.
-            if (__syncthreads_or(!waited)) {
-                if (tid == 0) {
-                    mbar_wait_bounded(&bar[buf], (buf == 0 ? phase0 : phase1) ^ 1u, a.err);
-                    if (k + 1 < ntiles) mbar_wait_bounded(&bar[buf ^ 1], buf == 0 ? phase1 : phase0, a.err);
-                }
-                return;
+            // The buffer is refilled in the next-but-one tile. A wait of tile k that ran out in
+            // any thread ends the tile loop (the sums are void).
+            __syncthreads();
+            if (s_timed_out) break;
+        }
+        if (s_timed_out) {
+            // Copies that may still be landing: tile k's (its wait ran out) and tile k + 1's
+            // (issued before that wait). Thread 0 waits for both, bounded again, so no copy
+            // is in flight into the CTA's shared memory when it exits. Tile k's phase parity
+            // is its buffer's phase before the flip above, tile k + 1's its buffer's current one.
+            if (tid == 0) {
+                const int buf = k & 1;
+                mbar_wait_bounded(&bar[buf], (buf == 0 ? phase0 : phase1) ^ 1u, a.err);
+                if (k + 1 < ntiles) mbar_wait_bounded(&bar[buf ^ 1], buf == 0 ? phase1 : phase0, a.err);
             }
+            return;
         }
 
 #pragma unroll
@@ -575,9 +582,8 @@ __device__ inline void store_factor(d3* factors, float2* split, int N, long long
 }
 
 // frozen_wake.rs:198-249: factors[c][p] = unit velocity of first-row panel p at control point c
-__global__ void k_unit_matrix(const PanelRec<double>* row0, const d3* ctrl, int N, int sym, int neglect,
-                              const int* wing_of_line, d3* factors, float2* split) {
-    long long id = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+__device__ inline void unit_matrix_elem(const PanelRec<double>* row0, const d3* ctrl, int N, int sym, int neglect,
+                                        const int* wing_of_line, d3* factors, float2* split, long long id) {
     if (id >= static_cast<long long>(N) * N) return;
     int c = static_cast<int>(id / N), p = static_cast<int>(id % N);
     d3 u = mk(0, 0, 0);
@@ -587,6 +593,12 @@ __global__ void k_unit_matrix(const PanelRec<double>* row0, const d3* ctrl, int 
         if (sym) u = sym_correct(sym, u, panel_unit_f64(row0[p].v, mirror(sym, x)));
     }
     store_factor(factors, split, N, id, c, p, u);
+}
+
+__global__ void k_unit_matrix(const PanelRec<double>* row0, const d3* ctrl, int N, int sym, int neglect,
+                              const int* wing_of_line, d3* factors, float2* split) {
+    unit_matrix_elem(row0, ctrl, N, sym, neglect, wing_of_line, factors, split,
+                     blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x);
 }
 
 // The same matrix from the FP32 panel records of row 0, two control points per thread as the
@@ -638,9 +650,9 @@ __device__ __forceinline__ void panel_unit2(const float* v, float2 X2h, float2 Y
     }
 }
 
-__global__ void k_unit_matrix_f32(const PanelRec<float>* row0_32, const PanelRec<double>* row0, const d3* ctrl, int N,
-                                  int sym, int neglect, const int* wing_of_line, d3* factors, float2* split) {
-    const long long id = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+__device__ inline void unit_matrix_f32_elem(const PanelRec<float>* row0_32, const PanelRec<double>* row0, const d3* ctrl,
+                                            int N, int sym, int neglect, const int* wing_of_line, d3* factors,
+                                            float2* split, long long id) {
     const int pairs = (N + 1) / 2;
     if (id >= static_cast<long long>(pairs) * N) return;
     const int cp = static_cast<int>(id / N), p = static_cast<int>(id % N);
@@ -689,6 +701,44 @@ __global__ void k_unit_matrix_f32(const PanelRec<float>* row0_32, const PanelRec
         }
         store_factor(factors, split, N, static_cast<long long>(c) * N + p, c, p, u);
     }
+}
+
+__global__ void k_unit_matrix_f32(const PanelRec<float>* row0_32, const PanelRec<double>* row0, const d3* ctrl, int N,
+                                  int sym, int neglect, const int* wing_of_line, d3* factors, float2* split) {
+    unit_matrix_f32_elem(row0_32, row0, ctrl, N, sym, neglect, wing_of_line, factors, split,
+                         blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x);
+}
+
+constexpr int kUnitMatrixThreads = 128;
+
+// The unit-strength matrices of every case of a batch in one launch (block -> case by a
+// binary search over the cases' first blocks, as the other job-list kernels).
+__global__ void k_unit_matrix_jobs(const CaseStepJob* jobs, int n) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].blk_matrix <= static_cast<long long>(blockIdx.x)) lo = mid;
+        else hi = mid - 1;
+    }
+    const CaseStepJob& J = jobs[lo];
+    const long long id = (blockIdx.x - J.blk_matrix) * static_cast<long long>(kUnitMatrixThreads) + threadIdx.x;
+    const DevModel& m = J.m;
+    if (J.row0_32)
+        unit_matrix_f32_elem(J.row0_32, J.w.row0_64, m.ctrl, m.N, m.symmetry, m.neglect_self, m.wing_of_line, J.factors,
+                             J.split, id);
+    else
+        unit_matrix_elem(J.w.row0_64, m.ctrl, m.N, m.symmetry, m.neglect_self, m.wing_of_line, J.factors, J.split, id);
+}
+
+long long unit_matrix_blocks(int N, bool fp32) {
+    const long long tot = fp32 ? static_cast<long long>((N + 1) / 2) * N : static_cast<long long>(N) * N;
+    return (tot + kUnitMatrixThreads - 1) / kUnitMatrixThreads;
+}
+
+cudaError_t launch_unit_matrix_jobs(const CaseStepJob* jobs, int n, long long blocks, cudaStream_t s) {
+    if (n <= 0 || blocks <= 0) return cudaSuccess;
+    k_unit_matrix_jobs<<<static_cast<unsigned>(blocks), kUnitMatrixThreads, 0, s>>>(jobs, n);
+    return cudaGetLastError();
 }
 
 // Quasi-steady wake: core length and wake vectors (frozen_wake.rs:74-100). One CTA: the
@@ -854,18 +904,14 @@ cudaError_t launch_bs_reduce_jobs(const BsJob* jobs, int n_jobs, long long block
 
 cudaError_t launch_unit_matrix(const PanelRec<double>* row0, const PanelRec<float>* row0_32, const d3* ctrl, int N,
                                int sym, int neglect, const int* wing_of_line, d3* factors, float2* split, cudaStream_t s) {
+    const long long blocks = unit_matrix_blocks(N, row0_32 != nullptr);
     if (row0_32) {
-        const long long tot = static_cast<long long>((N + 1) / 2) * N;
-        const int threads = 128;
-        const long long blocks = (tot + threads - 1) / threads;
-        k_unit_matrix_f32<<<static_cast<unsigned>(blocks), threads, 0, s>>>(row0_32, row0, ctrl, N, sym, neglect,
-                                                                            wing_of_line, factors, split);
+        k_unit_matrix_f32<<<static_cast<unsigned>(blocks), kUnitMatrixThreads, 0, s>>>(row0_32, row0, ctrl, N, sym, neglect,
+                                                                                        wing_of_line, factors, split);
         return cudaGetLastError();
     }
-    long long tot = static_cast<long long>(N) * N;
-    int threads = 128;
-    long long blocks = (tot + threads - 1) / threads;
-    k_unit_matrix<<<static_cast<unsigned>(blocks), threads, 0, s>>>(row0, ctrl, N, sym, neglect, wing_of_line, factors, split);
+    k_unit_matrix<<<static_cast<unsigned>(blocks), kUnitMatrixThreads, 0, s>>>(row0, ctrl, N, sym, neglect, wing_of_line,
+                                                                                factors, split);
     return cudaGetLastError();
 }
 

@@ -34,7 +34,10 @@ static double measure_peak(int device, int reps, int iters) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     const int blocks = sms * 8, threads = 256;
     T* out = nullptr;
-    if (cudaMalloc(&out, static_cast<size_t>(blocks) * threads * sizeof(T)) != cudaSuccess) return -1.0;
+    if (cudaMalloc(&out, static_cast<size_t>(blocks) * threads * sizeof(T)) != cudaSuccess) {
+        cudaGetLastError();  // leave no error behind for later launch checks
+        return -1.0;
+    }
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);

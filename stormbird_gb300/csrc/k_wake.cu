@@ -18,7 +18,7 @@ namespace sbgpu {
 // ---------------------------------------------------------------------------------------
 // Geometry of the line force model for one step. One CTA: O(N) work.
 // ---------------------------------------------------------------------------------------
-__global__ void k_prep_geometry(DevModel m, StepParams p, const d3* fs_ctrl, d3* mean_out) {
+__device__ void prep_geometry_block(const DevModel& m, const StepParams& p, const d3* fs_ctrl, d3* mean_out) {
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int i = tid; i < m.N; i += nt) {
         int w = m.wing_of_line[i];
@@ -55,8 +55,24 @@ __global__ void k_prep_geometry(DevModel m, StepParams p, const d3* fs_ctrl, d3*
     }
 }
 
+__global__ void k_prep_geometry(DevModel m, StepParams p, const d3* fs_ctrl, d3* mean_out) {
+    prep_geometry_block(m, p, fs_ctrl, mean_out);
+}
+
+// The geometry of every case of a batch: one CTA per case.
+__global__ void k_prep_geometry_jobs(const CaseStepJob* jobs) {
+    const CaseStepJob& J = jobs[blockIdx.x];
+    prep_geometry_block(J.m, J.p, J.fs_ctrl, nullptr);
+}
+
 cudaError_t launch_prep_geometry(const DevModel& m, const StepParams& p, const d3* fs_ctrl, d3* mean_out, cudaStream_t s) {
     k_prep_geometry<<<1, 512, 0, s>>>(m, p, fs_ctrl, mean_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prep_geometry_jobs(const CaseStepJob* jobs, int n, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_prep_geometry_jobs<<<n, 512, 0, s>>>(jobs);
     return cudaGetLastError();
 }
 
@@ -141,47 +157,47 @@ cudaError_t launch_wake_init(const DevModel& m, const WakeBuffers& w, const d3* 
 }
 
 // ---------------------------------------------------------------------------------------
-// Rows 0..W-1 of the next wake points (update_data.rs:65-82, 90-99, 205-252, 295-316).
+// The next wake points (update_data.rs:65-82, 90-99, 205-252, 262-316): rows 0..W-1 one per
+// thread, and the last row by the thread of row W-1, from rows W-1 and W-2 (row W-2
+// evaluated again there by the same expression, so it equals what its own thread writes).
 // ---------------------------------------------------------------------------------------
-__global__ void k_wake_advect(DevModel m, WakeBuffers w, double dt, int steps_done) {
-    long long id = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+// Row s < W of column j of the next points.
+__device__ inline d3 advected_point(const DevModel& m, const WakeBuffers& w, double dt, int steps_done, int s, int j) {
+    const long long Np = m.Np;
+    const double D = m.damping;
+    if (s == 0) return m.span_pts[j];
+    if (s == 1) {
+        d3 dir = first_row_direction(m, j, w.vel, w.vel + Np, steps_done, m.felt_span[j]);
+        d3 est = m.span_pts[j] + dir * (m.rep_chord * m.first_rel);
+        return D > 0.0 ? w.pts_old[Np + j] * D + est * (1.0 - D) : est;
+    }
+    const long long id = static_cast<long long>(s) * Np + j, pi = id - Np;
+    d3 integ = w.pts_old[pi] + dt * w.vel[pi];
+    return D > 0.0 ? w.pts_old[id] * D + integ * (1.0 - D) : integ;
+}
+
+__device__ inline void wake_advect_elem(const DevModel& m, const WakeBuffers& w, double dt, int steps_done, long long id) {
     const long long Np = m.Np;
     if (id >= static_cast<long long>(m.W) * Np) return;
     const int s = static_cast<int>(id / Np), j = static_cast<int>(id % Np);
-    const double D = m.damping;
-    d3 out;
-    if (s == 0) {
-        out = m.span_pts[j];
-    } else if (s == 1) {
-        d3 dir = first_row_direction(m, j, w.vel, w.vel + Np, steps_done, m.felt_span[j]);
-        d3 est = m.span_pts[j] + dir * (m.rep_chord * m.first_rel);
-        out = D > 0.0 ? w.pts_old[Np + j] * D + est * (1.0 - D) : est;
-    } else {
-        long long pi = id - Np;
-        d3 integ = w.pts_old[pi] + dt * w.vel[pi];
-        out = D > 0.0 ? w.pts_old[id] * D + integ * (1.0 - D) : integ;
-    }
+    const d3 out = advected_point(m, w, dt, steps_done, s, j);
     w.pts_new[id] = out;
+    if (s == m.W - 1) {  // last row (update_data.rs:262-292)
+        const d3 dir = m.W > 1 ? normalize(out - advected_point(m, w, dt, steps_done, s - 1, j)) : normalize(m.felt_span[j]);
+        w.pts_new[static_cast<long long>(m.W) * Np + j] = out + (m.last_rel * m.rep_chord) * dir;
+    }
 }
 
-// Last row (update_data.rs:262-292).
-__global__ void k_wake_last_row(DevModel m, WakeBuffers w) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= m.Np) return;
-    const long long Np = m.Np;
-    const int W = m.W;
-    d3 prev = w.pts_new[static_cast<long long>(W - 1) * Np + j];
-    d3 dir = W > 1 ? normalize(prev - w.pts_new[static_cast<long long>(W - 2) * Np + j]) : normalize(m.felt_span[j]);
-    w.pts_new[static_cast<long long>(W) * Np + j] = prev + (m.last_rel * m.rep_chord) * dir;
+__global__ void k_wake_advect(DevModel m, WakeBuffers w, double dt, int steps_done) {
+    wake_advect_elem(m, w, dt, steps_done, blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x);
 }
+
+constexpr int kAdvectThreads = 256;
 
 cudaError_t launch_wake_advect(const DevModel& m, const WakeBuffers& w, double dt, int steps_done, cudaStream_t s) {
-    long long tot = static_cast<long long>(m.W) * m.Np;
-    int threads = 256;
-    k_wake_advect<<<static_cast<unsigned>((tot + threads - 1) / threads), threads, 0, s>>>(m, w, dt, steps_done);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    k_wake_last_row<<<(m.Np + 127) / 128, 128, 0, s>>>(m, w);
+    const long long tot = static_cast<long long>(m.W) * m.Np;
+    k_wake_advect<<<static_cast<unsigned>((tot + kAdvectThreads - 1) / kAdvectThreads), kAdvectThreads, 0, s>>>(
+        m, w, dt, steps_done);
     return cudaGetLastError();
 }
 
@@ -260,8 +276,7 @@ __device__ void write_panel_records(const d3 (&pp)[4], double rc, double g, doub
     }
 }
 
-__global__ void k_wake_panels(DevModel m, WakeBuffers w, int shift) {
-    long long id = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+__device__ inline void wake_panel_elem(const DevModel& m, const WakeBuffers& w, int shift, long long id) {
     if (id >= m.P_pan) return;
     const int N = m.N;
     const long long Np = m.Np;
@@ -288,6 +303,10 @@ __global__ void k_wake_panels(DevModel m, WakeBuffers w, int shift) {
     if (w.rec64) w.rec64[id] = q;
 }
 
+__global__ void k_wake_panels(DevModel m, WakeBuffers w, int shift) {
+    wake_panel_elem(m, w, shift, blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x);
+}
+
 // ---------------------------------------------------------------------------------------
 // Chain records. Panel (s, j) of wing w has corners p0 = P[s][j+w], p1 = P[s][j+1+w],
 // p2 = P[s+1][j+1+w], p3 = P[s+1][j+w] and segments p0->p1, p1->p2, p2->p3, p3->p0
@@ -303,8 +322,7 @@ __device__ inline double chain_strength(const ChainArgs& a, int s, int j) {
     return (s >= 0 && s < a.W) ? a.str[static_cast<long long>(s) * a.N + j] : 0.0;
 }
 
-__global__ void k_chain_records(ChainArgs a, long long n_build) {
-    const long long id = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+__device__ inline void chain_record_elem(const ChainArgs& a, long long n_build, long long id) {
     if (id >= n_build) return;
     const long long q = id / a.Bq, local = id % a.Bq;
     const long long Np = a.Np;
@@ -377,6 +395,10 @@ __global__ void k_chain_records(ChainArgs a, long long n_build) {
     a.out[id] = rec;
 }
 
+__global__ void k_chain_records(ChainArgs a, long long n_build) {
+    chain_record_elem(a, n_build, blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x);
+}
+
 cudaError_t launch_chain_records(const ChainArgs& a, long long n_build, cudaStream_t s) {
     if (n_build <= 0) return cudaSuccess;
     k_chain_records<<<static_cast<unsigned>((n_build + 127) / 128), 128, 0, s>>>(a, n_build);
@@ -403,10 +425,70 @@ cudaError_t launch_panels_from_corners(const double* corners, const double* stre
     return cudaGetLastError();
 }
 
+constexpr int kPanelThreads = 128;
+constexpr int kChainThreads = 128;
+
 cudaError_t launch_wake_panels(const DevModel& m, const WakeBuffers& w, int shift, cudaStream_t s) {
-    int threads = 128;
-    long long blocks = (m.P_pan + threads - 1) / threads;
-    k_wake_panels<<<static_cast<unsigned>(blocks), threads, 0, s>>>(m, w, shift);
+    const long long blocks = (m.P_pan + kPanelThreads - 1) / kPanelThreads;
+    k_wake_panels<<<static_cast<unsigned>(blocks), kPanelThreads, 0, s>>>(m, w, shift);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------
+// The same per-case kernels for every case of a batch, one launch per kind: block b belongs
+// to the last job whose first block of that kind is at or before b (jobs [n] ascending in
+// each kind's first block), and runs that job's element at b's offset within it.
+// ---------------------------------------------------------------------------------------
+template <long long CaseStepJob::*First>
+__device__ inline int job_of_block(const CaseStepJob* jobs, int n, long long b) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].*First <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void k_wake_advect_jobs(const CaseStepJob* jobs, int n) {
+    const CaseStepJob& J = jobs[job_of_block<&CaseStepJob::blk_advect>(jobs, n, blockIdx.x)];
+    const long long id = (blockIdx.x - J.blk_advect) * static_cast<long long>(kAdvectThreads) + threadIdx.x;
+    wake_advect_elem(J.m, J.w, J.p.dt, J.steps_done, id);
+}
+
+__global__ void k_wake_panels_jobs(const CaseStepJob* jobs, int n) {
+    const CaseStepJob& J = jobs[job_of_block<&CaseStepJob::blk_panels>(jobs, n, blockIdx.x)];
+    const long long id = (blockIdx.x - J.blk_panels) * static_cast<long long>(kPanelThreads) + threadIdx.x;
+    wake_panel_elem(J.m, J.w, 1, id);
+}
+
+__global__ void k_chain_records_jobs(const CaseStepJob* jobs, int n) {
+    const CaseStepJob& J = jobs[job_of_block<&CaseStepJob::blk_chain>(jobs, n, blockIdx.x)];
+    const long long id = (blockIdx.x - J.blk_chain) * static_cast<long long>(kChainThreads) + threadIdx.x;
+    chain_record_elem(J.chain, J.chain_n, id);
+}
+
+long long wake_advect_blocks(const DevModel& m) {
+    return (static_cast<long long>(m.W) * m.Np + kAdvectThreads - 1) / kAdvectThreads;
+}
+long long wake_panels_blocks(const DevModel& m) { return (m.P_pan + kPanelThreads - 1) / kPanelThreads; }
+long long chain_records_blocks(long long n_build) { return (n_build + kChainThreads - 1) / kChainThreads; }
+
+cudaError_t launch_wake_jobs(const CaseStepJob* jobs, int n, long long advect_blocks, long long panel_blocks,
+                             cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    if (advect_blocks > 0) {
+        k_wake_advect_jobs<<<static_cast<unsigned>(advect_blocks), kAdvectThreads, 0, s>>>(jobs, n);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (panel_blocks > 0) k_wake_panels_jobs<<<static_cast<unsigned>(panel_blocks), kPanelThreads, 0, s>>>(jobs, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_chain_records_jobs(const CaseStepJob* jobs, int n, long long blocks, cudaStream_t s) {
+    if (n <= 0 || blocks <= 0) return cudaSuccess;
+    k_chain_records_jobs<<<static_cast<unsigned>(blocks), kChainThreads, 0, s>>>(jobs, n);
     return cudaGetLastError();
 }
 

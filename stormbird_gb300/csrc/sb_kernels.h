@@ -128,6 +128,37 @@ struct ChainArgs {
 };
 cudaError_t launch_chain_records(const ChainArgs& a, long long n_build, cudaStream_t s);
 
+// One dynamic case of a batched step, for the per-case kernels that a batch runs as ONE
+// launch per kind for all its cases (geometry, wake advection, panel records, unit-strength
+// matrix, chain records): the case's model, step parameters and wake buffers of the step,
+// and the first block of each kind that belongs to it (ascending over the job list).
+struct CaseStepJob {
+    DevModel m;
+    StepParams p;                             // p.dt: the step's time step
+    WakeBuffers w;                            // old -> new buffers of the step
+    const d3* fs_ctrl = nullptr;              // freestream at the control points
+    int steps_done = 0;                       // wake steps completed before the step
+    const PanelRec<float>* row0_32 = nullptr; // unit matrix from FP32 row-0 records (null: FP64)
+    d3* factors = nullptr;
+    float2* split = nullptr;
+    ChainArgs chain;                          // chain records (chain_n = 0: none)
+    long long chain_n = 0;
+    long long blk_advect = 0, blk_panels = 0, blk_matrix = 0, blk_chain = 0;
+};
+// Blocks a job needs per kind.
+long long wake_advect_blocks(const DevModel& m);
+long long wake_panels_blocks(const DevModel& m);
+long long chain_records_blocks(long long n_build);
+long long unit_matrix_blocks(int N, bool fp32);
+// One CTA per job: the geometry of every case (k_prep_geometry).
+cudaError_t launch_prep_geometry_jobs(const CaseStepJob* jobs, int n, cudaStream_t s);
+// Wake advection (with the last row) of every case, then its panel records with the strength
+// shift (k_wake_advect, k_wake_panels).
+cudaError_t launch_wake_jobs(const CaseStepJob* jobs, int n, long long advect_blocks, long long panel_blocks,
+                             cudaStream_t s);
+cudaError_t launch_unit_matrix_jobs(const CaseStepJob* jobs, int n, long long blocks, cudaStream_t s);
+cudaError_t launch_chain_records_jobs(const CaseStepJob* jobs, int n, long long blocks, cudaStream_t s);
+
 // Records of caller-given panels for the standalone sweep (corners [P][4][3] in ring order).
 cudaError_t launch_panels_from_corners(const double* corners, const double* strengths, const double* cores, long long P,
                                        double far_field_ratio, PanelRec<float>* r32, PanelRec<double>* r64,

@@ -37,7 +37,13 @@ struct SbFail {
 [[noreturn]] inline void raise(int code, const std::string& msg) { throw SbFail{code, msg}; }
 
 inline void ck(cudaError_t e, const char* what) {
-    if (e != cudaSuccess) raise(SB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    if (e != cudaSuccess) {
+        // a failed call (e.g. cudaMalloc out of memory) also leaves its code in the runtime's
+        // last-error slot, where the next launch check of any handle would find it: clear it
+        // (a sticky error stays in the context regardless)
+        cudaGetLastError();
+        raise(SB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    }
 }
 
 // Runs f, turning a thrown SbFail into its status code and the thread's last error.
@@ -312,7 +318,8 @@ struct sb_sim {
     OutLayout L{};
     std::vector<double> chord_lengths_h;
     bool timing = false;
-    double last_ms[9] = {0};
+    double last_ms[12] = {0};
+    bool chains_built = false;  // the step built chain records (timing slot 11)
     double last_counters[7] = {0};
     int launches = 0;
     bool swept[2] = {false, false};
@@ -342,7 +349,7 @@ struct sb_sim {
     DevBuf<d3> vel_out, hist0, hist1, fs, aux_targets, aux_out;
     PinnedBuf<double> h_out, h_fs;
     PinnedBuf<int> h_err;
-    cudaEvent_t ev[12] = {nullptr};
+    cudaEvent_t ev[15] = {nullptr};
     // The handle's own stream; `stream` is the one its work is enqueued on, which a batch
     // points at one of its streams.
     cudaStream_t home_stream = nullptr;
@@ -374,7 +381,7 @@ struct sb_sim {
         if (home_stream) cudaStreamDestroy(home_stream);
     }
 
-    WakeBuffers wake(bool step) {
+    WakeBuffers wake(bool step) const {
         WakeBuffers w;
         w.pts_old = pts[cur].p;
         w.pts_new = step ? pts[cur ^ 1].p : pts[cur].p;
@@ -651,8 +658,10 @@ struct sb_sim {
 
     bool use_chains() const { return chain_ok && share_segments && precision != 2; }
 
-    // Panel rows that can hold a nonzero strength (see active_panels).
-    int active_rows() const { return std::min(W, steps_completed + 2); }
+    // Panel rows that can hold a nonzero strength (see active_panels); row_extra covers the
+    // rows of a loaded state (set_state) that lie beyond what its age could have filled.
+    int row_extra = 0;
+    int active_rows() const { return std::min<long long>(W, static_cast<long long>(steps_completed) + 2 + row_extra); }
 
     // Chain records covering the active rows: the quads up to the one holding point row R
     // (its spanwise segments carry -strength of row R - 1).
@@ -660,10 +669,11 @@ struct sb_sim {
         return std::min<long long>(chain_Q, active_rows() / 4 + 1) * chain_Bq;
     }
 
-    void build_chains() {
+    // Chain records from wake buffer `buf` (after the step's begin: the current one).
+    ChainArgs chain_args(int buf) const {
         ChainArgs c;
-        c.pts = pts[cur].p;
-        c.str = str[cur].p;
+        c.pts = pts[buf].p;
+        c.str = str[buf].p;
         c.span_tab = chain_span_tab.p;
         c.col_tab = chain_col_tab.p;
         c.wing_start = wing_start.p;
@@ -675,9 +685,16 @@ struct sb_sim {
         c.Bq = chain_Bq;
         c.rc = chain_rc;
         c.out = chains.p;
+        return c;
+    }
+
+    void build_chains() {
         // all records, also the empty ones past the active rows: a captured step replays
         // this launch with its arguments unchanged while the wake grows
-        ck(launch_chain_records(c, chain_Q * chain_Bq, stream), "chain records");
+        record(13);
+        ck(launch_chain_records(chain_args(cur), chain_Q * chain_Bq, stream), "chain records");
+        record(14);
+        chains_built = true;
         launches += 1;
     }
 
@@ -777,9 +794,7 @@ struct sb_sim {
     // (rows 1..k before the solve) are the only nonzero ones. Panels beyond contribute
     // nothing (zero strengths are skipped, induced_velocity_calc.rs:203), so the sweeps
     // stop there (one row of margin).
-    long long active_panels() const {
-        return std::min<long long>(P_pan, static_cast<long long>(std::min(W, steps_completed + 2)) * N);
-    }
+    long long active_panels() const { return std::min<long long>(P_pan, static_cast<long long>(active_rows()) * N); }
 
     // frozen wake (frozen_wake.rs:189-261): the free wake at the control points
     SweepDesc fixed_desc() const {
@@ -829,6 +844,7 @@ struct sb_sim {
         const bool first = !first_step_completed;
         launches = 0;
         swept[0] = swept[1] = false;
+        chains_built = false;
         ck(launch_prep_geometry(dm, params, fs_p, first ? mean.p : nullptr, stream), "prep geometry");
         launches += 1;
         if (first) {
@@ -847,11 +863,46 @@ struct sb_sim {
         record(1);
         if (dynamic) {
             ck(launch_wake_advect(dm, wake(true), dt, steps_completed, stream), "wake advect");
+            record(12);
             ck(launch_wake_panels(dm, wake(true), 1, stream), "wake panels");
             launches += 3;
             cur ^= 1;
         }
         record(2);
+    }
+
+    // ---- a step whose per-case kernels a batch launches for all its cases at once
+    // A dynamic case past its first step: its geometry, wake update, unit-strength matrix and
+    // chain records come from the batch's job-list launches (CaseStepJob).
+    bool batch_kernels_ok() const { return dynamic && first_step_completed; }
+
+    // The case's job for a step, from the state before the step.
+    CaseStepJob step_job(double time, double dt) const {
+        CaseStepJob j;
+        j.m = dm;
+        j.p = params;
+        j.p.time = time;
+        j.p.dt = dt;
+        j.w = wake(true);
+        j.fs_ctrl = fs_p;
+        j.steps_done = steps_completed;
+        j.row0_32 = precision == 2 ? nullptr : rec32.p;
+        j.factors = factors.p;
+        j.split = factors_split.p;
+        if (use_chains() && rollup_active()) {
+            j.chain = chain_args(cur ^ 1);  // the buffer the step writes
+            j.chain_n = chain_Q * chain_Bq;
+        }
+        return j;
+    }
+
+    // step_begin's host side for such a case (its kernels come from the batch).
+    void step_begin_host(double time, double dt) {
+        params.time = time;
+        params.dt = dt;
+        launches = 0;
+        swept[0] = swept[1] = false;
+        cur ^= 1;
     }
 
     // Influence matrix (unit matrix of the first wake row, or horseshoes) and the solve.
@@ -987,9 +1038,14 @@ struct sb_sim {
             cudaEventElapsedTime(&ms, ev[4], ev[5]); last_ms[4] = ms;
             cudaEventElapsedTime(&ms, ev[5], ev[6]); last_ms[5] = ms;
             cudaEventElapsedTime(&ms, ev[6], ev[7]); last_ms[6] = ms;
-            last_ms[7] = last_ms[8] = 0.0;
+            last_ms[7] = last_ms[8] = last_ms[9] = last_ms[10] = last_ms[11] = 0.0;
             if (swept[1]) { cudaEventElapsedTime(&ms, ev[10], ev[11]); last_ms[7] = ms; }
             if (swept[0]) { cudaEventElapsedTime(&ms, ev[8], ev[9]); last_ms[8] = ms; }
+            if (dynamic) {
+                cudaEventElapsedTime(&ms, ev[1], ev[12]); last_ms[9] = ms;
+                cudaEventElapsedTime(&ms, ev[12], ev[2]); last_ms[10] = ms;
+            }
+            if (chains_built) { cudaEventElapsedTime(&ms, ev[13], ev[14]); last_ms[11] = ms; }
         }
         check_device_status();
         if (writer) writer->push(result_record());
@@ -1114,6 +1170,77 @@ struct sb_sim {
         ck(cudaMemcpyAsync(h_out.p, out.p, L.total * sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H output");
         ck(cudaStreamSynchronize(stream), "read output");
         write_output(o);
+    }
+
+    // ---------------------------------------------------------------- state between steps
+    // What a step reads from the steps before it, as the public fields of the reference's
+    // Simulation (simulation.rs:20-28) and DynamicWake (wake/dynamic_wake/mod.rs:41-64) hold
+    // it: [0] wake steps completed, [1] first step completed (0/1), [2] flow-derivative
+    // updates, then (dynamic) wake points [P_pts][3], velocity at the points [P_pts][3],
+    // panel strengths [P_pan], then the previous circulation [N] and the flow-derivative
+    // history (two earlier control-point velocities) [2][N][3]. Rigid-body motion and wing
+    // angles are not part of it (their setters set them).
+    static constexpr size_t kStateHead = 3;
+    size_t state_size() const {
+        const size_t wake = dynamic ? static_cast<size_t>(P_pts) * 6 + static_cast<size_t>(P_pan) : 0;
+        return kStateHead + wake + static_cast<size_t>(N) * 7;
+    }
+
+    void get_state(double* o, size_t n) {
+        if (n != state_size()) raise(SB_ERR_SIZE, "state buffer has " + std::to_string(n) + " values, expected " +
+                                                      std::to_string(state_size()));
+        o[0] = dynamic ? static_cast<double>(steps_completed) : 0.0;
+        o[1] = first_step_completed ? 1.0 : 0.0;
+        o[2] = static_cast<double>(fd_count);
+        double* p = o + kStateHead;
+        auto d2h = [&](const void* src, size_t count) {
+            ck(cudaMemcpyAsync(p, src, count * sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H state");
+            p += count;
+        };
+        if (dynamic) {
+            d2h(pts[cur].p, static_cast<size_t>(P_pts) * 3);
+            d2h(vel.p, static_cast<size_t>(P_pts) * 3);
+            d2h(str[cur].p, static_cast<size_t>(P_pan));
+        }
+        d2h(gamma_p, static_cast<size_t>(N));
+        d2h(hist0.p, static_cast<size_t>(N) * 3);
+        d2h(hist1.p, static_cast<size_t>(N) * 3);
+        ck(cudaStreamSynchronize(stream), "get state");
+    }
+
+    void set_state(const double* s, size_t n) {
+        if (n != state_size()) raise(SB_ERR_SIZE, "state buffer has " + std::to_string(n) + " values, expected " +
+                                                      std::to_string(state_size()));
+        for (size_t i = 0; i < n; ++i)
+            if (!std::isfinite(s[i])) raise(SB_ERR_NONFINITE, "non-finite state value at index " + std::to_string(i));
+        if (s[0] < 0.0 || s[0] > 2e9 || s[2] < 0.0 || s[2] > 2e9) raise(SB_ERR_SIZE, "step counters out of range");
+        const double* p = s + kStateHead;
+        auto h2d = [&](void* dst, size_t count) {
+            ck(cudaMemcpyAsync(dst, p, count * sizeof(double), cudaMemcpyHostToDevice, stream), "H2D state");
+            p += count;
+        };
+        row_extra = 0;
+        if (dynamic) {
+            h2d(pts[cur].p, static_cast<size_t>(P_pts) * 3);
+            h2d(vel.p, static_cast<size_t>(P_pts) * 3);
+            const double* g = p;
+            h2d(str[cur].p, static_cast<size_t>(P_pan));
+            // sweeps stop after the rows a wake of this age can have filled (active_rows);
+            // a loaded wake may hold strengths further downstream
+            long long last = -1;
+            for (long long i = P_pan - 1; i >= 0; --i)
+                if (g[i] != 0.0) { last = i / N; break; }
+            steps_completed = static_cast<int>(s[0]);
+            row_extra = static_cast<int>(std::max<long long>(0, last - steps_completed - 1));
+        }
+        h2d(gamma_p, static_cast<size_t>(N));
+        h2d(hist0.p, static_cast<size_t>(N) * 3);
+        h2d(hist1.p, static_cast<size_t>(N) * 3);
+        first_step_completed = s[1] != 0.0;
+        fd_count = static_cast<int>(s[2]);
+        // panel records of the loaded wake (sb_sim_induced_velocities may come before a step)
+        if (dynamic) ck(launch_wake_panels(dm, wake(false), 0, stream), "wake panels");
+        ck(cudaStreamSynchronize(stream), "set state");
     }
 
     // ---------------------------------------------------------------- wind model

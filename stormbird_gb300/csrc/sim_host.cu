@@ -193,6 +193,22 @@ int sb_sim_get_wake_state(sb_sim* sim, double* pts, double* str, double* vel) {
     });
 }
 
+int sb_sim_state_size(const sb_sim* sim, size_t* n) {
+    if (!sim || !n) { g_last_error = "null argument"; return SB_ERR_NULL_ARG; }
+    *n = sim->state_size();
+    return SB_OK;
+}
+
+int sb_sim_get_state(sb_sim* sim, double* state, size_t n) {
+    if (!sim || !state) { g_last_error = "null argument"; return SB_ERR_NULL_ARG; }
+    return guard([&] { sim->get_state(state, n); });
+}
+
+int sb_sim_set_state(sb_sim* sim, const double* state, size_t n) {
+    if (!sim || !state) { g_last_error = "null argument"; return SB_ERR_NULL_ARG; }
+    return guard([&] { sim->set_state(state, n); });
+}
+
 int sb_sim_set_precision(sb_sim* sim, int mode) {
     if (!sim) { g_last_error = "null handle"; return SB_ERR_NULL_ARG; }
     if (mode < 0 || mode > 2) { g_last_error = "precision mode must be 0, 1 or 2"; return SB_ERR_SIZE; }
@@ -208,7 +224,7 @@ int sb_sim_enable_timing(sb_sim* sim, int enable) {
 
 int sb_sim_last_step_timing(const sb_sim* sim, double* ms, size_t n) {
     if (!sim || !ms) { g_last_error = "null argument"; return SB_ERR_NULL_ARG; }
-    for (size_t i = 0; i < n && i < 9; ++i) ms[i] = sim->last_ms[i];
+    for (size_t i = 0; i < n && i < 12; ++i) ms[i] = sim->last_ms[i];
     return SB_OK;
 }
 

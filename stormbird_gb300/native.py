@@ -44,6 +44,9 @@ SIGNATURES = [
     ("sb_sim_get_previous_circulation", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
     ("sb_sim_wake_sizes", ctypes.c_int, [_vp, _szp, _szp, _szp, _szp]),
     ("sb_sim_get_wake_state", ctypes.c_int, [_vp, _dp, _dp, _dp]),
+    ("sb_sim_state_size", ctypes.c_int, [_vp, _szp]),
+    ("sb_sim_get_state", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
+    ("sb_sim_set_state", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
     ("sb_sim_set_precision", ctypes.c_int, [_vp, ctypes.c_int]),
     ("sb_sim_enable_timing", ctypes.c_int, [_vp, ctypes.c_int]),
     ("sb_sim_last_step_timing", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
@@ -74,6 +77,9 @@ SIGNATURES = [
     ("sb_batch_get_circulation", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
     ("sb_batch_get_summary", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
     ("sb_batch_read_case_output", ctypes.c_int, [_vp, ctypes.c_size_t, ctypes.POINTER(StepOutput)]),
+    ("sb_batch_case_state_size", ctypes.c_int, [_vp, ctypes.c_size_t, _szp]),
+    ("sb_batch_get_case_state", ctypes.c_int, [_vp, ctypes.c_size_t, _dp, ctypes.c_size_t]),
+    ("sb_batch_set_case_state", ctypes.c_int, [_vp, ctypes.c_size_t, _dp, ctypes.c_size_t]),
     ("sb_batch_set_initial_circulation", ctypes.c_int, [_vp, _dp, ctypes.c_size_t]),
     ("sb_batch_set_initial_circulation_device", ctypes.c_int, [_vp, _vp, ctypes.c_size_t]),
     ("sb_batch_previous_circulation_device", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_void_p)]),

@@ -129,6 +129,19 @@ class Simulation:
         _check(lib().sb_sim_get_wake_state(self._h, as_ptr(p), as_ptr(s), as_ptr(v)))
         return p, s, v
 
+    def state(self) -> np.ndarray:
+        """The state the next step reads (sb_sim_get_state layout): step counters, wake points,
+        velocity at the points, strengths, previous circulation and flow-derivative history."""
+        n = ctypes.c_size_t()
+        _check(lib().sb_sim_state_size(self._h, ctypes.byref(n)))
+        out = np.zeros(n.value)
+        _check(lib().sb_sim_get_state(self._h, as_ptr(out), out.size))
+        return out
+
+    def set_state(self, state):
+        a = np.ascontiguousarray(np.asarray(state, dtype=np.float64).reshape(-1))
+        _check(lib().sb_sim_set_state(self._h, as_ptr(a), a.size))
+
     def wake_sizes(self) -> dict:
         npts, npan, nspan, W = (ctypes.c_size_t() for _ in range(4))
         _check(lib().sb_sim_wake_sizes(self._h, ctypes.byref(npts), ctypes.byref(npan), ctypes.byref(nspan),
@@ -145,10 +158,11 @@ class Simulation:
         _check(lib().sb_sim_enable_timing(self._h, 1 if on else 0))
 
     def last_step_timing(self) -> dict:
-        ms = np.zeros(9)
-        _check(lib().sb_sim_last_step_timing(self._h, as_ptr(ms), 9))
+        ms = np.zeros(12)
+        _check(lib().sb_sim_last_step_timing(self._h, as_ptr(ms), 12))
         keys = ("step", "wake_update", "free_wake_sweep", "unit_matrix", "solve", "rollup_sweep", "forces",
-                "rollup_sweep_kernel", "free_wake_sweep_kernel")
+                "rollup_sweep_kernel", "free_wake_sweep_kernel", "wake_advect_kernel", "wake_panels_kernel",
+                "chain_records_kernel")
         return dict(zip(keys, ms.tolist()))
 
     def last_step_counters(self) -> dict:
