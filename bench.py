@@ -501,6 +501,195 @@ def batched_solves(args, device):
     return out
 
 
+def run_warm_start_training(args):
+    """Config 4's training set and training: the `--batch-cases` uneven cases of seed 77 (the
+    distribution of the evaluated cases, other seeds) stepped as one Batch for `--fill-steps`
+    steps with the warm-start data recorded (sb_batch_set_warm_start mode 2): features and the
+    correction beyond the extrapolation of every converged solve from step 2 on, across every
+    fill level of the wakes. The network (16 -> 4 x 256 GELU -> 1, BF16 tensor-core GEMMs) is
+    trained on it by the library's own kernels, 2 % of the rows held back for a validation
+    loss. Writes the parameters to `--save-net` (numpy .npy) and prints one JSON line."""
+    import torch
+
+    from stormbird_gb300 import setups as S
+    from stormbird_gb300 import warm_start as WS
+
+    n, steps, tol = args.batch_cases, args.fill_steps, args.batch_tolerance
+    cases = [(WS.tight_solver(js, residual_tolerance=tol), w) for js, w in S.uneven_cases(n, seed=77)]
+    t0 = time.perf_counter()
+    X, T = WS.collect(cases, steps=steps, device=0)
+    t_collect = time.perf_counter() - t0
+    print(f"collected {X.shape[0]} rows in {t_collect:.0f} s", file=sys.stderr, flush=True)
+    solves = n * (steps - 2)
+    g = torch.Generator(device=X.device)
+    g.manual_seed(5)
+    perm = torch.randperm(X.shape[0], device=X.device, generator=g)
+    n_val = X.shape[0] // 50
+    Xv, Tv = X[perm[:n_val]].contiguous(), T[perm[:n_val]].contiguous()
+    Xt, Tt = X[perm[n_val:]].contiguous(), T[perm[n_val:]].contiguous()
+    del X, T, perm
+    net = WS.WarmStartNet(WS.FEATURES, seed=1, device=0)
+    t0 = time.perf_counter()
+    losses = WS.train(net, Xt, Tt, epochs=args.big_train_epochs, batch_rows=16384, lr=5e-4, loss_every=16)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    val = []
+    for s0 in range(0, Xv.shape[0], 262144):
+        _, lv = net.gradients(Xv[s0:s0 + 262144], Tv[s0:s0 + 262144])
+        val.append(lv)
+    zero = float(torch.mean(Tv.double() ** 2))
+    if args.save_net:
+        np.save(args.save_net, net.get_params())
+    print(json.dumps({"mode": "warm-start-training", "cases": n, "seed": 77, "steps": steps,
+                      "solves": solves, "rows": int(Xt.shape[0] + Xv.shape[0]), "validation_rows": int(Xv.shape[0]),
+                      "collect_s": t_collect, "train_s": t_train, "epochs": len(losses),
+                      "loss_per_epoch": losses, "validation_loss": float(np.mean(val)),
+                      "validation_loss_of_zero_correction": zero,
+                      "targets": "correction beyond the linear extrapolation, -Gamma/(c|U|/2) units, clipped to +-0.25",
+                      "saved": args.save_net}), flush=True)
+
+
+def run_filled(args):
+    """Config 3 on filled wakes with config 4's network (batched_filled); the network's
+    parameters come from `--load-net` (run_warm_start_training's output)."""
+    from stormbird_gb300 import warm_start as WS
+
+    net = WS.WarmStartNet(WS.FEATURES, seed=1, device=0)
+    if args.load_net:
+        net.set_params(np.load(args.load_net))
+    print(json.dumps({"mode": "batched-filled", "network": args.load_net or "untrained",
+                      **batched_filled(args, 0, net)}), flush=True)
+
+
+def batched_filled(args, device, net):
+    """Solves/s of the uneven cases with every wake full (config 3 as specified: wake lengths
+    50-400 rows), all arms from one identical filled state.
+
+    One Batch of the `--batch-cases` cases (seed 2024, as the start-up window) is stepped
+    untimed for `--fill-steps` steps (past the longest wake). Every case's state
+    (sb_batch_get_case_state: wake points, velocities, strengths, previous circulation, flow
+    derivatives) then goes into the plain arm's Simulations (sb_sim_set_state) and into a fresh
+    Batch per warm-start arm (sb_batch_set_case_state), and every arm runs the same steps
+    fill .. fill + 1 + steps with the same freestream: two untimed (the extrapolation needs two
+    solutions of its own) and `--batch-steps` timed on the host clock around the public call,
+    host freestream in, results out. Circulation of every arm and timed step against the plain
+    arm's, and of sampled cases against the oracle loaded with the same state."""
+    from oracle.binding import OracleSimulation
+    from stormbird_gb300 import Batch, Simulation
+    from stormbird_gb300 import setups as S
+    from stormbird_gb300 import warm_start as WS
+
+    n, fill, pre, steps, tol = args.batch_cases, args.fill_steps, 2, args.batch_steps, args.batch_tolerance
+    cases = [(WS.tight_solver(js, residual_tolerance=tol), w) for js, w in S.uneven_cases(n, seed=2024)]
+    jsons, winds = [js for js, _ in cases], [w for _, w in cases]
+    src = Batch(jsons, device=device)
+    t0 = time.perf_counter()
+    for k in range(fill):
+        src.do_step(time=k * DT, time_step=DT, freestream_velocity=S.batch_freestream(src, winds, k * DT))
+        if k % 50 == 0:
+            print(f"spin-up step {k}: {src.info()['last_step_ms']:.0f} ms, {time.perf_counter() - t0:.0f} s",
+                  file=sys.stderr, flush=True)
+    spin_s = time.perf_counter() - t0
+    pairs = src.info()["pairs"]
+    states = [src.case_state(i) for i in range(n)]
+    window = list(range(fill, fill + pre + steps))
+    timed = window[pre:]
+
+    def run_arm(b, net_handle):
+        if net_handle is not None:
+            b.set_warm_start(net_handle)
+        out = {"seconds": 0.0, "gamma": [], "iterations": [], "start": [], "gpu_ms": []}
+        for k in window:
+            fs = S.batch_freestream(b, winds, k * DT)
+            t1 = time.perf_counter()
+            b.do_step(time=k * DT, time_step=DT, freestream_velocity=fs)
+            dt_ = time.perf_counter() - t1
+            if k in timed:
+                g = b.circulation()
+                sm = b.summary()
+                out["seconds"] += dt_
+                out["gpu_ms"].append(b.info()["last_step_ms"])
+                out["gamma"].append([g[b.case_slice(i)].copy() for i in range(n)])
+                out["iterations"].append(sm[:, 7].copy())
+                out["start"].append(sm[:, 10].copy())
+        return out
+
+    res = {}
+    sims = [Simulation(js, device=device) for js in jsons]
+    for sim, st in zip(sims, states):
+        sim.set_state(st)
+    plain = {"seconds": 0.0, "gamma": [], "iterations": []}
+    for k in window:
+        fss = [w.freestream(k * DT, sim.nr_freestream_points) for sim, w in zip(sims, winds)]
+        t1 = time.perf_counter()
+        rs = [sim.do_step(time=k * DT, time_step=DT, freestream_velocity=f) for sim, f in zip(sims, fss)]
+        dt_ = time.perf_counter() - t1
+        if k in timed:
+            plain["seconds"] += dt_
+            plain["gamma"].append([r.circulation_strength.copy() for r in rs])
+            plain["iterations"].append(np.array([r.iterations for r in rs], dtype=float))
+    for sim in sims:
+        sim.close()
+    del sims
+    print(f"plain arm {plain['seconds']:.1f} s", file=sys.stderr, flush=True)
+    res["plain"] = plain
+    res["batched"] = run_arm(src, None)
+    src.close()
+    ex_net = WS.extrapolation_only(device)
+    for mode, mnet in (("extrapolation", ex_net), ("warm", net)):
+        b = Batch(jsons, device=device)
+        for i, st in enumerate(states):
+            b.set_case_state(i, st)
+        res[mode] = run_arm(b, mnet.handle)
+        b.close()
+    ex_net.close()
+
+    # the oracle from the same filled state, for sampled cases whose roll-up it sweeps in about a second
+    sizes = sorted((S.setup_rollup_pairs(js), i) for i, js in enumerate(jsons))
+    sample = [i for p, i in sizes if p <= 2e9][-4:]
+    oracle_err = {m: 0.0 for m in res}
+    t1 = time.perf_counter()
+    for i in sample:
+        o = OracleSimulation(jsons[i], nthreads=os.cpu_count() or 1)
+        o.set_state(states[i])
+        ti = 0
+        for k in window:
+            r = o.do_step(time=k * DT, time_step=DT, freestream_velocity=winds[i].freestream(k * DT, o.nr_freestream_points))
+            if k in timed:
+                ref = r.circulation_strength
+                for m in res:
+                    e = float(np.max(np.abs(res[m]["gamma"][ti][i] - ref)) / np.max(np.abs(ref)))
+                    oracle_err[m] = max(oracle_err[m], e)
+                ti += 1
+    t_oracle = time.perf_counter() - t1
+
+    def worst_vs_plain(arm):
+        w = 0.0
+        for ga, gp in zip(res[arm]["gamma"], res["plain"]["gamma"]):
+            for x, y in zip(ga, gp):
+                w = max(w, float(np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1e-300)))
+        return w
+
+    arms = ("batched", "extrapolation", "warm")
+    solves = n * steps
+    return {"workload": f"{n} uneven cases (seed 2024) with every wake full: steps {timed[0]}-{timed[-1]} after "
+                        f"{fill} untimed steps (wakes of 50-400 rows), all arms from one state",
+            "spin_up_s": spin_s, "pairs_per_step": pairs,
+            "solves_per_s": {m: solves / res[m]["seconds"] for m in ("plain",) + arms},
+            "speedup_vs_plain": {m: res["plain"]["seconds"] / res[m]["seconds"] for m in arms},
+            "batched_step_gpu_ms": {m: float(np.mean(res[m]["gpu_ms"])) for m in arms},
+            "iterations_per_solve": {m: float(np.mean(res[m]["iterations"])) for m in ("plain",) + arms},
+            "start_taken_fraction": {m: {"plain": float(np.mean(np.array(res[m]["start"]) == 0.0)),
+                                         "extrapolation": float(np.mean(np.array(res[m]["start"]) == 1.0)),
+                                         "network": float(np.mean(np.array(res[m]["start"]) == 2.0))}
+                                     for m in ("extrapolation", "warm")},
+            "max_rel_circulation_diff_vs_plain": {m: worst_vs_plain(m) for m in arms},
+            "oracle": {"cases": sample, "max_rel_circulation_error": oracle_err,
+                       "how": "oracle (C++ f64) loaded with each sampled case's filled state and stepped through the "
+                              f"same window; {t_oracle:.1f} s"},
+            "timing": "host clock around each public call, host freestream in, circulation and force summary out"}
+
+
 def qs_sweep(args, device):
     """Solves/s of a quasi-steady sweep (the shape of CompleteSailModel wind-angle sweeps):
     seeded cases of 1-6 sails x 16-96 panels at AWA 20-180 deg, 5-20 m/s, quasi-steady
@@ -575,27 +764,32 @@ def qs_sweep(args, device):
 # profiling workload: a short run whose last sweep launch is a full roll-up
 # --------------------------------------------------------------------------------------
 def run_profile_rollup(args):
-    """4 sails x 64 panels, `rows` wake rows, all-near-field, run rows + 4 steps: the last
-    k_bs_sweep launch of the process is the roll-up of a full wake (shared segments unless
-    --rings). Prints the number of k_bs_sweep launches, so an ncu capture can select the last
-    one with -k regex:k_bs_sweep -s <launches - 1> -c 1."""
+    """4 sails x 64 panels, `rows` wake rows, all-near-field (or `--far-field-ratio`), run
+    rows + 4 steps: the last k_bs_sweep launch of the process is the roll-up of a full wake
+    (shared segments unless --rings or a finite far-field ratio). Prints the number of
+    k_bs_sweep launches, so an ncu capture can select the last one with -k regex:k_bs_sweep
+    -s <launches - 1> -c 1, and the event time of the last roll-up sweep."""
     from stormbird_gb300 import Simulation
     from stormbird_gb300 import setups as S
 
     rows = args.rows or 60
-    sim = Simulation(S.wing_sail_row(SAILS, PANELS, rows, time_step=DT, far_field_ratio=1e30))
+    sim = Simulation(S.wing_sail_row(SAILS, PANELS, rows, time_step=DT, far_field_ratio=args.far_field_ratio))
     if args.rings:
         sim.set_segment_sharing(False)
     wind = S.GustyWind(seed=0)
     n = sim.nr_freestream_points
     launches = 0
     for k in range(rows + 4):
+        if k == rows + 3:
+            sim.enable_timing(True)
         sim.do_step(time=k * DT, time_step=DT, freestream_velocity=wind.freestream(k * DT, n))
         c = sim.last_step_counters()
         launches += (1 if c["free_wake_panels"] > 0 else 0) + (1 if c["rollup_targets"] > 0 else 0)
-    print(json.dumps({"mode": "profile-rollup", "rows": rows, "k_bs_sweep_launches": launches,
+    print(json.dumps({"mode": "profile-rollup", "rows": rows, "far_field_ratio": args.far_field_ratio,
+                      "k_bs_sweep_launches": launches,
                       "shared_segments": sim.segment_sharing_active, "rollup_segments": c["rollup_segments"],
-                      "rollup_targets": c["rollup_targets"]}), flush=True)
+                      "rollup_targets": c["rollup_targets"], "rollup_panels": c["rollup_panels"],
+                      "rollup_sweep_kernel_ms": sim.last_step_timing()["rollup_sweep_kernel"]}), flush=True)
 
 
 def run_profile_batch(args):
@@ -621,6 +815,92 @@ def run_profile_batch(args):
     print(json.dumps({"mode": "profile-batch", "cases": n, "steps": steps, "step_gpu_ms": gpu_ms,
                       "step_host_ms": host_ms, "pairs_last_step": b.info()["pairs"]}), flush=True)
     b.close()
+
+
+def run_profile_fill(args):
+    """The batched part's uneven cases (`--batch-cases`) stepped as one Batch for
+    `--fill-steps` steps from a cold start (graph replay), so every wake fills (wake lengths
+    up to 400 rows). Prints the device time of every 20th step (also to stderr as it goes),
+    the host time of the whole run and the panel-target pairs of the last step."""
+    from stormbird_gb300 import Batch
+    from stormbird_gb300 import setups as S
+    from stormbird_gb300 import warm_start as WS
+
+    n = args.batch_cases
+    cases = [(WS.tight_solver(js, residual_tolerance=args.batch_tolerance), w) for js, w in S.uneven_cases(n, seed=2024)]
+    winds = [w for _, w in cases]
+    b = Batch([js for js, _ in cases], device=0)
+    gpu_ms, t0 = {}, time.perf_counter()
+    for k in range(args.fill_steps):
+        b.do_step(time=k * DT, time_step=DT, freestream_velocity=S.batch_freestream(b, winds, k * DT))
+        if k % 20 == 0 or k == args.fill_steps - 1:
+            gpu_ms[k] = b.info()["last_step_ms"]
+            print(f"step {k}: {gpu_ms[k]:.1f} ms, {time.perf_counter() - t0:.0f} s", file=sys.stderr, flush=True)
+    print(json.dumps({"mode": "profile-fill", "cases": n, "steps": args.fill_steps, "step_gpu_ms": gpu_ms,
+                      "host_s": time.perf_counter() - t0, "pairs_last_step": b.info()["pairs"]}), flush=True)
+    b.close()
+
+
+def wake_update_bytes(sails, panels, rows, chain_records):
+    """Algorithmic DRAM bytes per launch of the wake-update kernels (each byte that must cross
+    HBM once): advection reads the old point and the velocity of the point upstream and writes
+    the new point (72 B per point, f64); the panel kernel reads each wake point once (shared by
+    up to four panels), the old strength, writes the shifted strength and the 192-byte FP32
+    record (232 B per panel); the chain kernel writes a 192-byte record per chain and reads the
+    points and strengths it spans (points read by the spanwise and streamwise chains: twice)."""
+    npts_span = sails * (panels + 1)
+    pts = (rows + 1) * npts_span
+    pan = rows * sails * panels
+    return {"wake_advect": 72.0 * rows * npts_span + 24.0 * npts_span,
+            "wake_panels": 24.0 * pts + 16.0 * pan + 192.0 * pan,
+            "chain_records": 192.0 * chain_records + 2 * 24.0 * pts + 2 * 8.0 * pan}
+
+
+def measured_hbm_gbs():
+    """HBM copy rate of the GB300s (MEASURED_PEAKS.json, written by the pool's driver)."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(path))["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return 6800.0  # an earlier measurement on a GB300, when the file is absent
+
+
+def run_profile_wake(args):
+    """Wake-update kernels at the large single case (8 sails x 128 panels, 1000 wake rows:
+    1,033,032 points, 1,024,000 panels), all-near-field with the roll-up limited to one wake
+    point (ratio_of_wake_affected 1e-9: the chain records of the shared-segment roll-up are
+    built every step, the sweep is a single target), shed for 1002 steps; CUDA-event times of
+    the advection, panel-record and chain-record kernels over the last `--steps` steps, and
+    their algorithmic bytes per launch against the measured HBM copy rate."""
+    from stormbird_gb300 import Simulation
+    from stormbird_gb300 import setups as S
+
+    sails, panels, rows = 8, 128, args.rows or 1000
+    sim = Simulation(S.wing_sail_row(sails, panels, rows, time_step=DT, far_field_ratio=1e30,
+                                     ratio_of_wake_affected=1e-9))
+    wind = S.GustyWind(seed=3)
+    n = sim.nr_freestream_points
+    times = {"wake_advect": [], "wake_panels": [], "chain_records": []}
+    for k in range(rows + 2 + args.steps):
+        if k == rows + 2:
+            sim.enable_timing(True)
+        sim.do_step(time=k * DT, time_step=DT, freestream_velocity=wind.freestream(k * DT, n))
+        if k >= rows + 2:
+            tm = sim.last_step_timing()
+            for key in times:
+                times[key].append(tm[key + "_kernel"])
+    chain_n = ((rows + 1 + 3) // 4) * (4 * sails * ((panels + 3) // 4) + sails * (panels + 1))
+    nbytes = wake_update_bytes(sails, panels, rows, chain_n)
+    peak = measured_hbm_gbs()
+    out = {"mode": "profile-wake", "case": f"{sails} sails x {panels} panels, {rows} wake rows",
+           "wake_points": (rows + 1) * sails * (panels + 1), "panels": rows * sails * panels, "chain_records": chain_n,
+           "hbm_peak_gbs": peak, "kernels": {}}
+    for key, ms in times.items():
+        m = statistics.mean(ms)
+        gbs = nbytes[key] / (m * 1e-3) / 1e9 if m > 0 else None
+        out["kernels"][key] = {"mean_ms": m, "algorithmic_bytes": nbytes[key], "achieved_gbs": gbs,
+                               "frac_of_hbm_peak": gbs / peak if (gbs and peak) else None}
+    print(json.dumps(out), flush=True)
 
 
 def run_profile_mlp(args):
@@ -832,6 +1112,19 @@ def main():
     ap.add_argument("--precision-study", action="store_true",
                     help="FP32 / compensated FP32 / FP64 sweeps of the 8 x 128 panel, 1000-row case")
     ap.add_argument("--rows", type=int, default=0, help="wake rows of the --kernel-only wake (default 300)")
+    ap.add_argument("--far-field-ratio", type=float, default=1e30, help="far-field ratio of --profile-rollup")
+    ap.add_argument("--profile-fill", action="store_true",
+                    help="the batched part's uneven cases stepped until every wake is full (timing only)")
+    ap.add_argument("--fill-steps", type=int, default=402, help="steps of --profile-fill and of the filled-wake part")
+    ap.add_argument("--profile-wake", action="store_true",
+                    help="event-timed wake-update kernels of the 8 x 128 panel, 1000-row case")
+    ap.add_argument("--warm-start-training", action="store_true",
+                    help="config 4: 200k-solve training set from a filling batch, training, --save-net")
+    ap.add_argument("--save-net", default="", help="where --warm-start-training writes the parameters (.npy)")
+    ap.add_argument("--big-train-epochs", type=int, default=6, help="epochs of --warm-start-training")
+    ap.add_argument("--filled", action="store_true",
+                    help="config 3 on filled wakes: all arms from one filled state (network from --load-net)")
+    ap.add_argument("--load-net", default="", help="network parameters (.npy) for --filled")
     ap.add_argument("--batch-cases", type=int, default=512, help="uneven cases of the batched solves/s part (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=5, help="timed steps of the batched part")
     ap.add_argument("--tune-seconds", type=float, default=0.0,
@@ -865,6 +1158,14 @@ def main():
         run_profile_mlp(args)
     elif args.profile_batch:
         run_profile_batch(args)
+    elif args.profile_fill:
+        run_profile_fill(args)
+    elif args.profile_wake:
+        run_profile_wake(args)
+    elif args.warm_start_training:
+        run_warm_start_training(args)
+    elif args.filled:
+        run_filled(args)
     elif args.qs_only:
         print(json.dumps({"mode": "qs-sweep", **qs_sweep(args, 0)}), flush=True)
     else:

@@ -117,6 +117,11 @@ class Batch:
         _check(lib().sb_batch_get_case_state(self._h, int(i), as_ptr(out), out.size))
         return out
 
+    def set_warm_start(self, network_handle, mode: int = 1):
+        """Warm start of every case's solve (sb_batch_set_warm_start): mode 1 with a network
+        handle, 2 to record features and targets only, 0 off."""
+        _check(lib().sb_batch_set_warm_start(self._h, network_handle, int(mode)))
+
     def set_case_state(self, i: int, state):
         a = np.ascontiguousarray(np.asarray(state, dtype=np.float64).reshape(-1))
         _check(lib().sb_batch_set_case_state(self._h, int(i), as_ptr(a), a.size))

@@ -246,6 +246,9 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ long long s_item;
     __shared__ int s_timed_out;  // a tile wait of this CTA ran out
+    // far-field fast path (FP32 panel sweeps): bounding box of each warp's targets (hi parts)
+    __shared__ float s_wbox[kBsThreads / 32][6];
+    constexpr bool FAST_FAR = F32 && !CHAIN && !NEGLECT;
     __shared__ BsJob s_job;  // the current item's sweep (one copy per item, by thread 0)
 
     const int tid = threadIdx.x;
@@ -287,7 +290,10 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
         int tw[TT];
 #pragma unroll
         for (int t = 0; t < T; ++t) {
-            long long idx = ttile * TM + static_cast<long long>(t) * kBsThreads + tid;
+            // with the far-field fast path a thread's targets are adjacent (a warp's 64 targets
+            // are consecutive points, a compact box); else T rows of the tile apart
+            long long idx = ttile * TM + (FAST_FAR ? static_cast<long long>(tid) * T + t
+                                                   : static_cast<long long>(t) * kBsThreads + tid);
             valid[t] = idx < J.M;
             d3 p = valid[t] ? J.targets[idx] : mk(0, 0, 0);
             tw[t] = (NEGLECT && valid[t]) ? J.target_wing[idx] : -1;
@@ -313,6 +319,32 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
         if constexpr (F32) {
             X2h = make_float2(xh[0], xh[1]); Y2h = make_float2(yh[0], yh[1]); Z2h = make_float2(zh[0], zh[1]);
             X2l = make_float2(xl[0], xl[1]); Y2l = make_float2(yl[0], yl[1]); Z2l = make_float2(zl[0], zl[1]);
+        }
+        if constexpr (FAST_FAR) {
+            // box of the warp's valid targets (both lanes: 64 consecutive target points, compact
+            // along a wake row), reduced over the warp by butterflies
+            float b6[6] = {CUDART_INF_F, CUDART_INF_F, CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F};
+#pragma unroll
+            for (int u = 0; u < 2; ++u)
+                if (valid[u]) {
+                    b6[0] = fminf(b6[0], xh[u]);
+                    b6[1] = fminf(b6[1], yh[u]);
+                    b6[2] = fminf(b6[2], zh[u]);
+                    b6[3] = fmaxf(b6[3], xh[u]);
+                    b6[4] = fmaxf(b6[4], yh[u]);
+                    b6[5] = fmaxf(b6[5], zh[u]);
+                }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                for (int q = 0; q < 6; ++q) {
+                    const float w = __shfl_xor_sync(0xffffffffu, b6[q], o);
+                    b6[q] = q < 3 ? fminf(b6[q], w) : fmaxf(b6[q], w);
+                }
+            if ((tid & 31) == 0)
+#pragma unroll
+                for (int q = 0; q < 6; ++q) s_wbox[tid >> 5][q] = b6[q];
+            __syncwarp();
         }
 
         const int ntiles = static_cast<int>((pe - pb + TILE - 1) / TILE);
@@ -341,7 +373,65 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
 
             if constexpr (F32) {
                 float2 TX = bc(0.f), TY = bc(0.f), TZ = bc(0.f);
-                for (int p = 0; p < np; ++p) {
+                // Far-field fast path: when the box of the tile's panel centres lies farther from
+                // the box of the warp's targets than the tile's largest far-field radius (with a
+                // margin well beyond the FP32 rounding of the per-pair distance), every pair of
+                // the tile is a point doublet (panel.rs:53-57, 82-96) and the per-pair test
+                // below would decide so for every lane: the warp evaluates the doublets alone,
+                // with the same arithmetic (the same results), without the test and the votes.
+                bool all_far = false;
+                if constexpr (FAST_FAR) {
+                    const int lane = tid & 31;
+                    float c7[7] = {CUDART_INF_F, CUDART_INF_F, CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F,
+                                   0.f};
+                    for (int q = lane; q < np; q += 32) {
+                        const float4 c = *reinterpret_cast<const float4*>(&tile[buf][q].v[28]);  // centre hi, ff2
+                        c7[0] = fminf(c7[0], c.x);
+                        c7[1] = fminf(c7[1], c.y);
+                        c7[2] = fminf(c7[2], c.z);
+                        c7[3] = fmaxf(c7[3], c.x);
+                        c7[4] = fmaxf(c7[4], c.y);
+                        c7[5] = fmaxf(c7[5], c.z);
+                        c7[6] = fmaxf(c7[6], c.w);
+                    }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                        for (int q = 0; q < 7; ++q) {
+                            const float w = __shfl_xor_sync(0xffffffffu, c7[q], o);
+                            c7[q] = q < 3 ? fminf(c7[q], w) : fmaxf(c7[q], w);
+                        }
+                    const float* wb = s_wbox[tid >> 5];
+                    const float gx = fmaxf(0.f, fmaxf(c7[0] - wb[3], wb[0] - c7[3]));
+                    const float gy = fmaxf(0.f, fmaxf(c7[1] - wb[4], wb[1] - c7[4]));
+                    const float gz = fmaxf(0.f, fmaxf(c7[2] - wb[5], wb[2] - c7[5]));
+                    // (the reduced values are the same in every lane; the vote tells the compiler
+                    // the branch is warp-uniform, which keeps the register count of the kernel)
+                    all_far = __all_sync(0xffffffffu, c7[6] < CUDART_INF_F && gx * gx + gy * gy + gz * gz > 1.001f * c7[6]);
+                }
+                if (all_far) {
+                    // lanes of targets past the end compute values that are never stored; four
+                    // panels per trip give the scheduler independent chains to interleave
+#pragma unroll 4
+                    for (int p = 0; p < np; ++p) {
+                        const float* v = reinterpret_cast<const float*>(tile[buf][p].v);
+                        const float gam = v[kRec32Gamma];
+                        if (gam == 0.f) continue;  // uniform across the CTA
+                        const float2 ex = sub2s(X2h, v[28]);
+                        const float2 ey = sub2s(Y2h, v[29]);
+                        const float2 ez = sub2s(Z2h, v[30]);
+                        const float2 e2s = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
+                        const float2 ir = make_float2(rsqrt_n(fmaxf(e2s.x, FLT_MIN)), rsqrt_n(fmaxf(e2s.y, FLT_MIN)));
+                        const float2 ir2 = mul2(ir, ir);
+                        const float2 sd = mul2(bc(v[35] * gam), mul2(mul2(ir2, ir2), ir));
+                        const float nx = v[36], ny = v[37], nz = v[38];
+                        const float2 h3 = mul2(bc(3.f), fma2(ex, bc(nx), fma2(ey, bc(ny), mul2(ez, bc(nz)))));
+                        TX = fma2(sd, fma2(h3, ex, mul2(e2s, bc(-nx))), TX);
+                        TY = fma2(sd, fma2(h3, ey, mul2(e2s, bc(-ny))), TY);
+                        TZ = fma2(sd, fma2(h3, ez, mul2(e2s, bc(-nz))), TZ);
+                    }
+                }
+                for (int p = 0; p < (all_far ? 0 : np); ++p) {
                     const float* v = reinterpret_cast<const float*>(tile[buf][p].v);
                     if constexpr (CHAIN) {  // every pair near-field: the chain's segments
                         if (v[kChainAny] == 0.f) continue;  // uniform across the CTA
@@ -465,7 +555,8 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
 
 #pragma unroll
         for (int t = 0; t < T; ++t) {
-            long long idx = ttile * TM + static_cast<long long>(t) * kBsThreads + tid;
+            long long idx = ttile * TM + (FAST_FAR ? static_cast<long long>(tid) * T + t
+                                                   : static_cast<long long>(t) * kBsThreads + tid);
             if (idx < J.M) {
                 d3 u = mk(static_cast<double>(sx[t]) + static_cast<double>(cx[t]),
                           static_cast<double>(sy[t]) + static_cast<double>(cy[t]),

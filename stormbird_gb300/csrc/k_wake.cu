@@ -207,22 +207,22 @@ cudaError_t launch_wake_advect(const DevModel& m, const WakeBuffers& w, double d
 // ---------------------------------------------------------------------------------------
 // Panel::new (panel.rs:26-50, geometry_functions.rs:11-30) for corners p[0..3], written as
 // the FP32 sweep record (float-float positions) and, when r64 is not null, the FP64 record.
+// With an FP64 record (row 0, the FP64 mode) every field is evaluated in f64 as the reference
+// does and the FP32 record is its rounding. Without one, the fields that are only stored in
+// FP32 (edge reciprocals, area, normal) are evaluated in FP32 from the f64 edge vectors, and
+// the far-field radius^2 is max(|p1-p0|^2, |p2-p1|^2) * ratio^2, the reference's
+// (ratio * max(|p1-p0|, |p2-p1|))^2 without its square roots: this part's FP64 rate is 1/64 of
+// its FP32 rate, and the f64 square roots and divisions made the record kernel compute-bound.
 __device__ void write_panel_records(const d3 (&pp)[4], double rc, double g, double far_field_ratio, int wing,
                                     PanelRec<float>* r32, PanelRec<double>* r64) {
     const d3 c = 0.25 * (((pp[0] + pp[1]) + pp[2]) + pp[3]);
-    const double la = len(pp[1] - pp[0]), lb = len(pp[2] - pp[1]), lc = len(pp[3] - pp[2]), ld = len(pp[0] - pp[3]);
-    const double sp = (la + lb + lc + ld) * 0.5;
-    const double area = sqrt((sp - la) * (sp - lb) * (sp - lc) * (sp - ld));
-    const d3 n = normalize(cross(pp[2] - pp[0], pp[3] - pp[1]));
-    const double t = fmax(la, lb) * far_field_ratio;
-    const double ff2 = t * t;
-
     PanelRec<float> r;
     auto split = [](double x, float* hi, float* lo) {
         float h = static_cast<float>(x);
         *hi = h;
         *lo = static_cast<float>(x - static_cast<double>(h));
     };
+    double l2[4];
     for (int k = 0; k < 4; ++k) {
         const d3 ok = pp[k] - c;
         r.v[3 * k] = static_cast<float>(ok.x);
@@ -232,18 +232,12 @@ __device__ void write_panel_records(const d3 (&pp)[4], double rc, double g, doub
         r.v[12 + 3 * k] = static_cast<float>(dk.x);
         r.v[12 + 3 * k + 1] = static_cast<float>(dk.y);
         r.v[12 + 3 * k + 2] = static_cast<float>(dk.z);
-        const double l2 = len2(dk);
-        r.v[24 + k] = l2 > 0.0 ? static_cast<float>(1.0 / l2) : 0.f;
-        r.v[kRec32DD + k] = static_cast<float>(l2);
+        l2[k] = len2(dk);
+        r.v[kRec32DD + k] = static_cast<float>(l2[k]);
     }
     split(c.x, &r.v[28], &r.v[32]);
     split(c.y, &r.v[29], &r.v[33]);
     split(c.z, &r.v[30], &r.v[34]);
-    r.v[31] = static_cast<float>(ff2);
-    r.v[35] = static_cast<float>(area * kFourPiInv);
-    r.v[36] = static_cast<float>(n.x);
-    r.v[37] = static_cast<float>(n.y);
-    r.v[38] = static_cast<float>(n.z);
     r.v[kRec32Gamma] = static_cast<float>(g);
     // core length^4; a zero core (reference: factor 1) only occurs in the horseshoe path, which
     // runs in FP64, so the FP32 sweep always evaluates d^2 / sqrt(d^4 + rc^4)
@@ -251,8 +245,19 @@ __device__ void write_panel_records(const d3 (&pp)[4], double rc, double g, doub
     r.v[40] = static_cast<float>(rc2 * rc2);
     r.v[41] = static_cast<float>(wing);
     for (int k = kRec32DD + 4; k < 48; ++k) r.v[k] = 0.f;
-    *r32 = r;
     if (r64) {
+        const double la = sqrt(l2[0]), lb = sqrt(l2[1]), lc = sqrt(l2[2]), ld = sqrt(l2[3]);
+        const double sp = (la + lb + lc + ld) * 0.5;
+        const double area = sqrt((sp - la) * (sp - lb) * (sp - lc) * (sp - ld));
+        const d3 n = normalize(cross(pp[2] - pp[0], pp[3] - pp[1]));
+        const double t = fmax(la, lb) * far_field_ratio;
+        const double ff2 = t * t;
+        for (int k = 0; k < 4; ++k) r.v[24 + k] = l2[k] > 0.0 ? static_cast<float>(1.0 / l2[k]) : 0.f;
+        r.v[31] = static_cast<float>(ff2);
+        r.v[35] = static_cast<float>(area * kFourPiInv);
+        r.v[36] = static_cast<float>(n.x);
+        r.v[37] = static_cast<float>(n.y);
+        r.v[38] = static_cast<float>(n.z);
         PanelRec<double> q;
         for (int k = 0; k < 4; ++k) {
             q.v[3 * k] = pp[k].x;
@@ -273,7 +278,29 @@ __device__ void write_panel_records(const d3 (&pp)[4], double rc, double g, doub
         q.v[26] = static_cast<double>(wing);
         q.v[27] = 0.0;
         *r64 = q;
+    } else {
+        float lf[4];
+        for (int k = 0; k < 4; ++k) {
+            const float q = static_cast<float>(l2[k]);
+            r.v[24 + k] = q > 0.f ? __frcp_rn(q) : 0.f;
+            lf[k] = __fsqrt_rn(q);
+        }
+        const float sp = (lf[0] + lf[1] + lf[2] + lf[3]) * 0.5f;
+        // a degenerate quadrilateral can round the product below zero: area 0
+        const float prod = fmaxf((sp - lf[0]) * (sp - lf[1]) * (sp - lf[2]) * (sp - lf[3]), 0.f);
+        r.v[35] = __fsqrt_rn(prod) * static_cast<float>(kFourPiInv);
+        const d3 a = pp[2] - pp[0], b = pp[3] - pp[1];
+        const float ax = static_cast<float>(a.x), ay = static_cast<float>(a.y), az = static_cast<float>(a.z);
+        const float bx = static_cast<float>(b.x), by = static_cast<float>(b.y), bz = static_cast<float>(b.z);
+        const float nx = ay * bz - az * by, ny = az * bx - ax * bz, nz = ax * by - ay * bx;
+        const float nl = __fsqrt_rn(nx * nx + ny * ny + nz * nz);
+        const float inl = nl > 0.f ? __frcp_rn(nl) : 0.f;
+        r.v[36] = nx * inl;
+        r.v[37] = ny * inl;
+        r.v[38] = nz * inl;
+        r.v[31] = static_cast<float>(fmax(l2[0], l2[1]) * (far_field_ratio * far_field_ratio));
     }
+    *r32 = r;
 }
 
 __device__ inline void wake_panel_elem(const DevModel& m, const WakeBuffers& w, int shift, long long id) {
@@ -381,9 +408,9 @@ __device__ inline void chain_record_elem(const ChainArgs& a, long long n_build, 
             rec.v[kChainD + 3 * k] = static_cast<float>(dk.x);
             rec.v[kChainD + 3 * k + 1] = static_cast<float>(dk.y);
             rec.v[kChainD + 3 * k + 2] = static_cast<float>(dk.z);
-            const double l2 = len2(dk);
-            rec.v[kChainIl + k] = l2 > 0.0 ? static_cast<float>(1.0 / l2) : 0.f;
-            rec.v[kChainDD + k] = static_cast<float>(l2);
+            const float l2 = static_cast<float>(len2(dk));
+            rec.v[kChainIl + k] = l2 > 0.f ? __frcp_rn(l2) : 0.f;  // FP32: an f64 division costs ~10 FP64 instructions here
+            rec.v[kChainDD + k] = l2;
             rec.v[kChainG + k] = static_cast<float>(g[k] * kFourPiInv);
             any += fabs(g[k]);
         }

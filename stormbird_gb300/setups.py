@@ -307,6 +307,17 @@ def complete_sail_model(nr_sails=2, panels_per_sail=24, spacing=40.0, set_points
                        "controller": controller})
 
 
+def setup_rollup_pairs(setup_json: str) -> int:
+    """Panel-target pairs of a dynamic setup's roll-up sweep once its wake is full: every wake
+    point (rows + 1 per span point) against every panel (rows per span line)."""
+    d = json.loads(setup_json)
+    wings = d["line_force_model"]["wing_builders"]
+    nsec = d["line_force_model"]["nr_sections"]
+    lines = sum(int(w.get("nr_sections") or nsec) for w in wings)  # straight wings: one segment each
+    rows = d["simulation_settings"]["Dynamic"]["wake"]["nr_panels_per_line_element"]
+    return (rows + 1) * (lines + len(wings)) * rows * lines
+
+
 def batch_freestream(batch, winds, t: float) -> np.ndarray:
     """Freestream of every case of a Batch at time t, case after case."""
     return np.concatenate([w.freestream(t, c["freestream_points"]) for w, c in zip(winds, batch.cases)])

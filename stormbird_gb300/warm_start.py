@@ -128,7 +128,7 @@ def collect(cases, steps: int, dt: float = 0.05, skip: int = 2, device: int = 0,
     torch = _torch()
     b = Batch([js for js, _ in cases], device=device)
     winds = [w for _, w in cases]
-    _check(lib().sb_batch_set_warm_start(b._h, None, 2))
+    b.set_warm_start(None, 2)
     xs, ts = [], []
     for k in range(steps):
         b.do_step(time=k * dt, time_step=dt, freestream_velocity=S.batch_freestream(b, winds, k * dt))
@@ -140,13 +140,16 @@ def collect(cases, steps: int, dt: float = 0.05, skip: int = 2, device: int = 0,
             xs.append(x)
             ts.append(t)
     b.close()
-    return torch.cat(xs), torch.cat(ts).clamp_(-clip, clip)
+    X, T = torch.cat(xs), torch.cat(ts).clamp_(-clip, clip)
+    del xs, ts
+    return X, T
 
 
-def train(net: WarmStartNet, X, T, epochs: int = 4, batch_rows: int = 8192, lr: float = 5e-4, seed: int = 0):
-    """Mini-batch Adam over shuffled rows; returns the mean loss of each epoch. An epoch
-    whose loss is not finite is undone (parameters of the last good epoch) and the learning
-    rate halved."""
+def train(net: WarmStartNet, X, T, epochs: int = 4, batch_rows: int = 8192, lr: float = 5e-4, seed: int = 0,
+          loss_every: int = 1):
+    """Mini-batch Adam over shuffled rows; returns the mean loss of each epoch (over every
+    `loss_every`-th step). An epoch whose loss is not finite is undone (parameters of the last
+    good epoch) and the learning rate halved."""
     torch = _torch()
     g = torch.Generator(device=X.device)
     g.manual_seed(seed)
@@ -158,10 +161,12 @@ def train(net: WarmStartNet, X, T, epochs: int = 4, batch_rows: int = 8192, lr: 
         perm = torch.randperm(n, device=X.device, generator=g)
         Xs, Ts = X[perm].contiguous(), T[perm].contiguous()
         tot, cnt = 0.0, 0
-        for s0 in range(0, n - batch_rows + 1, batch_rows):
-            loss = net.train_step(Xs[s0:s0 + batch_rows], Ts[s0:s0 + batch_rows], lr)
-            tot += loss
-            cnt += 1
+        for k, s0 in enumerate(range(0, n - batch_rows + 1, batch_rows)):
+            want = k % loss_every == 0
+            loss = net.train_step(Xs[s0:s0 + batch_rows], Ts[s0:s0 + batch_rows], lr, want_loss=want)
+            if want:
+                tot += loss
+                cnt += 1
         m = tot / max(cnt, 1)
         if not np.isfinite(m):
             net.set_params(good)
@@ -193,7 +198,7 @@ def run_batch(cases, steps: int, net: WarmStartNet | None = None, dt: float = 0.
     winds = [w for _, w in cases]
     b = Batch([js for js, _ in cases], device=device)
     if net is not None:
-        _check(lib().sb_batch_set_warm_start(b._h, net.handle, 1))
+        b.set_warm_start(net.handle)
     its, taken, gam, t_run, t_tune = [], [], [], 0.0, 0.0
     for k in range(steps):
         if tune_seconds > 0.0 and k == timed_from and k >= 4:

@@ -90,4 +90,6 @@ def main(reference_root: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the reference checkout (NTNU-IMT/stormbird)>")
+    main(sys.argv[1])
