@@ -389,6 +389,8 @@ def run_gb300(args):
         line["batched"] = batched_solves(args, local)
     if args.qs_cases > 0:
         line["qs_sweep"] = qs_sweep(args, local)
+    if rank == 0 and not args.no_precision_study:
+        line["precision_study"] = precision_study()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -936,21 +938,31 @@ def run_profile_mlp(args):
 # precision study: 8 sails x 128 panels, 1000 wake rows (1,024,000 rings, 1,033,032 points)
 # --------------------------------------------------------------------------------------
 def run_precision_study(args):
-    """FP32 (plain), FP32 compensated and FP64 Biot-Savart sweeps of the large single case.
+    print(json.dumps({"mode": "precision-study", **precision_study(fp64_targets=16384)}), flush=True)
+
+
+def precision_study(fp64_targets=4096):
+    """FP32 (plain), FP32 compensated and FP64 Biot-Savart sweeps of the large single case
+    (8 sails x 128 panels, 1000 wake rows: 1,024,000 rings, 1,033,032 points).
 
     1. Sweep error: a shed-wake-shaped panel set of the case's size (seeded), all-near-field;
        induced velocity at a seeded sample of wake points and of points one chord behind the
        sails, each precision against the f64 oracle (C++ restatement of the reference's
-       sweep) over the same panels; rates of every precision over all wake points (FP32) or a
-       target subset (FP64), device time of the standalone sweep call, against the measured
-       FP32 / FP64 FMA rates.
-    2. Circulation and force error: three identical simulations of the case shed 999 steps
-       (frozen wake: ratio_of_wake_affected 0, so a step costs the control-point sweep
-       only), then the 1000th step in each precision; the FP32 results against the FP64 one.
+       sweep) over the same panels; rates of every precision over all wake points (FP32) or
+       `fp64_targets` of them (FP64), host time of the standalone sweep call, against the
+       measured FP32 / FP64 FMA rates.
+    2. Circulation and force error: three identical simulations of the case (all-near-field,
+       the wake's roll-up limited to its first point, ratio_of_wake_affected 1e-9, which only
+       moves with the wing: a step costs the control-point sweep) shed 999 steps, then the
+       1000th step in each precision; each against the oracle's 1000th step from the same
+       state (sb_sim_get_state), and the FP32 ones against the FP64 one.
+    3. Wake update at this size: CUDA-event times of the advection, panel-record and
+       chain-record kernels of the compensated run's last step, their algorithmic bytes and
+       rate against the measured HBM copy rate.
     """
     import torch
 
-    from oracle.binding import bs_sweep
+    from oracle.binding import OracleSimulation, bs_sweep
     from stormbird_gb300 import Simulation
     from stormbird_gb300 import setups as S
     from stormbird_gb300.simulation import measure_fp32_peak, measure_fp64_peak, panel_sweep
@@ -966,7 +978,7 @@ def run_precision_study(args):
     t0 = time.perf_counter()
     ref = bs_sweep(corners, cores, strengths, 1e30, sample, nthreads=threads)
     t_oracle = time.perf_counter() - t0
-    out = {"mode": "precision-study", "case": f"{sails} sails x {panels} panels, {rows} wake rows",
+    out = {"case": f"{sails} sails x {panels} panels, {rows} wake rows",
            "panels": P, "wake_points": len(pts), "far_field_ratio": 1e30,
            "error_sample": len(sample), "oracle_seconds": t_oracle, "oracle_threads": threads}
     fp32_peak, fp64_peak = measure_fp32_peak(0, 5), measure_fp64_peak(0, 3)
@@ -975,7 +987,7 @@ def run_precision_study(args):
     for mode in ("fp32", "kahan", "fp64"):
         got = panel_sweep(corners, strengths, cores, sample, far_field_ratio=1e30, precision=mode)
         err = float(np.max(np.linalg.norm(got - ref, axis=1)) / np.max(np.linalg.norm(ref, axis=1)))
-        targets = pts if mode != "fp64" else pts[rng.choice(len(pts), 16384, replace=False)]
+        targets = pts if mode != "fp64" else pts[rng.choice(len(pts), fp64_targets, replace=False)]
         panel_sweep(corners[:1024], strengths[:1024], cores[:1024], targets[:256], 1e30, precision=mode)  # warm-up
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -990,8 +1002,9 @@ def run_precision_study(args):
     out["sweep"] = sweep
     out["sweep_timing"] = "host clock around sb_panel_sweep (includes the H2D of corners and targets and the record build)"
 
-    # circulation and forces: identical states, last step in each precision
-    js = S.wing_sail_row(nr_sails=sails, panels_per_sail=panels, wake_rows=rows, ratio_of_wake_affected=0.0)
+    # circulation and forces: identical states, last step in each precision and in the oracle
+    js = S.wing_sail_row(nr_sails=sails, panels_per_sail=panels, wake_rows=rows, far_field_ratio=1e30,
+                         ratio_of_wake_affected=1e-9)
     wind = S.GustyWind(seed=3)
     sims = {m: Simulation(js) for m in ("kahan", "fp32", "fp64")}
     n = sims["kahan"].nr_freestream_points
@@ -1003,24 +1016,50 @@ def run_precision_study(args):
         for s in sims.values():
             s.do_step_device(time=k * DT, time_step=DT, freestream_device_ptr=fs_dev.data_ptr())
     t_spin = time.perf_counter() - t0
-    fs_dev.copy_(torch.from_numpy(wind.velocity((rows - 1) * DT)).expand(n, 3))
+    state = sims["kahan"].state()
+    t_last = (rows - 1) * DT
+    fs_dev.copy_(torch.from_numpy(wind.velocity(t_last)).expand(n, 3))
     torch.cuda.synchronize()
     res = {}
+    sims["kahan"].enable_timing(True)
     for m, s in sims.items():
         s.set_precision(m)
-        s.do_step_device(time=(rows - 1) * DT, time_step=DT, freestream_device_ptr=fs_dev.data_ptr())
+        s.do_step_device(time=t_last, time_step=DT, freestream_device_ptr=fs_dev.data_ptr())
         res[m] = s.read_output()
+    tm = sims["kahan"].last_step_timing()
+    t0 = time.perf_counter()
+    o = OracleSimulation(js, nthreads=threads)
+    o.set_state(state)
+    ro = o.do_step(time=t_last, time_step=DT, freestream_velocity=wind.freestream(t_last, n))
+    t_oracle_step = time.perf_counter() - t0
+    g_o, f_o = ro.circulation_strength, ro.integrated_forces_sum()
     g64, f64 = res["fp64"].circulation_strength, res["fp64"].integrated_forces_sum()
-    out["solution"] = {m: {"rel_circulation_error_vs_fp64": float(np.max(np.abs(res[m].circulation_strength - g64))
-                                                                  / np.max(np.abs(g64))),
-                           "rel_force_error_vs_fp64": float(np.linalg.norm(res[m].integrated_forces_sum() - f64)
-                                                            / np.linalg.norm(f64))}
-                       for m in ("kahan", "fp32")}
-    out["solution_setup"] = ("1000-step frozen-wake runs (ratio_of_wake_affected 0), identical through step 999, "
-                             f"last step in each precision; spin-up {t_spin:.1f} s for the three runs")
+
+    def rel(g, f, gr, fr):
+        return {"circulation": float(np.max(np.abs(g - gr)) / np.max(np.abs(gr))),
+                "force": float(np.linalg.norm(f - fr) / np.linalg.norm(fr))}
+
+    out["solution"] = {m: {"vs_oracle": rel(res[m].circulation_strength, res[m].integrated_forces_sum(), g_o, f_o),
+                           "vs_gpu_fp64": rel(res[m].circulation_strength, res[m].integrated_forces_sum(), g64, f64)}
+                       for m in ("kahan", "fp32", "fp64")}
+    out["solution_setup"] = ("1000-step runs, identical through step 999 (compensated FP32), last step in each "
+                             f"precision and in the oracle from the same state; spin-up {t_spin:.1f} s for the three "
+                             f"runs, oracle step {t_oracle_step:.1f} s")
+    chain_n = ((rows + 1 + 3) // 4) * (4 * sails * ((panels + 3) // 4) + sails * (panels + 1))
+    nbytes = wake_update_bytes(sails, panels, rows, chain_n)
+    peak = measured_hbm_gbs()
+    wk = {}
+    for key in ("wake_advect", "wake_panels", "chain_records"):
+        ms = tm[key + "_kernel"]
+        gbs = nbytes[key] / (ms * 1e-3) / 1e9 if ms > 0 else None
+        wk[key] = {"ms": ms, "algorithmic_bytes": nbytes[key], "achieved_gbs": gbs,
+                   "frac_of_hbm_peak": gbs / peak if (gbs and peak) else None}
+    out["wake_update"] = {"kernels": wk, "hbm_peak_gbs": peak,
+                          "how": "CUDA events around each kernel in the compensated run's 1000th step "
+                                 "(1,033,032 points, 1,024,000 panels, 516,056 chain records)"}
     for s in sims.values():
         s.close()
-    print(json.dumps(out), flush=True)
+    return out
 
 
 # --------------------------------------------------------------------------------------
@@ -1109,6 +1148,8 @@ def main():
     ap.add_argument("--profile-mlp", action="store_true", help="warm-start network forward passes (GEMM capture)")
     ap.add_argument("--profile-batch", action="store_true",
                     help="the batched part's uneven cases stepped as one batch (launch-list capture)")
+    ap.add_argument("--no-precision-study", action="store_true",
+                    help="leave the 8 x 128 panel, 1000-row precision study out of the default run")
     ap.add_argument("--precision-study", action="store_true",
                     help="FP32 / compensated FP32 / FP64 sweeps of the 8 x 128 panel, 1000-row case")
     ap.add_argument("--rows", type=int, default=0, help="wake rows of the --kernel-only wake (default 300)")
