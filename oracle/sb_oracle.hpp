@@ -340,6 +340,38 @@ struct Foil {
     double added_mass_coefficient(double acc) const { return p.added_mass_factor * acc; }
 };
 
+template <class T>
+inline T linear_interpolation(double xt, const std::vector<double>& xd, const std::vector<T>& yd);
+
+// section_models/rotating_cylinder.rs: coefficients tabulated over the spin ratio (the
+// surface speed over the flow speed), with the cylinder diameter = the chord length
+struct Cylinder {
+    sbsetup::RotatingCylinder p;
+    // rotating_cylinder.rs:76-83
+    double spin_ratio(double diameter, double velocity) const {
+        double circumference = PI * diameter;
+        double tangential_velocity = circumference * p.revolutions_per_second;
+        return -tangential_velocity / velocity;
+    }
+    // rotating_cylinder.rs:85-93
+    double lift_coefficient_from_spin_ratio(double sr) const {
+        return linear_interpolation(std::fabs(sr), p.spin_ratio_data, p.cl_data) * signum(sr);
+    }
+    // rotating_cylinder.rs:95-101
+    double drag_coefficient_from_spin_ratio(double sr) const {
+        return linear_interpolation(std::fabs(sr), p.spin_ratio_data, p.cd_data);
+    }
+    // rotating_cylinder.rs:103-113
+    double lift_coefficient(double diameter, double velocity) const {
+        return lift_coefficient_from_spin_ratio(spin_ratio(diameter, velocity));
+    }
+    double drag_coefficient(double diameter, double velocity) const {
+        return drag_coefficient_from_spin_ratio(spin_ratio(diameter, velocity));
+    }
+    // rotating_cylinder.rs:127-129
+    double added_mass_coefficient(double acc) const { return p.added_mass_factor * acc; }
+};
+
 // ---------------------------------------------------------------------------------------
 // Rigid body motion (stormath/src/rigid_body_motion.rs)
 // ---------------------------------------------------------------------------------------
@@ -409,6 +441,8 @@ struct LineForceModel {
     std::vector<double> chord_lengths;
     std::vector<bool> is_virtual;
     std::vector<Foil> foils;
+    std::vector<Cylinder> cylinders;  // per wing; used where is_cylinder
+    std::vector<char> is_cylinder;
     std::vector<Range> wing_indices;
     double density = 1.225;
     sbsetup::CoordinateSystem output_cs = sbsetup::CoordinateSystem::Global;
@@ -506,23 +540,38 @@ struct LineForceModel {
         return a;
     }
     const Foil& foil(size_t i) const { return foils[wing_index(i)]; }
-    // force_calculations.rs:138-160
-    std::vector<double> cl_pre_stall_drop(const std::vector<double>& a) const {
+    // section model of line i: a rotating cylinder (else the foil)
+    const Cylinder* cylinder(size_t i) const {
+        size_t w = wing_index(i);
+        return is_cylinder[w] ? &cylinders[w] : nullptr;
+    }
+    // force_calculations.rs:138-160 (a rotating cylinder's lift depends on the speed, not the angle)
+    std::vector<double> cl_pre_stall_drop(const std::vector<double>& a, const std::vector<V3>& v) const {
         std::vector<double> o(a.size());
-        for (size_t i = 0; i < a.size(); ++i) o[i] = foil(i).cl_pre_stall_with_drop_off(a[i]);
+        for (size_t i = 0; i < a.size(); ++i) {
+            const Cylinder* c = cylinder(i);
+            o[i] = c ? c->lift_coefficient(chord_lengths[i], length(v[i])) : foil(i).cl_pre_stall_with_drop_off(a[i]);
+        }
         return o;
     }
+    // force_calculations.rs:162-183 (zero for a rotating cylinder)
+    double cl_post_stall(size_t i, double a) const { return cylinder(i) ? 0.0 : foil(i).cl_post_stall_with_weight(a); }
     // force_calculations.rs:188-210
-    std::vector<double> cl_linear(const std::vector<double>& a) const {
+    std::vector<double> cl_linear(const std::vector<double>& a, const std::vector<V3>& v) const {
         std::vector<double> o(a.size());
-        for (size_t i = 0; i < a.size(); ++i) o[i] = foil(i).cl_linear(a[i]);
+        for (size_t i = 0; i < a.size(); ++i) {
+            const Cylinder* c = cylinder(i);
+            o[i] = c ? c->lift_coefficient(chord_lengths[i], length(v[i])) : foil(i).cl_linear(a[i]);
+        }
         return o;
     }
+    // force_calculations.rs:212-229
+    double cl_derivative(size_t i) const { return cylinder(i) ? 0.0 : foil(i).p.cl_initial_slope; }
     // force_calculations.rs:271-292 (circulation_strength with CirculationCorrection::None, :237-261)
     std::vector<double> circulation_strength(const std::vector<double>& a, const std::vector<V3>& v) const {
-        std::vector<double> cl = cl_pre_stall_drop(a);
+        std::vector<double> cl = cl_pre_stall_drop(a, v);
         if (include_viscous_lift)
-            for (size_t i = 0; i < cl.size(); ++i) cl[i] += foil(i).cl_post_stall_with_weight(a[i]);
+            for (size_t i = 0; i < cl.size(); ++i) cl[i] += cl_post_stall(i, a[i]);
         std::vector<double> g(v.size());
         for (size_t i = 0; i < v.size(); ++i) g[i] = -0.5 * chord_lengths[i] * length(v[i]) * cl[i];
         return g;
@@ -550,7 +599,7 @@ struct LineForceModel {
     // force_calculations.rs:591-627
     double average_residual_absolute(const std::vector<double>& g, const std::vector<double>& a, const std::vector<V3>& v) const {
         std::vector<double> cg = lift_coefficient_from_circulation(g, v);
-        std::vector<double> cd = cl_pre_stall_drop(a);
+        std::vector<double> cd = cl_pre_stall_drop(a, v);
         double s = 0.0;
         for (size_t i = 0; i < cg.size(); ++i) s += std::fabs(cg[i] - cd[i]);
         return s / static_cast<double>(cg.size());
@@ -601,6 +650,10 @@ inline LineForceModel build_line_force_model(const sbsetup::LineForceModelBuilde
         Foil f;
         f.p = wb.foil;
         m.foils.push_back(f);
+        Cylinder cy;
+        cy.p = wb.cylinder;
+        m.cylinders.push_back(cy);
+        m.is_cylinder.push_back(wb.rotating_cylinder ? 1 : 0);
         m.local_wing_angles.push_back(0.0);
     }
     if (!b.local_wing_angles.empty()) m.local_wing_angles = b.local_wing_angles;
@@ -1043,11 +1096,11 @@ inline SolverResult solve_linearized(const sbsetup::Linearized& st, const LineFo
         ndir[i] = cross(un, sd);
     }
     std::vector<double> aoa = lfm.angles_of_attack(vel);
-    std::vector<double> cll = lfm.cl_linear(aoa);
+    std::vector<double> cll = lfm.cl_linear(aoa, vel);
     std::vector<double> A(n * n), rhs(n);
     for (size_t r = 0; r < n; ++r) {
         double ut = dot(vel[r], vdir[r]);
-        double dcl = lfm.foil(r).p.cl_initial_slope;  // force_calculations.rs:212-229
+        double dcl = lfm.cl_derivative(r);  // force_calculations.rs:212-229
         for (size_t c = 0; c < n; ++c) {
             double uin = dot(fw.factors[r * n + c], ndir[r]);
             A[r * n + c] = -dcl * uin / ut;
@@ -1065,8 +1118,8 @@ inline SolverResult solve_linearized(const sbsetup::Linearized& st, const LineFo
     total_velocity(vel);
     if (!st.disable_viscous_corrections) {
         std::vector<double> a2 = lfm.angles_of_attack(vel);
-        std::vector<double> cl_lin = lfm.cl_linear(a2);
-        std::vector<double> cl_full = lfm.cl_pre_stall_drop(a2);
+        std::vector<double> cl_lin = lfm.cl_linear(a2, vel);
+        std::vector<double> cl_full = lfm.cl_pre_stall_drop(a2, vel);
         for (size_t i = 0; i < n; ++i) if (std::fabs(cl_lin[i]) > MIN_POSITIVE) g[i] *= cl_full[i] / cl_lin[i];
         if (st.full_induced_velocity_correction) fw.update_induced_velocities_at_control_points(g);
         total_velocity(vel);
@@ -1177,7 +1230,6 @@ inline StepResult calculate_simulation_result(const LineForceModel& lfm, const S
         }
         rot_vel = lfm.rbm.to_body(rot_vel);
     }
-    (void)rot_vel;  // gyroscopic forces are zero for foils
     const auto& v = R.force_velocity;
     const auto& sl = lfm.span_lines_out();
     const auto& cv = body ? lfm.chord_local : lfm.chord_global;
@@ -1185,24 +1237,35 @@ inline StepResult calculate_simulation_result(const LineForceModel& lfm, const S
     R.sectional[0] = lfm.sectional_circulatory_forces(sr.circulation, v);
     for (size_t i = 0; i < n; ++i) {
         const Foil& f = lfm.foil(i);
+        const Cylinder* cyl = lfm.cylinder(i);
         double area = lfm.chord_lengths[i] * lfm.span_lines_local[i].len();
         double ff = 0.5 * area * lfm.density * length_squared(v[i]);
         // viscous lift :413-433
         if (!lfm.include_viscous_lift) {
-            double clv = f.cl_post_stall_with_weight(R.aoa[i]);
+            double clv = lfm.cl_post_stall(i, R.aoa[i]);
             V3 ld = normalize(cross(lfm.span_lines_local[i].rel(), v[i]));
             R.sectional[1][i] = ld * clv * ff;
         }
-        // drag :438-452
-        double cd = f.cd(R.aoa[i]);
+        // drag :438-452 (viscous_drag_coefficients :301-320)
+        double cd = cyl ? cyl->drag_coefficient(lfm.chord_lengths[i], length(v[i])) : f.cd(R.aoa[i]);
         R.sectional[2][i] = normalize(v[i]) * cd * ff;
-        // added mass :467-513
+        // added mass :467-513 (a foil's acceleration along its chord is left out, a cylinder's not)
         double strip = lfm.chord_lengths[i] * sl[i].len();
         V3 ra = R.acceleration[i];
         ra -= project(ra, sl[i].dir());
-        ra -= project(ra, cv[i]);
-        if (length(ra) != 0.0) R.sectional[3][i] = f.added_mass_coefficient(length(ra)) * lfm.density * strip * normalize(ra);
-        // gyroscopic: zero for Foil (:520-548)
+        if (!cyl) ra -= project(ra, cv[i]);
+        if (length(ra) != 0.0) {
+            double cam = cyl ? cyl->added_mass_coefficient(length(ra)) : f.added_mass_coefficient(length(ra));
+            R.sectional[3][i] = cam * lfm.density * strip * normalize(ra);
+        }
+        // gyroscopic :520-548: zero for a foil; a cylinder's spin angular momentum crossed with
+        // the body's rotation velocity
+        if (cyl) {
+            double i_zz = cyl->p.moment_of_inertia_2d * sl[i].len();
+            double radial_velocity = 2.0 * PI * cyl->p.revolutions_per_second;
+            V3 angular_momentum = i_zz * radial_velocity * sl[i].rel();
+            R.sectional[4][i] = cross(angular_momentum, rot_vel);
+        }
         V3 t = R.sectional[0][i];  // compute_total :163-172
         t += R.sectional[1][i];
         t += R.sectional[2][i];
@@ -1248,7 +1311,7 @@ struct Simulation {
     bool first_step_completed = false;
 
     explicit Simulation(const std::string& json, int nthreads = 1) {
-        setup = sbsetup::parse_setup(json);
+        setup = sbsetup::parse_setup(json, /*allow_rotating_cylinder=*/true);
         lfm = build_line_force_model(setup.line_force_model);
         size_t n = lfm.nr_span_lines();
         dynamic = setup.dynamic;

@@ -61,10 +61,26 @@ struct Foil {
     double added_mass_factor = 0.0;
 };
 
+// RotatingCylinder (section_models/rotating_cylinder.rs:10-61): lift and drag coefficients
+// tabulated over the spin ratio. Read for the oracle's rotor test only; the GPU path rejects
+// it (parse_setup without allow_rotating_cylinder).
+struct RotatingCylinder {
+    double revolutions_per_second = 0.0;
+    std::vector<double> spin_ratio_data = {0.0, 0.5, 1.0, 2.0, 3.0, 4.0, 5.0, 6.0, 8.0};
+    std::vector<double> cl_data = {0.0, 1.22, 2.56, 5.93, 9.10, 10.77, 12.80, 13.71, 16.90};
+    std::vector<double> cd_data = {0.457, 0.411, 0.296, 0.093, 0.066, 0.042, 0.064, 0.05, 0.076};
+    bool has_wake_angle_data = false;
+    std::vector<double> wake_angle_data;
+    double added_mass_factor = 0.0;
+    double moment_of_inertia_2d = 0.0;
+};
+
 struct WingBuilder {
     std::vector<Vec3> section_points;
     std::vector<Vec3> chord_vectors;
     Foil foil;
+    bool rotating_cylinder = false;  // the section model is `cylinder`, not `foil`
+    RotatingCylinder cylinder;
     bool has_virtual = false;
     std::vector<bool> line_segment_is_virtual;
     bool non_zero_circulation_at_ends[2] = {false, false};
@@ -310,7 +326,35 @@ inline Foil foil(const Value& v, const std::string& path) {
     return f;
 }
 
-inline WingBuilder wing_builder(const Value& v, const std::string& path) {
+inline RotatingCylinder rotating_cylinder(const Value& v, const std::string& path) {
+    RotatingCylinder c;
+    auto nums = [](const Value& x, const std::string& p) {
+        std::vector<double> o;
+        const auto& a = array(x, p);
+        for (size_t i = 0; i < a.size(); ++i) o.push_back(num(a[i], p + "[" + std::to_string(i) + "]"));
+        return o;
+    };
+    fields(v, path, {"revolutions_per_second", "spin_ratio_data", "cl_data", "cd_data", "wake_angle_data",
+                     "added_mass_factor", "moment_of_inertia_2d"},
+           [&](const std::string& k, const Value& x, const std::string& p) {
+               if (k == "revolutions_per_second") c.revolutions_per_second = num(x, p);
+               else if (k == "spin_ratio_data") c.spin_ratio_data = nums(x, p);
+               else if (k == "cl_data") c.cl_data = nums(x, p);
+               else if (k == "cd_data") c.cd_data = nums(x, p);
+               else if (k == "wake_angle_data") {
+                   if (x.is_null()) return;
+                   c.has_wake_angle_data = true;
+                   c.wake_angle_data = nums(x, p);
+               } else if (k == "added_mass_factor") c.added_mass_factor = num(x, p);
+               else c.moment_of_inertia_2d = num(x, p);
+           });
+    if (c.spin_ratio_data.empty() || c.cl_data.size() != c.spin_ratio_data.size() ||
+        c.cd_data.size() != c.spin_ratio_data.size())
+        bad(path, "spin_ratio_data, cl_data and cd_data must be non-empty and of one length");
+    return c;
+}
+
+inline WingBuilder wing_builder(const Value& v, const std::string& path, bool allow_rotating_cylinder) {
     WingBuilder w;
     require(v, path, {"section_points", "chord_vectors", "section_model"});
     fields(v, path, {"section_points", "chord_vectors", "section_model", "line_segment_is_virtual",
@@ -323,6 +367,11 @@ inline WingBuilder wing_builder(const Value& v, const std::string& path) {
                } else if (k == "section_model") {
                    const Value* payload;
                    std::string name = variant(x, p, &payload);
+                   if (name == "RotatingCylinder" && allow_rotating_cylinder) {
+                       w.rotating_cylinder = true;
+                       if (payload) w.cylinder = rotating_cylinder(*payload, p + ".RotatingCylinder");
+                       return;
+                   }
                    if (name != "Foil")
                        bad(p, "section model `" + name + "` is not supported by the GPU lifting-line path (Foil only)");
                    if (!payload) bad(p, "Foil needs an object");
@@ -351,7 +400,8 @@ inline WingBuilder wing_builder(const Value& v, const std::string& path) {
     return w;
 }
 
-inline LineForceModelBuilder line_force_model(const Value& v, const std::string& path) {
+inline LineForceModelBuilder line_force_model(const Value& v, const std::string& path,
+                                              bool allow_rotating_cylinder = false) {
     LineForceModelBuilder b;
     require(v, path, {"wing_builders", "nr_sections"});
     fields(v, path, {"wing_builders", "nr_sections", "density", "circulation_correction", "angle_of_attack_correction",
@@ -360,7 +410,8 @@ inline LineForceModelBuilder line_force_model(const Value& v, const std::string&
            [&](const std::string& k, const Value& x, const std::string& p) {
                if (k == "wing_builders") {
                    const auto& a = array(x, p);
-                   for (size_t i = 0; i < a.size(); ++i) b.wing_builders.push_back(wing_builder(a[i], p + "[" + std::to_string(i) + "]"));
+                   for (size_t i = 0; i < a.size(); ++i) b.wing_builders.push_back(
+                       wing_builder(a[i], p + "[" + std::to_string(i) + "]", allow_rotating_cylinder));
                } else if (k == "nr_sections") b.nr_sections = uint_(x, p);
                else if (k == "density") b.density = num(x, p);
                else if (k == "circulation_correction") {
@@ -523,8 +574,9 @@ inline QuasiSteadyWakeSettings quasi_steady_wake(const Value& v, const std::stri
 
 }  // namespace detail
 
-// Parses a `SimulationBuilder` JSON document (simulation_builder.rs:62-88).
-inline Setup parse_setup(const std::string& text) {
+// Parses a `SimulationBuilder` JSON document (simulation_builder.rs:62-88). Rotating-cylinder
+// section models are accepted only with allow_rotating_cylinder (the oracle's rotor test).
+inline Setup parse_setup(const std::string& text, bool allow_rotating_cylinder = false) {
     using namespace detail;
     sbjson::Value root;
     try {
@@ -538,7 +590,7 @@ inline Setup parse_setup(const std::string& text) {
     fields(root, "SimulationBuilder", {"line_force_model", "simulation_settings"},
            [&](const std::string& k, const Value& x, const std::string& p) {
                if (k == "line_force_model") {
-                   s.line_force_model = line_force_model(x, p);
+                   s.line_force_model = line_force_model(x, p, allow_rotating_cylinder);
                    return;
                }
                have_settings = true;

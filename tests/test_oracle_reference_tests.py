@@ -248,3 +248,46 @@ def test_panel_corner_reconstruction_matches_oracle_wake(oracle_mod):
     a = oracle_mod.bs_sweep(corners, np.full(len(strengths), 1.0), strengths, 5.0, targets, nthreads=2)
     b = sim.induced_velocities(targets)
     assert np.array_equal(a, b)
+
+
+def test_no_self_induced_velocity_rotor_sails(oracle_mod):
+    """lifting_line/tests/no_self_induced_velocity.rs:22-137: two rotor sails (rotating
+    cylinders, spin ratio 2) far apart with neglect_self_induced_velocities set, 100 dynamic
+    steps of 0.5 s in a uniform 1.2 m/s flow: the force coefficients equal the section table's
+    values at spin ratio 2, CD 1.497 within 5e-4 and CL 4.638 within 1e-4 (relative), the
+    reference's own tolerances. Rotating cylinders run in the oracle only (the GPU path takes
+    foil sections); the test pins the oracle's dynamic neglect-self path, its SimpleIterative
+    defaults and its force integration against the reference's tabulated numbers."""
+    diameter, span, u = 1.0, 5.0, 1.2
+    rps = -(u * 2.0) / (math.pi * diameter)  # -revolutions_per_second_from_spin_ratio(2, D, U)
+    cylinder = {"RotatingCylinder": {
+        "revolutions_per_second": rps,
+        "spin_ratio_data": [0.0, 1.0, 2.0, 3.0, 4.0, 5.0],
+        "cd_data": [0.554, 0.674, 1.497, 2.877, 3.556, 3.816],
+        "cl_data": [0.0, 1.889, 4.638, 6.794, 7.680, 7.950],
+        "wake_angle_data": [0.0, math.radians(20.0), math.radians(25.0), math.radians(35.0), math.radians(45.0),
+                            math.radians(60.0)]}}
+    wings = [S.wing_builder([(x, y, 0.0), (x, y, span)], [(diameter, 0, 0), (diameter, 0, 0)], cylinder)
+             for x, y in ((-1.0 * span, -10.0 * span), (1.0 * span, 10.0 * span))]
+    lfm = {"wing_builders": wings, "nr_sections": 10}
+    setup = S.simulation(lfm, dynamic=True, wake={"neglect_self_induced_velocities": True})
+    sim = oracle_mod.OracleSimulation(setup, nthreads=2)
+    n = sim.nr_freestream_points
+    fs = np.tile([u, 0.0, 0.0], (n, 1))
+    for i in range(100):
+        r = sim.do_step(time=0.5 * i, time_step=0.5, freestream_velocity=fs)
+    area = 2 * diameter * span  # total_projected_area: chord x span length of every strip
+    force_factor = 0.5 * 1.225 * u ** 2 * area
+    f = r.integrated_forces_sum()
+    cd, cl = f[0] / force_factor, f[1] / force_factor
+    assert abs(cd - 1.497) / 1.497 < 0.0005, cd
+    assert abs(cl - 4.638) / 4.638 < 0.0001, cl
+
+
+def test_rotating_cylinder_is_rejected_by_the_gpu_path_but_read_by_the_oracle(oracle_mod, gpu_lib):
+    """The setup schema reads rotating cylinders for the oracle; the GPU library's setup
+    rejects them as valid reference input outside its path (SB_ERR_UNSUPPORTED)."""
+    wings = [S.wing_builder([(0, 0, 0), (0, 0, 5)], [(1, 0, 0), (1, 0, 0)], {"RotatingCylinder": {}})]
+    setup = S.simulation({"wing_builders": wings, "nr_sections": 4}, dynamic=True)
+    oracle_mod.OracleSimulation(setup)
+    assert not gpu_lib.sb_sim_new(setup.encode(), 0) and gpu_lib.sb_last_status() == -7
