@@ -333,8 +333,10 @@ typedef struct sb_batch sb_batch;
 #define SB_BATCH_SUMMARY 11
 /* sb_batch_info fields: last step ms, panel-target pairs swept in the last step, tuning
  * waves, tuning CTAs per SM (0 = occupancy limit), roll-up grid, roll-up work items,
- * tuned (0/1), candidates timed, best tuned roll-up ms, graph in use (0/1), steps done. */
-#define SB_BATCH_INFO 11
+ * tuned (0/1), candidates timed, best tuned roll-up ms, graph in use (0/1), steps done,
+ * panels per shared-memory stage of the compensated panel sweeps, item schedule (0 the
+ * costliest case's items first, 1 case order). */
+#define SB_BATCH_INFO 13
 
 /* n_cases setup JSON strings (as sb_sim_new). NULL on error (sb_last_error names the case). */
 sb_batch* sb_batch_new(const char* const* setup_jsons, size_t n_cases, int device);
@@ -377,9 +379,12 @@ int sb_batch_previous_circulation_device(sb_batch* batch, double** circulation_d
 int sb_batch_set_precision(sb_batch* batch, int mode);
 /* CUDA-graph replay of the steady step (default on). */
 int sb_batch_use_graph(sb_batch* batch, int enable);
-/* Times the roll-up sweep of the current state for each work-decomposition candidate within
- * about budget_seconds and keeps the fastest for this batch and for later batches of the
- * same workload bucket in this process. Needs a batch whose roll-up has started. */
+/* Times the roll-up sweep of the current state for each candidate within about
+ * budget_seconds and keeps the fastest for this batch and for later batches of the same
+ * workload bucket in this process: first the tile shape (panels per shared-memory stage of
+ * the compensated panel sweeps: 64, 32, 96), then items per persistent CTA x CTAs per SM,
+ * then the item schedule (costliest case first, or case order). Needs a batch whose
+ * roll-up has started. */
 int sb_batch_autotune(sb_batch* batch, double budget_seconds);
 int sb_batch_info(const sb_batch* batch, double* info, size_t n);
 

@@ -17,7 +17,7 @@ from .native import lib
 
 SUMMARY = 11  # SB_BATCH_SUMMARY
 INFO_KEYS = ("last_step_ms", "pairs", "waves", "blocks_per_sm", "rollup_grid", "rollup_items", "tuned",
-             "tune_candidates", "tune_best_ms", "graph", "steps")
+             "tune_candidates", "tune_best_ms", "graph", "steps", "tile", "schedule")
 
 
 def _check(rc: int):

@@ -75,6 +75,8 @@ __global__ void k_gather(const GatherJob* jobs) {
 struct Tuning {
     int waves = 8;          // items per persistent CTA the item size aims at
     int blocks_per_sm = 0;  // persistent CTAs per SM (0: the occupancy limit)
+    int tile = 0;           // panels per shared-memory stage of the compensated FP32 sweeps (0: default)
+    int order = 0;          // item schedule: 0 the costliest case's items first, 1 case order
 };
 
 // Process-wide tuning results per workload bucket.
@@ -145,6 +147,7 @@ struct sb_batch {
         int sym = 0, neglect = 0;
         int chain = 0;  // sources are chain records (shared-segment roll-up)
         std::vector<int> cases;           // case of each job, costliest items first
+        int tile = 64;                    // panels per shared-memory stage of this group's launch
         std::vector<int> chunk;           // panels per source chunk of each job
         std::vector<long long> part_off;  // offset of each job's partial sums
         std::vector<long long> block_off; // first reduce block of each job
@@ -387,13 +390,14 @@ struct sb_batch {
     // Chunk sizes, item order, partial-sum offsets and grids for the tuning t.
     void plan(const Tuning& t) {
         drop_graphs();
-        const int tile = bs_tile_panels(precision);
         long long part_total = 0;
         job_entries = 0;
         for (auto& g : groups) {
+            const int tile = bs_tile_panels(precision, g.sym, g.chain, t.tile);
+            g.tile = tile;
             const int T = bs_targets_per_thread(g.sym);
             const long long TM = static_cast<long long>(kBsThreads) * T;
-            const int occ = bs_occupancy_blocks_per_sm(precision, g.sym, g.neglect);
+            const int occ = bs_occupancy_blocks_per_sm(precision, g.sym, g.neglect, g.chain ? 0 : t.tile);
             const int bps = t.blocks_per_sm > 0 ? std::min(t.blocks_per_sm, occ) : occ;
             g.grid = sms * bps;
             double total = 0.0;
@@ -416,10 +420,11 @@ struct sb_batch {
                 ch = std::min(std::max<long long>({ch, static_cast<long long>(tile), min_for_cap}), whole);
                 g.chunk[k] = static_cast<int>(ch);
             }
-            // costliest items first (LPT order); the order is fixed for the batch's life
+            // schedule 0: costliest items first (LPT order); 1: case order. Fixed until re-planned
             std::vector<size_t> order(n);
             std::iota(order.begin(), order.end(), 0);
-            std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return g.chunk[a] > g.chunk[b]; });
+            if (t.order == 0)
+                std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return g.chunk[a] > g.chunk[b]; });
             std::vector<int> cs(n), ch(n);
             for (size_t k = 0; k < n; ++k) {
                 cs[k] = g.cases[order[k]];
@@ -512,6 +517,7 @@ struct sb_batch {
         a.symmetry = g.sym;
         a.neglect = g.neglect;
         a.chain = g.chain;
+        a.tile = g.tile;
         ck(cudaMemsetAsync(a.work_counter, 0, sizeof(unsigned long long), main), "memset counter");
         ck(launch_bs_sweep(a, precision, g.grid, main), "batched Biot-Savart sweep");
         ck(launch_bs_reduce_jobs(a.jobs, a.n_jobs, g.reduce_blocks, main), "batched sweep reduce");
@@ -956,17 +962,10 @@ struct sb_batch {
         for (const auto& c : cases) active = active || (c->dynamic && c->rollup_active());
         if (!active) raise(SB_ERR_STATE, "autotuning needs a batch whose wake roll-up has started (4 steps)");
         ck(cudaStreamSynchronize(main), "sync");
-        int occ = 1;
-        for (const auto& g : groups) occ = std::max(occ, bs_occupancy_blocks_per_sm(precision, g.sym, g.neglect));
-        std::vector<Tuning> cand;
-        for (int w : {1, 2, 4, 8, 16, 32})
-            for (int b : {occ, occ - 1})
-                if (b >= 1) cand.push_back(Tuning{w, b});
-        Tuning best = tuning;
-        double best_ms = 1e300;
+        // times the roll-up sweeps of the current state under tuning t (best of two)
         double spent = 0.0;
         tune_candidates = 0;
-        for (const Tuning& t : cand) {
+        auto time_candidate = [&](const Tuning& t) {
             plan(t);
             fill_jobs();
             ck(cudaMemcpyAsync(d_jobs.p, h_jobs.p, job_entries * sizeof(BsJob), cudaMemcpyHostToDevice, main), "H2D jobs");
@@ -983,12 +982,36 @@ struct sb_batch {
             }
             spent += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
             tune_candidates += 1;
+            return ms;
+        };
+        Tuning best = tuning;
+        double best_ms = 1e300;
+        auto consider = [&](const Tuning& t) {
+            if (spent > budget_s) return;
+            const double ms = time_candidate(t);
             if (ms < best_ms) {
                 best_ms = ms;
                 best = t;
             }
-            if (spent > budget_s) break;
-        }
+        };
+        // 1. tile shape (panels per shared-memory stage) at the default decomposition
+        int tiles[4] = {0, 0, 0, 0};
+        const int n_tiles = bs_tile_choices(tiles, 4);
+        for (int k = 0; k < n_tiles; ++k) consider(Tuning{8, 0, tiles[k] == 64 ? 0 : tiles[k], 0});
+        // 2. items per persistent CTA x CTAs per SM for that tile
+        int occ = 1;
+        for (const auto& g : groups)
+            occ = std::max(occ, bs_occupancy_blocks_per_sm(precision, g.sym, g.neglect, g.chain ? 0 : best.tile));
+        const Tuning after_tile = best;
+        std::vector<int> blocks = {0};  // 0: the occupancy limit
+        if (occ >= 2) blocks.push_back(occ - 1);
+        for (int w : {1, 2, 4, 8, 16, 32})
+            for (int b : blocks)
+                if (!(w == after_tile.waves && b == after_tile.blocks_per_sm)) consider(Tuning{w, b, after_tile.tile, 0});
+        // 3. item schedule
+        Tuning alt = best;
+        alt.order = 1;
+        consider(alt);
         plan(best);
         fill_jobs();
         ck(cudaMemcpyAsync(d_jobs.p, h_jobs.p, job_entries * sizeof(BsJob), cudaMemcpyHostToDevice, main), "H2D jobs");
@@ -1237,7 +1260,9 @@ int sb_batch_info(const sb_batch* b, double* info, size_t n) {
                                      static_cast<double>(b->tune_candidates),
                                      b->tune_best_ms,
                                      (b->graph[0] || b->graph[1]) ? 1.0 : 0.0,
-                                     static_cast<double>(b->steps)};
+                                     static_cast<double>(b->steps),
+                                     static_cast<double>(bs_tile_panels(b->precision, 0, 0, b->tuning.tile)),
+                                     static_cast<double>(b->tuning.order)};
     for (size_t i = 0; i < n && i < SB_BATCH_INFO; ++i) info[i] = v[i];
     return SB_OK;
 }

@@ -235,9 +235,10 @@ __device__ __forceinline__ int find_job(const BsJob* jobs, int n, long long item
     return lo;
 }
 
-template <class R, int T, bool KAHAN, int SYM, bool NEGLECT, bool CHAIN>
+template <class R, int T, bool KAHAN, int SYM, bool NEGLECT, bool CHAIN, int TILE_PANELS = 0>
 __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
-    constexpr int TILE = TileSize<R>::value;
+    // panels per shared-memory stage: the precision's default, or a tuned shape (batched sweeps)
+    constexpr int TILE = TILE_PANELS ? TILE_PANELS : TileSize<R>::value;
     constexpr int TT = SYM ? 2 * T : T;  // mirrored targets ride along as extra targets
     constexpr bool F32 = sizeof(R) == 4;
     static_assert(!F32 || TT == 2, "the packed FP32 path holds exactly two targets per thread");
@@ -899,10 +900,17 @@ cudaError_t launch_horseshoe_matrix(const DevModel& m, int core_kind, double cor
 // ---------------------------------------------------------------------------------------
 // Host launchers
 // ---------------------------------------------------------------------------------------
-template <class R, int T, bool KAHAN, int SYM, bool NEGLECT, bool CHAIN = false>
+template <class R, int T, bool KAHAN, int SYM, bool NEGLECT, bool CHAIN = false, int TILE_PANELS = 0>
 static cudaError_t launch_t(const BsArgs& a, int grid, cudaStream_t s) {
-    k_bs_sweep<R, T, KAHAN, SYM, NEGLECT, CHAIN><<<grid, kBsThreads, 0, s>>>(a);
+    k_bs_sweep<R, T, KAHAN, SYM, NEGLECT, CHAIN, TILE_PANELS><<<grid, kBsThreads, 0, s>>>(a);
     return cudaGetLastError();
+}
+
+// Tile shapes the autotuner may pick for the compensated FP32 panel sweeps without symmetry
+// (the batch's sweeps): panels per shared-memory stage. 64 is the default.
+constexpr int kTunedTiles[3] = {64, 32, 96};
+static bool tuned_tile_variant(int precision, int symmetry, int chain, int tile) {
+    return precision == 0 && symmetry == 0 && !chain && (tile == 32 || tile == 96);
 }
 
 template <bool KAHAN>
@@ -917,6 +925,14 @@ static cudaError_t launch_chain(const BsArgs& a, int grid, cudaStream_t s) {
 
 template <class R, bool KAHAN>
 static cudaError_t launch_sym(const BsArgs& a, int grid, cudaStream_t s) {
+    if constexpr (KAHAN) {
+        if (a.symmetry == 0 && a.tile == 32)
+            return a.neglect ? launch_t<R, 2, KAHAN, 0, true, false, 32>(a, grid, s)
+                             : launch_t<R, 2, KAHAN, 0, false, false, 32>(a, grid, s);
+        if (a.symmetry == 0 && a.tile == 96)
+            return a.neglect ? launch_t<R, 2, KAHAN, 0, true, false, 96>(a, grid, s)
+                             : launch_t<R, 2, KAHAN, 0, false, false, 96>(a, grid, s);
+    }
     if (a.neglect) {
         switch (a.symmetry) {
             case 0: return launch_t<R, 2, KAHAN, 0, true>(a, grid, s);
@@ -935,6 +951,15 @@ static cudaError_t launch_sym(const BsArgs& a, int grid, cudaStream_t s) {
 
 int bs_targets_per_thread(int symmetry) { return symmetry == 0 ? 2 : 1; }
 int bs_tile_panels(int precision) { return precision == 2 ? TileSize<double>::value : TileSize<float>::value; }
+int bs_tile_panels(int precision, int symmetry, int chain, int tile) {
+    return tuned_tile_variant(precision, symmetry, chain, tile) ? tile : bs_tile_panels(precision);
+}
+int bs_tile_choices(int* tiles, int n) {
+    int k = 0;
+    for (int t : kTunedTiles)
+        if (k < n) tiles[k++] = t;
+    return k;
+}
 
 static std::atomic<int> g_sweep_wait_polls{-1};
 
@@ -950,12 +975,20 @@ cudaError_t launch_bs_sweep(const BsArgs& args, int precision, int grid, cudaStr
     }
     if (precision == 2) return launch_sym<double, false>(a, grid, s);
     if (precision == 1) return launch_sym<float, false>(a, grid, s);
+    if (!tuned_tile_variant(precision, a.symmetry, a.chain, a.tile)) a.tile = 0;
     return launch_sym<float, true>(a, grid, s);
 }
 
-int bs_occupancy_blocks_per_sm(int precision, int symmetry, int neglect) {
+int bs_occupancy_blocks_per_sm(int precision, int symmetry, int neglect, int tile) {
     int nb = 0;
     cudaError_t e;
+    if (tuned_tile_variant(precision, symmetry, 0, tile)) {
+        if (tile == 32) e = neglect ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bs_sweep<float, 2, true, 0, true, false, 32>, kBsThreads, 0)
+                                    : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bs_sweep<float, 2, true, 0, false, false, 32>, kBsThreads, 0);
+        else e = neglect ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bs_sweep<float, 2, true, 0, true, false, 96>, kBsThreads, 0)
+                         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bs_sweep<float, 2, true, 0, false, false, 96>, kBsThreads, 0);
+        return (e != cudaSuccess || nb < 1) ? 1 : nb;
+    }
 #define SB_OCC(R, T, K, S, NG) \
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bs_sweep<R, T, K, S, NG, false>, kBsThreads, 0)
     if (precision == 2) {

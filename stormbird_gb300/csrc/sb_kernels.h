@@ -45,6 +45,7 @@ struct BsArgs {
     int neglect = 0;
     int chain = 0;  // the sources are chain records (FP32 only, no neglect-self)
     int wait_polls = kWaitPolls;  // polls of each bounded wait on a tile copy
+    int tile = 0;  // panels per shared-memory stage (0: the precision's default; see bs_tile_panels)
 };
 
 // Polls of the bounded tile waits of later sweep launches (launch_bs_sweep overrides
@@ -59,7 +60,12 @@ constexpr int kBsReduceThreads = 256;
 
 int bs_targets_per_thread(int symmetry);
 int bs_tile_panels(int precision);
-int bs_occupancy_blocks_per_sm(int precision, int symmetry, int neglect);
+// Panels per stage a launch with BsArgs::tile = `tile` uses: the tuned shape where a variant
+// exists (compensated FP32, no symmetry, panel records), else the default.
+int bs_tile_panels(int precision, int symmetry, int chain, int tile);
+// The tile shapes the autotuner may try (the default first); returns how many were written.
+int bs_tile_choices(int* tiles, int n);
+int bs_occupancy_blocks_per_sm(int precision, int symmetry, int neglect, int tile = 0);
 cudaError_t launch_bs_sweep(const BsArgs& a, int precision, int grid, cudaStream_t s);
 cudaError_t launch_bs_reduce(const double* partial, int n_chunks, long long M, long long M_total, const d3* base, d3* out,
                              cudaStream_t s);

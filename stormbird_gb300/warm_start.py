@@ -218,7 +218,7 @@ def run_batch(cases, steps: int, net: WarmStartNet | None = None, dt: float = 0.
     info = b.info()
     b.close()
     return {"iterations": np.array(its), "start": np.array(taken), "gamma": gam, "seconds": t_run,
-            "tune_seconds": t_tune, "tuning": {k: info[k] for k in ("waves", "blocks_per_sm", "tuned")}}
+            "tune_seconds": t_tune, "tuning": {k: info[k] for k in ("waves", "blocks_per_sm", "tile", "schedule", "tuned")}}
 
 
 def max_rel_diff(a, ref) -> float:
