@@ -365,7 +365,9 @@ int sb_batch_get_summary(const sb_batch* batch, double* summary, size_t n);
 int sb_batch_read_case_output(sb_batch* batch, size_t i, sb_step_output* out);
 /* State of case i after the last step, in the layout of sb_sim_get_state (n = its size), and
  * the same to load a state into case i (a batch of the same setups can so start where
- * another stopped; the cases of a batch step together, so load every case's state). */
+ * another stopped; the cases of a batch step together, so load every case's state). A loaded
+ * case's warm-start history (previous freestream and solution) starts empty: its candidates
+ * wait for two steps of this batch. */
 int sb_batch_case_state_size(const sb_batch* batch, size_t i, size_t* n);
 int sb_batch_get_case_state(sb_batch* batch, size_t i, double* state, size_t n);
 int sb_batch_set_case_state(sb_batch* batch, size_t i, const double* state, size_t n);

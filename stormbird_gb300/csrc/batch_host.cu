@@ -177,6 +177,9 @@ struct sb_batch {
     DevBuf<d3> w_fs_old;
     PinnedBuf<FeatJob> h_feat;
     DevBuf<FeatJob> d_feat;
+    // per case, the steps whose freestream and solution w_fs_old / w_gamma_old hold (capped at
+    // 2): a case's own step count says nothing about them after a loaded state or a mode change
+    std::vector<int> warm_hist;
 
     // freestream from per-case wind models: [cases][time, ship velocity] staged per step
     bool has_wind = false;
@@ -645,6 +648,7 @@ struct sb_batch {
         if (mode == 1) mlp_reserve(m, N_total);
         mlp = mode == 1 ? m : nullptr;
         warm_mode = mode;
+        warm_hist.assign(cases.size(), 0);
         for (size_t i = 0; i < cases.size(); ++i) {
             cases[i]->candidate_p[0] = mode == 1 ? w_cand_ex.p + line_off[i] : nullptr;
             cases[i]->candidate_p[1] = mode == 1 ? w_cand.p + line_off[i] : nullptr;
@@ -671,6 +675,7 @@ struct sb_batch {
             f.S = c.S;
             f.W = c.W;
             f.steps = c.dynamic ? c.steps_completed : c.fd_count;
+            f.hist = warm_hist[i];
             f.row0 = line_off[i];
             h_feat.p[i] = f;
         }
@@ -772,6 +777,8 @@ struct sb_batch {
         cudaEventElapsedTime(&ms, ev_t0, ev_t1);
         last_ms = ms;
         steps += 1;
+        if (warm_mode != 0)
+            for (auto& h : warm_hist) h = std::min(h + 1, 2);
         if (mlp) mlp_check(mlp);
         if (h_err.p[0] != kDevOk) {
             ck(cudaMemset(err.p, 0, sizeof(int)), "memset");
@@ -791,11 +798,13 @@ struct sb_batch {
 
     // Loads case i's state (sb_sim_set_state layout). Every dynamic case of a batch must be
     // at the same wake-buffer parity and step count for the batched step; a state taken from
-    // another batch's case i at the same step keeps that.
+    // another batch's case i at the same step keeps that. The case's warm-start history starts
+    // again: its extrapolation candidate waits for two solutions of this batch's own.
     void set_case_state(size_t i, const double* state, size_t n) {
         ck(cudaStreamSynchronize(main), "sync");
         sb_sim& c = *cases[i];
         c.set_state(state, n);
+        if (i < warm_hist.size()) warm_hist[i] = 0;
         drop_graphs();
     }
 

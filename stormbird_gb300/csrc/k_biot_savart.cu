@@ -223,6 +223,36 @@ __device__ __forceinline__ void chain2(const float* v, float2 ex, float2 ey, flo
     }
 }
 
+// panel.rs:53-57 in f64 for one target given as float-float coordinates: the squared
+// distance of the float-float target from the float-float centre against the far-field
+// length squared (hi + lo). The points are the f64 points to within 2^-48 relative.
+__device__ __noinline__ bool near_f64(const float* v, float xh, float xl, float yh, float yl, float zh, float zl) {
+    const double dx = (static_cast<double>(xh) - v[28]) + (static_cast<double>(xl) - v[32]);
+    const double dy = (static_cast<double>(yh) - v[29]) + (static_cast<double>(yl) - v[33]);
+    const double dz = (static_cast<double>(zh) - v[30]) + (static_cast<double>(zl) - v[34]);
+    return dx * dx + dy * dy + dz * dz <= static_cast<double>(v[31]) + static_cast<double>(v[kRec32FF2Lo]);
+}
+
+// Near/far test (panel.rs:53-57) of one FP32 panel record at two targets, given the
+// float-float difference e = x - centre: n = (|e|^2 <= ff2) in FP32, except where |e|^2 lies
+// within kNearFarBand of ff2, where near_f64 decides. VOTE: every lane of the warp calls it
+// together, and the rare f64 branch is taken as one warp-uniform branch.
+template <bool VOTE>
+__device__ __forceinline__ void near_far2(const float* v, float2 X2h, float2 Y2h, float2 Z2h, float2 X2l, float2 Y2l,
+                                          float2 Z2l, float2 ex, float2 ey, float2 ez, bool& n0, bool& n1) {
+    const float ff2 = v[31];
+    const float2 e2 = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
+    n0 = e2.x <= ff2;
+    n1 = e2.y <= ff2;
+    const float2 d = sub2s(e2, ff2);
+    const float band = kNearFarBand * ff2;
+    const bool u0 = fabsf(d.x) <= band, u1 = fabsf(d.y) <= band;
+    if (VOTE ? __any_sync(0xffffffffu, u0 || u1) : (u0 || u1)) {
+        if (u0) n0 = near_f64(v, X2h.x, X2l.x, Y2h.x, Y2l.x, Z2h.x, Z2l.x);
+        if (u1) n1 = near_f64(v, X2h.y, X2l.y, Y2h.y, Y2l.y, Z2h.y, Z2l.y);
+    }
+}
+
 // Job holding global item `item` of a batched launch: the last job whose first item is
 // at or before it (item_begin ascending, jobs[0].item_begin == 0).
 __device__ __forceinline__ int find_job(const BsJob* jobs, int n, long long item) {
@@ -379,7 +409,7 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
                 // margin well beyond the FP32 rounding of the per-pair distance), every pair of
                 // the tile is a point doublet (panel.rs:53-57, 82-96) and the per-pair test
                 // below would decide so for every lane: the warp evaluates the doublets alone,
-                // with the same arithmetic (the same results), without the test and the votes.
+                // without the test and the votes.
                 bool all_far = false;
                 if constexpr (FAST_FAR) {
                     const int lane = tid & 31;
@@ -403,9 +433,13 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
                             c7[q] = q < 3 ? fminf(c7[q], w) : fmaxf(c7[q], w);
                         }
                     const float* wb = s_wbox[tid >> 5];
-                    const float gx = fmaxf(0.f, fmaxf(c7[0] - wb[3], wb[0] - c7[3]));
-                    const float gy = fmaxf(0.f, fmaxf(c7[1] - wb[4], wb[1] - c7[4]));
-                    const float gz = fmaxf(0.f, fmaxf(c7[2] - wb[5], wb[2] - c7[5]));
+                    // the boxes are of hi parts, each within 2^-24 |x| of its point: the gaps
+                    // shrink by both sides' bound before the test
+                    auto gap = [&](int q) {
+                        const float m = fmaxf(fmaxf(fabsf(c7[q]), fabsf(c7[q + 3])), fmaxf(fabsf(wb[q]), fabsf(wb[q + 3])));
+                        return fmaxf(0.f, fmaxf(c7[q] - wb[q + 3], wb[q] - c7[q + 3]) - 0x1p-23f * m);
+                    };
+                    const float gx = gap(0), gy = gap(1), gz = gap(2);
                     // (the reduced values are the same in every lane; the vote tells the compiler
                     // the branch is warp-uniform, which keeps the register count of the kernel)
                     all_far = __all_sync(0xffffffffu, c7[6] < CUDART_INF_F && gx * gx + gy * gy + gz * gz > 1.001f * c7[6]);
@@ -448,20 +482,16 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
                     }
                     const float gam = v[kRec32Gamma];
                     if (gam == 0.f) continue;  // uniform across the CTA
-                    const float ff2 = v[31];
-                    // target - centre from the hi parts alone: enough for the near/far test and
-                    // the far-field doublet (at least ff_ratio panel sizes away, where its
-                    // relative error stays near FP32 rounding); the ring below adds the lo parts
-                    float2 ex = sub2s(X2h, v[28]);
-                    float2 ey = sub2s(Y2h, v[29]);
-                    float2 ez = sub2s(Z2h, v[30]);
-                    float2 e2 = bc(0.f);
+                    // target - centre from the hi parts: the far-field doublet's, as in the
+                    // fast path above (at least ff_ratio panel sizes away); the float-float
+                    // difference (x_hi - c_hi) + (x_lo - c_lo) for the near/far test and the ring
+                    const float2 hx = sub2s(X2h, v[28]), hy = sub2s(Y2h, v[29]), hz = sub2s(Z2h, v[30]);
+                    const float2 ex = add2(hx, sub2s(X2l, v[32]));
+                    const float2 ey = add2(hy, sub2s(Y2l, v[33]));
+                    const float2 ez = add2(hz, sub2s(Z2l, v[34]));
                     bool n0 = true, n1 = true;
-                    if (ff2 != CUDART_INF_F) {  // panel.rs:53-57; uniform per panel
-                        e2 = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
-                        n0 = e2.x <= ff2;
-                        n1 = e2.y <= ff2;
-                    }
+                    if (v[31] != CUDART_INF_F)  // panel.rs:53-57; uniform per panel
+                        near_far2<true>(v, X2h, Y2h, Z2h, X2l, Y2l, Z2l, ex, ey, ez, n0, n1);
                     bool a0 = valid[0], a1 = valid[1];
                     if (NEGLECT) {
                         const int pw = static_cast<int>(v[41]);
@@ -470,7 +500,8 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
                     }
                     const bool any_near = __any_sync(0xffffffffu, (a0 && n0) || (a1 && n1));
                     const bool any_far = __any_sync(0xffffffffu, (a0 && !n0) || (a1 && !n1));
-                    if (any_far) {  // point doublet (panel.rs:82-96)
+                    if (any_far) {  // point doublet (panel.rs:82-96), the fast path's arithmetic
+                        const float2 e2 = fma2(hx, hx, fma2(hy, hy, mul2(hz, hz)));
                         const float2 e2s = make_float2(n0 ? 1.f : e2.x, n1 ? 1.f : e2.y);
                         // a subnormal |e|^2 (a degenerate panel) overflows s to inf either way
                         const float2 ir = make_float2(rsqrt_n(fmaxf(e2s.x, FLT_MIN)), rsqrt_n(fmaxf(e2s.y, FLT_MIN)));
@@ -479,16 +510,12 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
                         const float2 sm = make_float2((a0 && !n0) ? at : 0.f, (a1 && !n1) ? at : 0.f);
                         const float2 s = mul2(sm, mul2(mul2(ir2, ir2), ir));
                         const float nx = v[36], ny = v[37], nz = v[38];
-                        const float2 h3 = mul2(bc(3.f), fma2(ex, bc(nx), fma2(ey, bc(ny), mul2(ez, bc(nz)))));
-                        TX = fma2(s, fma2(h3, ex, mul2(e2s, bc(-nx))), TX);
-                        TY = fma2(s, fma2(h3, ey, mul2(e2s, bc(-ny))), TY);
-                        TZ = fma2(s, fma2(h3, ez, mul2(e2s, bc(-nz))), TZ);
+                        const float2 h3 = mul2(bc(3.f), fma2(hx, bc(nx), fma2(hy, bc(ny), mul2(hz, bc(nz)))));
+                        TX = fma2(s, fma2(h3, hx, mul2(e2s, bc(-nx))), TX);
+                        TY = fma2(s, fma2(h3, hy, mul2(e2s, bc(-ny))), TY);
+                        TZ = fma2(s, fma2(h3, hz, mul2(e2s, bc(-nz))), TZ);
                     }
                     if (any_near) {  // vortex ring (panel.rs:99-118)
-                        // float-float difference: (x_hi - c_hi) + (x_lo - c_lo)
-                        ex = add2(ex, sub2s(X2l, v[32]));
-                        ey = add2(ey, sub2s(Y2l, v[33]));
-                        ez = add2(ez, sub2s(Z2l, v[34]));
                         float2 ax, ay, az;
                         ring2(v, ex, ey, ez, ax, ay, az);
                         const float g4 = gam * static_cast<float>(kFourPiInv);
@@ -706,32 +733,28 @@ __device__ __forceinline__ void split2(double a, double b, float2& h, float2& l)
 }
 __device__ __forceinline__ void panel_unit2(const float* v, float2 X2h, float2 Y2h, float2 Z2h, float2 X2l, float2 Y2l,
                                             float2 Z2l, float2& ux, float2& uy, float2& uz) {
-    float2 ex = sub2s(X2h, v[28]), ey = sub2s(Y2h, v[29]), ez = sub2s(Z2h, v[30]);
-    const float ff2 = v[31];
-    float2 e2 = bc(0.f);
+    // hi-part difference for the doublet, float-float for the test and the ring (as k_bs_sweep)
+    const float2 hx = sub2s(X2h, v[28]), hy = sub2s(Y2h, v[29]), hz = sub2s(Z2h, v[30]);
+    const float2 ex = add2(hx, sub2s(X2l, v[32]));
+    const float2 ey = add2(hy, sub2s(Y2l, v[33]));
+    const float2 ez = add2(hz, sub2s(Z2l, v[34]));
     bool n0 = true, n1 = true;
-    if (ff2 != CUDART_INF_F) {
-        e2 = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
-        n0 = e2.x <= ff2;
-        n1 = e2.y <= ff2;
-    }
+    if (v[31] != CUDART_INF_F) near_far2<false>(v, X2h, Y2h, Z2h, X2l, Y2l, Z2l, ex, ey, ez, n0, n1);
     ux = uy = uz = bc(0.f);
     if (!n0 || !n1) {  // point doublet (panel.rs:82-96), unit strength
+        const float2 e2 = fma2(hx, hx, fma2(hy, hy, mul2(hz, hz)));
         const float2 e2s = make_float2(n0 ? 1.f : e2.x, n1 ? 1.f : e2.y);
         const float2 ir = make_float2(rsqrt_n(fmaxf(e2s.x, FLT_MIN)), rsqrt_n(fmaxf(e2s.y, FLT_MIN)));
         const float2 ir2 = mul2(ir, ir);
         const float2 sm = make_float2(n0 ? 0.f : v[35], n1 ? 0.f : v[35]);
         const float2 sd = mul2(sm, mul2(mul2(ir2, ir2), ir));
         const float nx = v[36], ny = v[37], nz = v[38];
-        const float2 h3 = mul2(bc(3.f), fma2(ex, bc(nx), fma2(ey, bc(ny), mul2(ez, bc(nz)))));
-        ux = mul2(sd, fma2(h3, ex, mul2(e2s, bc(-nx))));
-        uy = mul2(sd, fma2(h3, ey, mul2(e2s, bc(-ny))));
-        uz = mul2(sd, fma2(h3, ez, mul2(e2s, bc(-nz))));
+        const float2 h3 = mul2(bc(3.f), fma2(hx, bc(nx), fma2(hy, bc(ny), mul2(hz, bc(nz)))));
+        ux = mul2(sd, fma2(h3, hx, mul2(e2s, bc(-nx))));
+        uy = mul2(sd, fma2(h3, hy, mul2(e2s, bc(-ny))));
+        uz = mul2(sd, fma2(h3, hz, mul2(e2s, bc(-nz))));
     }
     if (n0 || n1) {  // vortex ring (panel.rs:99-118), unit strength
-        ex = add2(ex, sub2s(X2l, v[32]));
-        ey = add2(ey, sub2s(Y2l, v[33]));
-        ez = add2(ez, sub2s(Z2l, v[34]));
         float2 ax, ay, az;
         ring2(v, ex, ey, ez, ax, ay, az);
         const float g4 = static_cast<float>(kFourPiInv);

@@ -396,9 +396,9 @@ __global__ void k_batch_features(const FeatJob* jobs, int n_jobs, long long rows
     double gm = 0.0;
     for (int k = ws; k < we; ++k) gm += gn(k);
     gm /= static_cast<double>(we - ws);
-    const d3 fs_prev = J.steps > 0 ? J.fs_old[i] : fs;
+    const d3 fs_prev = J.hist > 0 ? J.fs_old[i] : fs;
     const double Up = len(fs_prev);
-    const double gold = J.steps > 1 ? J.gamma_old[i] : J.gamma[i];
+    const double gold = J.hist > 1 ? J.gamma_old[i] : J.gamma[i];
     const double trend = q > 0.0 ? -(J.gamma[i] - gold) / q : 0.0;
     const d3 span_rel = J.span_e[i] - J.span_s[i];
     const double a_t = geometric_aoa(J.chord[i], span_rel, fs);

@@ -213,6 +213,13 @@ cudaError_t launch_wake_advect(const DevModel& m, const WakeBuffers& w, double d
 // the far-field radius^2 is max(|p1-p0|^2, |p2-p1|^2) * ratio^2, the reference's
 // (ratio * max(|p1-p0|, |p2-p1|))^2 without its square roots: this part's FP64 rate is 1/64 of
 // its FP32 rate, and the f64 square roots and divisions made the record kernel compute-bound.
+// far-field length squared as hi + lo (the f64 near/far decision of the sweeps reads both)
+__device__ inline void split_ff2(double ff2, float* hi, float* lo) {
+    const float h = static_cast<float>(ff2);
+    *hi = h;
+    *lo = isinf(h) ? 0.f : static_cast<float>(ff2 - static_cast<double>(h));
+}
+
 __device__ void write_panel_records(const d3 (&pp)[4], double rc, double g, double far_field_ratio, int wing,
                                     PanelRec<float>* r32, PanelRec<double>* r64) {
     const d3 c = 0.25 * (((pp[0] + pp[1]) + pp[2]) + pp[3]);
@@ -253,7 +260,7 @@ __device__ void write_panel_records(const d3 (&pp)[4], double rc, double g, doub
         const double t = fmax(la, lb) * far_field_ratio;
         const double ff2 = t * t;
         for (int k = 0; k < 4; ++k) r.v[24 + k] = l2[k] > 0.0 ? static_cast<float>(1.0 / l2[k]) : 0.f;
-        r.v[31] = static_cast<float>(ff2);
+        split_ff2(ff2, &r.v[31], &r.v[kRec32FF2Lo]);
         r.v[35] = static_cast<float>(area * kFourPiInv);
         r.v[36] = static_cast<float>(n.x);
         r.v[37] = static_cast<float>(n.y);
@@ -298,7 +305,7 @@ __device__ void write_panel_records(const d3 (&pp)[4], double rc, double g, doub
         r.v[36] = nx * inl;
         r.v[37] = ny * inl;
         r.v[38] = nz * inl;
-        r.v[31] = static_cast<float>(fmax(l2[0], l2[1]) * (far_field_ratio * far_field_ratio));
+        split_ff2(fmax(l2[0], l2[1]) * (far_field_ratio * far_field_ratio), &r.v[31], &r.v[kRec32FF2Lo]);
     }
     *r32 = r;
 }

@@ -191,10 +191,11 @@ __device__ inline double foil_cd(const FoilP& f, double a) {
 //   [0..11]  corner offsets o_k = p_k - centre (rounded from f64)
 //   [12..23] segment vectors d_k = p_{k+1} - p_k (rounded from f64)
 //   [24..27] 1/|d_k|^2 per ring segment k (0 for a degenerate segment)
-//   [28..30] centre hi, [31] far-field length squared
+//   [28..30] centre hi, [31] far-field length squared (hi)
 //   [32..34] centre lo, [35] area / (4 pi)
 //   [36..38] unit normal, [39] strength Gamma
-//   [40] core length^4, [41] wing index, [42..47] 0
+//   [40] core length^4, [41] wing index, [42..45] |d_k|^2,
+//   [46] far-field length squared lo (fl32(ff2 - hi), 0 when hi is infinite), [47] 0
 // FP64 record (PanelRec<double>, 28 doubles = 224 B):
 //   [0..11] corners, [16..18] centre, [19] far-field length squared, [20..22] normal,
 //   [23] area / (4 pi), [24] Gamma, [25] core length, [26] wing index.
@@ -214,6 +215,11 @@ static_assert(sizeof(PanelRec<double>) == 224, "FP64 panel record is 224 bytes")
 
 constexpr int kRec32Gamma = 39;  // strength slot of the FP32 record
 constexpr int kRec32DD = 42;     // |d_k|^2 of the FP32 record's four segments (slots 42..45)
+constexpr int kRec32FF2Lo = 46;  // lo part of the far-field length squared
+// Near/far decisions (panel.rs:53-57) that FP32 cannot make: the squared distance from the
+// float-float difference carries a relative error of a few 2^-24, so within this relative
+// band of the far-field length squared the f64 distance of the float-float points decides.
+constexpr float kNearFarBand = 4.0e-6f;
 constexpr int kRec64Gamma = 24;  // strength slot of the FP64 record
 
 // Chain record (FP32, same 48-float size): an open chain of up to 4 wake segments that

@@ -94,6 +94,8 @@ struct FeatJob {
     const int* wing_start = nullptr;
     const int* wing_end = nullptr;
     int N = 0, S = 0, W = 0, steps = 0;
+    int hist = 0;                    // steps whose history this job's arrays hold (0, 1 or 2):
+                                     // fs_old is read from 1, gamma_old from 2
     long long row0 = 0;              // first row of the case in the batch arrays
 };
 // Per panel, with q = chord |U| / 2 and the lift-coefficient-like variable g = -Gamma / q:

@@ -8,7 +8,7 @@ apparent wind angle and speed drawn per case):
   * against the f64 oracle for a subset of cases (relative circulation and force <= 1e-5);
   * CUDA-graph replay against eager launches of the same batch: bit-identical (the same
     kernels, work lists and chunk-ordered reductions);
-  * after autotuning, still within tolerance of the plain path;
+  * after autotuning, the batch and the plain path both within 1e-5 of the oracle;
   * the warm-start hook, size checks and the error that names a bad case;
   * quasi-steady cases in a batch (bit-identical to their own Simulations).
 """
@@ -107,7 +107,10 @@ def test_graph_replay_is_bit_identical_to_eager(gpu_lib):
         assert np.array_equal(sa[k], sb[k]), f"step {k}"
 
 
-def test_autotuned_batch_stays_within_tolerance(gpu_lib):
+def test_autotuned_batch_stays_within_tolerance(gpu_lib, oracle_mod):
+    """Autotuning changes the tile shape (panels summed in FP32 before the compensated fold)
+    and the chunking, so the tuned batch's sums round differently from the single-case
+    path's and the difference grows over steps: both are held to the oracle's bar."""
     from stormbird_gb300 import Batch
 
     cases = _small_cases(6, seed=17)
@@ -123,9 +126,15 @@ def test_autotuned_batch_stays_within_tolerance(gpu_lib):
     for k in range(5, steps):
         b.do_step(time=k * DT, time_step=DT, freestream_velocity=S.batch_freestream(b, winds, k * DT))
         g2.append(b.circulation())
-    for i in range(len(cases)):
-        for j, k in enumerate(range(5, steps)):
-            assert rel_inf(g2[j][b.case_slice(i)], single[i][0][k]) <= TOL_GPU, f"case {i} step {k}"
+    for i, (js, w) in enumerate(cases):
+        o = oracle_mod.OracleSimulation(js)
+        for k in range(steps):
+            r = o.do_step(time=k * DT, time_step=DT, freestream_velocity=w.freestream(k * DT, o.nr_freestream_points))
+            if k < 5:
+                continue
+            ref = r.force_input.circulation_strength
+            eb, es = rel_inf(g2[k - 5][b.case_slice(i)], ref), rel_inf(single[i][0][k], ref)
+            assert eb <= TOL_ORACLE and es <= TOL_ORACLE, f"case {i} step {k}: tuned batch {eb:.2e}, single {es:.2e}"
 
 
 def test_warm_start_hook_cuts_iterations(gpu_lib):

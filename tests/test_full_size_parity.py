@@ -7,8 +7,7 @@ flow-derivative history; sb_sim_get_state) is loaded into the oracle, and both t
 step from that same state with the same freestream. Bar: relative circulation error
 max|dGamma| / max|Gamma| <= 1e-5 and relative total-force error |dF| / |F| <= 1e-5, the
 hot path's stated tolerance; where the oracle runs its roll-up too (far-field ratio 5), the
-induced velocity at the wake points within 1e-5 of the largest, except at the few points where
-a panel pair sits at the near/far threshold within FP32 rounding (_check_rollup_velocities).
+induced velocity at every wake point within 1e-5 of the largest (_check_rollup_velocities).
 """
 import numpy as np
 import pytest
@@ -66,29 +65,26 @@ def test_wing_sail_row_full_size_step_from_shared_state(gpu_lib, oracle_mod, far
         gg.close()
 
 
-AMBIGUOUS = 3e-5  # relative width of the band around the near/far threshold that FP32 cannot decide as f64 does
-
-
 def _check_rollup_velocities(ind_g, ind_o, pts, strengths, ratio):
-    """Induced velocity at every wake point within 1e-5 of the largest, except at points where
-    a panel sits within the band around the near/far threshold (|x - c|^2 = far-field
-    radius^2, panel.rs:53-57) that FP32 distances cannot decide as the f64 reference does:
-    there the GPU may evaluate the ring where the oracle takes the point doublet (or the
-    reverse), which differ by up to a few percent of that one panel's contribution. Such
-    points must be rare."""
+    """Induced velocity at every wake point within 1e-5 of the largest. The near/far decision
+    (|x - c|^2 <= far-field radius^2, panel.rs:53-57) is the f64 reference's at every pair: a
+    pair whose FP32 distance lies in the narrow band FP32 cannot resolve is decided in f64,
+    so no point takes the ring where the oracle takes the point doublet (which would differ by
+    up to a few percent of that panel's contribution). On a miss, the message says whether a
+    panel sits at the threshold."""
     err = np.linalg.norm(ind_g - ind_o, axis=1) / np.max(np.linalg.norm(ind_o, axis=1))
     bad = np.nonzero(err > TOL)[0]
-    assert bad.size <= 1e-3 * len(err), f"{bad.size} wake points beyond {TOL}"
-    corners = panel_corners(pts, 4 * 65, row_wing_ranges(4, 64), 300)
-    c = 0.25 * (((corners[:, 0] + corners[:, 1]) + corners[:, 2]) + corners[:, 3])
-    la = np.linalg.norm(corners[:, 1] - corners[:, 0], axis=1)
-    lb = np.linalg.norm(corners[:, 2] - corners[:, 1], axis=1)
-    ff2 = (np.maximum(la, lb) * ratio) ** 2
-    live = strengths != 0.0
-    for i in bad:
-        e2 = np.sum((pts[i] - c[live]) ** 2, axis=1)
-        assert np.any(np.abs(e2 - ff2[live]) <= AMBIGUOUS * ff2[live]), \
-            f"wake point {i}: error {err[i]:.2e} with no panel at the near/far threshold"
+    if bad.size:
+        corners = panel_corners(pts, 4 * 65, row_wing_ranges(4, 64), 300)
+        c = 0.25 * (((corners[:, 0] + corners[:, 1]) + corners[:, 2]) + corners[:, 3])
+        la = np.linalg.norm(corners[:, 1] - corners[:, 0], axis=1)
+        lb = np.linalg.norm(corners[:, 2] - corners[:, 1], axis=1)
+        ff2 = (np.maximum(la, lb) * ratio) ** 2
+        live = strengths != 0.0
+        i = bad[np.argmax(err[bad])]
+        gap = np.min(np.abs(np.sum((pts[i] - c[live]) ** 2, axis=1) / ff2[live] - 1.0))
+        raise AssertionError(f"{bad.size} wake points beyond {TOL}; worst {i}: {err[i]:.2e}, nearest panel "
+                             f"at the near/far threshold within {gap:.1e} relative")
 
 
 def test_filled_uneven_case_in_a_batch_from_shared_state(gpu_lib, oracle_mod):

@@ -283,3 +283,35 @@ def test_standalone_panel_sweep_matches_oracle(gpu_lib, oracle_mod, symmetry, ff
     if uo is not None:
         assert rel_inf(u64, uo) < 1e-12
     assert rel_inf(ug, u64) < 2e-6
+
+
+@pytest.mark.parametrize("precision", ["kahan", "fp32"])
+def test_near_far_decision_at_the_threshold_is_the_f64_one(gpu_lib, oracle_mod, precision):
+    """panel.rs:53-57 decides ring or point doublet by |x - c|^2 <= far-field radius^2 in f64.
+    Targets at relative offsets 1e-9 .. 3e-5 on both sides of that radius, around a panel
+    400 m from the origin (where FP32 coordinates alone are off by ~3e-5 m): the sweep takes
+    the oracle's side at every one. The two sides differ by about a percent of the panel's
+    velocity there, far above the FP32 evaluation error allowed below."""
+    from stormbird_gb300.simulation import panel_sweep
+
+    rng = np.random.default_rng(7)
+    c0 = np.array([412.3, 287.9, 17.1])
+    corners = c0 + np.array([[-0.25, -0.31, 0.0], [0.26, -0.3, 0.01], [0.24, 0.3, 0.0], [-0.25, 0.29, -0.01]])
+    c = 0.25 * (((corners[0] + corners[1]) + corners[2]) + corners[3])
+    r = 5.0 * max(np.linalg.norm(corners[1] - corners[0]), np.linalg.norm(corners[2] - corners[1]))
+    offsets = np.array([s * d for d in (1e-9, 1e-8, 1e-7, 1e-6, 1e-5, 3e-5) for s in (-1.0, 1.0)])
+    dirs = rng.normal(size=(16, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    targets = np.array([c + r * np.sqrt(1.0 + o) * d for d in dirs for o in offsets])
+    core = 0.1
+    uo = np.array([oracle_mod.panel_unit_velocity(corners, 5.0, core, x) for x in targets])
+    ring = np.array([oracle_mod.panel_unit_velocity(corners, 5.0, core, x, mode=1) for x in targets])
+    dbl = np.array([oracle_mod.panel_unit_velocity(corners, 5.0, core, x, mode=2) for x in targets])
+    scale = np.linalg.norm(uo, axis=1)
+    side_gap = np.linalg.norm(ring - dbl, axis=1) / scale
+    assert side_gap.min() > 1e-3
+    near = np.sum((targets - c) ** 2, axis=1) <= r * r
+    assert np.array_equal(np.linalg.norm(uo - ring, axis=1) == 0.0, near)
+    ug = panel_sweep(corners.reshape(1, 12), [1.0], [core], targets, far_field_ratio=5.0, precision=precision)
+    err = np.linalg.norm(ug - uo, axis=1) / scale
+    assert err.max() < 1e-4, f"worst target {np.argmax(err)}: {err.max():.2e} (side gap {side_gap.min():.1e})"

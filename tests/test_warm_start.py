@@ -118,3 +118,39 @@ def test_warm_start_on_held_out_cases(gpu_lib):
         assert rep[f"max_rel_circulation_diff_{arm}"] <= 1e-5
         assert rep[f"iterations_{arm}"] <= 1.05 * rep["iterations_plain"]
         assert 0.0 <= rep[f"fallback_rate_{arm}"] <= 1.0
+
+
+def test_loaded_state_restarts_the_warm_start_history(gpu_lib):
+    """A state loaded into a batch (sb_batch_set_case_state) carries no warm-start history:
+    the first step after it has no trend and no freestream change in its features (both
+    need the batch's own earlier steps), the second a freestream change but no trend, the
+    third both, although the loaded case's step count is past two from the start."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+
+    from stormbird_gb300 import Batch
+    from stormbird_gb300 import setups as S
+    from stormbird_gb300.native import lib
+
+    dt = 0.05
+    cs = S.uneven_cases(2, 31, sails=(1, 2), panels=(6, 10), wake_rows=(12, 20), wind_speed=(8.0, 12.0))
+    setups, winds = [js for js, _ in cs], [w for _, w in cs]
+    src, dst = Batch(setups), Batch(setups)
+    for k in range(16):
+        src.do_step(time=k * dt, time_step=dt, freestream_velocity=S.batch_freestream(src, winds, k * dt))
+    # dst records features from its own early steps, then takes src's later state
+    dst.set_warm_start(None, 2)
+    for k in range(4):
+        dst.do_step(time=k * dt, time_step=dt, freestream_velocity=S.batch_freestream(dst, winds, k * dt))
+    for i in range(len(setups)):
+        dst.set_case_state(i, src.case_state(i))
+    x = torch.empty((dst.total_lines, 16), dtype=torch.float32, device="cuda:0")
+    for j, k in enumerate(range(16, 19)):
+        dst.do_step(time=k * dt, time_step=dt, freestream_velocity=S.batch_freestream(dst, winds, k * dt))
+        assert lib().sb_batch_copy_warm_start_data(dst._h, ctypes.c_void_p(x.data_ptr()), None, dst.total_lines) == 0
+        f = x.cpu().numpy()
+        trend, du = np.abs(f[:, 4]).max(), np.abs(f[:, 5]).max()
+        assert (trend == 0.0) == (j < 2), f"step {j} after the load: trend feature {trend}"
+        assert (du == 0.0) == (j < 1), f"step {j} after the load: freestream-change feature {du}"
+    src.close()
+    dst.close()
