@@ -233,23 +233,29 @@ __device__ __noinline__ bool near_f64(const float* v, float xh, float xl, float 
     return dx * dx + dy * dy + dz * dz <= static_cast<double>(v[31]) + static_cast<double>(v[kRec32FF2Lo]);
 }
 
-// Near/far test (panel.rs:53-57) of one FP32 panel record at two targets, given the
-// float-float difference e = x - centre: n = (|e|^2 <= ff2) in FP32, except where |e|^2 lies
-// within kNearFarBand of ff2, where near_f64 decides. VOTE: every lane of the warp calls it
-// together, and the rare f64 branch is taken as one warp-uniform branch.
+// Near/far test (panel.rs:53-57) of one FP32 panel record at two targets, from e2 = the
+// FP32 |x_hi - c_hi|^2 (the far-field doublet's own distance): outside the record's band
+// around ff2 (kRec32FF2Band bounds the error of e2 there) that is the f64 decision. A target
+// inside it (rare) is decided from the float-float difference, and where that one lies within
+// kNearFarBand of ff2, by near_f64. VOTE: every lane of the warp calls it together, and the
+// rare branch is taken as one warp-uniform branch.
 template <bool VOTE>
-__device__ __forceinline__ void near_far2(const float* v, float2 X2h, float2 Y2h, float2 Z2h, float2 X2l, float2 Y2l,
-                                          float2 Z2l, float2 ex, float2 ey, float2 ez, bool& n0, bool& n1) {
-    const float ff2 = v[31];
-    const float2 e2 = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
+__device__ __forceinline__ void near_far2(const float* v, float2 e2, float2 X2h, float2 Y2h, float2 Z2h, float2 X2l,
+                                          float2 Y2l, float2 Z2l, bool& n0, bool& n1) {
+    const float ff2 = v[31], w = v[kRec32FF2Band];
     n0 = e2.x <= ff2;
     n1 = e2.y <= ff2;
     const float2 d = sub2s(e2, ff2);
-    const float band = kNearFarBand * ff2;
-    const bool u0 = fabsf(d.x) <= band, u1 = fabsf(d.y) <= band;
+    const bool u0 = fabsf(d.x) <= w, u1 = fabsf(d.y) <= w;
     if (VOTE ? __any_sync(0xffffffffu, u0 || u1) : (u0 || u1)) {
-        if (u0) n0 = near_f64(v, X2h.x, X2l.x, Y2h.x, Y2l.x, Z2h.x, Z2l.x);
-        if (u1) n1 = near_f64(v, X2h.y, X2l.y, Y2h.y, Y2l.y, Z2h.y, Z2l.y);
+        const float2 ex = add2(sub2s(X2h, v[28]), sub2s(X2l, v[32]));
+        const float2 ey = add2(sub2s(Y2h, v[29]), sub2s(Y2l, v[33]));
+        const float2 ez = add2(sub2s(Z2h, v[30]), sub2s(Z2l, v[34]));
+        const float2 f2 = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
+        const float2 g = sub2s(f2, ff2);
+        const float nb = kNearFarBand * ff2;
+        if (u0) n0 = fabsf(g.x) <= nb ? near_f64(v, X2h.x, X2l.x, Y2h.x, Y2l.x, Z2h.x, Z2l.x) : f2.x <= ff2;
+        if (u1) n1 = fabsf(g.y) <= nb ? near_f64(v, X2h.y, X2l.y, Y2h.y, Y2l.y, Z2h.y, Z2l.y) : f2.y <= ff2;
     }
 }
 
@@ -482,16 +488,18 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
                     }
                     const float gam = v[kRec32Gamma];
                     if (gam == 0.f) continue;  // uniform across the CTA
-                    // target - centre from the hi parts: the far-field doublet's, as in the
-                    // fast path above (at least ff_ratio panel sizes away); the float-float
-                    // difference (x_hi - c_hi) + (x_lo - c_lo) for the near/far test and the ring
-                    const float2 hx = sub2s(X2h, v[28]), hy = sub2s(Y2h, v[29]), hz = sub2s(Z2h, v[30]);
-                    const float2 ex = add2(hx, sub2s(X2l, v[32]));
-                    const float2 ey = add2(hy, sub2s(Y2l, v[33]));
-                    const float2 ez = add2(hz, sub2s(Z2l, v[34]));
+                    // target - centre from the hi parts: the near/far test's first look and the
+                    // far-field doublet's (at least ff_ratio panel sizes away), as in the fast
+                    // path above; the ring below adds the lo parts
+                    float2 ex = sub2s(X2h, v[28]);
+                    float2 ey = sub2s(Y2h, v[29]);
+                    float2 ez = sub2s(Z2h, v[30]);
+                    float2 e2 = bc(0.f);
                     bool n0 = true, n1 = true;
-                    if (v[31] != CUDART_INF_F)  // panel.rs:53-57; uniform per panel
-                        near_far2<true>(v, X2h, Y2h, Z2h, X2l, Y2l, Z2l, ex, ey, ez, n0, n1);
+                    if (v[31] != CUDART_INF_F) {  // panel.rs:53-57; uniform per panel
+                        e2 = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
+                        near_far2<true>(v, e2, X2h, Y2h, Z2h, X2l, Y2l, Z2l, n0, n1);
+                    }
                     bool a0 = valid[0], a1 = valid[1];
                     if (NEGLECT) {
                         const int pw = static_cast<int>(v[41]);
@@ -501,7 +509,6 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
                     const bool any_near = __any_sync(0xffffffffu, (a0 && n0) || (a1 && n1));
                     const bool any_far = __any_sync(0xffffffffu, (a0 && !n0) || (a1 && !n1));
                     if (any_far) {  // point doublet (panel.rs:82-96), the fast path's arithmetic
-                        const float2 e2 = fma2(hx, hx, fma2(hy, hy, mul2(hz, hz)));
                         const float2 e2s = make_float2(n0 ? 1.f : e2.x, n1 ? 1.f : e2.y);
                         // a subnormal |e|^2 (a degenerate panel) overflows s to inf either way
                         const float2 ir = make_float2(rsqrt_n(fmaxf(e2s.x, FLT_MIN)), rsqrt_n(fmaxf(e2s.y, FLT_MIN)));
@@ -510,12 +517,16 @@ __global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
                         const float2 sm = make_float2((a0 && !n0) ? at : 0.f, (a1 && !n1) ? at : 0.f);
                         const float2 s = mul2(sm, mul2(mul2(ir2, ir2), ir));
                         const float nx = v[36], ny = v[37], nz = v[38];
-                        const float2 h3 = mul2(bc(3.f), fma2(hx, bc(nx), fma2(hy, bc(ny), mul2(hz, bc(nz)))));
-                        TX = fma2(s, fma2(h3, hx, mul2(e2s, bc(-nx))), TX);
-                        TY = fma2(s, fma2(h3, hy, mul2(e2s, bc(-ny))), TY);
-                        TZ = fma2(s, fma2(h3, hz, mul2(e2s, bc(-nz))), TZ);
+                        const float2 h3 = mul2(bc(3.f), fma2(ex, bc(nx), fma2(ey, bc(ny), mul2(ez, bc(nz)))));
+                        TX = fma2(s, fma2(h3, ex, mul2(e2s, bc(-nx))), TX);
+                        TY = fma2(s, fma2(h3, ey, mul2(e2s, bc(-ny))), TY);
+                        TZ = fma2(s, fma2(h3, ez, mul2(e2s, bc(-nz))), TZ);
                     }
                     if (any_near) {  // vortex ring (panel.rs:99-118)
+                        // float-float difference: (x_hi - c_hi) + (x_lo - c_lo)
+                        ex = add2(ex, sub2s(X2l, v[32]));
+                        ey = add2(ey, sub2s(Y2l, v[33]));
+                        ez = add2(ez, sub2s(Z2l, v[34]));
                         float2 ax, ay, az;
                         ring2(v, ex, ey, ez, ax, ay, az);
                         const float g4 = gam * static_cast<float>(kFourPiInv);
@@ -690,19 +701,24 @@ __global__ void __launch_bounds__(kBsReduceThreads) k_bs_reduce_jobs(const BsJob
 }
 
 // one matrix entry into the f64 and/or split matrix (row c, column j)
-__device__ inline void store_factor(d3* factors, float2* split, int N, long long id, int c, int j, d3 u) {
+__device__ inline void store_factor(d3* factors, float* split, int N, long long id, int c, int j, d3 u) {
     if (factors) factors[id] = u;
-    if (split) {
-        float2* r = split + static_cast<long long>(c) * 3 * N + j;
-        r[0] = split_f64(u.x);
-        r[N] = split_f64(u.y);
-        r[2 * N] = split_f64(u.z);
+    if (split) {  // hi plane [N][3][N], then the lo plane
+        float* r = split + static_cast<long long>(c) * 3 * N + j;
+        const long long lo = 3LL * N * N;
+        const float2 x = split_f64(u.x), y = split_f64(u.y), z = split_f64(u.z);
+        r[0] = x.x;
+        r[N] = y.x;
+        r[2 * N] = z.x;
+        r[lo] = x.y;
+        r[lo + N] = y.y;
+        r[lo + 2 * N] = z.y;
     }
 }
 
 // frozen_wake.rs:198-249: factors[c][p] = unit velocity of first-row panel p at control point c
 __device__ inline void unit_matrix_elem(const PanelRec<double>* row0, const d3* ctrl, int N, int sym, int neglect,
-                                        const int* wing_of_line, d3* factors, float2* split, long long id) {
+                                        const int* wing_of_line, d3* factors, float* split, long long id) {
     if (id >= static_cast<long long>(N) * N) return;
     int c = static_cast<int>(id / N), p = static_cast<int>(id % N);
     d3 u = mk(0, 0, 0);
@@ -715,7 +731,7 @@ __device__ inline void unit_matrix_elem(const PanelRec<double>* row0, const d3* 
 }
 
 __global__ void k_unit_matrix(const PanelRec<double>* row0, const d3* ctrl, int N, int sym, int neglect,
-                              const int* wing_of_line, d3* factors, float2* split) {
+                              const int* wing_of_line, d3* factors, float* split) {
     unit_matrix_elem(row0, ctrl, N, sym, neglect, wing_of_line, factors, split,
                      blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x);
 }
@@ -733,28 +749,30 @@ __device__ __forceinline__ void split2(double a, double b, float2& h, float2& l)
 }
 __device__ __forceinline__ void panel_unit2(const float* v, float2 X2h, float2 Y2h, float2 Z2h, float2 X2l, float2 Y2l,
                                             float2 Z2l, float2& ux, float2& uy, float2& uz) {
-    // hi-part difference for the doublet, float-float for the test and the ring (as k_bs_sweep)
-    const float2 hx = sub2s(X2h, v[28]), hy = sub2s(Y2h, v[29]), hz = sub2s(Z2h, v[30]);
-    const float2 ex = add2(hx, sub2s(X2l, v[32]));
-    const float2 ey = add2(hy, sub2s(Y2l, v[33]));
-    const float2 ez = add2(hz, sub2s(Z2l, v[34]));
+    float2 ex = sub2s(X2h, v[28]), ey = sub2s(Y2h, v[29]), ez = sub2s(Z2h, v[30]);
+    float2 e2 = bc(0.f);
     bool n0 = true, n1 = true;
-    if (v[31] != CUDART_INF_F) near_far2<false>(v, X2h, Y2h, Z2h, X2l, Y2l, Z2l, ex, ey, ez, n0, n1);
+    if (v[31] != CUDART_INF_F) {
+        e2 = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
+        near_far2<false>(v, e2, X2h, Y2h, Z2h, X2l, Y2l, Z2l, n0, n1);
+    }
     ux = uy = uz = bc(0.f);
     if (!n0 || !n1) {  // point doublet (panel.rs:82-96), unit strength
-        const float2 e2 = fma2(hx, hx, fma2(hy, hy, mul2(hz, hz)));
         const float2 e2s = make_float2(n0 ? 1.f : e2.x, n1 ? 1.f : e2.y);
         const float2 ir = make_float2(rsqrt_n(fmaxf(e2s.x, FLT_MIN)), rsqrt_n(fmaxf(e2s.y, FLT_MIN)));
         const float2 ir2 = mul2(ir, ir);
         const float2 sm = make_float2(n0 ? 0.f : v[35], n1 ? 0.f : v[35]);
         const float2 sd = mul2(sm, mul2(mul2(ir2, ir2), ir));
         const float nx = v[36], ny = v[37], nz = v[38];
-        const float2 h3 = mul2(bc(3.f), fma2(hx, bc(nx), fma2(hy, bc(ny), mul2(hz, bc(nz)))));
-        ux = mul2(sd, fma2(h3, hx, mul2(e2s, bc(-nx))));
-        uy = mul2(sd, fma2(h3, hy, mul2(e2s, bc(-ny))));
-        uz = mul2(sd, fma2(h3, hz, mul2(e2s, bc(-nz))));
+        const float2 h3 = mul2(bc(3.f), fma2(ex, bc(nx), fma2(ey, bc(ny), mul2(ez, bc(nz)))));
+        ux = mul2(sd, fma2(h3, ex, mul2(e2s, bc(-nx))));
+        uy = mul2(sd, fma2(h3, ey, mul2(e2s, bc(-ny))));
+        uz = mul2(sd, fma2(h3, ez, mul2(e2s, bc(-nz))));
     }
     if (n0 || n1) {  // vortex ring (panel.rs:99-118), unit strength
+        ex = add2(ex, sub2s(X2l, v[32]));
+        ey = add2(ey, sub2s(Y2l, v[33]));
+        ez = add2(ez, sub2s(Z2l, v[34]));
         float2 ax, ay, az;
         ring2(v, ex, ey, ez, ax, ay, az);
         const float g4 = static_cast<float>(kFourPiInv);
@@ -767,7 +785,7 @@ __device__ __forceinline__ void panel_unit2(const float* v, float2 X2h, float2 Y
 
 __device__ inline void unit_matrix_f32_elem(const PanelRec<float>* row0_32, const PanelRec<double>* row0, const d3* ctrl,
                                             int N, int sym, int neglect, const int* wing_of_line, d3* factors,
-                                            float2* split, long long id) {
+                                            float* split, long long id) {
     const int pairs = (N + 1) / 2;
     if (id >= static_cast<long long>(pairs) * N) return;
     const int cp = static_cast<int>(id / N), p = static_cast<int>(id % N);
@@ -819,7 +837,7 @@ __device__ inline void unit_matrix_f32_elem(const PanelRec<float>* row0_32, cons
 }
 
 __global__ void k_unit_matrix_f32(const PanelRec<float>* row0_32, const PanelRec<double>* row0, const d3* ctrl, int N,
-                                  int sym, int neglect, const int* wing_of_line, d3* factors, float2* split) {
+                                  int sym, int neglect, const int* wing_of_line, d3* factors, float* split) {
     unit_matrix_f32_elem(row0_32, row0, ctrl, N, sym, neglect, wing_of_line, factors, split,
                          blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x);
 }
@@ -883,7 +901,7 @@ __global__ void __launch_bounds__(kQsPrepThreads) k_qs_prep(DevModel m, int core
 // factors[c][j] = unit velocity of horseshoe j (bound + start trailing + end trailing) at
 // control point c. Horseshoe j of wing w uses wake vectors j + w and j + w + 1.
 __global__ void k_horseshoe_matrix(DevModel m, const d3* wake_vec, const double* rc_dev, int sym, d3* factors,
-                                   float2* split) {
+                                   float* split) {
     long long id = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
     const int N = m.N;
     if (id >= static_cast<long long>(N) * N) return;
@@ -906,7 +924,7 @@ __global__ void k_horseshoe_matrix(DevModel m, const d3* wake_vec, const double*
 }
 
 cudaError_t launch_horseshoe_matrix(const DevModel& m, int core_kind, double core_value, double wake_length, d3* wake_vec,
-                                    double* rc_dev, int sym, d3* factors, float2* split, cudaStream_t s) {
+                                    double* rc_dev, int sym, d3* factors, float* split, cudaStream_t s) {
     const size_t smem = static_cast<size_t>(m.N) * sizeof(double);
     if (smem > 48 * 1024) {
         cudaError_t a = cudaFuncSetAttribute(k_qs_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
@@ -1050,7 +1068,7 @@ cudaError_t launch_bs_reduce_jobs(const BsJob* jobs, int n_jobs, long long block
 }
 
 cudaError_t launch_unit_matrix(const PanelRec<double>* row0, const PanelRec<float>* row0_32, const d3* ctrl, int N,
-                               int sym, int neglect, const int* wing_of_line, d3* factors, float2* split, cudaStream_t s) {
+                               int sym, int neglect, const int* wing_of_line, d3* factors, float* split, cudaStream_t s) {
     const long long blocks = unit_matrix_blocks(N, row0_32 != nullptr);
     if (row0_32) {
         k_unit_matrix_f32<<<static_cast<unsigned>(blocks), kUnitMatrixThreads, 0, s>>>(row0_32, row0, ctrl, N, sym, neglect,

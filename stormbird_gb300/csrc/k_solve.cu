@@ -221,15 +221,28 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
     // induced velocity of own rows for the circulation Gc: fixed + M * Gc. One warp per row;
     // double-float arithmetic on the FP32 pipes (this part's FP64 rate is 1/64 of its FP32
     // rate): the split matrix row and the split circulation, ~2^-44 relative per product.
+    const long long lo_plane = 3LL * N * N;
     auto induced_rows = [&](const float2* Gc) {
         for (int row = r0 + warp; row < r1; row += nwarps) {
-            const float2* fr = b.factors_split + static_cast<long long>(row) * 3 * N;
+            const float* fh = b.factors_split + static_cast<long long>(row) * 3 * N;
+            const float* fl = fh + lo_plane;
             float sxh = 0.f, sxl = 0.f, syh = 0.f, syl = 0.f, szh = 0.f, szl = 0.f;
-            for (int j = lane; j < N; j += 32) {
-                const float2 g = Gc[j];
-                ff_mac(sxh, sxl, __ldg(fr + j), g);
-                ff_mac(syh, syl, __ldg(fr + N + j), g);
-                ff_mac(szh, szl, __ldg(fr + 2 * N + j), g);
+            if (b.split_full) {
+                for (int j = lane; j < N; j += 32) {
+                    const float2 g = Gc[j];
+                    ff_mac(sxh, sxl, make_float2(__ldg(fh + j), __ldg(fl + j)), g);
+                    ff_mac(syh, syl, make_float2(__ldg(fh + N + j), __ldg(fl + N + j)), g);
+                    ff_mac(szh, szl, make_float2(__ldg(fh + 2 * N + j), __ldg(fl + 2 * N + j)), g);
+                }
+            } else {
+                // FP32 entries (lo = 0) except the diagonal: half the matrix bytes, same sums
+                for (int j = lane; j < N; j += 32) {
+                    const float2 g = Gc[j];
+                    const bool d = j == row;
+                    ff_mac(sxh, sxl, make_float2(__ldg(fh + j), d ? __ldg(fl + j) : 0.f), g);
+                    ff_mac(syh, syl, make_float2(__ldg(fh + N + j), d ? __ldg(fl + N + j) : 0.f), g);
+                    ff_mac(szh, szl, make_float2(__ldg(fh + 2 * N + j), d ? __ldg(fl + 2 * N + j) : 0.f), g);
+                }
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {

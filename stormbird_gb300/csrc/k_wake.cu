@@ -213,11 +213,26 @@ cudaError_t launch_wake_advect(const DevModel& m, const WakeBuffers& w, double d
 // the far-field radius^2 is max(|p1-p0|^2, |p2-p1|^2) * ratio^2, the reference's
 // (ratio * max(|p1-p0|, |p2-p1|))^2 without its square roots: this part's FP64 rate is 1/64 of
 // its FP32 rate, and the f64 square roots and divisions made the record kernel compute-bound.
-// far-field length squared as hi + lo (the f64 near/far decision of the sweeps reads both)
-__device__ inline void split_ff2(double ff2, float* hi, float* lo) {
+// Far-field length squared as hi + lo (the f64 near/far decision of the sweeps reads both),
+// and the band of the sweeps' FP32 test from hi parts alone (panel.rs:53-57). A target x at
+// the far-field radius r from the centre c has |x_k| <= |c|_inf + r; the hi parts of x and c
+// are within 2^-24 of each coordinate and their FP32 difference within 2^-24 of itself, so
+// |e_hi - e| <= d = sqrt(3) 2^-24 (2 |c|_inf + 2 r) and ||e_hi|^2 - r^2| <= 2 r d + d^2, plus
+// the FP32 rounding of |e_hi|^2 and of ff2 (below 2^-21 ff2). The band is twice that sum.
+__device__ inline void far_field_fields(double ff2, d3 c, float* hi, float* lo, float* band) {
     const float h = static_cast<float>(ff2);
     *hi = h;
-    *lo = isinf(h) ? 0.f : static_cast<float>(ff2 - static_cast<double>(h));
+    if (isinf(h)) {
+        *lo = 0.f;
+        *band = 0.f;
+        return;
+    }
+    *lo = static_cast<float>(ff2 - static_cast<double>(h));
+    const float r = __fsqrt_ru(h);
+    const float cm = fmaxf(fmaxf(fabsf(static_cast<float>(c.x)), fabsf(static_cast<float>(c.y))),
+                           fabsf(static_cast<float>(c.z)));
+    const float d = 1.7320509f * 0x1p-24f * (2.f * cm + 2.f * r);
+    *band = 2.f * ((2.f * r * d + d * d) + 0x1p-21f * h);
 }
 
 __device__ void write_panel_records(const d3 (&pp)[4], double rc, double g, double far_field_ratio, int wing,
@@ -260,7 +275,7 @@ __device__ void write_panel_records(const d3 (&pp)[4], double rc, double g, doub
         const double t = fmax(la, lb) * far_field_ratio;
         const double ff2 = t * t;
         for (int k = 0; k < 4; ++k) r.v[24 + k] = l2[k] > 0.0 ? static_cast<float>(1.0 / l2[k]) : 0.f;
-        split_ff2(ff2, &r.v[31], &r.v[kRec32FF2Lo]);
+        far_field_fields(ff2, c, &r.v[31], &r.v[kRec32FF2Lo], &r.v[kRec32FF2Band]);
         r.v[35] = static_cast<float>(area * kFourPiInv);
         r.v[36] = static_cast<float>(n.x);
         r.v[37] = static_cast<float>(n.y);
@@ -305,7 +320,8 @@ __device__ void write_panel_records(const d3 (&pp)[4], double rc, double g, doub
         r.v[36] = nx * inl;
         r.v[37] = ny * inl;
         r.v[38] = nz * inl;
-        split_ff2(fmax(l2[0], l2[1]) * (far_field_ratio * far_field_ratio), &r.v[31], &r.v[kRec32FF2Lo]);
+        far_field_fields(fmax(l2[0], l2[1]) * (far_field_ratio * far_field_ratio), c, &r.v[31], &r.v[kRec32FF2Lo],
+                         &r.v[kRec32FF2Band]);
     }
     *r32 = r;
 }

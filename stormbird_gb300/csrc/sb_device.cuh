@@ -195,7 +195,9 @@ __device__ inline double foil_cd(const FoilP& f, double a) {
 //   [32..34] centre lo, [35] area / (4 pi)
 //   [36..38] unit normal, [39] strength Gamma
 //   [40] core length^4, [41] wing index, [42..45] |d_k|^2,
-//   [46] far-field length squared lo (fl32(ff2 - hi), 0 when hi is infinite), [47] 0
+//   [46] far-field length squared lo (fl32(ff2 - hi), 0 when hi is infinite),
+//   [47] near/far band: a bound on |fl32 |x_hi - c_hi|^2 - |x - c|^2| for targets x at the
+//        far-field radius (0 when hi is infinite)
 // FP64 record (PanelRec<double>, 28 doubles = 224 B):
 //   [0..11] corners, [16..18] centre, [19] far-field length squared, [20..22] normal,
 //   [23] area / (4 pi), [24] Gamma, [25] core length, [26] wing index.
@@ -215,7 +217,8 @@ static_assert(sizeof(PanelRec<double>) == 224, "FP64 panel record is 224 bytes")
 
 constexpr int kRec32Gamma = 39;  // strength slot of the FP32 record
 constexpr int kRec32DD = 42;     // |d_k|^2 of the FP32 record's four segments (slots 42..45)
-constexpr int kRec32FF2Lo = 46;  // lo part of the far-field length squared
+constexpr int kRec32FF2Lo = 46;    // lo part of the far-field length squared
+constexpr int kRec32FF2Band = 47;  // band of the hi-part near/far test (above)
 // Near/far decisions (panel.rs:53-57) that FP32 cannot make: the squared distance from the
 // float-float difference carries a relative error of a few 2^-24, so within this relative
 // band of the far-field length squared the f64 distance of the float-float points decides.

@@ -73,16 +73,17 @@ cudaError_t launch_bs_reduce(const double* partial, int n_chunks, long long M, l
 // ceil(M_total / kBsReduceThreads), job k starting at its block_begin.
 cudaError_t launch_bs_reduce_jobs(const BsJob* jobs, int n_jobs, long long blocks, cudaStream_t s);
 // The influence matrices are written in f64 (`factors`, [N][N] d3, for the Linearized
-// solver) and/or as f32 (hi, lo) pairs (`split`, [N][3][N] float2: row c, component, column;
-// hi = the nearest float, lo = the nearest float of the remainder, for the SimpleIterative
-// solver's matrix-vector products). Either pointer may be null.
+// solver) and/or as f32 (hi, lo) pairs (`split`: the hi plane [N][3][N] floats, row c,
+// component, column, then the lo plane; hi = the nearest float, lo = the nearest float of
+// the remainder, for the SimpleIterative solver's matrix-vector products). Either pointer
+// may be null.
 // Frozen-wake unit matrix of the first wake row: from the FP32 row-0 records when row0_32 is
 // given (k_unit_matrix_f32; the control point's own panel in FP64), else all in FP64.
 cudaError_t launch_unit_matrix(const PanelRec<double>* row0, const PanelRec<float>* row0_32, const d3* ctrl, int N,
-                               int sym, int neglect, const int* wing_of_line, d3* factors, float2* split, cudaStream_t s);
+                               int sym, int neglect, const int* wing_of_line, d3* factors, float* split, cudaStream_t s);
 // Quasi-steady horseshoe matrix; core_kind 0 relative, 1 absolute, 2 none.
 cudaError_t launch_horseshoe_matrix(const DevModel& m, int core_kind, double core_value, double wake_length, d3* wake_vec,
-                                    double* rc_dev, int sym, d3* factors, float2* split, cudaStream_t s);
+                                    double* rc_dev, int sym, d3* factors, float* split, cudaStream_t s);
 
 // ---- wake and geometry (k_wake.cu) ------------------------------------------------------
 struct WakeBuffers {
@@ -146,7 +147,7 @@ struct CaseStepJob {
     int steps_done = 0;                       // wake steps completed before the step
     const PanelRec<float>* row0_32 = nullptr; // unit matrix from FP32 row-0 records (null: FP64)
     d3* factors = nullptr;
-    float2* split = nullptr;
+    float* split = nullptr;
     ChainArgs chain;                          // chain records (chain_n = 0: none)
     long long chain_n = 0;
     long long blk_advect = 0, blk_panels = 0, blk_matrix = 0, blk_chain = 0;
@@ -188,7 +189,11 @@ struct SolveSettings {
 struct SolveBuffers {
     const d3* fixed = nullptr;      // [N]
     const d3* factors = nullptr;    // [N][N] (Linearized)
-    const float2* factors_split = nullptr;  // [N][3][N] (hi, lo) pairs (SimpleIterative)
+    // SimpleIterative matrix as floats: hi plane [N][3][N] (row, component, column), then the
+    // lo plane (the nearest float of the remainder); split_full = 0 when only the diagonal
+    // carries lo parts (the FP32 unit matrix: every other entry is an FP32 value, lo = 0)
+    const float* factors_split = nullptr;
+    int split_full = 1;
     double* gamma_prev = nullptr;   // [N] in: initial solution, out: solution
     d3* vel_out = nullptr;          // [N] output control-point velocity
     double* scalars = nullptr;      // [8]: residual, iterations, converged, singular, start (below)

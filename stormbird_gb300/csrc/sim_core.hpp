@@ -340,7 +340,7 @@ struct sb_sim {
     int cur = 0;
     // frozen wake and sweeps
     DevBuf<d3> fixed, factors, qs_wake_vec;
-    DevBuf<float2> factors_split;  // the SimpleIterative solver's matrix as (hi, lo) float pairs
+    DevBuf<float> factors_split;  // the SimpleIterative solver's matrix: hi plane, then lo plane
     DevBuf<double> qs_rc, partial;
     DevBuf<unsigned long long> counters;
     DevBuf<int> err;
@@ -546,7 +546,7 @@ struct sb_sim {
         // f64 matrix for the Linearized solve (also the start of a SimpleIterative one),
         // split matrix for the SimpleIterative iterations
         if (solver_kind == 1 || solve.start_with_linearized) factors.alloc(static_cast<size_t>(N) * N);
-        if (solver_kind == 0) factors_split.alloc(static_cast<size_t>(N) * N * 3);
+        if (solver_kind == 0) factors_split.alloc(static_cast<size_t>(N) * N * 6);
         ck(cudaMemset(fixed.p, 0, N * sizeof(d3)), "memset");
         counters.alloc(4); err.alloc(4);
         ck(cudaMemset(err.p, 0, 4 * sizeof(int)), "memset");
@@ -933,6 +933,8 @@ struct sb_sim {
         sb.fixed = fixed.p;
         sb.factors = factors.p;
         sb.factors_split = factors_split.p;
+        // off-diagonal lo parts are zero when the unit matrix came from the FP32 records
+        sb.split_full = (dynamic && precision != 2) ? 0 : 1;
         sb.gamma_prev = gamma_p;
         sb.vel_out = vel_out.p;
         sb.scalars = scalars.p;

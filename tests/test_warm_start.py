@@ -123,8 +123,10 @@ def test_warm_start_on_held_out_cases(gpu_lib):
 def test_loaded_state_restarts_the_warm_start_history(gpu_lib):
     """A state loaded into a batch (sb_batch_set_case_state) carries no warm-start history:
     the first step after it has no trend and no freestream change in its features (both
-    need the batch's own earlier steps), the second a freestream change but no trend, the
-    third both, although the loaded case's step count is past two from the start."""
+    need the batch's own earlier steps; the freestream change compares |U| with itself, two
+    f64 evaluations that may differ in the last bit), the second a freestream change but no
+    trend, the third both, although the loaded case's step count is past two from the start.
+    Stale history (the batch's own step 3) would give changes of the gust's size, ~1e-2."""
     torch = pytest.importorskip("torch")
     import ctypes
 
@@ -151,6 +153,6 @@ def test_loaded_state_restarts_the_warm_start_history(gpu_lib):
         f = x.cpu().numpy()
         trend, du = np.abs(f[:, 4]).max(), np.abs(f[:, 5]).max()
         assert (trend == 0.0) == (j < 2), f"step {j} after the load: trend feature {trend}"
-        assert (du == 0.0) == (j < 1), f"step {j} after the load: freestream-change feature {du}"
+        assert (du < 1e-12) == (j < 1) and (j < 1 or du > 1e-6), f"step {j} after the load: freestream change {du}"
     src.close()
     dst.close()
