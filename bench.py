@@ -483,7 +483,7 @@ def batched_solves(args, device):
     def worst(a, ref):
         return max(float(np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1e-300)) for x, y in zip(a, ref))
 
-    arms = ("batched", "extrapolation", "warm")
+    arms = ("batched", "extrapolation", *warm_arms)
     solves = n * steps
     out["solves_per_s"] = {m: solves / results[m]["seconds"] for m in ("plain",) + arms}
     out["speedup_vs_plain"] = {m: results["plain"]["seconds"] / results[m]["seconds"] for m in arms}
@@ -574,8 +574,10 @@ def batched_filled(args, device, net):
     Batch per warm-start arm (sb_batch_set_case_state), and every arm runs the same steps
     fill .. fill + 1 + steps with the same freestream: two untimed (the extrapolation needs two
     solutions of its own) and `--batch-steps` timed on the host clock around the public call,
-    host freestream in, results out. Circulation of every arm and timed step against the plain
-    arm's, and of sampled cases against the oracle loaded with the same state."""
+    host freestream in, results out. The network runs once per guard factor of `--warm-guards`
+    (sb_batch_set_warm_start_guard; "warm" is the default 0.5). Circulation of every arm and
+    timed step against the plain arm's, and of sampled cases against the oracle loaded with the
+    same state."""
     from oracle.binding import OracleSimulation
     from stormbird_gb300 import Batch, Simulation
     from stormbird_gb300 import setups as S
@@ -638,10 +640,13 @@ def batched_filled(args, device, net):
     res["batched"] = run_arm(src, None)
     src.close()
     ex_net = WS.extrapolation_only(device)
-    for mode, mnet in (("extrapolation", ex_net), ("warm", net)):
+    guards = [float(g) for g in args.warm_guards.split(",")]
+    warm_arms = ["warm" if g == 0.5 else f"warm_guard_{g:g}" for g in guards]
+    for mode, mnet, guard in [("extrapolation", ex_net, 0.5)] + [(a, net, g) for a, g in zip(warm_arms, guards)]:
         b = Batch(jsons, device=device)
         for i, st in enumerate(states):
             b.set_case_state(i, st)
+        b.set_warm_start_guard(guard)
         res[mode] = run_arm(b, mnet.handle)
         b.close()
     ex_net.close()
@@ -672,7 +677,7 @@ def batched_filled(args, device, net):
                 w = max(w, float(np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1e-300)))
         return w
 
-    arms = ("batched", "extrapolation", "warm")
+    arms = ("batched", "extrapolation", *warm_arms)
     solves = n * steps
     return {"workload": f"{n} uneven cases (seed 2024) with every wake full: steps {timed[0]}-{timed[-1]} after "
                         f"{fill} untimed steps (wakes of 50-400 rows), all arms from one state",
@@ -684,7 +689,8 @@ def batched_filled(args, device, net):
             "start_taken_fraction": {m: {"plain": float(np.mean(np.array(res[m]["start"]) == 0.0)),
                                          "extrapolation": float(np.mean(np.array(res[m]["start"]) == 1.0)),
                                          "network": float(np.mean(np.array(res[m]["start"]) == 2.0))}
-                                     for m in ("extrapolation", "warm")},
+                                     for m in ("extrapolation", *warm_arms)},
+            "warm_start_guards": dict(zip(warm_arms, guards)),
             "max_rel_circulation_diff_vs_plain": {m: worst_vs_plain(m) for m in arms},
             "oracle": {"cases": sample, "max_rel_circulation_error": oracle_err,
                        "how": "oracle (C++ f64) loaded with each sampled case's filled state and stepped through the "
@@ -1166,6 +1172,8 @@ def main():
     ap.add_argument("--filled", action="store_true",
                     help="config 3 on filled wakes: all arms from one filled state (network from --load-net)")
     ap.add_argument("--load-net", default="", help="network parameters (.npy) for --filled")
+    ap.add_argument("--warm-guards", default="0.5,0.8,1.0",
+                    help="guard factors of the network arms of --filled (sb_batch_set_warm_start_guard)")
     ap.add_argument("--batch-cases", type=int, default=512, help="uneven cases of the batched solves/s part (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=5, help="timed steps of the batched part")
     ap.add_argument("--tune-seconds", type=float, default=0.0,

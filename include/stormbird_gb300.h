@@ -423,6 +423,11 @@ int sb_mlp_train_step(sb_mlp* network, const float* x_dev, const float* target_d
 /* Warm start of a batch: mode 0 off, 1 the network's candidates (SimpleIterative cases),
  * 2 features and targets recorded each step without a candidate (training data). */
 int sb_batch_set_warm_start(sb_batch* batch, sb_mlp* network, int mode);
+/* Guard on the network's start (mode 1): each case's solve starts from the plain start, the
+ * extrapolation in time if its mean and largest per-line residual are both lower, and the
+ * network's candidate only if both of its residuals are below `margin` times the best start's
+ * (0 < margin <= 1; default 0.5). */
+int sb_batch_set_warm_start_guard(sb_batch* batch, double margin);
 /* The last step's features [total_lines][SB_WARM_START_FEATURES] and targets [total_lines]
  * (device or host pointers; either may be NULL). */
 int sb_batch_copy_warm_start_data(sb_batch* batch, float* features, float* targets, size_t rows);

@@ -122,6 +122,11 @@ class Batch:
         handle, 2 to record features and targets only, 0 off."""
         _check(lib().sb_batch_set_warm_start(self._h, network_handle, int(mode)))
 
+    def set_warm_start_guard(self, margin: float):
+        """Factor the network's start must beat the best other start by, on the mean and the
+        largest per-line residual (sb_batch_set_warm_start_guard; default 0.5)."""
+        _check(lib().sb_batch_set_warm_start_guard(self._h, float(margin)))
+
     def set_case_state(self, i: int, state):
         a = np.ascontiguousarray(np.asarray(state, dtype=np.float64).reshape(-1))
         _check(lib().sb_batch_set_case_state(self._h, int(i), as_ptr(a), a.size))

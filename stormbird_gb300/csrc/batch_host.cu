@@ -172,6 +172,7 @@ struct sb_batch {
     // warm start: 0 off, 1 network candidates, 2 features and targets only (training data)
     sb_mlp* mlp = nullptr;
     int warm_mode = 0;
+    double warm_margin = 0.5;  // SolveBuffers::second_margin of every case
     DevBuf<float> w_feat, w_y, w_target;
     DevBuf<double> w_q, w_g0, w_tr, w_cand_ex, w_cand, w_gamma_old;
     DevBuf<d3> w_fs_old;
@@ -858,6 +859,7 @@ struct sb_batch {
                 j.m = c.dm;
                 j.st = c.solve;
                 j.b = c.solve_buffers();
+                j.b.second_margin = warm_margin;
             }
     }
 
@@ -1242,6 +1244,14 @@ int sb_batch_autotune(sb_batch* b, double budget_seconds) {
 int sb_batch_set_warm_start(sb_batch* b, sb_mlp* network, int mode) {
     if (!b) return null_arg();
     return guard([&] { b->set_warm_start(network, mode); });
+}
+
+int sb_batch_set_warm_start_guard(sb_batch* b, double margin) {
+    if (!b) return null_arg();
+    return guard([&] {
+        if (!(margin > 0.0 && margin <= 1.0)) raise(SB_ERR_SIZE, "the warm-start guard must lie in (0, 1]");
+        b->warm_margin = margin;
+    });
 }
 
 int sb_batch_copy_warm_start_data(sb_batch* b, float* features, float* targets, size_t rows) {

@@ -703,16 +703,17 @@ __global__ void __launch_bounds__(kBsReduceThreads) k_bs_reduce_jobs(const BsJob
 // one matrix entry into the f64 and/or split matrix (row c, column j)
 __device__ inline void store_factor(d3* factors, float* split, int N, long long id, int c, int j, d3 u) {
     if (factors) factors[id] = u;
-    if (split) {  // hi plane [N][3][N], then the lo plane
-        float* r = split + static_cast<long long>(c) * 3 * N + j;
-        const long long lo = 3LL * N * N;
+    if (split) {  // hi plane [N][3][stride], then the lo plane
+        const int S = si_matrix_stride(N);
+        float* r = split + static_cast<long long>(c) * 3 * S + j;
+        const long long lo = 3LL * N * S;
         const float2 x = split_f64(u.x), y = split_f64(u.y), z = split_f64(u.z);
         r[0] = x.x;
-        r[N] = y.x;
-        r[2 * N] = z.x;
+        r[S] = y.x;
+        r[2 * S] = z.x;
         r[lo] = x.y;
-        r[lo + N] = y.y;
-        r[lo + 2 * N] = z.y;
+        r[lo + S] = y.y;
+        r[lo + 2 * S] = z.y;
     }
 }
 

@@ -43,7 +43,6 @@ namespace sbgpu {
 constexpr int kSolveThreads = 256;
 constexpr int kSolveRowsPerThread = 4;  // most rows per thread (1024 per CTA)
 constexpr int kMaxCluster = 8;
-constexpr double kSecondCandidateMargin = 0.5;  // warm-start guard, see si_solve
 
 int solve_cluster_size(int N) {
     if (N <= 64) return 1;
@@ -117,6 +116,15 @@ __device__ __forceinline__ void ff_mac(float& S, float& C, float2 x, float2 g) {
     S = s;
     C = __fadd_rn(C, __fadd_rn(err, t));
 }
+// Four consecutive columns: matrix (a + al) against the circulation pairs (g01.x + g01.y),
+// (g01.z + g01.w), (g23.x + g23.y), (g23.z + g23.w)
+__device__ __forceinline__ void ff_mac4(float& S, float& C, float4 a, float4 al, float4 g01, float4 g23) {
+    ff_mac(S, C, make_float2(a.x, al.x), make_float2(g01.x, g01.y));
+    ff_mac(S, C, make_float2(a.y, al.y), make_float2(g01.z, g01.w));
+    ff_mac(S, C, make_float2(a.z, al.z), make_float2(g23.x, g23.y));
+    ff_mac(S, C, make_float2(a.w, al.w), make_float2(g23.z, g23.w));
+}
+__device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
 // (S, C) += (h, l), another double-float partial sum
 __device__ __forceinline__ void ff_add(float& S, float& C, float h, float l) {
     const float s = __fadd_rn(S, h);
@@ -162,11 +170,13 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
     const int N = m.N;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = kSolveThreads / 32;
     extern __shared__ double smem[];
-    // circulation of every line as (hi, lo) float pairs for the matrix-vector products; the
-    // f64 circulation of the thread's own rows stays in registers (gown)
-    float2* G[2] = {reinterpret_cast<float2*>(smem), reinterpret_cast<float2*>(smem + N)};
-    double* RR[2] = {smem + 2 * N, smem + 3 * N};
-    double* MX[2] = {smem + 4 * N, smem + 4 * N + kMaxCluster};
+    // circulation of every line as (hi, lo) float pairs for the matrix-vector products, padded
+    // with zeros to the matrix's row stride; the f64 circulation of the thread's own rows
+    // stays in registers (gown)
+    const int S = si_matrix_stride(N);
+    float2* G[2] = {reinterpret_cast<float2*>(smem), reinterpret_cast<float2*>(smem + S)};
+    double* RR[2] = {smem + 2 * S, smem + 2 * S + N};
+    double* MX[2] = {smem + 2 * S + 2 * N, smem + 2 * S + 2 * N + kMaxCluster};
     const int rp = (N + CS - 1) / CS;
     const int r0 = min(N, rank * rp), r1 = min(N, r0 + rp);
     // The thread's k-th own row (offset from r0): consecutive rows on consecutive threads, so
@@ -175,7 +185,7 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
     auto own_row = [&](int k) { return tid + k * kSolveThreads; };
     // M * Gamma of the CTA's rows as double-float pairs (x hi, x lo, y hi, y lo, z hi, z lo);
     // the row's owner adds them to the fixed part in f64
-    float* uff = reinterpret_cast<float*>(smem + 4 * N + 2 * kMaxCluster);
+    float* uff = reinterpret_cast<float*>(smem + 2 * S + 2 * N + 2 * kMaxCluster);
     __shared__ double s_res;
     __shared__ unsigned long long s_umax[kSolveThreads / 32];
     __shared__ int s_conv;
@@ -186,6 +196,7 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
         if (scale0) g *= st.correction_factor_initial;
         G[0][i] = split_f64(g);
     }
+    for (int i = N + tid; i < S; i += kSolveThreads) G[0][i] = G[1][i] = make_float2(0.f, 0.f);
     // per-thread rows
     RowGeom rg[RPT];
     d3 u_last[RPT];
@@ -220,29 +231,30 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
 
     // induced velocity of own rows for the circulation Gc: fixed + M * Gc. One warp per row;
     // double-float arithmetic on the FP32 pipes (this part's FP64 rate is 1/64 of its FP32
-    // rate): the split matrix row and the split circulation, ~2^-44 relative per product.
-    const long long lo_plane = 3LL * N * N;
+    // rate): the split matrix row and the split circulation, ~2^-44 relative per product. A
+    // lane takes four consecutive columns per 16-byte load, so a row of up to 640 columns is
+    // at most five trips of loads from L2 (the matrix does not stay in shared memory).
+    const long long lo_plane = 3LL * N * S;
     auto induced_rows = [&](const float2* Gc) {
+        const bool full = b.split_full != 0;
         for (int row = r0 + warp; row < r1; row += nwarps) {
-            const float* fh = b.factors_split + static_cast<long long>(row) * 3 * N;
+            const float* fh = b.factors_split + static_cast<long long>(row) * 3 * S;
             const float* fl = fh + lo_plane;
             float sxh = 0.f, sxl = 0.f, syh = 0.f, syl = 0.f, szh = 0.f, szl = 0.f;
-            if (b.split_full) {
-                for (int j = lane; j < N; j += 32) {
-                    const float2 g = Gc[j];
-                    ff_mac(sxh, sxl, make_float2(__ldg(fh + j), __ldg(fl + j)), g);
-                    ff_mac(syh, syl, make_float2(__ldg(fh + N + j), __ldg(fl + N + j)), g);
-                    ff_mac(szh, szl, make_float2(__ldg(fh + 2 * N + j), __ldg(fl + 2 * N + j)), g);
+#pragma unroll 2
+            for (int k = 4 * lane; k < S; k += 128) {
+                const float4 g01 = *reinterpret_cast<const float4*>(Gc + k);  // (hi, lo) of columns k, k + 1
+                const float4 g23 = *reinterpret_cast<const float4*>(Gc + k + 2);
+                const float4 ax = ldg4(fh + k), ay = ldg4(fh + S + k), az = ldg4(fh + 2 * S + k);
+                float4 lx = make_float4(0.f, 0.f, 0.f, 0.f), ly = lx, lz = lx;
+                if (full) {
+                    lx = ldg4(fl + k);
+                    ly = ldg4(fl + S + k);
+                    lz = ldg4(fl + 2 * S + k);
                 }
-            } else {
-                // FP32 entries (lo = 0) except the diagonal: half the matrix bytes, same sums
-                for (int j = lane; j < N; j += 32) {
-                    const float2 g = Gc[j];
-                    const bool d = j == row;
-                    ff_mac(sxh, sxl, make_float2(__ldg(fh + j), d ? __ldg(fl + j) : 0.f), g);
-                    ff_mac(syh, syl, make_float2(__ldg(fh + N + j), d ? __ldg(fl + N + j) : 0.f), g);
-                    ff_mac(szh, szl, make_float2(__ldg(fh + 2 * N + j), d ? __ldg(fl + 2 * N + j) : 0.f), g);
-                }
+                ff_mac4(sxh, sxl, ax, lx, g01, g23);
+                ff_mac4(syh, syl, ay, ly, g01, g23);
+                ff_mac4(szh, szl, az, lz, g01, g23);
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
@@ -251,6 +263,12 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
                 ff_add(szh, szl, __shfl_down_sync(0xffffffffu, szh, o), __shfl_down_sync(0xffffffffu, szl, o));
             }
             if (lane == 0) {
+                if (!full) {  // the own panel's entry is f64: its lo parts times Gamma hi
+                    const float2 g = Gc[row];
+                    ff_mac(sxh, sxl, make_float2(0.f, fl[row]), g);
+                    ff_mac(syh, syl, make_float2(0.f, fl[S + row]), g);
+                    ff_mac(szh, szl, make_float2(0.f, fl[2 * S + row]), g);
+                }
                 float* o = uff + 6 * (row - r0);
                 o[0] = sxh;
                 o[1] = sxl;
@@ -276,8 +294,8 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
     // when both its mean residual (the solver's own measure) and its largest per-line term
     // are lower: the solver stops on the mean, which a start with its error on a few lines
     // could pass while those lines are still off. The plain start wins ties. The second
-    // candidate (the network's) must beat the best start so far by kSecondCandidateMargin
-    // on both measures: its per-line error is noise-like, and a start that is only slightly
+    // candidate (the network's) must beat the best start so far by b.second_margin (0.5 by
+    // default) on both measures: its per-line error is noise-like, and a start that is only slightly
     // better by the initial residual took more iterations than the extrapolation (566 of
     // 2,560 solves of the uneven-case batch: 108 iterations against 107 from the plain start).
     if (b.candidate[0] || b.candidate[1]) {
@@ -323,8 +341,8 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
             if (v == 0) {
                 best = rv;
                 best_max = rmax;
-            } else if (isfinite(rv) && rv < (v == 2 ? kSecondCandidateMargin : 1.0) * best &&
-                       rmax < (v == 2 ? kSecondCandidateMargin : 1.0) * best_max) {  // same decision in every CTA
+            } else if (isfinite(rv) && rv < (v == 2 ? b.second_margin : 1.0) * best &&
+                       rmax < (v == 2 ? b.second_margin : 1.0) * best_max) {  // same decision in every CTA
                 best = rv;
                 best_max = rmax;
                 taken = v;
@@ -450,7 +468,9 @@ int si_rows_per_thread(int N) {
 size_t si_smem_bytes(int N) {
     const int CS = solve_cluster_size(N);
     const int rp = (N + CS - 1) / CS;
-    return (4 * static_cast<size_t>(N) + 2 * kMaxCluster) * sizeof(double) + static_cast<size_t>(rp) * sizeof(d3);
+    return (2 * static_cast<size_t>(si_matrix_stride(N)) + 2 * static_cast<size_t>(N) + 2 * kMaxCluster) *
+               sizeof(double) +
+           static_cast<size_t>(rp) * sizeof(d3);
 }
 
 cudaError_t launch_solve_simple_iterative_jobs(const SolveJob* jobs, int n, int cluster, int rows_per_thread,

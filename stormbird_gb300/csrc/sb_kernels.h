@@ -73,10 +73,10 @@ cudaError_t launch_bs_reduce(const double* partial, int n_chunks, long long M, l
 // ceil(M_total / kBsReduceThreads), job k starting at its block_begin.
 cudaError_t launch_bs_reduce_jobs(const BsJob* jobs, int n_jobs, long long blocks, cudaStream_t s);
 // The influence matrices are written in f64 (`factors`, [N][N] d3, for the Linearized
-// solver) and/or as f32 (hi, lo) pairs (`split`: the hi plane [N][3][N] floats, row c,
-// component, column, then the lo plane; hi = the nearest float, lo = the nearest float of
-// the remainder, for the SimpleIterative solver's matrix-vector products). Either pointer
-// may be null.
+// solver) and/or as f32 (hi, lo) pairs (`split`: the hi plane [N][3][si_matrix_stride(N)]
+// floats, row c, component, column, then the lo plane; hi = the nearest float, lo = the
+// nearest float of the remainder, for the SimpleIterative solver's matrix-vector products;
+// the padding columns are left untouched). Either pointer may be null.
 // Frozen-wake unit matrix of the first wake row: from the FP32 row-0 records when row0_32 is
 // given (k_unit_matrix_f32; the control point's own panel in FP64), else all in FP64.
 cudaError_t launch_unit_matrix(const PanelRec<double>* row0, const PanelRec<float>* row0_32, const d3* ctrl, int N,
@@ -186,12 +186,17 @@ struct SolveSettings {
     int full_induced_correction = 1;
 };
 
+// Row length of the SimpleIterative matrix planes: N rounded up to a multiple of 4, so that a
+// row's entries load as 16-byte vectors (the padding entries are zero).
+__host__ __device__ inline int si_matrix_stride(int N) { return (N + 3) & ~3; }
+
 struct SolveBuffers {
     const d3* fixed = nullptr;      // [N]
     const d3* factors = nullptr;    // [N][N] (Linearized)
-    // SimpleIterative matrix as floats: hi plane [N][3][N] (row, component, column), then the
-    // lo plane (the nearest float of the remainder); split_full = 0 when only the diagonal
-    // carries lo parts (the FP32 unit matrix: every other entry is an FP32 value, lo = 0)
+    // SimpleIterative matrix as floats: hi plane [N][3][stride] (row, component, column;
+    // stride = si_matrix_stride(N)), then the lo plane (the nearest float of the remainder);
+    // split_full = 0 when only the diagonal carries lo parts (the FP32 unit matrix: every
+    // other entry is an FP32 value, lo = 0)
     const float* factors_split = nullptr;
     int split_full = 1;
     double* gamma_prev = nullptr;   // [N] in: initial solution, out: solution
@@ -206,6 +211,9 @@ struct SolveBuffers {
     // scalars[4] = k + 1 when candidate k was taken, 0 when the plain start was (fallback),
     // -1 without candidates.
     const double* candidate[2] = {nullptr, nullptr};  // [N] each, or nullptr
+    // factor the second candidate's mean and largest residual must stay under, times the
+    // best start's before it (the warm-start guard, see si_solve)
+    double second_margin = 0.5;
     int* err = nullptr;
 };
 

@@ -546,7 +546,10 @@ struct sb_sim {
         // f64 matrix for the Linearized solve (also the start of a SimpleIterative one),
         // split matrix for the SimpleIterative iterations
         if (solver_kind == 1 || solve.start_with_linearized) factors.alloc(static_cast<size_t>(N) * N);
-        if (solver_kind == 0) factors_split.alloc(static_cast<size_t>(N) * N * 6);
+        if (solver_kind == 0) {  // two planes of N rows x 3 x stride; the padding columns stay 0
+            factors_split.alloc(static_cast<size_t>(N) * si_matrix_stride(N) * 6);
+            ck(cudaMemset(factors_split.p, 0, factors_split.n * sizeof(float)), "memset");
+        }
         ck(cudaMemset(fixed.p, 0, N * sizeof(d3)), "memset");
         counters.alloc(4); err.alloc(4);
         ck(cudaMemset(err.p, 0, 4 * sizeof(int)), "memset");

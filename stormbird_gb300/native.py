@@ -96,6 +96,7 @@ SIGNATURES = [
     ("sb_mlp_gradients", ctypes.c_int, [_vp, _vp, _vp, ctypes.c_size_t, _fp, _dp]),
     ("sb_mlp_train_step", ctypes.c_int, [_vp, _vp, _vp, ctypes.c_size_t, ctypes.c_float, _dp]),
     ("sb_batch_set_warm_start", ctypes.c_int, [_vp, _vp, ctypes.c_int]),
+    ("sb_batch_set_warm_start_guard", ctypes.c_int, [_vp, ctypes.c_double]),
     ("sb_batch_copy_warm_start_data", ctypes.c_int, [_vp, _vp, _vp, ctypes.c_size_t]),
     ("sb_sim_result_json", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_size_t, _szp]),
     ("sb_sim_result_csv", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t]),
