@@ -602,7 +602,7 @@ def batched_filled(args, device, net):
     def run_arm(b, net_handle):
         if net_handle is not None:
             b.set_warm_start(net_handle)
-        out = {"seconds": 0.0, "gamma": [], "iterations": [], "start": [], "gpu_ms": []}
+        out = {"seconds": 0.0, "gamma": [], "iterations": [], "start": [], "gpu_ms": [], "converged": []}
         for k in window:
             fs = S.batch_freestream(b, winds, k * DT)
             t1 = time.perf_counter()
@@ -615,6 +615,7 @@ def batched_filled(args, device, net):
                 out["gpu_ms"].append(b.info()["last_step_ms"])
                 out["gamma"].append([g[b.case_slice(i)].copy() for i in range(n)])
                 out["iterations"].append(sm[:, 7].copy())
+                out["converged"].append(sm[:, 8].copy())
                 out["start"].append(sm[:, 10].copy())
         return out
 
@@ -622,7 +623,7 @@ def batched_filled(args, device, net):
     sims = [Simulation(js, device=device) for js in jsons]
     for sim, st in zip(sims, states):
         sim.set_state(st)
-    plain = {"seconds": 0.0, "gamma": [], "iterations": []}
+    plain = {"seconds": 0.0, "gamma": [], "iterations": [], "converged": []}
     for k in window:
         fss = [w.freestream(k * DT, sim.nr_freestream_points) for sim, w in zip(sims, winds)]
         t1 = time.perf_counter()
@@ -632,6 +633,7 @@ def batched_filled(args, device, net):
             plain["seconds"] += dt_
             plain["gamma"].append([r.circulation_strength.copy() for r in rs])
             plain["iterations"].append(np.array([r.iterations for r in rs], dtype=float))
+            plain["converged"].append(np.array([1.0 if r.converged else 0.0 for r in rs]))
     for sim in sims:
         sim.close()
     del sims
@@ -677,6 +679,24 @@ def batched_filled(args, device, net):
                 w = max(w, float(np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1e-300)))
         return w
 
+    def worst_case(arm):
+        """The case and timed step of the arm's largest difference from the plain arm, with both
+        solves' iterations and convergence flags there."""
+        best = (-1.0, 0, 0)
+        for si, (ga, gp) in enumerate(zip(res[arm]["gamma"], res["plain"]["gamma"])):
+            for i, (x, y) in enumerate(zip(ga, gp)):
+                e = float(np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1e-300))
+                if e > best[0]:
+                    best = (e, i, si)
+        e, i, si = best
+        return {"rel_diff": e, "case": i, "timed_step": si,
+                "iterations": float(res[arm]["iterations"][si][i]), "converged": float(res[arm]["converged"][si][i]),
+                "plain_iterations": float(res["plain"]["iterations"][si][i]),
+                "plain_converged": float(res["plain"]["converged"][si][i]),
+                "start": float(res[arm]["start"][si][i]) if "start" in res[arm] else None,
+                "rel_diff_per_step": [float(np.max(np.abs(ga[i] - gp[i])) / max(np.max(np.abs(gp[i])), 1e-300))
+                                      for ga, gp in zip(res[arm]["gamma"], res["plain"]["gamma"])]}
+
     arms = ("batched", "extrapolation", *warm_arms)
     solves = n * steps
     return {"workload": f"{n} uneven cases (seed 2024) with every wake full: steps {timed[0]}-{timed[-1]} after "
@@ -692,6 +712,8 @@ def batched_filled(args, device, net):
                                      for m in ("extrapolation", *warm_arms)},
             "warm_start_guards": dict(zip(warm_arms, guards)),
             "max_rel_circulation_diff_vs_plain": {m: worst_vs_plain(m) for m in arms},
+            "worst_case_vs_plain": {m: worst_case(m) for m in arms},
+            "unconverged_solves": {m: int(np.sum(np.array(res[m]["converged"]) == 0.0)) for m in ("plain",) + arms},
             "oracle": {"cases": sample, "max_rel_circulation_error": oracle_err,
                        "how": "oracle (C++ f64) loaded with each sampled case's filled state and stepped through the "
                               f"same window; {t_oracle:.1f} s"},

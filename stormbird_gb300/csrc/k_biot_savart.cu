@@ -226,11 +226,32 @@ __device__ __forceinline__ void chain2(const float* v, float2 ex, float2 ey, flo
 // panel.rs:53-57 in f64 for one target given as float-float coordinates: the squared
 // distance of the float-float target from the float-float centre against the far-field
 // length squared (hi + lo). The points are the f64 points to within 2^-48 relative.
-__device__ __noinline__ bool near_f64(const float* v, float xh, float xl, float yh, float yl, float zh, float zl) {
+__device__ inline bool near_f64(const float* v, float xh, float xl, float yh, float yl, float zh, float zl) {
     const double dx = (static_cast<double>(xh) - v[28]) + (static_cast<double>(xl) - v[32]);
     const double dy = (static_cast<double>(yh) - v[29]) + (static_cast<double>(yl) - v[33]);
     const double dz = (static_cast<double>(zh) - v[30]) + (static_cast<double>(zl) - v[34]);
     return dx * dx + dy * dy + dz * dz <= static_cast<double>(v[31]) + static_cast<double>(v[kRec32FF2Lo]);
+}
+
+// The near/far decision of the targets in `which` (bit 0: the first lane of the pair, bit 1:
+// the second) from the float-float difference, and where that lies within kNearFarBand of
+// ff2, by near_f64; bit k of the result: target k is near. Out of line: the rare branch's
+// registers stay out of the sweep's loop.
+__device__ __noinline__ int near_recheck(const float* v, float2 X2h, float2 Y2h, float2 Z2h, float2 X2l, float2 Y2l,
+                                         float2 Z2l, int which) {
+    const float ff2 = v[31];
+    const float2 ex = add2(sub2s(X2h, v[28]), sub2s(X2l, v[32]));
+    const float2 ey = add2(sub2s(Y2h, v[29]), sub2s(Y2l, v[33]));
+    const float2 ez = add2(sub2s(Z2h, v[30]), sub2s(Z2l, v[34]));
+    const float2 f2 = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
+    const float2 g = sub2s(f2, ff2);
+    const float nb = kNearFarBand * ff2;
+    int n = 0;
+    if (which & 1)
+        n |= (fabsf(g.x) <= nb ? near_f64(v, X2h.x, X2l.x, Y2h.x, Y2l.x, Z2h.x, Z2l.x) : f2.x <= ff2) ? 1 : 0;
+    if (which & 2)
+        n |= (fabsf(g.y) <= nb ? near_f64(v, X2h.y, X2l.y, Y2h.y, Y2l.y, Z2h.y, Z2l.y) : f2.y <= ff2) ? 2 : 0;
+    return n;
 }
 
 // Near/far test (panel.rs:53-57) of one FP32 panel record at two targets, from e2 = the
@@ -248,14 +269,9 @@ __device__ __forceinline__ void near_far2(const float* v, float2 e2, float2 X2h,
     const float2 d = sub2s(e2, ff2);
     const bool u0 = fabsf(d.x) <= w, u1 = fabsf(d.y) <= w;
     if (VOTE ? __any_sync(0xffffffffu, u0 || u1) : (u0 || u1)) {
-        const float2 ex = add2(sub2s(X2h, v[28]), sub2s(X2l, v[32]));
-        const float2 ey = add2(sub2s(Y2h, v[29]), sub2s(Y2l, v[33]));
-        const float2 ez = add2(sub2s(Z2h, v[30]), sub2s(Z2l, v[34]));
-        const float2 f2 = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
-        const float2 g = sub2s(f2, ff2);
-        const float nb = kNearFarBand * ff2;
-        if (u0) n0 = fabsf(g.x) <= nb ? near_f64(v, X2h.x, X2l.x, Y2h.x, Y2l.x, Z2h.x, Z2l.x) : f2.x <= ff2;
-        if (u1) n1 = fabsf(g.y) <= nb ? near_f64(v, X2h.y, X2l.y, Y2h.y, Y2l.y, Z2h.y, Z2l.y) : f2.y <= ff2;
+        const int n = near_recheck(v, X2h, Y2h, Z2h, X2l, Y2l, Z2l, (u0 ? 1 : 0) | (u1 ? 2 : 0));
+        if (u0) n0 = (n & 1) != 0;
+        if (u1) n1 = (n & 2) != 0;
     }
 }
 
@@ -271,8 +287,10 @@ __device__ __forceinline__ int find_job(const BsJob* jobs, int n, long long item
     return lo;
 }
 
+// FP32 panel sweeps: at most 96 registers, five CTAs (20 warps) per SM; this issue-bound
+// kernel lost a fifth of its speed at four (98 registers round up to 104 per thread)
 template <class R, int T, bool KAHAN, int SYM, bool NEGLECT, bool CHAIN, int TILE_PANELS = 0>
-__global__ void __launch_bounds__(kBsThreads) k_bs_sweep(const BsArgs a) {
+__global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1) k_bs_sweep(const BsArgs a) {
     // panels per shared-memory stage: the precision's default, or a tuned shape (batched sweeps)
     constexpr int TILE = TILE_PANELS ? TILE_PANELS : TileSize<R>::value;
     constexpr int TT = SYM ? 2 * T : T;  // mirrored targets ride along as extra targets

@@ -53,6 +53,8 @@ int solve_cluster_size(int N) {
 struct RowGeom {
     d3 felt, span_dir, chord, span_rel_out;  // span_dir = normalize(span end - span start)
     double chord_len, area;
+    double chord_norm;  // |chord vector|
+    double cl_gamma;    // 2 |span_rel| / area (0 if the area or density is 0): see residual_of_row
     int wing;
 };
 
@@ -65,8 +67,23 @@ __device__ inline RowGeom row_geom(const DevModel& m, int i) {
     g.span_rel_out = m.output_body ? (m.span_e_local[i] - m.span_s_local[i]) : span_rel;
     g.chord_len = m.chord_len[i];
     g.area = m.chord_len[i] * m.span_len_local[i];
+    g.chord_norm = len(g.chord);
+    g.cl_gamma = (g.area == 0.0 || m.density == 0.0) ? 0.0 : 2.0 * len(span_rel) / g.area;
     g.wing = m.wing_of_line[i];
     return g;
+}
+
+// signed_angle_between(chord, u, span_dir) (vector_math.rs:65-95) with |chord| and |u| known:
+// cos = chord.u / (|chord| |u|) instead of / sqrt(|chord|^2 |u|^2) (the same to an ulp)
+__device__ inline double row_angle(const RowGeom& g, d3 u, double ul) {
+    const double triple = dot(g.chord, cross(u, g.span_dir));
+    double ang = 0.0;
+    if (!(g.chord_norm == 0.0 || ul == 0.0)) {
+        double c = dot(g.chord, u) / (g.chord_norm * ul);
+        c = fmin(fmax(c, -1.0), 1.0);
+        ang = acos(c);
+    }
+    return triple > 0.0 ? ang : -ang;
 }
 
 // velocity_corrections.rs:28-100 (returns freestream + induced, corrected)
@@ -99,6 +116,17 @@ __device__ inline double residual_from_cl(const DevModel& m, const RowGeom& g, d
 }
 __device__ inline double residual_term(const DevModel& m, const RowGeom& g, const FoilP& f, double gam, d3 u, double aoa) {
     return residual_from_cl(m, g, gam, u, foil_cl_pre_stall(f, aoa));
+}
+// The same in the iterations, with |u| known. In the global output frame the line's span
+// vector is span_rel, to which u was made perpendicular (the projection before the angle),
+// so |u x span_rel| = |u| |span_rel| and the lift coefficient of the force is
+// -gam |u| |span_rel| rho / (area rho |u|^2 / 2) = -gam cl_gamma / |u|: one division for
+// the cross product, two square roots and the quotient of residual_from_cl. (Body-frame
+// output keeps that function: there the span vector is the body frame's.)
+__device__ inline double residual_of_row(const DevModel& m, const RowGeom& g, double gam, d3 u, double ul, double cl_pre) {
+    if (m.output_body) return residual_from_cl(m, g, gam, u, cl_pre);
+    const double clg = ul == 0.0 ? 0.0 : -gam * g.cl_gamma / ul;
+    return fabs(clg - cl_pre);
 }
 
 // Double-float accumulation for the matrix-vector product: (S, C) += (xh + xl) * (gh + gl).
@@ -358,6 +386,7 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
 
     int it = 0, cur = 0;
     bool conv = false;
+    const bool want_max = st.strength_tolerance > 0.0;
     while (it < st.max_iterations && !conv) {
         it += 1;
         const float2* Gc = G[cur];
@@ -371,16 +400,19 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
             const FoilP f = m.foils[g.wing];
             d3 u = total_velocity(st, g.felt, induced_of(i));
             u = u - g.span_dir * dot(u, g.span_dir);  // project(u, span_rel)
-            double aoa = len(u) > kMinPositive ? signed_angle_between(g.chord, u, g.span_dir) : 0.0;
+            const double ul = len(u);
+            double aoa = ul > kMinPositive ? row_angle(g, u, ul) : 0.0;
             // the pre-stall lift coefficient serves the estimate and the residual alike
             const double clp = foil_cl_pre_stall(f, aoa);
             const double clc = m.include_viscous_lift ? clp + foil_cl_post_stall(f, aoa) : clp;  // circulation_cl
-            double est = -0.5 * g.chord_len * len(u) * clc;
+            double est = -0.5 * g.chord_len * ul * clc;
             double gold = gown[k];
-            double r = residual_from_cl(m, g, gold, u, clp);
+            double r = residual_of_row(m, g, gold, u, ul, clp);
             double d = est - gold;
-            const unsigned long long db = mag_bits(d);
-            lmax = db > lmax ? db : lmax;
+            if (want_max) {
+                const unsigned long long db = mag_bits(d);
+                lmax = db > lmax ? db : lmax;
+            }
             double gnew = gold + st.damping * d;
             gown[k] = gnew;
             u_last[k] = u;
@@ -393,14 +425,17 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
                 Rr[i] = r;
             }
         }
-        // block max
-        lmax = warp_umax_to_lane0(lmax);
-        if (lane == 0) s_umax[warp] = lmax;
-        __syncthreads();
-        if (tid == 0) {
-            unsigned long long v = 0;
-            for (int w = 0; w < nwarps; ++w) v = s_umax[w] > v ? s_umax[w] : v;
-            for (int q = 0; q < CS; ++q) cl.map_shared_rank(MX[cur], q)[rank] = bits_value(v);
+        // block max of |dGamma|, only where a strength tolerance can stop the solve (with a
+        // tolerance <= 0 the test `max < tolerance` never holds)
+        if (want_max) {
+            lmax = warp_umax_to_lane0(lmax);
+            if (lane == 0) s_umax[warp] = lmax;
+            __syncthreads();
+            if (tid == 0) {
+                unsigned long long v = 0;
+                for (int w = 0; w < nwarps; ++w) v = s_umax[w] > v ? s_umax[w] : v;
+                for (int q = 0; q < CS; ++q) cl.map_shared_rank(MX[cur], q)[rank] = bits_value(v);
+            }
         }
         cl.sync();
         if (warp == 0) {
@@ -410,13 +445,14 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
             if (lane == 0) {
                 double res = s / static_cast<double>(N);
                 unsigned long long mb = 0;
-                for (int q = 0; q < CS; ++q) {
-                    const unsigned long long bq = static_cast<unsigned long long>(__double_as_longlong(MX[cur][q]));
-                    mb = bq > mb ? bq : mb;
-                }
+                if (want_max)
+                    for (int q = 0; q < CS; ++q) {
+                        const unsigned long long bq = static_cast<unsigned long long>(__double_as_longlong(MX[cur][q]));
+                        mb = bq > mb ? bq : mb;
+                    }
                 const double mx = bits_value(mb);
                 s_res = res;
-                s_conv = (res < st.residual_tolerance) || (mx < st.strength_tolerance);
+                s_conv = (res < st.residual_tolerance) || (want_max && mx < st.strength_tolerance);
             }
         }
         __syncthreads();
