@@ -119,7 +119,6 @@ struct sb_batch {
     // names the wake buffer of the step's parity
     struct SiGroup {
         int cluster = 0, rows_per_thread = 1;
-        size_t smem = 0;
         std::vector<int> cases;
         long long off = 0;
     };
@@ -305,7 +304,6 @@ struct sb_batch {
             const int g = (CS == 1 ? 0 : (CS == 4 ? 1 : 2)) + (rpt == 1 ? 0 : 3);
             si_groups[g].cluster = CS;
             si_groups[g].rows_per_thread = rpt;
-            si_groups[g].smem = std::max(si_groups[g].smem, si_smem_bytes(c.N));
             si_groups[g].cases.push_back(static_cast<int>(i));
             si_batched[i] = 1;
         }
@@ -588,10 +586,16 @@ struct sb_batch {
                     ck(launch_solve_linearized_jobs(g.jobs.p, g.n, g.plan, n_launch > 1 ? pool[k++] : main),
                        "batched linearized solve");
             for (const auto& g : si_groups)
-                if (!g.cases.empty())
+                if (!g.cases.empty()) {
+                    // shared memory of the group's largest case (its matrix slab depends on
+                    // whether the matrix has lo parts off the diagonal, i.e. on the precision)
+                    size_t smem = 0;
+                    for (int ci : g.cases)
+                        smem = std::max(smem, si_smem_bytes(cases[ci]->N, cases[ci]->solve_buffers().split_full));
                     ck(launch_solve_simple_iterative_jobs(d_si_jobs.p + g.off, static_cast<int>(g.cases.size()), g.cluster,
-                                                          g.rows_per_thread, g.smem, n_launch > 1 ? pool[k++] : main),
+                                                          g.rows_per_thread, smem, n_launch > 1 ? pool[k++] : main),
                        "batched simple iterative solve");
+                }
             if (n_launch > 1) join(1);
         }
         // what follows a solve in its case (chain records of the wake), after the batched solves

@@ -35,6 +35,7 @@
 
 #include "sb_device.cuh"
 #include "sb_kernels.h"
+#include "sb_ptx.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -44,10 +45,41 @@ constexpr int kSolveThreads = 256;
 constexpr int kSolveRowsPerThread = 4;  // most rows per thread (1024 per CTA)
 constexpr int kMaxCluster = 8;
 
-int solve_cluster_size(int N) {
+__host__ __device__ inline int si_cluster_size(int N) {
     if (N <= 64) return 1;
     if (N <= 256) return 4;
     return 8;
+}
+int solve_cluster_size(int N) { return si_cluster_size(N); }
+
+// Matrix slab of a CTA (its rows of the split matrix) in shared memory. Bytes of one row:
+// 3 components x stride floats, twice with the lo plane. When all of the CTA's rows fit
+// kSlabBudget they are copied once per solve and stay; else chunks of 4 to 8 rows (a row per
+// warp) stream through two buffers of half the budget each, every iteration. 0: not even 4
+// rows fit a buffer (N above about 900): the warps read their rows from global memory.
+constexpr long long kSlabBudget = 88 * 1024;
+__host__ __device__ inline long long si_row_bytes(int N, int full) {
+    return 12LL * si_matrix_stride(N) * (full ? 2 : 1);
+}
+// Shared memory before the slab, in doubles: circulation pairs 2 x stride, residual terms
+// 2 x N, maxima 2 x kMaxCluster, the CTA's M * Gamma pairs (3 doubles per row), the own
+// panels' lo parts (2 doubles per row), rounded to 16 bytes.
+__host__ __device__ inline long long si_slab_offset(int N) {
+    const int CS = si_cluster_size(N);
+    const long long rp = (N + CS - 1) / CS;
+    const long long d = 2LL * si_matrix_stride(N) + 2LL * N + 2 * kMaxCluster + 3 * rp + 2 * rp;
+    return (d + 1) & ~1LL;
+}
+__host__ __device__ inline int si_slab_rows(int N, int full) {
+    const int CS = si_cluster_size(N);
+    const int rp = (N + CS - 1) / CS;
+    const long long rowb = si_row_bytes(N, full);
+    // two CTAs of a cluster per SM: at most ~110 KB of shared memory each
+    const long long rest = 110 * 1024 - si_slab_offset(N) * 8;
+    const long long budget = rest < kSlabBudget ? rest : kSlabBudget;
+    if (rp * rowb <= budget) return rp;
+    const long long r = budget / (2 * rowb);
+    return r < 4 ? 0 : (r > 8 ? 8 : static_cast<int>(r));
 }
 
 struct RowGeom {
@@ -144,15 +176,28 @@ __device__ __forceinline__ void ff_mac(float& S, float& C, float2 x, float2 g) {
     S = s;
     C = __fadd_rn(C, __fadd_rn(err, t));
 }
-// Four consecutive columns: matrix (a + al) against the circulation pairs (g01.x + g01.y),
-// (g01.z + g01.w), (g23.x + g23.y), (g23.z + g23.w)
-__device__ __forceinline__ void ff_mac4(float& S, float& C, float4 a, float4 al, float4 g01, float4 g23) {
-    ff_mac(S, C, make_float2(a.x, al.x), make_float2(g01.x, g01.y));
-    ff_mac(S, C, make_float2(a.y, al.y), make_float2(g01.z, g01.w));
-    ff_mac(S, C, make_float2(a.z, al.z), make_float2(g23.x, g23.y));
-    ff_mac(S, C, make_float2(a.w, al.w), make_float2(g23.z, g23.w));
+// Four consecutive columns into one component's sums: the hi products x * g_hi by Kahan's
+// compensated summation into (S, kc), their exact rounding errors (FMA) and x * g_lo (and,
+// with lo parts, x_lo * g_hi) plainly into C. The pair (S, C - kc) carries the sum to
+// ~N u^2 of its terms' magnitudes, as the two-sum form, with 8 FP32 operations per product
+// (9 with lo parts) instead of 11.
+__device__ __forceinline__ void kahan_mac(float& S, float& kc, float& C, float x, float xl, float gh, float gl, bool lo) {
+    const float p = __fmul_rn(x, gh);
+    C = __fadd_rn(C, fmaf(x, gh, -p));
+    C = fmaf(x, gl, C);
+    if (lo) C = fmaf(xl, gh, C);
+    const float y = __fsub_rn(p, kc);
+    const float t = __fadd_rn(S, y);
+    kc = __fsub_rn(__fsub_rn(t, S), y);
+    S = t;
 }
-__device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+__device__ __forceinline__ void kahan_mac4(float& S, float& kc, float& C, float4 a, float4 al, float4 g01, float4 g23,
+                                           bool lo) {
+    kahan_mac(S, kc, C, a.x, al.x, g01.x, g01.y, lo);
+    kahan_mac(S, kc, C, a.y, al.y, g01.z, g01.w, lo);
+    kahan_mac(S, kc, C, a.z, al.z, g23.x, g23.y, lo);
+    kahan_mac(S, kc, C, a.w, al.w, g23.z, g23.w, lo);
+}
 // (S, C) += (h, l), another double-float partial sum
 __device__ __forceinline__ void ff_add(float& S, float& C, float h, float l) {
     const float s = __fadd_rn(S, h);
@@ -197,7 +242,7 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
     const int rank = static_cast<int>(cl.block_rank());
     const int N = m.N;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = kSolveThreads / 32;
-    extern __shared__ double smem[];
+    extern __shared__ __align__(16) double smem[];
     // circulation of every line as (hi, lo) float pairs for the matrix-vector products, padded
     // with zeros to the matrix's row stride; the f64 circulation of the thread's own rows
     // stays in registers (gown)
@@ -214,9 +259,14 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
     // M * Gamma of the CTA's rows as double-float pairs (x hi, x lo, y hi, y lo, z hi, z lo);
     // the row's owner adds them to the fixed part in f64
     float* uff = reinterpret_cast<float*>(smem + 2 * S + 2 * N + 2 * kMaxCluster);
+    const int rp_max = (N + CS - 1) / CS;
+    // lo parts of the own panels' entries (x, y, z), when the matrix has none elsewhere
+    float* diag_lo = reinterpret_cast<float*>(smem + 2 * S + 2 * N + 2 * kMaxCluster + 3 * rp_max);
+    float* slab = reinterpret_cast<float*>(smem + si_slab_offset(N));
     __shared__ double s_res;
     __shared__ unsigned long long s_umax[kSolveThreads / 32];
     __shared__ int s_conv;
+    __shared__ __align__(8) uint64_t s_mbar[2];
 
     const bool scale0 = fabs(st.correction_factor_initial - 1.0) > kMinPositive;
     for (int i = tid; i < N; i += kSolveThreads) {
@@ -244,6 +294,28 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
     }
     __syncthreads();
 
+    const int full = b.split_full;
+    const int slab_rows = si_slab_rows(N, full);
+    const int nrows_cta = r1 - r0;
+    const int nch = slab_rows > 0 ? (nrows_cta + slab_rows - 1) / slab_rows : 0;
+    const bool resident = slab_rows > 0 && slab_rows >= rp_max;  // copied once, kept
+    const long long rowf = 3LL * S;                                // floats of a row, one plane
+    const long long buf_floats = static_cast<long long>(slab_rows) * rowf * (full ? 2 : 1);
+    const long long lo_plane = 3LL * N * S;
+    if (tid == 0) {
+        mbar_init(&s_mbar[0], 1);
+        mbar_init(&s_mbar[1], 1);
+        fence_mbar_init();
+    }
+    if (!full)
+        for (int k = tid; k < nrows_cta; k += kSolveThreads) {
+            const long long row = r0 + k;
+            const float* fl = b.factors_split + lo_plane + row * rowf;
+            diag_lo[3 * k] = fl[row];
+            diag_lo[3 * k + 1] = fl[S + row];
+            diag_lo[3 * k + 2] = fl[2 * S + row];
+        }
+
     // residual of the initial solution with zero velocity (simple_iterative.rs:180-184)
     double residual = 0.0;
     if (st.max_iterations == 0) {
@@ -259,54 +331,101 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
 
     // induced velocity of own rows for the circulation Gc: fixed + M * Gc. One warp per row;
     // double-float arithmetic on the FP32 pipes (this part's FP64 rate is 1/64 of its FP32
-    // rate): the split matrix row and the split circulation, ~2^-44 relative per product. A
-    // lane takes four consecutive columns per 16-byte load, so a row of up to 640 columns is
-    // at most five trips of loads from L2 (the matrix does not stay in shared memory).
-    const long long lo_plane = 3LL * N * S;
-    auto induced_rows = [&](const float2* Gc) {
-        const bool full = b.split_full != 0;
-        for (int row = r0 + warp; row < r1; row += nwarps) {
-            const float* fh = b.factors_split + static_cast<long long>(row) * 3 * S;
-            const float* fl = fh + lo_plane;
-            float sxh = 0.f, sxl = 0.f, syh = 0.f, syl = 0.f, szh = 0.f, szl = 0.f;
+    // rate), a lane taking four consecutive columns per 16-byte shared-memory load. The
+    // CTA's matrix rows come from its slab in shared memory: thread 0 copies them by bulk
+    // asynchronous copies (cp.async.bulk, completion on an mbarrier; bounded waits), kept for
+    // the whole solve when they fit, else streamed in chunks through two buffers (the copy
+    // of chunk c + 1 runs while the warps work on chunk c).
+    // A slab wait that runs out records kDevTimeout (the host raises SB_ERR_TIMEOUT after the
+    // launch); that thread then waits no more and thread 0 issues no more copies, and the
+    // solve runs its remaining (bounded) iterations on whatever the buffers hold, through the
+    // same barriers as the other CTAs of the cluster, so that none waits for it forever.
+    uint32_t mph[2] = {0u, 0u};
+    bool pending[2] = {false, false};  // thread 0: a copy into the buffer not yet waited for
+    bool slab_loaded = false, dead = false;
+    auto issue = [&](int c, int bufi) {  // thread 0
+        const long long row0 = r0 + static_cast<long long>(c) * slab_rows;
+        const int nr = min(slab_rows, r1 - static_cast<int>(row0));
+        const uint32_t bytes = static_cast<uint32_t>(nr * rowf * 4);
+        float* dst = slab + bufi * buf_floats;
+        mbar_expect_tx(&s_mbar[bufi], full ? 2 * bytes : bytes);
+        bulk_g2s(dst, b.factors_split + row0 * rowf, bytes, &s_mbar[bufi]);
+        if (full) bulk_g2s(dst + slab_rows * rowf, b.factors_split + lo_plane + row0 * rowf, bytes, &s_mbar[bufi]);
+        pending[bufi] = true;
+    };
+    // (S, C) += row . Gc over the lane's columns, from fh (hi) and fl (lo, full only)
+    auto row_dot = [&](const float* fh, const float* fl, const float2* Gc, float (&acc)[6]) {
+        float kc[3] = {0.f, 0.f, 0.f};  // Kahan compensations of the hi sums
 #pragma unroll 2
-            for (int k = 4 * lane; k < S; k += 128) {
-                const float4 g01 = *reinterpret_cast<const float4*>(Gc + k);  // (hi, lo) of columns k, k + 1
-                const float4 g23 = *reinterpret_cast<const float4*>(Gc + k + 2);
-                const float4 ax = ldg4(fh + k), ay = ldg4(fh + S + k), az = ldg4(fh + 2 * S + k);
-                float4 lx = make_float4(0.f, 0.f, 0.f, 0.f), ly = lx, lz = lx;
-                if (full) {
-                    lx = ldg4(fl + k);
-                    ly = ldg4(fl + S + k);
-                    lz = ldg4(fl + 2 * S + k);
-                }
-                ff_mac4(sxh, sxl, ax, lx, g01, g23);
-                ff_mac4(syh, syl, ay, ly, g01, g23);
-                ff_mac4(szh, szl, az, lz, g01, g23);
-            }
+        for (int k = 4 * lane; k < S; k += 128) {
+            const float4 g01 = *reinterpret_cast<const float4*>(Gc + k);  // (hi, lo) of columns k, k + 1
+            const float4 g23 = *reinterpret_cast<const float4*>(Gc + k + 2);
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                ff_add(sxh, sxl, __shfl_down_sync(0xffffffffu, sxh, o), __shfl_down_sync(0xffffffffu, sxl, o));
-                ff_add(syh, syl, __shfl_down_sync(0xffffffffu, syh, o), __shfl_down_sync(0xffffffffu, syl, o));
-                ff_add(szh, szl, __shfl_down_sync(0xffffffffu, szh, o), __shfl_down_sync(0xffffffffu, szl, o));
-            }
-            if (lane == 0) {
-                if (!full) {  // the own panel's entry is f64: its lo parts times Gamma hi
-                    const float2 g = Gc[row];
-                    ff_mac(sxh, sxl, make_float2(0.f, fl[row]), g);
-                    ff_mac(syh, syl, make_float2(0.f, fl[S + row]), g);
-                    ff_mac(szh, szl, make_float2(0.f, fl[2 * S + row]), g);
-                }
-                float* o = uff + 6 * (row - r0);
-                o[0] = sxh;
-                o[1] = sxl;
-                o[2] = syh;
-                o[3] = syl;
-                o[4] = szh;
-                o[5] = szl;
+            for (int q = 0; q < 3; ++q) {
+                const float4 a = *reinterpret_cast<const float4*>(fh + q * S + k);
+                const float4 al = full ? *reinterpret_cast<const float4*>(fl + q * S + k) : make_float4(0.f, 0.f, 0.f, 0.f);
+                kahan_mac4(acc[2 * q], kc[q], acc[2 * q + 1], a, al, g01, g23, full != 0);
             }
         }
-        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 3; ++q) acc[2 * q + 1] = __fsub_rn(acc[2 * q + 1], kc[q]);
+    };
+    auto finish_row = [&](int row, float (&acc)[6], const float2* Gc) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int q = 0; q < 3; ++q)
+                ff_add(acc[2 * q], acc[2 * q + 1], __shfl_down_sync(0xffffffffu, acc[2 * q], o),
+                       __shfl_down_sync(0xffffffffu, acc[2 * q + 1], o));
+        if (lane == 0) {
+            if (!full) {  // the own panel's entry is f64: its lo parts times Gamma hi
+                const float2 g = Gc[row];
+                const float* dl = diag_lo + 3 * (row - r0);
+#pragma unroll
+                for (int q = 0; q < 3; ++q) ff_mac(acc[2 * q], acc[2 * q + 1], make_float2(0.f, dl[q]), g);
+            }
+            float* o = uff + 6 * (row - r0);
+#pragma unroll
+            for (int q = 0; q < 6; ++q) o[q] = acc[q];
+        }
+    };
+    auto induced_rows = [&](const float2* Gc) {
+        if (slab_rows == 0) {  // rows from global memory
+            for (int row = r0 + warp; row < r1; row += nwarps) {
+                const float* fh = b.factors_split + static_cast<long long>(row) * rowf;
+                float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                row_dot(fh, fh + lo_plane, Gc, acc);
+                finish_row(row, acc, Gc);
+            }
+            __syncthreads();
+            return;
+        }
+        const bool copy = !(resident && slab_loaded);
+        if (copy && tid == 0 && !dead) {
+            issue(0, 0);
+            if (nch > 1) issue(1, 1);
+        }
+        for (int c = 0; c < nch; ++c) {
+            const int bufi = c & 1;
+            if (copy) {
+                if (!dead) {
+                    if (mbar_wait_bounded(&s_mbar[bufi], mph[bufi], b.err)) pending[bufi] = false;
+                    else dead = true;
+                }
+                mph[bufi] ^= 1u;
+            }
+            const int row0 = r0 + c * slab_rows;
+            const int nr = min(slab_rows, r1 - row0);
+            const float* base = slab + bufi * buf_floats;
+            for (int w = warp; w < nr; w += nwarps) {
+                float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                row_dot(base + w * rowf, base + (slab_rows + w) * rowf, Gc, acc);
+                finish_row(row0 + w, acc, Gc);
+            }
+            __syncthreads();  // every warp is done with this buffer
+            if (copy && !resident && tid == 0 && !dead && c + 2 < nch) issue(c + 2, bufi);
+        }
+        slab_loaded = true;
     };
     // induced velocity of own row i: fixed + M * Gamma
     auto induced_of = [&](int i) {
@@ -477,6 +596,10 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
         b.scalars[1] = static_cast<double>(it);
         b.scalars[2] = conv ? 1.0 : 0.0;
     }
+    // a copy whose wait ran out may still be in flight: wait for it (bounded) before leaving
+    if (tid == 0)
+        for (int q = 0; q < 2; ++q)
+            if (pending[q]) mbar_wait_bounded(&s_mbar[q], mph[q] ^ 1u, b.err);
     cl.sync();  // no CTA leaves while others may still write into its shared memory
 }
 
@@ -501,12 +624,12 @@ int si_rows_per_thread(int N) {
     return rp <= kSolveThreads ? 1 : kSolveRowsPerThread;
 }
 
-size_t si_smem_bytes(int N) {
-    const int CS = solve_cluster_size(N);
+size_t si_smem_bytes(int N, int full) {
+    const int CS = si_cluster_size(N);
     const int rp = (N + CS - 1) / CS;
-    return (2 * static_cast<size_t>(si_matrix_stride(N)) + 2 * static_cast<size_t>(N) + 2 * kMaxCluster) *
-               sizeof(double) +
-           static_cast<size_t>(rp) * sizeof(d3);
+    const int sr = si_slab_rows(N, full);
+    const long long bufs = sr == 0 ? 0 : (sr >= rp ? 1 : 2);
+    return static_cast<size_t>(si_slab_offset(N) * 8 + bufs * sr * si_row_bytes(N, full));
 }
 
 cudaError_t launch_solve_simple_iterative_jobs(const SolveJob* jobs, int n, int cluster, int rows_per_thread,
@@ -538,7 +661,7 @@ cudaError_t launch_solve_simple_iterative(const DevModel& m, const SolveSettings
     const int CS = solve_cluster_size(m.N);
     const int rp = (m.N + CS - 1) / CS;
     if (rp > kSolveThreads * kSolveRowsPerThread) return cudaErrorInvalidValue;
-    size_t smem = si_smem_bytes(m.N);
+    size_t smem = si_smem_bytes(m.N, b.split_full);
     auto kernel = si_rows_per_thread(m.N) == 1 ? k_solve_si<1> : k_solve_si<kSolveRowsPerThread>;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));

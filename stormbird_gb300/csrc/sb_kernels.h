@@ -241,7 +241,7 @@ LinPlan linearized_plan(int N);
 cudaError_t launch_solve_linearized_jobs(const SolveJob* jobs, int n, const LinPlan& plan, cudaStream_t s);
 // SimpleIterative solves of a batch: n cases of one cluster size (solve_cluster_size of
 // their N) in one launch, a cluster per case; smem = the largest si_smem_bytes of the jobs.
-size_t si_smem_bytes(int N);
+size_t si_smem_bytes(int N, int full);  // full: the matrix's lo plane is read (SolveBuffers::split_full)
 int si_rows_per_thread(int N);  // 1 or 4: a launch holds one kind (rows_per_thread below)
 cudaError_t launch_solve_simple_iterative_jobs(const SolveJob* jobs, int n, int cluster, int rows_per_thread,
                                                size_t smem, cudaStream_t s);

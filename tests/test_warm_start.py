@@ -100,6 +100,15 @@ def test_training_reads_rows_after_the_callers_stream(gpu_lib):
 
 
 def test_warm_start_on_held_out_cases(gpu_lib):
+    """The three starts on held-out cases: every arm ends within 1e-5 of the plain solves, the
+    extrapolation in time saves iterations over the plain start, and the network arm is no
+    worse than the extrapolation alone (the guard takes the network's start only when its
+    residuals are half the extrapolation's). What the network gains over the extrapolation,
+    as measured at full scale (config-4 network trained on 204,800 converged solves of the
+    512 uneven cases, evaluated on those cases with every wake full): nothing. Its start was
+    taken in 0 %, 0.23 % and 1.5 % of solves at guard factors 0.5, 0.8 and 1.0, and the
+    iterations per solve were 88.21, 88.21 and 88.24 against 88.21 for the extrapolation
+    alone and 97.03 for the plain start."""
     pytest.importorskip("torch")
     from stormbird_gb300 import setups as S
     from stormbird_gb300 import warm_start as WS
@@ -116,8 +125,9 @@ def test_warm_start_on_held_out_cases(gpu_lib):
     print("warm start on held-out cases:", rep)
     for arm in ("extrapolation", "warm"):
         assert rep[f"max_rel_circulation_diff_{arm}"] <= 1e-5
-        assert rep[f"iterations_{arm}"] <= 1.05 * rep["iterations_plain"]
         assert 0.0 <= rep[f"fallback_rate_{arm}"] <= 1.0
+    assert rep["iterations_extrapolation"] < rep["iterations_plain"]
+    assert rep["iterations_warm"] <= 1.02 * rep["iterations_extrapolation"]
 
 
 def test_loaded_state_restarts_the_warm_start_history(gpu_lib):
