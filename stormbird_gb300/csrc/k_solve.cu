@@ -176,27 +176,16 @@ __device__ __forceinline__ void ff_mac(float& S, float& C, float2 x, float2 g) {
     S = s;
     C = __fadd_rn(C, __fadd_rn(err, t));
 }
-// Four consecutive columns into one component's sums: the hi products x * g_hi by Kahan's
-// compensated summation into (S, kc), their exact rounding errors (FMA) and x * g_lo (and,
-// with lo parts, x_lo * g_hi) plainly into C. The pair (S, C - kc) carries the sum to
-// ~N u^2 of its terms' magnitudes, as the two-sum form, with 8 FP32 operations per product
-// (9 with lo parts) instead of 11.
-__device__ __forceinline__ void kahan_mac(float& S, float& kc, float& C, float x, float xl, float gh, float gl, bool lo) {
-    const float p = __fmul_rn(x, gh);
-    C = __fadd_rn(C, fmaf(x, gh, -p));
-    C = fmaf(x, gl, C);
-    if (lo) C = fmaf(xl, gh, C);
-    const float y = __fsub_rn(p, kc);
-    const float t = __fadd_rn(S, y);
-    kc = __fsub_rn(__fsub_rn(t, S), y);
-    S = t;
-}
-__device__ __forceinline__ void kahan_mac4(float& S, float& kc, float& C, float4 a, float4 al, float4 g01, float4 g23,
-                                           bool lo) {
-    kahan_mac(S, kc, C, a.x, al.x, g01.x, g01.y, lo);
-    kahan_mac(S, kc, C, a.y, al.y, g01.z, g01.w, lo);
-    kahan_mac(S, kc, C, a.z, al.z, g23.x, g23.y, lo);
-    kahan_mac(S, kc, C, a.w, al.w, g23.z, g23.w, lo);
+// Four consecutive columns into one component's double-float sum (S, C): matrix entries
+// (a + al) (al = 0 without lo parts) against the circulation pairs (g01.x + g01.y),
+// (g01.z + g01.w), (g23.x + g23.y), (g23.z + g23.w), each by ff_mac (two-sum: exact for any
+// magnitudes; a Kahan-compensated sum, two operations cheaper, is exact only while the
+// running sum outweighs the new term and left the solve a residual floor near 1e-11).
+__device__ __forceinline__ void ff_mac4(float& S, float& C, float4 a, float4 al, float4 g01, float4 g23) {
+    ff_mac(S, C, make_float2(a.x, al.x), make_float2(g01.x, g01.y));
+    ff_mac(S, C, make_float2(a.y, al.y), make_float2(g01.z, g01.w));
+    ff_mac(S, C, make_float2(a.z, al.z), make_float2(g23.x, g23.y));
+    ff_mac(S, C, make_float2(a.w, al.w), make_float2(g23.z, g23.w));
 }
 // (S, C) += (h, l), another double-float partial sum
 __device__ __forceinline__ void ff_add(float& S, float& C, float h, float l) {
@@ -355,7 +344,6 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
     };
     // (S, C) += row . Gc over the lane's columns, from fh (hi) and fl (lo, full only)
     auto row_dot = [&](const float* fh, const float* fl, const float2* Gc, float (&acc)[6]) {
-        float kc[3] = {0.f, 0.f, 0.f};  // Kahan compensations of the hi sums
 #pragma unroll 2
         for (int k = 4 * lane; k < S; k += 128) {
             const float4 g01 = *reinterpret_cast<const float4*>(Gc + k);  // (hi, lo) of columns k, k + 1
@@ -364,11 +352,9 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
             for (int q = 0; q < 3; ++q) {
                 const float4 a = *reinterpret_cast<const float4*>(fh + q * S + k);
                 const float4 al = full ? *reinterpret_cast<const float4*>(fl + q * S + k) : make_float4(0.f, 0.f, 0.f, 0.f);
-                kahan_mac4(acc[2 * q], kc[q], acc[2 * q + 1], a, al, g01, g23, full != 0);
+                ff_mac4(acc[2 * q], acc[2 * q + 1], a, al, g01, g23);
             }
         }
-#pragma unroll
-        for (int q = 0; q < 3; ++q) acc[2 * q + 1] = __fsub_rn(acc[2 * q + 1], kc[q]);
     };
     auto finish_row = [&](int row, float (&acc)[6], const float2* Gc) {
 #pragma unroll
