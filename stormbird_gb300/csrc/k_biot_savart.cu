@@ -417,179 +417,187 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
         for (; k < ntiles; ++k) {
             const int buf = k & 1;
             if (tid == 0 && k + 1 < ntiles) issue(k + 1);
+            bool ok;
             if (buf == 0) {
-                if (!mbar_wait_bounded(&bar[0], phase0, a.err, a.wait_polls)) s_timed_out = 1;
+                ok = mbar_wait_bounded(&bar[0], phase0, a.err, a.wait_polls);
                 phase0 ^= 1;
             } else {
-                if (!mbar_wait_bounded(&bar[1], phase1, a.err, a.wait_polls)) s_timed_out = 1;
+                ok = mbar_wait_bounded(&bar[1], phase1, a.err, a.wait_polls);
                 phase1 ^= 1;
             }
+            if (!ok) s_timed_out = 1;
             const int np = static_cast<int>(min(static_cast<long long>(TILE), pe - (pb + static_cast<long long>(k) * TILE)));
 
-            if constexpr (F32) {
-                float2 TX = bc(0.f), TY = bc(0.f), TZ = bc(0.f);
-                // Far-field fast path: when the box of the tile's panel centres lies farther from
-                // the box of the warp's targets than the tile's largest far-field radius (with a
-                // margin well beyond the FP32 rounding of the per-pair distance), every pair of
-                // the tile is a point doublet (panel.rs:53-57, 82-96) and the per-pair test
-                // below would decide so for every lane: the warp evaluates the doublets alone,
-                // without the test and the votes.
-                bool all_far = false;
-                if constexpr (FAST_FAR) {
-                    const int lane = tid & 31;
-                    float c7[7] = {CUDART_INF_F, CUDART_INF_F, CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F,
-                                   0.f};
-                    for (int q = lane; q < np; q += 32) {
-                        const float4 c = *reinterpret_cast<const float4*>(&tile[buf][q].v[28]);  // centre hi, ff2
-                        c7[0] = fminf(c7[0], c.x);
-                        c7[1] = fminf(c7[1], c.y);
-                        c7[2] = fminf(c7[2], c.z);
-                        c7[3] = fmaxf(c7[3], c.x);
-                        c7[4] = fmaxf(c7[4], c.y);
-                        c7[5] = fmaxf(c7[5], c.z);
-                        c7[6] = fmaxf(c7[6], c.w);
-                    }
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1)
-#pragma unroll
-                        for (int q = 0; q < 7; ++q) {
-                            const float w = __shfl_xor_sync(0xffffffffu, c7[q], o);
-                            c7[q] = q < 3 ? fminf(c7[q], w) : fmaxf(c7[q], w);
+            // A warp with a lane whose wait ran out leaves the tile alone: its copy may still be
+            // landing, and lanes reading a word while it lands can see different values, which
+            // would split the warp at the uniform branches, votes and shuffles below (the sums
+            // are void anyway).
+            if (!__any_sync(0xffffffffu, !ok)) {
+                if constexpr (F32) {
+                    float2 TX = bc(0.f), TY = bc(0.f), TZ = bc(0.f);
+                    // Far-field fast path: when the box of the tile's panel centres lies farther from
+                    // the box of the warp's targets than the tile's largest far-field radius (with a
+                    // margin well beyond the FP32 rounding of the per-pair distance), every pair of
+                    // the tile is a point doublet (panel.rs:53-57, 82-96) and the per-pair test
+                    // below would decide so for every lane: the warp evaluates the doublets alone,
+                    // without the test and the votes.
+                    bool all_far = false;
+                    if constexpr (FAST_FAR) {
+                        const int lane = tid & 31;
+                        float c7[7] = {CUDART_INF_F, CUDART_INF_F, CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F,
+                                       0.f};
+                        for (int q = lane; q < np; q += 32) {
+                            const float4 c = *reinterpret_cast<const float4*>(&tile[buf][q].v[28]);  // centre hi, ff2
+                            c7[0] = fminf(c7[0], c.x);
+                            c7[1] = fminf(c7[1], c.y);
+                            c7[2] = fminf(c7[2], c.z);
+                            c7[3] = fmaxf(c7[3], c.x);
+                            c7[4] = fmaxf(c7[4], c.y);
+                            c7[5] = fmaxf(c7[5], c.z);
+                            c7[6] = fmaxf(c7[6], c.w);
                         }
-                    const float* wb = s_wbox[tid >> 5];
-                    // the boxes are of hi parts, each within 2^-24 |x| of its point: the gaps
-                    // shrink by both sides' bound before the test
-                    auto gap = [&](int q) {
-                        const float m = fmaxf(fmaxf(fabsf(c7[q]), fabsf(c7[q + 3])), fmaxf(fabsf(wb[q]), fabsf(wb[q + 3])));
-                        return fmaxf(0.f, fmaxf(c7[q] - wb[q + 3], wb[q] - c7[q + 3]) - 0x1p-23f * m);
-                    };
-                    const float gx = gap(0), gy = gap(1), gz = gap(2);
-                    // (the reduced values are the same in every lane; the vote tells the compiler
-                    // the branch is warp-uniform, which keeps the register count of the kernel)
-                    all_far = __all_sync(0xffffffffu, c7[6] < CUDART_INF_F && gx * gx + gy * gy + gz * gz > 1.001f * c7[6]);
-                }
-                if (all_far) {
-                    // lanes of targets past the end compute values that are never stored; four
-                    // panels per trip give the scheduler independent chains to interleave
-#pragma unroll 4
-                    for (int p = 0; p < np; ++p) {
+    #pragma unroll
+                        for (int o = 16; o > 0; o >>= 1)
+    #pragma unroll
+                            for (int q = 0; q < 7; ++q) {
+                                const float w = __shfl_xor_sync(0xffffffffu, c7[q], o);
+                                c7[q] = q < 3 ? fminf(c7[q], w) : fmaxf(c7[q], w);
+                            }
+                        const float* wb = s_wbox[tid >> 5];
+                        // the boxes are of hi parts, each within 2^-24 |x| of its point: the gaps
+                        // shrink by both sides' bound before the test
+                        auto gap = [&](int q) {
+                            const float m = fmaxf(fmaxf(fabsf(c7[q]), fabsf(c7[q + 3])), fmaxf(fabsf(wb[q]), fabsf(wb[q + 3])));
+                            return fmaxf(0.f, fmaxf(c7[q] - wb[q + 3], wb[q] - c7[q + 3]) - 0x1p-23f * m);
+                        };
+                        const float gx = gap(0), gy = gap(1), gz = gap(2);
+                        // (the reduced values are the same in every lane; the vote tells the compiler
+                        // the branch is warp-uniform, which keeps the register count of the kernel)
+                        all_far = __all_sync(0xffffffffu, c7[6] < CUDART_INF_F && gx * gx + gy * gy + gz * gz > 1.001f * c7[6]);
+                    }
+                    if (all_far) {
+                        // lanes of targets past the end compute values that are never stored; four
+                        // panels per trip give the scheduler independent chains to interleave
+    #pragma unroll 4
+                        for (int p = 0; p < np; ++p) {
+                            const float* v = reinterpret_cast<const float*>(tile[buf][p].v);
+                            const float gam = v[kRec32Gamma];
+                            if (gam == 0.f) continue;  // uniform across the CTA
+                            const float2 ex = sub2s(X2h, v[28]);
+                            const float2 ey = sub2s(Y2h, v[29]);
+                            const float2 ez = sub2s(Z2h, v[30]);
+                            const float2 e2s = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
+                            const float2 ir = make_float2(rsqrt_n(fmaxf(e2s.x, FLT_MIN)), rsqrt_n(fmaxf(e2s.y, FLT_MIN)));
+                            const float2 ir2 = mul2(ir, ir);
+                            const float2 sd = mul2(bc(v[35] * gam), mul2(mul2(ir2, ir2), ir));
+                            const float nx = v[36], ny = v[37], nz = v[38];
+                            const float2 h3 = mul2(bc(3.f), fma2(ex, bc(nx), fma2(ey, bc(ny), mul2(ez, bc(nz)))));
+                            TX = fma2(sd, fma2(h3, ex, mul2(e2s, bc(-nx))), TX);
+                            TY = fma2(sd, fma2(h3, ey, mul2(e2s, bc(-ny))), TY);
+                            TZ = fma2(sd, fma2(h3, ez, mul2(e2s, bc(-nz))), TZ);
+                        }
+                    }
+                    for (int p = 0; p < (all_far ? 0 : np); ++p) {
                         const float* v = reinterpret_cast<const float*>(tile[buf][p].v);
+                        if constexpr (CHAIN) {  // every pair near-field: the chain's segments
+                            if (v[kChainAny] == 0.f) continue;  // uniform across the CTA
+                            const float2 ex = add2(sub2s(X2h, v[0]), sub2s(X2l, v[3]));
+                            const float2 ey = add2(sub2s(Y2h, v[1]), sub2s(Y2l, v[4]));
+                            const float2 ez = add2(sub2s(Z2h, v[2]), sub2s(Z2l, v[5]));
+                            float2 ax, ay, az;
+                            chain2(v, ex, ey, ez, ax, ay, az);
+                            TX = add2(TX, ax);
+                            TY = add2(TY, ay);
+                            TZ = add2(TZ, az);
+                            continue;
+                        }
                         const float gam = v[kRec32Gamma];
                         if (gam == 0.f) continue;  // uniform across the CTA
-                        const float2 ex = sub2s(X2h, v[28]);
-                        const float2 ey = sub2s(Y2h, v[29]);
-                        const float2 ez = sub2s(Z2h, v[30]);
-                        const float2 e2s = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
-                        const float2 ir = make_float2(rsqrt_n(fmaxf(e2s.x, FLT_MIN)), rsqrt_n(fmaxf(e2s.y, FLT_MIN)));
-                        const float2 ir2 = mul2(ir, ir);
-                        const float2 sd = mul2(bc(v[35] * gam), mul2(mul2(ir2, ir2), ir));
-                        const float nx = v[36], ny = v[37], nz = v[38];
-                        const float2 h3 = mul2(bc(3.f), fma2(ex, bc(nx), fma2(ey, bc(ny), mul2(ez, bc(nz)))));
-                        TX = fma2(sd, fma2(h3, ex, mul2(e2s, bc(-nx))), TX);
-                        TY = fma2(sd, fma2(h3, ey, mul2(e2s, bc(-ny))), TY);
-                        TZ = fma2(sd, fma2(h3, ez, mul2(e2s, bc(-nz))), TZ);
+                        // target - centre from the hi parts: the near/far test's first look and the
+                        // far-field doublet's (at least ff_ratio panel sizes away), as in the fast
+                        // path above; the ring below adds the lo parts
+                        float2 ex = sub2s(X2h, v[28]);
+                        float2 ey = sub2s(Y2h, v[29]);
+                        float2 ez = sub2s(Z2h, v[30]);
+                        float2 e2 = bc(0.f);
+                        bool n0 = true, n1 = true;
+                        if (v[31] != CUDART_INF_F) {  // panel.rs:53-57; uniform per panel
+                            e2 = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
+                            near_far2<true>(v, e2, X2h, Y2h, Z2h, X2l, Y2l, Z2l, n0, n1);
+                        }
+                        bool a0 = valid[0], a1 = valid[1];
+                        if (NEGLECT) {
+                            const int pw = static_cast<int>(v[41]);
+                            a0 = a0 && tw[0] != pw;
+                            a1 = a1 && tw[1] != pw;
+                        }
+                        const bool any_near = __any_sync(0xffffffffu, (a0 && n0) || (a1 && n1));
+                        const bool any_far = __any_sync(0xffffffffu, (a0 && !n0) || (a1 && !n1));
+                        if (any_far) {  // point doublet (panel.rs:82-96), the fast path's arithmetic
+                            const float2 e2s = make_float2(n0 ? 1.f : e2.x, n1 ? 1.f : e2.y);
+                            // a subnormal |e|^2 (a degenerate panel) overflows s to inf either way
+                            const float2 ir = make_float2(rsqrt_n(fmaxf(e2s.x, FLT_MIN)), rsqrt_n(fmaxf(e2s.y, FLT_MIN)));
+                            const float2 ir2 = mul2(ir, ir);
+                            const float at = v[35] * gam;
+                            const float2 sm = make_float2((a0 && !n0) ? at : 0.f, (a1 && !n1) ? at : 0.f);
+                            const float2 s = mul2(sm, mul2(mul2(ir2, ir2), ir));
+                            const float nx = v[36], ny = v[37], nz = v[38];
+                            const float2 h3 = mul2(bc(3.f), fma2(ex, bc(nx), fma2(ey, bc(ny), mul2(ez, bc(nz)))));
+                            TX = fma2(s, fma2(h3, ex, mul2(e2s, bc(-nx))), TX);
+                            TY = fma2(s, fma2(h3, ey, mul2(e2s, bc(-ny))), TY);
+                            TZ = fma2(s, fma2(h3, ez, mul2(e2s, bc(-nz))), TZ);
+                        }
+                        if (any_near) {  // vortex ring (panel.rs:99-118)
+                            // float-float difference: (x_hi - c_hi) + (x_lo - c_lo)
+                            ex = add2(ex, sub2s(X2l, v[32]));
+                            ey = add2(ey, sub2s(Y2l, v[33]));
+                            ez = add2(ez, sub2s(Z2l, v[34]));
+                            float2 ax, ay, az;
+                            ring2(v, ex, ey, ez, ax, ay, az);
+                            const float g4 = gam * static_cast<float>(kFourPiInv);
+                            const float2 gm = make_float2((a0 && n0) ? g4 : 0.f, (a1 && n1) ? g4 : 0.f);
+                            TX = fma2(gm, ax, TX);
+                            TY = fma2(gm, ay, TY);
+                            TZ = fma2(gm, az, TZ);
+                        }
                     }
-                }
-                for (int p = 0; p < (all_far ? 0 : np); ++p) {
-                    const float* v = reinterpret_cast<const float*>(tile[buf][p].v);
-                    if constexpr (CHAIN) {  // every pair near-field: the chain's segments
-                        if (v[kChainAny] == 0.f) continue;  // uniform across the CTA
-                        const float2 ex = add2(sub2s(X2h, v[0]), sub2s(X2l, v[3]));
-                        const float2 ey = add2(sub2s(Y2h, v[1]), sub2s(Y2l, v[4]));
-                        const float2 ez = add2(sub2s(Z2h, v[2]), sub2s(Z2l, v[5]));
-                        float2 ax, ay, az;
-                        chain2(v, ex, ey, ez, ax, ay, az);
-                        TX = add2(TX, ax);
-                        TY = add2(TY, ay);
-                        TZ = add2(TZ, az);
-                        continue;
+                    const float txa[2] = {TX.x, TX.y}, tya[2] = {TY.x, TY.y}, tza[2] = {TZ.x, TZ.y};
+    #pragma unroll
+                    for (int t = 0; t < 2; ++t) {
+                        if (KAHAN) {
+                            two_sum_acc(sx[t], cx[t], static_cast<R>(txa[t]));
+                            two_sum_acc(sy[t], cy[t], static_cast<R>(tya[t]));
+                            two_sum_acc(sz[t], cz[t], static_cast<R>(tza[t]));
+                        } else {
+                            sx[t] += static_cast<R>(txa[t]);
+                            sy[t] += static_cast<R>(tya[t]);
+                            sz[t] += static_cast<R>(tza[t]);
+                        }
                     }
-                    const float gam = v[kRec32Gamma];
-                    if (gam == 0.f) continue;  // uniform across the CTA
-                    // target - centre from the hi parts: the near/far test's first look and the
-                    // far-field doublet's (at least ff_ratio panel sizes away), as in the fast
-                    // path above; the ring below adds the lo parts
-                    float2 ex = sub2s(X2h, v[28]);
-                    float2 ey = sub2s(Y2h, v[29]);
-                    float2 ez = sub2s(Z2h, v[30]);
-                    float2 e2 = bc(0.f);
-                    bool n0 = true, n1 = true;
-                    if (v[31] != CUDART_INF_F) {  // panel.rs:53-57; uniform per panel
-                        e2 = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
-                        near_far2<true>(v, e2, X2h, Y2h, Z2h, X2l, Y2l, Z2l, n0, n1);
+                } else {
+                    R tx[TT], ty[TT], tz[TT];
+    #pragma unroll
+                    for (int t = 0; t < TT; ++t) tx[t] = ty[t] = tz[t] = R(0);
+                    for (int p = 0; p < np; ++p) {
+                        const double* v = reinterpret_cast<const double*>(tile[buf][p].v);
+                        const double gam = v[kRec64Gamma];
+                        if (gam == 0.0) continue;
+                        const int pw = NEGLECT ? static_cast<int>(v[26]) : 0;
+    #pragma unroll
+                        for (int t = 0; t < TT; ++t) {
+                            if (!valid[t] || (NEGLECT && tw[t] == pw)) continue;
+                            d3 u = panel_unit_f64(v, mk(xh[t], yh[t], zh[t]));
+                            tx[t] += gam * u.x;
+                            ty[t] += gam * u.y;
+                            tz[t] += gam * u.z;
+                        }
                     }
-                    bool a0 = valid[0], a1 = valid[1];
-                    if (NEGLECT) {
-                        const int pw = static_cast<int>(v[41]);
-                        a0 = a0 && tw[0] != pw;
-                        a1 = a1 && tw[1] != pw;
-                    }
-                    const bool any_near = __any_sync(0xffffffffu, (a0 && n0) || (a1 && n1));
-                    const bool any_far = __any_sync(0xffffffffu, (a0 && !n0) || (a1 && !n1));
-                    if (any_far) {  // point doublet (panel.rs:82-96), the fast path's arithmetic
-                        const float2 e2s = make_float2(n0 ? 1.f : e2.x, n1 ? 1.f : e2.y);
-                        // a subnormal |e|^2 (a degenerate panel) overflows s to inf either way
-                        const float2 ir = make_float2(rsqrt_n(fmaxf(e2s.x, FLT_MIN)), rsqrt_n(fmaxf(e2s.y, FLT_MIN)));
-                        const float2 ir2 = mul2(ir, ir);
-                        const float at = v[35] * gam;
-                        const float2 sm = make_float2((a0 && !n0) ? at : 0.f, (a1 && !n1) ? at : 0.f);
-                        const float2 s = mul2(sm, mul2(mul2(ir2, ir2), ir));
-                        const float nx = v[36], ny = v[37], nz = v[38];
-                        const float2 h3 = mul2(bc(3.f), fma2(ex, bc(nx), fma2(ey, bc(ny), mul2(ez, bc(nz)))));
-                        TX = fma2(s, fma2(h3, ex, mul2(e2s, bc(-nx))), TX);
-                        TY = fma2(s, fma2(h3, ey, mul2(e2s, bc(-ny))), TY);
-                        TZ = fma2(s, fma2(h3, ez, mul2(e2s, bc(-nz))), TZ);
-                    }
-                    if (any_near) {  // vortex ring (panel.rs:99-118)
-                        // float-float difference: (x_hi - c_hi) + (x_lo - c_lo)
-                        ex = add2(ex, sub2s(X2l, v[32]));
-                        ey = add2(ey, sub2s(Y2l, v[33]));
-                        ez = add2(ez, sub2s(Z2l, v[34]));
-                        float2 ax, ay, az;
-                        ring2(v, ex, ey, ez, ax, ay, az);
-                        const float g4 = gam * static_cast<float>(kFourPiInv);
-                        const float2 gm = make_float2((a0 && n0) ? g4 : 0.f, (a1 && n1) ? g4 : 0.f);
-                        TX = fma2(gm, ax, TX);
-                        TY = fma2(gm, ay, TY);
-                        TZ = fma2(gm, az, TZ);
-                    }
-                }
-                const float txa[2] = {TX.x, TX.y}, tya[2] = {TY.x, TY.y}, tza[2] = {TZ.x, TZ.y};
-#pragma unroll
-                for (int t = 0; t < 2; ++t) {
-                    if (KAHAN) {
-                        two_sum_acc(sx[t], cx[t], static_cast<R>(txa[t]));
-                        two_sum_acc(sy[t], cy[t], static_cast<R>(tya[t]));
-                        two_sum_acc(sz[t], cz[t], static_cast<R>(tza[t]));
-                    } else {
-                        sx[t] += static_cast<R>(txa[t]);
-                        sy[t] += static_cast<R>(tya[t]);
-                        sz[t] += static_cast<R>(tza[t]);
-                    }
-                }
-            } else {
-                R tx[TT], ty[TT], tz[TT];
-#pragma unroll
-                for (int t = 0; t < TT; ++t) tx[t] = ty[t] = tz[t] = R(0);
-                for (int p = 0; p < np; ++p) {
-                    const double* v = reinterpret_cast<const double*>(tile[buf][p].v);
-                    const double gam = v[kRec64Gamma];
-                    if (gam == 0.0) continue;
-                    const int pw = NEGLECT ? static_cast<int>(v[26]) : 0;
-#pragma unroll
+    #pragma unroll
                     for (int t = 0; t < TT; ++t) {
-                        if (!valid[t] || (NEGLECT && tw[t] == pw)) continue;
-                        d3 u = panel_unit_f64(v, mk(xh[t], yh[t], zh[t]));
-                        tx[t] += gam * u.x;
-                        ty[t] += gam * u.y;
-                        tz[t] += gam * u.z;
+                        sx[t] += tx[t];
+                        sy[t] += ty[t];
+                        sz[t] += tz[t];
                     }
-                }
-#pragma unroll
-                for (int t = 0; t < TT; ++t) {
-                    sx[t] += tx[t];
-                    sy[t] += ty[t];
-                    sz[t] += tz[t];
                 }
             }
             // The buffer is refilled in the next-but-one tile. A wait of tile k that ran out in
