@@ -483,7 +483,7 @@ def batched_solves(args, device):
     def worst(a, ref):
         return max(float(np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1e-300)) for x, y in zip(a, ref))
 
-    arms = ("batched", "extrapolation", *warm_arms)
+    arms = ("batched", "extrapolation", "warm")
     solves = n * steps
     out["solves_per_s"] = {m: solves / results[m]["seconds"] for m in ("plain",) + arms}
     out["speedup_vs_plain"] = {m: results["plain"]["seconds"] / results[m]["seconds"] for m in arms}
