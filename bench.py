@@ -356,7 +356,7 @@ def run_gb300(args):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "fp32 sweeps (compensated, float-float positions) / fp64 solve+positions",
+        "vs_baseline": None, "dtype": "fp32 sweeps (fp32 within a 64-panel tile, two-sum fold across tiles; float-float positions) / fp64 solve+positions",
         "data": "synthetic (seeded gusty wind, reference JSON setup)",
         "config": workload_config({"parallelism": f"{ws} independent replica(s), one per GPU"}),
         "roofline": {"kernel": "k_bs_sweep (wake roll-up)", "bound": "fp32", "achieved": achieved, "peak": peak,
@@ -474,11 +474,31 @@ def batched_solves(args, device):
 
     ex_net = WS.extrapolation_only(device)
     for mode, mnet in (("batched", None), ("extrapolation", ex_net), ("warm", net)):
-        r = WS.run_batch(cases, warm + steps, mnet, DT, device, timed_from=warm, tune_seconds=args.tune_seconds)
+        r = WS.run_batch(cases, warm + steps, mnet, DT, device, timed_from=warm, tune_seconds=args.tune_seconds,
+                         state_before_last=True)
         results[mode] = {"seconds": r["seconds"], "gamma": r["gamma"][-1],
                          "iterations": float(np.mean(r["iterations"][warm:])), "start": r["start"][warm:],
-                         "tune_seconds": r["tune_seconds"], "tuning": r["tuning"]}
+                         "tune_seconds": r["tune_seconds"], "tuning": r["tuning"], "states": r["states_before_last"]}
     ex_net.close()
+
+    # Each arm's last solve against the plain single-case solve from the same state (the arm's
+    # own state before that step): the start's effect on one solve. The arms' trajectories from
+    # the cold start are compared too (below), where a sensitive case grows any difference of
+    # earlier steps (by up to about ten times a step).
+    k_last = warm + steps - 1
+    same_state = {}
+    for mode in ("batched", "extrapolation", "warm"):
+        worst_same = 0.0
+        for i, (js, w) in enumerate(cases):
+            sim = Simulation(js, device=device)
+            sim.set_state(results[mode]["states"][i])
+            rr = sim.do_step(time=k_last * DT, time_step=DT,
+                             freestream_velocity=w.freestream(k_last * DT, sim.nr_freestream_points))
+            y = rr.circulation_strength
+            worst_same = max(worst_same, float(np.max(np.abs(results[mode]["gamma"][i] - y)) / max(np.max(np.abs(y)), 1e-300)))
+            sim.close()
+        same_state[mode] = worst_same
+        del results[mode]["states"]
 
     def worst(a, ref):
         return max(float(np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1e-300)) for x, y in zip(a, ref))
@@ -493,6 +513,10 @@ def batched_solves(args, device):
                                        "network": float(np.mean(results[m]["start"] == 2.0))}
                                    for m in ("extrapolation", "warm")}
     out["max_rel_circulation_diff_vs_plain"] = {m: worst(results[m]["gamma"], results["plain"]["gamma"]) for m in arms}
+    out["max_rel_circulation_diff_vs_plain_same_state"] = same_state
+    out["circulation_diff_how"] = ("max_rel_circulation_diff_vs_plain: each arm's last timed step against the plain "
+                                   "arm's, every arm on its own trajectory from the cold start; _same_state: each arm's "
+                                   "last solve against a plain single-case solve from that arm's own state before the step")
     out["arms"] = {"plain": "one Simulation per case, sb_sim_do_step each (previous-step start)",
                    "batched": "one Batch, graph replay, previous-step start",
                    "extrapolation": "batched, candidate = linear extrapolation in time (network output zero)",

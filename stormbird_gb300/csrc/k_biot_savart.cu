@@ -142,8 +142,10 @@ __device__ __forceinline__ void corner2(float2 ex, float2 ey, float2 ez, const f
     ry = sub2s(ey, o[1]);
     rz = sub2s(ez, o[2]);
     rs = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
-    // r = 0 (target on a corner) gives l = 0; the clamp runs on the ALU pipe
-    rl = mul2(rs, make_float2(rsqrt_n(fmaxf(rs.x, 1e-30f)), rsqrt_n(fmaxf(rs.y, 1e-30f))));
+    // r = 0 (target on a corner) gives l = 0: the floor is one packed add on the FMA pipe
+    // (the same value as a maximum wherever |r|^2 > 4e-23, where 1e-30 is below its rounding)
+    const float2 rsf = add2(rs, bc(1e-30f));
+    rl = mul2(rs, make_float2(rsqrt_n(rsf.x), rsqrt_n(rsf.y)));
 }
 
 // One segment from corner 1 (r1) to corner 2 (r2 = r1 - d): s * c with c = d x r1, i.e.
@@ -173,11 +175,11 @@ __device__ __forceinline__ void segment2(float2 rx, float2 ry, float2 rz, float2
     d2.x = tp.x < 0.f ? rs1.x : d2.x;
     d2.y = tp.y < 0.f ? rs1.y : d2.y;
     // X = 0 only where B = 0 too (target on the segment or a corner); the select below
-    // then discards the lane, so the clamp only keeps rsqrt finite
-    const float2 X = mul2(mul2(Bx, Bx), fma2(d2, d2, bc(rc4)));
+    // then discards the lane, so the floor (a packed add) only keeps rsqrt finite
+    const float2 X = add2(mul2(mul2(Bx, Bx), fma2(d2, d2, bc(rc4))), bc(1e-37f));
     const float2 Aw = WEIGHTED ? mul2(Ax, bc(g)) : Ax;
     const float2 s0 = mul2(mul2(mul2(d2, add2(rl1, rl2)), Aw),
-                           make_float2(rsqrt_n(fmaxf(X.x, 1e-37f)), rsqrt_n(fmaxf(X.y, 1e-37f))));
+                           make_float2(rsqrt_n(X.x), rsqrt_n(X.y)));
     const float2 lim = mul2(Ax, bc(1.0e-10f));
     const float2 sg = make_float2(Bx.x > lim.x ? s0.x : 0.f, Bx.y > lim.y ? s0.y : 0.f);
     ax = fma2(sg, cx, ax);
@@ -456,9 +458,9 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
                             c7[5] = fmaxf(c7[5], c.z);
                             c7[6] = fmaxf(c7[6], c.w);
                         }
-    #pragma unroll
+#pragma unroll
                         for (int o = 16; o > 0; o >>= 1)
-    #pragma unroll
+#pragma unroll
                             for (int q = 0; q < 7; ++q) {
                                 const float w = __shfl_xor_sync(0xffffffffu, c7[q], o);
                                 c7[q] = q < 3 ? fminf(c7[q], w) : fmaxf(c7[q], w);
@@ -477,17 +479,19 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
                     }
                     if (all_far) {
                         // lanes of targets past the end compute values that are never stored; four
-                        // panels per trip give the scheduler independent chains to interleave
-    #pragma unroll 4
+                        // panels per trip give the scheduler independent chains to interleave. A
+                        // zero-strength panel is not skipped here: every pair is far (|e|^2 > 0),
+                        // so it adds exactly 0 (the sums are the same), and the trip has no branch
+#pragma unroll 4
                         for (int p = 0; p < np; ++p) {
                             const float* v = reinterpret_cast<const float*>(tile[buf][p].v);
                             const float gam = v[kRec32Gamma];
-                            if (gam == 0.f) continue;  // uniform across the CTA
                             const float2 ex = sub2s(X2h, v[28]);
                             const float2 ey = sub2s(Y2h, v[29]);
                             const float2 ez = sub2s(Z2h, v[30]);
                             const float2 e2s = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
-                            const float2 ir = make_float2(rsqrt_n(fmaxf(e2s.x, FLT_MIN)), rsqrt_n(fmaxf(e2s.y, FLT_MIN)));
+                            const float2 e2f = add2(e2s, bc(FLT_MIN));
+                            const float2 ir = make_float2(rsqrt_n(e2f.x), rsqrt_n(e2f.y));
                             const float2 ir2 = mul2(ir, ir);
                             const float2 sd = mul2(bc(v[35] * gam), mul2(mul2(ir2, ir2), ir));
                             const float nx = v[36], ny = v[37], nz = v[38];
@@ -536,7 +540,8 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
                         if (any_far) {  // point doublet (panel.rs:82-96), the fast path's arithmetic
                             const float2 e2s = make_float2(n0 ? 1.f : e2.x, n1 ? 1.f : e2.y);
                             // a subnormal |e|^2 (a degenerate panel) overflows s to inf either way
-                            const float2 ir = make_float2(rsqrt_n(fmaxf(e2s.x, FLT_MIN)), rsqrt_n(fmaxf(e2s.y, FLT_MIN)));
+                            const float2 e2f = add2(e2s, bc(FLT_MIN));
+                            const float2 ir = make_float2(rsqrt_n(e2f.x), rsqrt_n(e2f.y));
                             const float2 ir2 = mul2(ir, ir);
                             const float at = v[35] * gam;
                             const float2 sm = make_float2((a0 && !n0) ? at : 0.f, (a1 && !n1) ? at : 0.f);
@@ -562,7 +567,7 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
                         }
                     }
                     const float txa[2] = {TX.x, TX.y}, tya[2] = {TY.x, TY.y}, tza[2] = {TZ.x, TZ.y};
-    #pragma unroll
+#pragma unroll
                     for (int t = 0; t < 2; ++t) {
                         if (KAHAN) {
                             two_sum_acc(sx[t], cx[t], static_cast<R>(txa[t]));
@@ -576,14 +581,14 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
                     }
                 } else {
                     R tx[TT], ty[TT], tz[TT];
-    #pragma unroll
+#pragma unroll
                     for (int t = 0; t < TT; ++t) tx[t] = ty[t] = tz[t] = R(0);
                     for (int p = 0; p < np; ++p) {
                         const double* v = reinterpret_cast<const double*>(tile[buf][p].v);
                         const double gam = v[kRec64Gamma];
                         if (gam == 0.0) continue;
                         const int pw = NEGLECT ? static_cast<int>(v[26]) : 0;
-    #pragma unroll
+#pragma unroll
                         for (int t = 0; t < TT; ++t) {
                             if (!valid[t] || (NEGLECT && tw[t] == pw)) continue;
                             d3 u = panel_unit_f64(v, mk(xh[t], yh[t], zh[t]));
@@ -592,7 +597,7 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
                             tz[t] += gam * u.z;
                         }
                     }
-    #pragma unroll
+#pragma unroll
                     for (int t = 0; t < TT; ++t) {
                         sx[t] += tx[t];
                         sy[t] += ty[t];
@@ -786,7 +791,8 @@ __device__ __forceinline__ void panel_unit2(const float* v, float2 X2h, float2 Y
     ux = uy = uz = bc(0.f);
     if (!n0 || !n1) {  // point doublet (panel.rs:82-96), unit strength
         const float2 e2s = make_float2(n0 ? 1.f : e2.x, n1 ? 1.f : e2.y);
-        const float2 ir = make_float2(rsqrt_n(fmaxf(e2s.x, FLT_MIN)), rsqrt_n(fmaxf(e2s.y, FLT_MIN)));
+        const float2 e2f = add2(e2s, bc(FLT_MIN));
+        const float2 ir = make_float2(rsqrt_n(e2f.x), rsqrt_n(e2f.y));
         const float2 ir2 = mul2(ir, ir);
         const float2 sm = make_float2(n0 ? 0.f : v[35], n1 ? 0.f : v[35]);
         const float2 sd = mul2(sm, mul2(mul2(ir2, ir2), ir));

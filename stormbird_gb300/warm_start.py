@@ -185,13 +185,14 @@ def extrapolation_only(device: int = 0) -> WarmStartNet:
 
 
 def run_batch(cases, steps: int, net: WarmStartNet | None = None, dt: float = 0.05, device: int = 0,
-              timed_from: int = 1, tune_seconds: float = 0.0) -> dict:
+              timed_from: int = 1, tune_seconds: float = 0.0, state_before_last: bool = False) -> dict:
     """Steps the cases as one batch (warm-started when `net` is given) on their freestream.
 
     Returns per step the circulation, iterations and start taken of every case, the host
     time of steps timed_from.. (one solve = one case advanced by one step) and, with
     tune_seconds > 0, the time the autotuner took before step timed_from (untimed; it
-    needs 4 steps of wake, so timed_from >= 4).
+    needs 4 steps of wake, so timed_from >= 4). With state_before_last, also every case's
+    state before the last step (sb_batch_get_case_state, outside the timed calls).
     """
     import time
 
@@ -199,8 +200,10 @@ def run_batch(cases, steps: int, net: WarmStartNet | None = None, dt: float = 0.
     b = Batch([js for js, _ in cases], device=device)
     if net is not None:
         b.set_warm_start(net.handle)
-    its, taken, gam, t_run, t_tune = [], [], [], 0.0, 0.0
+    its, taken, gam, t_run, t_tune, states = [], [], [], 0.0, 0.0, None
     for k in range(steps):
+        if state_before_last and k == steps - 1:
+            states = [b.case_state(i) for i in range(b.n_cases)]
         if tune_seconds > 0.0 and k == timed_from and k >= 4:
             t0 = time.perf_counter()
             b.autotune(tune_seconds)
@@ -218,7 +221,8 @@ def run_batch(cases, steps: int, net: WarmStartNet | None = None, dt: float = 0.
     info = b.info()
     b.close()
     return {"iterations": np.array(its), "start": np.array(taken), "gamma": gam, "seconds": t_run,
-            "tune_seconds": t_tune, "tuning": {k: info[k] for k in ("waves", "blocks_per_sm", "tile", "schedule", "tuned")}}
+            "tune_seconds": t_tune, "tuning": {k: info[k] for k in ("waves", "blocks_per_sm", "tile", "schedule", "tuned")},
+            "states_before_last": states}
 
 
 def max_rel_diff(a, ref) -> float:
