@@ -480,12 +480,13 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
                     if (all_far) {
                         // lanes of targets past the end compute values that are never stored; four
                         // panels per trip give the scheduler independent chains to interleave. A
-                        // zero-strength panel is not skipped here: every pair is far (|e|^2 > 0),
-                        // so it adds exactly 0 (the sums are the same), and the trip has no branch
+                        // zero-strength panel must be skipped: only its strength slot is written
+                        // (its other fields may hold anything, and 0 times NaN is NaN)
 #pragma unroll 4
                         for (int p = 0; p < np; ++p) {
                             const float* v = reinterpret_cast<const float*>(tile[buf][p].v);
                             const float gam = v[kRec32Gamma];
+                            if (gam == 0.f) continue;  // uniform across the CTA
                             const float2 ex = sub2s(X2h, v[28]);
                             const float2 ey = sub2s(Y2h, v[29]);
                             const float2 ez = sub2s(Z2h, v[30]);
