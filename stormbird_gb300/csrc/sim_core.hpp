@@ -1034,6 +1034,14 @@ struct sb_sim {
         ck(cudaMemcpyAsync(h_out.p, out.p, L.total * sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H output");
         ck(cudaMemcpyAsync(h_err.p, err.p, sizeof(int), cudaMemcpyDeviceToHost, stream), "D2H status");
         ck(cudaStreamSynchronize(stream), "step");
+        collect_timing();
+        check_device_status();
+        if (writer) writer->push(result_record());
+        if (dynamic && setup.dynamic_wake.write_wake_data_to_file) push_wake_file();
+    }
+
+    // Phase and kernel times of the step just synchronised (sb_sim_enable_timing).
+    void collect_timing() {
         if (timing) {
             float ms = 0.f;
             cudaEventElapsedTime(&ms, ev[0], ev[7]); last_ms[0] = ms;
@@ -1052,9 +1060,6 @@ struct sb_sim {
             }
             if (chains_built) { cudaEventElapsedTime(&ms, ev[13], ev[14]); last_ms[11] = ms; }
         }
-        check_device_status();
-        if (writer) writer->push(result_record());
-        if (dynamic && setup.dynamic_wake.write_wake_data_to_file) push_wake_file();
     }
 
     // The wake after the step as a VTK file `{wake_files_folder_path}/wake_{time / dt}.vtp`
@@ -1168,6 +1173,7 @@ struct sb_sim {
         enqueue_step(time, dt);
         ck(cudaMemcpyAsync(h_err.p, err.p, sizeof(int), cudaMemcpyDeviceToHost, stream), "D2H status");
         ck(cudaStreamSynchronize(stream), "step");
+        collect_timing();
         check_device_status();
     }
 
