@@ -437,21 +437,10 @@ def batched_solves(args, device):
                        f"steps {warm}-{warm + steps - 1} from a cold start",
            "cases": n, "timed_steps": steps}
 
-    # train the network on other seeds
-    t0 = time.perf_counter()
-    X, T = WS.collect([(WS.tight_solver(js, residual_tolerance=tol), w)
-                       for js, w in S.uneven_cases(args.train_cases, seed=77)],
-                      steps=warm + steps, device=device)
-    t_collect = time.perf_counter() - t0
-    net = WS.WarmStartNet(WS.FEATURES, seed=1, device=device)
-    t0 = time.perf_counter()
-    losses = WS.train(net, X, T, epochs=args.train_epochs, batch_rows=4096)
-    torch.cuda.synchronize()
-    out["training"] = {"rows": int(X.shape[0]), "cases": args.train_cases, "epochs": args.train_epochs,
-                       "collect_s": t_collect, "train_s": time.perf_counter() - t0,
-                       "loss_first_epoch": losses[0] if losses else None,
-                       "loss_last_epoch": losses[-1] if losses else None}
-    del X, T
+    # config 4: the network trained on converged solves of other seeds (2,048 cases x 100
+    # recorded steps = 204,800 solves by default, wakes filling to 100 rows)
+    net, rep = config4_training(args.train_cases, args.train_steps, args.train_epochs, tol, device)
+    out["training"] = rep
 
     results = {}
     # plain: one simulation per case
@@ -524,39 +513,41 @@ def batched_solves(args, device):
                            "the solve starts from the lowest-residual of plain / extrapolation / network"}
     out["autotune"] = {m: {"seconds": results[m]["tune_seconds"], **results[m]["tuning"]} for m in arms}
     out["timing"] = "host clock around each public call, host freestream in, circulation and force summary out"
+    if args.filled_cases > 0:  # config 3 with every wake full, on the first cases of the same seed
+        out["filled"] = batched_filled(args, device, net, args.filled_cases, [0.5], oracle_cases=2)
+    net.close()
     return out
 
 
-def run_warm_start_training(args):
-    """Config 4's training set and training: the `--batch-cases` uneven cases of seed 77 (the
-    distribution of the evaluated cases, other seeds) stepped as one Batch for `--fill-steps`
-    steps with the warm-start data recorded (sb_batch_set_warm_start mode 2): features and the
-    correction beyond the extrapolation of every converged solve from step 2 on, across every
-    fill level of the wakes. The network (16 -> 4 x 256 GELU -> 1, BF16 tensor-core GEMMs) is
-    trained on it by the library's own kernels, 2 % of the rows held back for a validation
-    loss. Writes the parameters to `--save-net` (numpy .npy) and prints one JSON line."""
+def config4_training(n, steps, epochs, tol, device):
+    """Config 4's training set and training: `n` uneven cases of seed 77 (the distribution of
+    the evaluated cases, other seeds) stepped as one Batch for `steps` steps with the
+    warm-start data recorded (sb_batch_set_warm_start mode 2): features and the correction
+    beyond the extrapolation of every converged solve from step 2 on, over the fill levels
+    the steps reach. The network (16 -> 4 x 256 GELU -> 1, BF16 tensor-core GEMMs) is trained
+    on it by the library's own kernels, 2 % of the rows held back for a validation loss.
+    Returns (network, report)."""
     import torch
 
     from stormbird_gb300 import setups as S
     from stormbird_gb300 import warm_start as WS
 
-    n, steps, tol = args.batch_cases, args.fill_steps, args.batch_tolerance
     cases = [(WS.tight_solver(js, residual_tolerance=tol), w) for js, w in S.uneven_cases(n, seed=77)]
     t0 = time.perf_counter()
-    X, T = WS.collect(cases, steps=steps, device=0)
+    X, T = WS.collect(cases, steps=steps, device=device)
     t_collect = time.perf_counter() - t0
     print(f"collected {X.shape[0]} rows in {t_collect:.0f} s", file=sys.stderr, flush=True)
-    solves = n * (steps - 2)
     g = torch.Generator(device=X.device)
     g.manual_seed(5)
     perm = torch.randperm(X.shape[0], device=X.device, generator=g)
     n_val = X.shape[0] // 50
     Xv, Tv = X[perm[:n_val]].contiguous(), T[perm[:n_val]].contiguous()
     Xt, Tt = X[perm[n_val:]].contiguous(), T[perm[n_val:]].contiguous()
+    rows = int(X.shape[0])
     del X, T, perm
-    net = WS.WarmStartNet(WS.FEATURES, seed=1, device=0)
+    net = WS.WarmStartNet(WS.FEATURES, seed=1, device=device)
     t0 = time.perf_counter()
-    losses = WS.train(net, Xt, Tt, epochs=args.big_train_epochs, batch_rows=16384, lr=5e-4, loss_every=16)
+    losses = WS.train(net, Xt, Tt, epochs=epochs, batch_rows=16384, lr=5e-4, loss_every=16)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     val = []
@@ -564,15 +555,23 @@ def run_warm_start_training(args):
         _, lv = net.gradients(Xv[s0:s0 + 262144], Tv[s0:s0 + 262144])
         val.append(lv)
     zero = float(torch.mean(Tv.double() ** 2))
+    del Xt, Tt, Xv, Tv
+    torch.cuda.empty_cache()
+    return net, {"cases": n, "seed": 77, "steps": steps, "solves": n * (steps - 2), "rows": rows,
+                 "validation_rows": n_val, "collect_s": t_collect, "train_s": t_train, "epochs": len(losses),
+                 "loss_per_epoch": losses, "validation_loss": float(np.mean(val)),
+                 "validation_loss_of_zero_correction": zero,
+                 "targets": "correction beyond the linear extrapolation, -Gamma/(c|U|/2) units, clipped to +-0.25"}
+
+
+def run_warm_start_training(args):
+    """Config 4 at full fill: `--batch-cases` cases for `--fill-steps` steps (every wake fills;
+    512 x 402 = 204,800 solves), `--big-train-epochs` epochs (config4_training). Writes the
+    parameters to `--save-net` (numpy .npy) and prints one JSON line."""
+    net, rep = config4_training(args.batch_cases, args.fill_steps, args.big_train_epochs, args.batch_tolerance, 0)
     if args.save_net:
         np.save(args.save_net, net.get_params())
-    print(json.dumps({"mode": "warm-start-training", "cases": n, "seed": 77, "steps": steps,
-                      "solves": solves, "rows": int(Xt.shape[0] + Xv.shape[0]), "validation_rows": int(Xv.shape[0]),
-                      "collect_s": t_collect, "train_s": t_train, "epochs": len(losses),
-                      "loss_per_epoch": losses, "validation_loss": float(np.mean(val)),
-                      "validation_loss_of_zero_correction": zero,
-                      "targets": "correction beyond the linear extrapolation, -Gamma/(c|U|/2) units, clipped to +-0.25",
-                      "saved": args.save_net}), flush=True)
+    print(json.dumps({"mode": "warm-start-training", **rep, "saved": args.save_net}), flush=True)
 
 
 def run_filled(args):
@@ -583,11 +582,12 @@ def run_filled(args):
     net = WS.WarmStartNet(WS.FEATURES, seed=1, device=0)
     if args.load_net:
         net.set_params(np.load(args.load_net))
+    guards = [float(g) for g in args.warm_guards.split(",")]
     print(json.dumps({"mode": "batched-filled", "network": args.load_net or "untrained",
-                      **batched_filled(args, 0, net)}), flush=True)
+                      **batched_filled(args, 0, net, args.batch_cases, guards)}), flush=True)
 
 
-def batched_filled(args, device, net):
+def batched_filled(args, device, net, n, guards, oracle_cases=4):
     """Solves/s of the uneven cases with every wake full (config 3 as specified: wake lengths
     50-400 rows), all arms from one identical filled state.
 
@@ -607,7 +607,7 @@ def batched_filled(args, device, net):
     from stormbird_gb300 import setups as S
     from stormbird_gb300 import warm_start as WS
 
-    n, fill, pre, steps, tol = args.batch_cases, args.fill_steps, 2, args.batch_steps, args.batch_tolerance
+    fill, pre, steps, tol = args.fill_steps, 2, args.batch_steps, args.batch_tolerance
     cases = [(WS.tight_solver(js, residual_tolerance=tol), w) for js, w in S.uneven_cases(n, seed=2024)]
     jsons, winds = [js for js, _ in cases], [w for _, w in cases]
     src = Batch(jsons, device=device)
@@ -666,7 +666,6 @@ def batched_filled(args, device, net):
     res["batched"] = run_arm(src, None)
     src.close()
     ex_net = WS.extrapolation_only(device)
-    guards = [float(g) for g in args.warm_guards.split(",")]
     warm_arms = ["warm" if g == 0.5 else f"warm_guard_{g:g}" for g in guards]
     for mode, mnet, guard in [("extrapolation", ex_net, 0.5)] + [(a, net, g) for a, g in zip(warm_arms, guards)]:
         b = Batch(jsons, device=device)
@@ -679,7 +678,7 @@ def batched_filled(args, device, net):
 
     # the oracle from the same filled state, for sampled cases whose roll-up it sweeps in about a second
     sizes = sorted((S.setup_rollup_pairs(js), i) for i, js in enumerate(jsons))
-    sample = [i for p, i in sizes if p <= 2e9][-4:]
+    sample = [i for p, i in sizes if p <= 2e9][-oracle_cases:]
     oracle_err = {m: 0.0 for m in res}
     t1 = time.perf_counter()
     for i in sample:
@@ -1226,8 +1225,12 @@ def main():
                     help="autotuner budget of each batched arm before its timed steps (0: default plan)")
     ap.add_argument("--batch-tolerance", type=float, default=1e-8,
                     help="SimpleIterative mean-residual tolerance of the batched part's cases")
-    ap.add_argument("--train-cases", type=int, default=128, help="cases whose solves train the warm-start network")
-    ap.add_argument("--train-epochs", type=int, default=40)
+    ap.add_argument("--train-cases", type=int, default=2048, help="cases whose solves train the warm-start network")
+    ap.add_argument("--train-steps", type=int, default=102,
+                    help="steps of the training batch (solves recorded from step 2 on: 2048 x 100 = 204,800)")
+    ap.add_argument("--train-epochs", type=int, default=6)
+    ap.add_argument("--filled-cases", type=int, default=64,
+                    help="cases of the filled-wake part of the default run (0: skip; --filled runs all 512)")
     ap.add_argument("--qs-cases", type=int, default=512, help="cases of the quasi-steady sweep part (0: skip)")
     ap.add_argument("--qs-only", action="store_true", help="only the quasi-steady sweep part")
     args = ap.parse_args()
