@@ -383,13 +383,16 @@ def run_gb300(args):
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cb, _ = cpu_baseline_sweep(pts, strengths)
         line["cpu_baseline"] = cb
-    if args.batch_cases > 0:
+    # the configs beyond the headline (batched uneven cases with the learned warm start,
+    # quasi-steady sweeps, the precision study) in single-GPU runs: a scaling run holds its
+    # GPUs for the headline alone
+    if ws == 1 and args.batch_cases > 0:
         del sim
         torch.cuda.empty_cache()
         line["batched"] = batched_solves(args, local)
-    if args.qs_cases > 0:
+    if ws == 1 and args.qs_cases > 0:
         line["qs_sweep"] = qs_sweep(args, local)
-    if rank == 0 and not args.no_precision_study:
+    if ws == 1 and not args.no_precision_study:
         line["precision_study"] = precision_study()
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -315,3 +315,26 @@ def test_near_far_decision_at_the_threshold_is_the_f64_one(gpu_lib, oracle_mod, 
     ug = panel_sweep(corners.reshape(1, 12), [1.0], [core], targets, far_field_ratio=5.0, precision=precision)
     err = np.linalg.norm(ug - uo, axis=1) / scale
     assert err.max() < 1e-4, f"worst target {np.argmax(err)}: {err.max():.2e} (side gap {side_gap.min():.1e})"
+
+
+def test_step_timing_on_both_step_paths(gpu_lib):
+    """sb_sim_enable_timing: phase and kernel times after a step with the freestream in host
+    memory and after one with it in device memory (both paths read the step's events)."""
+    torch = pytest.importorskip("torch")
+    dt = 0.05
+    sim = Simulation(S.wing_sail_row(2, 8, 12, time_step=dt))
+    wind = S.GustyWind(seed=1)
+    n = sim.nr_freestream_points
+    for k in range(4):
+        sim.do_step(time=k * dt, time_step=dt, freestream_velocity=wind.freestream(k * dt, n))
+    sim.enable_timing(True)
+    sim.do_step(time=4 * dt, time_step=dt, freestream_velocity=wind.freestream(4 * dt, n))
+    t_host = sim.last_step_timing()
+    fs = torch.from_numpy(np.ascontiguousarray(wind.freestream(5 * dt, n))).cuda()
+    torch.cuda.synchronize()
+    sim.do_step_device(time=5 * dt, time_step=dt, freestream_device_ptr=fs.data_ptr())
+    t_dev = sim.last_step_timing()
+    for t in (t_host, t_dev):
+        for key in ("step", "solve", "wake_advect_kernel", "wake_panels_kernel", "rollup_sweep_kernel"):
+            assert t[key] > 0.0, (key, t)
+    sim.close()
