@@ -591,7 +591,8 @@ struct sb_batch {
                     // whether the matrix has lo parts off the diagonal, i.e. on the precision)
                     size_t smem = 0;
                     for (int ci : g.cases)
-                        smem = std::max(smem, si_smem_bytes(cases[ci]->N, cases[ci]->solve_buffers().split_full));
+                        smem = std::max(smem, si_smem_bytes(cases[ci]->N, cases[ci]->solve_buffers().split_full,
+                                                              cases[ci]->solve_buffers().split_comps));
                     ck(launch_solve_simple_iterative_jobs(d_si_jobs.p + g.off, static_cast<int>(g.cases.size()), g.cluster,
                                                           g.rows_per_thread, smem, n_launch > 1 ? pool[k++] : main),
                        "batched simple iterative solve");

@@ -732,26 +732,42 @@ __global__ void __launch_bounds__(kBsReduceThreads) k_bs_reduce_jobs(const BsJob
     J.out[i] = v;
 }
 
-// one matrix entry into the f64 and/or split matrix (row c, column j)
-__device__ inline void store_factor(d3* factors, float* split, int N, long long id, int c, int j, d3 u) {
+// one matrix entry into the f64 and/or split matrix (row c, column j). With a basis (two
+// components per entry, the influence matrix of the SimpleIterative solve) the entry is
+// projected on the in-plane basis of row c: in FP32 for an FP32-evaluated entry (fp32: its
+// components stay single floats, lo parts 0), else in f64.
+__device__ inline void store_factor(d3* factors, float* split, int N, const d3* basis, long long id, int c, int j, d3 u,
+                                    bool fp32 = false) {
     if (factors) factors[id] = u;
-    if (split) {  // hi plane [N][3][stride], then the lo plane
+    if (split) {  // hi plane [N][C][stride], then the lo plane
         const int S = si_matrix_stride(N);
-        float* r = split + static_cast<long long>(c) * 3 * S + j;
-        const long long lo = 3LL * N * S;
-        const float2 x = split_f64(u.x), y = split_f64(u.y), z = split_f64(u.z);
-        r[0] = x.x;
-        r[S] = y.x;
-        r[2 * S] = z.x;
-        r[lo] = x.y;
-        r[lo + S] = y.y;
-        r[lo + 2 * S] = z.y;
+        const int C = basis ? 2 : 3;
+        double comp[3] = {u.x, u.y, u.z};
+        if (basis) {
+            const d3 e1 = basis[2 * c], e2 = basis[2 * c + 1];
+            if (fp32) {
+                const float ux = static_cast<float>(u.x), uy = static_cast<float>(u.y), uz = static_cast<float>(u.z);
+                comp[0] = fmaf(ux, static_cast<float>(e1.x), fmaf(uy, static_cast<float>(e1.y), uz * static_cast<float>(e1.z)));
+                comp[1] = fmaf(ux, static_cast<float>(e2.x), fmaf(uy, static_cast<float>(e2.y), uz * static_cast<float>(e2.z)));
+            } else {
+                comp[0] = dot(u, e1);
+                comp[1] = dot(u, e2);
+            }
+        }
+        float* r = split + static_cast<long long>(c) * C * S + j;
+        const long long lo = static_cast<long long>(C) * N * S;
+        for (int q = 0; q < C; ++q) {
+            const float2 h = split_f64(comp[q]);
+            r[q * S] = h.x;
+            r[lo + q * S] = h.y;
+        }
     }
 }
 
 // frozen_wake.rs:198-249: factors[c][p] = unit velocity of first-row panel p at control point c
 __device__ inline void unit_matrix_elem(const PanelRec<double>* row0, const d3* ctrl, int N, int sym, int neglect,
-                                        const int* wing_of_line, d3* factors, float* split, long long id) {
+                                        const int* wing_of_line, d3* factors, float* split, const d3* basis,
+                                        long long id) {
     if (id >= static_cast<long long>(N) * N) return;
     int c = static_cast<int>(id / N), p = static_cast<int>(id % N);
     d3 u = mk(0, 0, 0);
@@ -760,12 +776,12 @@ __device__ inline void unit_matrix_elem(const PanelRec<double>* row0, const d3* 
         u = panel_unit_f64(row0[p].v, x);
         if (sym) u = sym_correct(sym, u, panel_unit_f64(row0[p].v, mirror(sym, x)));
     }
-    store_factor(factors, split, N, id, c, p, u);
+    store_factor(factors, split, N, basis, id, c, p, u);
 }
 
 __global__ void k_unit_matrix(const PanelRec<double>* row0, const d3* ctrl, int N, int sym, int neglect,
-                              const int* wing_of_line, d3* factors, float* split) {
-    unit_matrix_elem(row0, ctrl, N, sym, neglect, wing_of_line, factors, split,
+                              const int* wing_of_line, d3* factors, float* split, const d3* basis) {
+    unit_matrix_elem(row0, ctrl, N, sym, neglect, wing_of_line, factors, split, basis,
                      blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x);
 }
 
@@ -819,7 +835,7 @@ __device__ __forceinline__ void panel_unit2(const float* v, float2 X2h, float2 Y
 
 __device__ inline void unit_matrix_f32_elem(const PanelRec<float>* row0_32, const PanelRec<double>* row0, const d3* ctrl,
                                             int N, int sym, int neglect, const int* wing_of_line, d3* factors,
-                                            float* split, long long id) {
+                                            float* split, const d3* basis, long long id) {
     const int pairs = (N + 1) / 2;
     if (id >= static_cast<long long>(pairs) * N) return;
     const int cp = static_cast<int>(id / N), p = static_cast<int>(id % N);
@@ -859,20 +875,23 @@ __device__ inline void unit_matrix_f32_elem(const PanelRec<float>* row0_32, cons
         const int c = l == 0 ? c0 : c1;
         if (l == 1 && c1 == c0) break;
         d3 u = mk(uxa[l], uya[l], uza[l]);
+        bool fp32 = true;
         if (neglect && wing_of_line[c] == wing_of_line[p]) {
             u = mk(0, 0, 0);
         } else if (c == p) {
             const d3 x = ctrl[c];
             u = panel_unit_f64(row0[p].v, x);
             if (sym) u = sym_correct(sym, u, panel_unit_f64(row0[p].v, mirror(sym, x)));
+            fp32 = false;
         }
-        store_factor(factors, split, N, static_cast<long long>(c) * N + p, c, p, u);
+        store_factor(factors, split, N, basis, static_cast<long long>(c) * N + p, c, p, u, fp32);
     }
 }
 
 __global__ void k_unit_matrix_f32(const PanelRec<float>* row0_32, const PanelRec<double>* row0, const d3* ctrl, int N,
-                                  int sym, int neglect, const int* wing_of_line, d3* factors, float* split) {
-    unit_matrix_f32_elem(row0_32, row0, ctrl, N, sym, neglect, wing_of_line, factors, split,
+                                  int sym, int neglect, const int* wing_of_line, d3* factors, float* split,
+                                  const d3* basis) {
+    unit_matrix_f32_elem(row0_32, row0, ctrl, N, sym, neglect, wing_of_line, factors, split, basis,
                          blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x);
 }
 
@@ -892,9 +911,10 @@ __global__ void k_unit_matrix_jobs(const CaseStepJob* jobs, int n) {
     const DevModel& m = J.m;
     if (J.row0_32)
         unit_matrix_f32_elem(J.row0_32, J.w.row0_64, m.ctrl, m.N, m.symmetry, m.neglect_self, m.wing_of_line, J.factors,
-                             J.split, id);
+                             J.split, J.basis, id);
     else
-        unit_matrix_elem(J.w.row0_64, m.ctrl, m.N, m.symmetry, m.neglect_self, m.wing_of_line, J.factors, J.split, id);
+        unit_matrix_elem(J.w.row0_64, m.ctrl, m.N, m.symmetry, m.neglect_self, m.wing_of_line, J.factors, J.split,
+                         J.basis, id);
 }
 
 long long unit_matrix_blocks(int N, bool fp32) {
@@ -935,7 +955,7 @@ __global__ void __launch_bounds__(kQsPrepThreads) k_qs_prep(DevModel m, int core
 // factors[c][j] = unit velocity of horseshoe j (bound + start trailing + end trailing) at
 // control point c. Horseshoe j of wing w uses wake vectors j + w and j + w + 1.
 __global__ void k_horseshoe_matrix(DevModel m, const d3* wake_vec, const double* rc_dev, int sym, d3* factors,
-                                   float* split) {
+                                   float* split, const d3* basis) {
     long long id = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
     const int N = m.N;
     if (id >= static_cast<long long>(N) * N) return;
@@ -954,11 +974,12 @@ __global__ void k_horseshoe_matrix(DevModel m, const d3* wake_vec, const double*
     d3 x = m.ctrl[c];
     d3 u = hs(x);
     if (sym) u = sym_correct(sym, u, hs(mirror(sym, x)));
-    store_factor(factors, split, N, id, c, j, u);
+    store_factor(factors, split, N, basis, id, c, j, u);
 }
 
 cudaError_t launch_horseshoe_matrix(const DevModel& m, int core_kind, double core_value, double wake_length, d3* wake_vec,
-                                    double* rc_dev, int sym, d3* factors, float* split, cudaStream_t s) {
+                                    double* rc_dev, int sym, d3* factors, float* split, const d3* basis,
+                                    cudaStream_t s) {
     const size_t smem = static_cast<size_t>(m.N) * sizeof(double);
     if (smem > 48 * 1024) {
         cudaError_t a = cudaFuncSetAttribute(k_qs_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
@@ -968,7 +989,8 @@ cudaError_t launch_horseshoe_matrix(const DevModel& m, int core_kind, double cor
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     long long tot = static_cast<long long>(m.N) * m.N;
-    k_horseshoe_matrix<<<static_cast<unsigned>((tot + 127) / 128), 128, 0, s>>>(m, wake_vec, rc_dev, sym, factors, split);
+    k_horseshoe_matrix<<<static_cast<unsigned>((tot + 127) / 128), 128, 0, s>>>(m, wake_vec, rc_dev, sym, factors, split,
+                                                                               basis);
     return cudaGetLastError();
 }
 
@@ -1102,15 +1124,16 @@ cudaError_t launch_bs_reduce_jobs(const BsJob* jobs, int n_jobs, long long block
 }
 
 cudaError_t launch_unit_matrix(const PanelRec<double>* row0, const PanelRec<float>* row0_32, const d3* ctrl, int N,
-                               int sym, int neglect, const int* wing_of_line, d3* factors, float* split, cudaStream_t s) {
+                               int sym, int neglect, const int* wing_of_line, d3* factors, float* split, const d3* basis,
+                               cudaStream_t s) {
     const long long blocks = unit_matrix_blocks(N, row0_32 != nullptr);
     if (row0_32) {
         k_unit_matrix_f32<<<static_cast<unsigned>(blocks), kUnitMatrixThreads, 0, s>>>(row0_32, row0, ctrl, N, sym, neglect,
-                                                                                        wing_of_line, factors, split);
+                                                                                        wing_of_line, factors, split, basis);
         return cudaGetLastError();
     }
     k_unit_matrix<<<static_cast<unsigned>(blocks), kUnitMatrixThreads, 0, s>>>(row0, ctrl, N, sym, neglect, wing_of_line,
-                                                                                factors, split);
+                                                                                factors, split, basis);
     return cudaGetLastError();
 }
 

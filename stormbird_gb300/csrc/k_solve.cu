@@ -53,27 +53,28 @@ __host__ __device__ inline int si_cluster_size(int N) {
 int solve_cluster_size(int N) { return si_cluster_size(N); }
 
 // Matrix slab of a CTA (its rows of the split matrix) in shared memory. Bytes of one row:
-// 3 components x stride floats, twice with the lo plane. When all of the CTA's rows fit
+// 2 or 3 components (SolveBuffers::split_comps) x stride floats, twice with the lo plane. When all of the CTA's rows fit
 // kSlabBudget they are copied once per solve and stay; else chunks of 4 to 8 rows (a row per
 // warp) stream through two buffers of half the budget each, every iteration. 0: not even 4
 // rows fit a buffer (N above about 900): the warps read their rows from global memory.
 constexpr long long kSlabBudget = 88 * 1024;
-__host__ __device__ inline long long si_row_bytes(int N, int full) {
-    return 12LL * si_matrix_stride(N) * (full ? 2 : 1);
+__host__ __device__ inline long long si_row_bytes(int N, int full, int comps) {
+    return 4LL * comps * si_matrix_stride(N) * (full ? 2 : 1);
 }
 // Shared memory before the slab, in doubles: circulation pairs 2 x stride, residual terms
 // 2 x N, maxima 2 x kMaxCluster, the CTA's M * Gamma pairs (3 doubles per row), the own
-// panels' lo parts (2 doubles per row), rounded to 16 bytes.
+// panels' lo parts (2 doubles per row), the own rows' in-plane bases (6 doubles per row),
+// rounded to 16 bytes.
 __host__ __device__ inline long long si_slab_offset(int N) {
     const int CS = si_cluster_size(N);
     const long long rp = (N + CS - 1) / CS;
-    const long long d = 2LL * si_matrix_stride(N) + 2LL * N + 2 * kMaxCluster + 3 * rp + 2 * rp;
+    const long long d = 2LL * si_matrix_stride(N) + 2LL * N + 2 * kMaxCluster + 3 * rp + 2 * rp + 6 * rp;
     return (d + 1) & ~1LL;
 }
-__host__ __device__ inline int si_slab_rows(int N, int full) {
+__host__ __device__ inline int si_slab_rows(int N, int full, int comps) {
     const int CS = si_cluster_size(N);
     const int rp = (N + CS - 1) / CS;
-    const long long rowb = si_row_bytes(N, full);
+    const long long rowb = si_row_bytes(N, full, comps);
     // two CTAs of a cluster per SM: at most ~110 KB of shared memory each
     const long long rest = 110 * 1024 - si_slab_offset(N) * 8;
     const long long budget = rest < kSlabBudget ? rest : kSlabBudget;
@@ -187,6 +188,24 @@ __device__ __forceinline__ void ff_mac4(float& S, float& C, float4 a, float4 al,
     ff_mac(S, C, make_float2(a.z, al.z), make_float2(g23.x, g23.y));
     ff_mac(S, C, make_float2(a.w, al.w), make_float2(g23.z, g23.w));
 }
+
+// One lane's share of a row of the split matrix times the circulation: columns 4*lane + 128*t,
+// NC components (planes of S floats), hi plane fh and (full) lo plane fl.
+template <int NC>
+__device__ __forceinline__ void row_dot_lane(const float* fh, const float* fl, const float2* Gc, float (&acc)[6], int S,
+                                             int lane, int full) {
+#pragma unroll 2
+    for (int k = 4 * lane; k < S; k += 128) {
+        const float4 g01 = *reinterpret_cast<const float4*>(Gc + k);  // (hi, lo) of columns k, k + 1
+        const float4 g23 = *reinterpret_cast<const float4*>(Gc + k + 2);
+#pragma unroll
+        for (int q = 0; q < NC; ++q) {
+            const float4 a = *reinterpret_cast<const float4*>(fh + q * S + k);
+            const float4 al = full ? *reinterpret_cast<const float4*>(fl + q * S + k) : make_float4(0.f, 0.f, 0.f, 0.f);
+            ff_mac4(acc[2 * q], acc[2 * q + 1], a, al, g01, g23);
+        }
+    }
+}
 // (S, C) += (h, l), another double-float partial sum
 __device__ __forceinline__ void ff_add(float& S, float& C, float h, float l) {
     const float s = __fadd_rn(S, h);
@@ -251,6 +270,7 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
     const int rp_max = (N + CS - 1) / CS;
     // lo parts of the own panels' entries (x, y, z), when the matrix has none elsewhere
     float* diag_lo = reinterpret_cast<float*>(smem + 2 * S + 2 * N + 2 * kMaxCluster + 3 * rp_max);
+    d3* basis_sm = reinterpret_cast<d3*>(smem + 2 * S + 2 * N + 2 * kMaxCluster + 5 * rp_max);  // e1, e2 per own row
     float* slab = reinterpret_cast<float*>(smem + si_slab_offset(N));
     __shared__ double s_res;
     __shared__ unsigned long long s_umax[kSolveThreads / 32];
@@ -284,26 +304,30 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
     __syncthreads();
 
     const int full = b.split_full;
-    const int slab_rows = si_slab_rows(N, full);
+    const int C = b.split_comps;  // 2: in-plane components in the rows' bases, 3: x, y, z
+    const int slab_rows = si_slab_rows(N, full, C);
     const int nrows_cta = r1 - r0;
     const int nch = slab_rows > 0 ? (nrows_cta + slab_rows - 1) / slab_rows : 0;
     const bool resident = slab_rows > 0 && slab_rows >= rp_max;  // copied once, kept
-    const long long rowf = 3LL * S;                                // floats of a row, one plane
+    const long long rowf = static_cast<long long>(C) * S;         // floats of a row, one plane
     const long long buf_floats = static_cast<long long>(slab_rows) * rowf * (full ? 2 : 1);
-    const long long lo_plane = 3LL * N * S;
+    const long long lo_plane = static_cast<long long>(C) * N * S;
     if (tid == 0) {
         mbar_init(&s_mbar[0], 1);
         mbar_init(&s_mbar[1], 1);
         fence_mbar_init();
     }
-    if (!full)
-        for (int k = tid; k < nrows_cta; k += kSolveThreads) {
-            const long long row = r0 + k;
+    for (int k = tid; k < nrows_cta; k += kSolveThreads) {
+        const long long row = r0 + k;
+        if (!full) {
             const float* fl = b.factors_split + lo_plane + row * rowf;
-            diag_lo[3 * k] = fl[row];
-            diag_lo[3 * k + 1] = fl[S + row];
-            diag_lo[3 * k + 2] = fl[2 * S + row];
+            for (int q = 0; q < C; ++q) diag_lo[3 * k + q] = fl[q * S + row];
         }
+        if (C == 2) {
+            basis_sm[2 * k] = b.basis[2 * row];
+            basis_sm[2 * k + 1] = b.basis[2 * row + 1];
+        }
+    }
 
     // residual of the initial solution with zero velocity (simple_iterative.rs:180-184)
     double residual = 0.0;
@@ -344,31 +368,24 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
     };
     // (S, C) += row . Gc over the lane's columns, from fh (hi) and fl (lo, full only)
     auto row_dot = [&](const float* fh, const float* fl, const float2* Gc, float (&acc)[6]) {
-#pragma unroll 2
-        for (int k = 4 * lane; k < S; k += 128) {
-            const float4 g01 = *reinterpret_cast<const float4*>(Gc + k);  // (hi, lo) of columns k, k + 1
-            const float4 g23 = *reinterpret_cast<const float4*>(Gc + k + 2);
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                const float4 a = *reinterpret_cast<const float4*>(fh + q * S + k);
-                const float4 al = full ? *reinterpret_cast<const float4*>(fl + q * S + k) : make_float4(0.f, 0.f, 0.f, 0.f);
-                ff_mac4(acc[2 * q], acc[2 * q + 1], a, al, g01, g23);
-            }
-        }
+        if (C == 2) row_dot_lane<2>(fh, fl, Gc, acc, S, lane, full);
+        else row_dot_lane<3>(fh, fl, Gc, acc, S, lane, full);
     };
     auto finish_row = [&](int row, float (&acc)[6], const float2* Gc) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
             for (int q = 0; q < 3; ++q)
-                ff_add(acc[2 * q], acc[2 * q + 1], __shfl_down_sync(0xffffffffu, acc[2 * q], o),
-                       __shfl_down_sync(0xffffffffu, acc[2 * q + 1], o));
+                if (q < C)
+                    ff_add(acc[2 * q], acc[2 * q + 1], __shfl_down_sync(0xffffffffu, acc[2 * q], o),
+                           __shfl_down_sync(0xffffffffu, acc[2 * q + 1], o));
         if (lane == 0) {
             if (!full) {  // the own panel's entry is f64: its lo parts times Gamma hi
                 const float2 g = Gc[row];
                 const float* dl = diag_lo + 3 * (row - r0);
 #pragma unroll
-                for (int q = 0; q < 3; ++q) ff_mac(acc[2 * q], acc[2 * q + 1], make_float2(0.f, dl[q]), g);
+                for (int q = 0; q < 3; ++q)
+                    if (q < C) ff_mac(acc[2 * q], acc[2 * q + 1], make_float2(0.f, dl[q]), g);
             }
             float* o = uff + 6 * (row - r0);
 #pragma unroll
@@ -413,13 +430,25 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
         }
         slab_loaded = true;
     };
-    // induced velocity of own row i: fixed + M * Gamma
-    auto induced_of = [&](int i) {
+    // Velocity of own row i with its span component taken out (project(u, span_rel) before
+    // the angle): freestream + fixed + M * Gamma. With two components the products are already
+    // the in-plane coordinates along the row's basis (e1, e2), and the velocity correction is
+    // off (the only mode the two-component matrix is built for).
+    auto row_velocity = [&](int i, const RowGeom& g) {
         const float* o = uff + 6 * (i - r0);
         const d3 fx = b.fixed[i];
-        return mk(fx.x + (static_cast<double>(o[0]) + static_cast<double>(o[1])),
-                  fx.y + (static_cast<double>(o[2]) + static_cast<double>(o[3])),
-                  fx.z + (static_cast<double>(o[4]) + static_cast<double>(o[5])));
+        if (C == 2) {
+            const d3 e1 = basis_sm[2 * (i - r0)], e2 = basis_sm[2 * (i - r0) + 1];
+            const d3 base = g.felt + fx;
+            const double a = dot(base, e1) + (static_cast<double>(o[0]) + static_cast<double>(o[1]));
+            const double c = dot(base, e2) + (static_cast<double>(o[2]) + static_cast<double>(o[3]));
+            return e1 * a + e2 * c;
+        }
+        const d3 ind = mk(fx.x + (static_cast<double>(o[0]) + static_cast<double>(o[1])),
+                          fx.y + (static_cast<double>(o[2]) + static_cast<double>(o[3])),
+                          fx.z + (static_cast<double>(o[4]) + static_cast<double>(o[5])));
+        const d3 u = total_velocity(st, g.felt, ind);
+        return u - g.span_dir * dot(u, g.span_dir);
     };
 
     // Guarded warm start: residual (simple_iterative.rs:160-176) of the plain start G[0]
@@ -447,8 +476,7 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
                 int i = r0 + own_row(k);
                 const RowGeom& g = rg[k];
                 const FoilP f = m.foils[g.wing];
-                d3 u = total_velocity(st, g.felt, induced_of(i));
-                u = u - g.span_dir * dot(u, g.span_dir);  // project(u, span_rel)
+                const d3 u = row_velocity(i, g);
                 double aoa = len(u) > kMinPositive ? signed_angle_between(g.chord, u, g.span_dir) : 0.0;
                 double r = residual_term(m, g, f, v == 0 ? gown[k] : src[i], u, aoa);
                 for (int q = 0; q < CS; ++q) cl.map_shared_rank(RR[0], q)[i] = r;
@@ -503,8 +531,7 @@ __device__ void si_solve(const DevModel& m, const SolveSettings& st, const Solve
             int i = r0 + own_row(k);
             const RowGeom& g = rg[k];
             const FoilP f = m.foils[g.wing];
-            d3 u = total_velocity(st, g.felt, induced_of(i));
-            u = u - g.span_dir * dot(u, g.span_dir);  // project(u, span_rel)
+            const d3 u = row_velocity(i, g);
             const double ul = len(u);
             double aoa = ul > kMinPositive ? row_angle(g, u, ul) : 0.0;
             // the pre-stall lift coefficient serves the estimate and the residual alike
@@ -610,12 +637,12 @@ int si_rows_per_thread(int N) {
     return rp <= kSolveThreads ? 1 : kSolveRowsPerThread;
 }
 
-size_t si_smem_bytes(int N, int full) {
+size_t si_smem_bytes(int N, int full, int comps) {
     const int CS = si_cluster_size(N);
     const int rp = (N + CS - 1) / CS;
-    const int sr = si_slab_rows(N, full);
+    const int sr = si_slab_rows(N, full, comps);
     const long long bufs = sr == 0 ? 0 : (sr >= rp ? 1 : 2);
-    return static_cast<size_t>(si_slab_offset(N) * 8 + bufs * sr * si_row_bytes(N, full));
+    return static_cast<size_t>(si_slab_offset(N) * 8 + bufs * sr * si_row_bytes(N, full, comps));
 }
 
 cudaError_t launch_solve_simple_iterative_jobs(const SolveJob* jobs, int n, int cluster, int rows_per_thread,
@@ -647,7 +674,7 @@ cudaError_t launch_solve_simple_iterative(const DevModel& m, const SolveSettings
     const int CS = solve_cluster_size(m.N);
     const int rp = (m.N + CS - 1) / CS;
     if (rp > kSolveThreads * kSolveRowsPerThread) return cudaErrorInvalidValue;
-    size_t smem = si_smem_bytes(m.N, b.split_full);
+    size_t smem = si_smem_bytes(m.N, b.split_full, b.split_comps);
     auto kernel = si_rows_per_thread(m.N) == 1 ? k_solve_si<1> : k_solve_si<kSolveRowsPerThread>;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));

@@ -33,6 +33,7 @@ __device__ void prep_geometry_block(const DevModel& m, const StepParams& p, cons
         m.span_e[i] = e;
         d3 c = 0.5 * (s + e);
         m.ctrl[i] = c;
+        if (m.solve_basis) line_basis(m.chord_global[i], s, e, m.solve_basis[2 * i], m.solve_basis[2 * i + 1]);
         if (fs_ctrl) {
             // rigid_body_motion.rs:53-60
             d3 mv = p.velocity_linear + cross(p.velocity_angular, c - p.translation);

@@ -280,7 +280,25 @@ struct DevModel {
     d3* ctrl = nullptr;
     d3* felt_ctrl = nullptr;
     d3* felt_span = nullptr;
+    // [2N] per line, the plane perpendicular to its span: e1 = the chord made perpendicular
+    // to the span, unit; e2 = span direction x e1 (line_basis)
+    d3* solve_basis = nullptr;
 };
+
+// In-plane basis of a line (the plane perpendicular to its span direction): the solver only
+// uses the velocity's components in that plane (the span component is projected out before
+// the angle of attack), so its influence matrix can hold two components per entry. A chord
+// along the span (degenerate) takes the in-plane axis closest to x or y instead.
+__device__ inline void line_basis(d3 chord, d3 span_s, d3 span_e, d3& e1, d3& e2) {
+    const d3 sd = normalize(span_e - span_s);
+    d3 c = chord - sd * dot(chord, sd);
+    if (!(len2(c) > 1e-300)) {
+        c = mk(1, 0, 0) - sd * sd.x;
+        if (!(len2(c) > 1e-300)) c = mk(0, 1, 0) - sd * sd.y;
+    }
+    e1 = normalize(c);
+    e2 = cross(sd, e1);
+}
 
 struct StepParams {
     double time = 0.0, dt = 0.0;

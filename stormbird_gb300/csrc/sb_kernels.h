@@ -79,11 +79,15 @@ cudaError_t launch_bs_reduce_jobs(const BsJob* jobs, int n_jobs, long long block
 // the padding columns are left untouched). Either pointer may be null.
 // Frozen-wake unit matrix of the first wake row: from the FP32 row-0 records when row0_32 is
 // given (k_unit_matrix_f32; the control point's own panel in FP64), else all in FP64.
+// basis: the rows' in-plane bases (DevModel::solve_basis) for a two-component split matrix,
+// or nullptr for three components.
 cudaError_t launch_unit_matrix(const PanelRec<double>* row0, const PanelRec<float>* row0_32, const d3* ctrl, int N,
-                               int sym, int neglect, const int* wing_of_line, d3* factors, float* split, cudaStream_t s);
+                               int sym, int neglect, const int* wing_of_line, d3* factors, float* split, const d3* basis,
+                               cudaStream_t s);
 // Quasi-steady horseshoe matrix; core_kind 0 relative, 1 absolute, 2 none.
 cudaError_t launch_horseshoe_matrix(const DevModel& m, int core_kind, double core_value, double wake_length, d3* wake_vec,
-                                    double* rc_dev, int sym, d3* factors, float* split, cudaStream_t s);
+                                    double* rc_dev, int sym, d3* factors, float* split, const d3* basis,
+                                    cudaStream_t s);
 
 // ---- wake and geometry (k_wake.cu) ------------------------------------------------------
 struct WakeBuffers {
@@ -148,6 +152,7 @@ struct CaseStepJob {
     const PanelRec<float>* row0_32 = nullptr; // unit matrix from FP32 row-0 records (null: FP64)
     d3* factors = nullptr;
     float* split = nullptr;
+    const d3* basis = nullptr;                // two-component split matrix (nullptr: three)
     ChainArgs chain;                          // chain records (chain_n = 0: none)
     long long chain_n = 0;
     long long blk_advect = 0, blk_panels = 0, blk_matrix = 0, blk_chain = 0;
@@ -193,12 +198,16 @@ __host__ __device__ inline int si_matrix_stride(int N) { return (N + 3) & ~3; }
 struct SolveBuffers {
     const d3* fixed = nullptr;      // [N]
     const d3* factors = nullptr;    // [N][N] (Linearized)
-    // SimpleIterative matrix as floats: hi plane [N][3][stride] (row, component, column;
+    // SimpleIterative matrix as floats: hi plane [N][split_comps][stride] (row, component, column;
     // stride = si_matrix_stride(N)), then the lo plane (the nearest float of the remainder);
     // split_full = 0 when only the diagonal carries lo parts (the FP32 unit matrix: every
     // other entry is an FP32 value, lo = 0)
     const float* factors_split = nullptr;
     int split_full = 1;
+    // components per entry: 2 in the rows' in-plane bases (basis, [2N]: the velocity's span
+    // component is projected out anyway; no velocity correction), else 3 (x, y, z)
+    int split_comps = 3;
+    const d3* basis = nullptr;
     double* gamma_prev = nullptr;   // [N] in: initial solution, out: solution
     d3* vel_out = nullptr;          // [N] output control-point velocity
     double* scalars = nullptr;      // [8]: residual, iterations, converged, singular, start (below)
@@ -241,7 +250,8 @@ LinPlan linearized_plan(int N);
 cudaError_t launch_solve_linearized_jobs(const SolveJob* jobs, int n, const LinPlan& plan, cudaStream_t s);
 // SimpleIterative solves of a batch: n cases of one cluster size (solve_cluster_size of
 // their N) in one launch, a cluster per case; smem = the largest si_smem_bytes of the jobs.
-size_t si_smem_bytes(int N, int full);  // full: the matrix's lo plane is read (SolveBuffers::split_full)
+// full: the matrix's lo plane is read (SolveBuffers::split_full); comps: SolveBuffers::split_comps
+size_t si_smem_bytes(int N, int full, int comps);
 int si_rows_per_thread(int N);  // 1 or 4: a launch holds one kind (rows_per_thread below)
 cudaError_t launch_solve_simple_iterative_jobs(const SolveJob* jobs, int n, int cluster, int rows_per_thread,
                                                size_t smem, cudaStream_t s);

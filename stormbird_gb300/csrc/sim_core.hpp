@@ -332,6 +332,7 @@ struct sb_sim {
     DevBuf<FoilP> foils;
     // geometry
     DevBuf<d3> chord_local, chord_global, chord_span_pts, span_s, span_e, span_pts, ctrl, felt_ctrl, felt_span, mean;
+    DevBuf<d3> solve_basis;  // [2N] in-plane basis of each line (line_basis)
     // wake
     DevBuf<d3> pts[2], vel;
     DevBuf<double> str[2];
@@ -538,6 +539,8 @@ struct sb_sim {
 
     void allocate() {
         chord_local.alloc(N); chord_global.alloc(N); chord_span_pts.alloc(Np); span_s.alloc(N); span_e.alloc(N);
+        solve_basis.alloc(2 * static_cast<size_t>(N));
+        dm.solve_basis = solve_basis.p;
         span_pts.alloc(Np); ctrl.alloc(N); felt_ctrl.alloc(N); felt_span.alloc(Np); mean.alloc(1);
         dm.chord_local = chord_local.p; dm.chord_global = chord_global.p; dm.chord_span_pts = chord_span_pts.p;
         dm.span_s = span_s.p; dm.span_e = span_e.p; dm.span_pts = span_pts.p; dm.ctrl = ctrl.p;
@@ -892,6 +895,7 @@ struct sb_sim {
         j.row0_32 = precision == 2 ? nullptr : rec32.p;
         j.factors = factors.p;
         j.split = factors_split.p;
+        j.basis = split_basis();
         if (use_chains() && rollup_active()) {
             j.chain = chain_args(cur ^ 1);  // the buffer the step writes
             j.chain_n = chain_Q * chain_Bq;
@@ -910,12 +914,16 @@ struct sb_sim {
 
     // Influence matrix (unit matrix of the first wake row, or horseshoes) and the solve.
     // The frozen wake's matrix: unit first-row panels (dynamic) or horseshoes (quasi-steady).
+    // In-plane bases for a two-component SimpleIterative matrix (no velocity correction: the
+    // solve uses the velocity's in-plane part only), else nullptr (three components).
+    const d3* split_basis() const { return solve.velocity_correction == 0 ? dm.solve_basis : nullptr; }
+
     void step_matrix() {
         if (dynamic) {
             // FP32 records unless the sweeps run in FP64
             ck(launch_unit_matrix(row0_64.p, precision == 2 ? nullptr : rec32.p, ctrl.p, N, dm.symmetry, dm.neglect_self,
                                   wing_of_line.p, factors.p,
-                                  factors_split.p, stream),
+                                  factors_split.p, split_basis(), stream),
                "unit matrix");
             launches += 1;
         } else {
@@ -923,7 +931,7 @@ struct sb_sim {
             double wl = q.wake_length_factor * dm.rep_chord;
             ck(launch_horseshoe_matrix(dm, static_cast<int>(q.viscous_core_length.kind), q.viscous_core_length.value, wl,
                                        qs_wake_vec.p, qs_rc.p, static_cast<int>(q.symmetry_condition), factors.p,
-                                       factors_split.p, stream),
+                                       factors_split.p, split_basis(), stream),
                "horseshoe matrix");
             launches += 2;
             record(3);
@@ -938,6 +946,8 @@ struct sb_sim {
         sb.factors_split = factors_split.p;
         // off-diagonal lo parts are zero when the unit matrix came from the FP32 records
         sb.split_full = (dynamic && precision != 2) ? 0 : 1;
+        sb.basis = split_basis();
+        sb.split_comps = sb.basis ? 2 : 3;
         sb.gamma_prev = gamma_p;
         sb.vel_out = vel_out.p;
         sb.scalars = scalars.p;
