@@ -479,7 +479,8 @@ struct sb_batch {
                 J.chunk_panels = g.chunk[k];
                 const long long P = d.p1 - d.p0;
                 J.n_chunks = (P > 0 && d.M > 0) ? static_cast<int>((P + g.chunk[k] - 1) / g.chunk[k]) : 0;
-                J.n_ttiles = (d.M + TM - 1) / TM;
+                c.target_layout(d, J);
+                J.n_ttiles = (bs_slots(J) + TM - 1) / TM;
                 J.partial = partial.p + g.part_off[k];
                 J.item_begin = item;
                 J.M_total = d.M_total;

@@ -126,6 +126,26 @@ __device__ __forceinline__ float rsqrt_n(float x) {
     return r;
 }
 
+// Point doublet (panel.rs:82-96) at two targets, e = target - centre, |e|^2 = e2, added to
+// (TX, TY, TZ): Gamma area/(4 pi) (3 (n.e) e / |e|^5 - n / |e|^3). The record's slot 35 holds
+// area/(4 pi) / (3 sqrt 3) and f = Gamma x slot 35 per lane (0 for a lane that takes no
+// doublet). With q = 1/sqrt(|e|^2 / 3): q^2 = 3/|e|^2, f q^3 = Gamma area/(4 pi) / |e|^3, so
+// the doublet is B (g e - n) with B = f q^3 and g = q^2 (n.e): 20 packed operations. The
+// floor keeps q finite where a degenerate panel meets a target at its centre (its doublet
+// then overflows, as the f64 formula would).
+__device__ __forceinline__ void doublet2(float2 f, const float* v, float2 ex, float2 ey, float2 ez, float2 e2,
+                                         float2& TX, float2& TY, float2& TZ) {
+    const float2 e3 = fma2(e2, bc(1.f / 3.f), bc(FLT_MIN));
+    const float2 q = make_float2(rsqrt_n(e3.x), rsqrt_n(e3.y));
+    const float2 q2 = mul2(q, q);
+    const float2 B = mul2(mul2(f, q), q2);
+    const float nx = v[36], ny = v[37], nz = v[38];
+    const float2 g = mul2(q2, fma2(ex, bc(nx), fma2(ey, bc(ny), mul2(ez, bc(nz)))));
+    TX = fma2(B, fma2(g, ex, bc(-nx)), TX);
+    TY = fma2(B, fma2(g, ey, bc(-ny)), TY);
+    TZ = fma2(B, fma2(g, ez, bc(-nz)), TZ);
+}
+
 // Vortex ring of one FP32 panel record at two targets (the two lanes of the float2s), given
 // e = x - centre (float-float difference). r_k = e - o_k. Per segment, with c = d x r1 = r1 x r2:
 //   r1.r2 = |r1|^2 - r1.d,
@@ -299,47 +319,76 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
     constexpr bool F32 = sizeof(R) == 4;
     static_assert(!F32 || TT == 2, "the packed FP32 path holds exactly two targets per thread");
     static_assert(!CHAIN || (F32 && !NEGLECT), "chain records: FP32 sweeps without neglect-self only");
-    __shared__ __align__(128) PanelRec<R> tile[2][TILE];
-    __shared__ __align__(8) uint64_t bar[2];
+    // Stages of panel tiles: three where five CTAs per SM still fit (the 64-panel FP32 tile),
+    // else two. A warp runs ahead of the CTA's slowest by up to the stages less one: a stage
+    // is refilled by the warp that releases it last, with no CTA barrier per tile (the far-field
+    // fast path takes warps through a tile at different speeds).
+    constexpr int NS = (TILE * sizeof(PanelRec<R>) <= 12288) ? 3 : 2;
+    constexpr int kWarps = kBsThreads / 32;
+    __shared__ __align__(128) PanelRec<R> tile[NS][TILE];
+    __shared__ __align__(8) uint64_t bar[NS];
+    __shared__ unsigned s_done[NS];    // releases of the stage in this launch (kWarps per tile)
+    __shared__ unsigned s_issued[NS];  // copies issued into the stage in this launch
     __shared__ long long s_item;
+    // the item's target tile, source chunk and panel range (read from shared memory where used,
+    // so that no register holds them through the tile loop)
+    __shared__ long long s_ttile, s_pb, s_pe;
+    __shared__ int s_chunk;
     __shared__ int s_timed_out;  // a tile wait of this CTA ran out
     // far-field fast path (FP32 panel sweeps): bounding box of each warp's targets (hi parts)
     __shared__ float s_wbox[kBsThreads / 32][6];
     constexpr bool FAST_FAR = F32 && !CHAIN && !NEGLECT;
     __shared__ BsJob s_job;  // the current item's sweep (one copy per item, by thread 0)
 
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31;
     if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        for (int q = 0; q < NS; ++q) {
+            mbar_init(&bar[q], 1);
+            s_done[q] = 0;
+            s_issued[q] = 0;
+        }
         fence_mbar_init();
         s_timed_out = 0;
     }
     __syncthreads();
-    uint32_t phase0 = 0, phase1 = 0;
+    uint32_t phases = 0;  // bit q: parity of stage q's phase that the next wait on it waits for
     const long long n_items = a.jobs ? a.jobs[a.n_jobs].item_begin : a.job0.n_ttiles * static_cast<long long>(a.job0.n_chunks);
     constexpr int TM = kBsThreads * T;
 
     while (true) {
-        __syncthreads();  // every thread is done with the previous item's s_item and s_job
+        __syncthreads();  // every thread is done with the previous item's s_item, s_job and tiles
+        if (s_timed_out) {
+            // A tile wait ran out (every warp has left its tile loop): the launch's results are
+            // void. Thread 0 waits, bounded again, for the last copy issued into each stage, so
+            // that no copy is in flight into the CTA's shared memory when it exits; the n-th copy
+            // into a stage completes its phase n - 1.
+            if (tid == 0)
+                for (int q = 0; q < NS; ++q)
+                    if (s_issued[q] > 0) mbar_wait_bounded(&bar[q], (s_issued[q] - 1u) & 1u, a.err);
+            return;
+        }
         if (tid == 0) {
             // once a wait of any CTA has run out the launch's results are void: take no more items
             const bool stop = *reinterpret_cast<volatile const int*>(a.err) == kDevTimeout;
             const long long it = stop ? n_items : static_cast<long long>(atomicAdd(a.work_counter, 1ULL));
             s_item = it;
-            if (it < n_items) s_job = a.jobs ? a.jobs[find_job(a.jobs, a.n_jobs, it)] : a.job0;
+            if (it < n_items) {
+                const BsJob& Jt = a.jobs ? a.jobs[find_job(a.jobs, a.n_jobs, it)] : a.job0;
+                s_job = Jt;
+                const long long local = it - Jt.item_begin;
+                // chunk-major order: CTAs running together share a source chunk in L2
+                const int chunk = static_cast<int>(local / Jt.n_ttiles);
+                s_chunk = chunk;
+                s_ttile = local % Jt.n_ttiles;
+                const long long pb = Jt.p_begin + static_cast<long long>(chunk) * Jt.chunk_panels;
+                s_pb = pb;
+                s_pe = min(pb + static_cast<long long>(Jt.chunk_panels), Jt.p_end);
+            }
         }
         __syncthreads();
-        const long long item = s_item;
-        if (item >= n_items) break;
+        if (s_item >= n_items) break;
         const BsJob& J = s_job;
-        const long long local = item - J.item_begin;
-        const PanelRec<R>* P = reinterpret_cast<const PanelRec<R>*>(J.panels);
-        // chunk-major order: CTAs running together share a source chunk in L2
-        const int chunk = static_cast<int>(local / J.n_ttiles);
-        const long long ttile = local % J.n_ttiles;
-        const long long pb = J.p_begin + static_cast<long long>(chunk) * J.chunk_panels;
-        const long long pe = min(pb + static_cast<long long>(J.chunk_panels), J.p_end);
+        const long long ttile = s_ttile;
 
         // targets: float-float pairs (FP32) or doubles (FP64 path, lo parts 0)
         R xh[TT], yh[TT], zh[TT], xl[TT], yl[TT], zl[TT];
@@ -349,9 +398,10 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
         for (int t = 0; t < T; ++t) {
             // with the far-field fast path a thread's targets are adjacent (a warp's 64 targets
             // are consecutive points, a compact box); else T rows of the tile apart
-            long long idx = ttile * TM + (FAST_FAR ? static_cast<long long>(tid) * T + t
-                                                   : static_cast<long long>(t) * kBsThreads + tid);
-            valid[t] = idx < J.M;
+            const long long slot = ttile * TM + (FAST_FAR ? static_cast<long long>(tid) * T + t
+                                                          : static_cast<long long>(t) * kBsThreads + tid);
+            const long long idx = FAST_FAR ? bs_slot_target(J, slot) : slot;
+            valid[t] = slot < bs_slots(J) && idx < J.M;
             d3 p = valid[t] ? J.targets[idx] : mk(0, 0, 0);
             tw[t] = (NEGLECT && valid[t]) ? J.target_wing[idx] : -1;
             d3 q[2] = {p, SYM ? mirror(SYM, p) : p};
@@ -404,37 +454,39 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
             __syncwarp();
         }
 
-        const int ntiles = static_cast<int>((pe - pb + TILE - 1) / TILE);
-        auto issue = [&](int k) {
-            long long p0 = pb + static_cast<long long>(k) * TILE;
-            int np = static_cast<int>(min(static_cast<long long>(TILE), pe - p0));
-            uint32_t bytes = static_cast<uint32_t>(np) * static_cast<uint32_t>(sizeof(PanelRec<R>));
-            uint64_t* b = &bar[k & 1];
-            mbar_expect_tx(b, bytes);
-            bulk_g2s(&tile[k & 1][0], P + p0, bytes, b);
+        const int ntiles = static_cast<int>((s_pe - s_pb + TILE - 1) / TILE);
+        // panels of tile k
+        auto tile_panels = [&](int k) {
+            return static_cast<int>(min(static_cast<long long>(TILE), s_pe - s_pb - static_cast<long long>(k) * TILE));
         };
-        if (tid == 0 && ntiles > 0) issue(0);
+        // tile k goes into stage k % NS
+        auto issue = [&](int k, int q) {
+            const long long p0 = s_pb + static_cast<long long>(k) * TILE;
+            const uint32_t bytes = static_cast<uint32_t>(tile_panels(k)) * static_cast<uint32_t>(sizeof(PanelRec<R>));
+            uint64_t* b = &bar[q];
+            atomicAdd(&s_issued[q], 1u);
+            mbar_expect_tx(b, bytes);
+            bulk_g2s(&tile[q][0], reinterpret_cast<const PanelRec<R>*>(s_job.panels) + p0, bytes, b);
+        };
+        if (tid == 0)
+            for (int q = 0; q < NS && q < ntiles; ++q) issue(q, q);
 
-        int k = 0;
-        for (; k < ntiles; ++k) {
-            const int buf = k & 1;
-            if (tid == 0 && k + 1 < ntiles) issue(k + 1);
-            bool ok;
-            if (buf == 0) {
-                ok = mbar_wait_bounded(&bar[0], phase0, a.err, a.wait_polls);
-                phase0 ^= 1;
-            } else {
-                ok = mbar_wait_bounded(&bar[1], phase1, a.err, a.wait_polls);
-                phase1 ^= 1;
-            }
-            if (!ok) s_timed_out = 1;
-            const int np = static_cast<int>(min(static_cast<long long>(TILE), pe - (pb + static_cast<long long>(k) * TILE)));
-
+        int buf = 0;  // stage of tile k
+        for (int k = 0; k < ntiles; ++k, buf = buf + 1 == NS ? 0 : buf + 1) {
+            // a wait of another warp ran out: the item's sums are void, and the stages that
+            // warp did not release are never refilled
+            if (__any_sync(0xffffffffu, *reinterpret_cast<volatile int*>(&s_timed_out) != 0)) break;
+            const bool ok = mbar_wait_bounded(&bar[buf], (phases >> buf) & 1u, a.err, a.wait_polls);
+            phases ^= 1u << buf;
             // A warp with a lane whose wait ran out leaves the tile alone: its copy may still be
             // landing, and lanes reading a word while it lands can see different values, which
-            // would split the warp at the uniform branches, votes and shuffles below (the sums
-            // are void anyway).
-            if (!__any_sync(0xffffffffu, !ok)) {
+            // would split the warp at the uniform branches, votes and shuffles below.
+            if (__any_sync(0xffffffffu, !ok)) {
+                if (lane == 0) s_timed_out = 1;
+                break;
+            }
+            const int np = tile_panels(k);
+            {
                 if constexpr (F32) {
                     float2 TX = bc(0.f), TY = bc(0.f), TZ = bc(0.f);
                     // Far-field fast path: when the box of the tile's panel centres lies farther from
@@ -445,7 +497,6 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
                     // without the test and the votes.
                     bool all_far = false;
                     if constexpr (FAST_FAR) {
-                        const int lane = tid & 31;
                         float c7[7] = {CUDART_INF_F, CUDART_INF_F, CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F,
                                        0.f};
                         for (int q = lane; q < np; q += 32) {
@@ -491,15 +542,7 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
                             const float2 ey = sub2s(Y2h, v[29]);
                             const float2 ez = sub2s(Z2h, v[30]);
                             const float2 e2s = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
-                            const float2 e2f = add2(e2s, bc(FLT_MIN));
-                            const float2 ir = make_float2(rsqrt_n(e2f.x), rsqrt_n(e2f.y));
-                            const float2 ir2 = mul2(ir, ir);
-                            const float2 sd = mul2(bc(v[35] * gam), mul2(mul2(ir2, ir2), ir));
-                            const float nx = v[36], ny = v[37], nz = v[38];
-                            const float2 h3 = mul2(bc(3.f), fma2(ex, bc(nx), fma2(ey, bc(ny), mul2(ez, bc(nz)))));
-                            TX = fma2(sd, fma2(h3, ex, mul2(e2s, bc(-nx))), TX);
-                            TY = fma2(sd, fma2(h3, ey, mul2(e2s, bc(-ny))), TY);
-                            TZ = fma2(sd, fma2(h3, ez, mul2(e2s, bc(-nz))), TZ);
+                            doublet2(bc(v[35] * gam), v, ex, ey, ez, e2s, TX, TY, TZ);
                         }
                     }
                     for (int p = 0; p < (all_far ? 0 : np); ++p) {
@@ -540,18 +583,9 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
                         const bool any_far = __any_sync(0xffffffffu, (a0 && !n0) || (a1 && !n1));
                         if (any_far) {  // point doublet (panel.rs:82-96), the fast path's arithmetic
                             const float2 e2s = make_float2(n0 ? 1.f : e2.x, n1 ? 1.f : e2.y);
-                            // a subnormal |e|^2 (a degenerate panel) overflows s to inf either way
-                            const float2 e2f = add2(e2s, bc(FLT_MIN));
-                            const float2 ir = make_float2(rsqrt_n(e2f.x), rsqrt_n(e2f.y));
-                            const float2 ir2 = mul2(ir, ir);
                             const float at = v[35] * gam;
                             const float2 sm = make_float2((a0 && !n0) ? at : 0.f, (a1 && !n1) ? at : 0.f);
-                            const float2 s = mul2(sm, mul2(mul2(ir2, ir2), ir));
-                            const float nx = v[36], ny = v[37], nz = v[38];
-                            const float2 h3 = mul2(bc(3.f), fma2(ex, bc(nx), fma2(ey, bc(ny), mul2(ez, bc(nz)))));
-                            TX = fma2(s, fma2(h3, ex, mul2(e2s, bc(-nx))), TX);
-                            TY = fma2(s, fma2(h3, ey, mul2(e2s, bc(-ny))), TY);
-                            TZ = fma2(s, fma2(h3, ez, mul2(e2s, bc(-nz))), TZ);
+                            doublet2(sm, v, ex, ey, ez, e2s, TX, TY, TZ);
                         }
                         if (any_near) {  // vortex ring (panel.rs:99-118)
                             // float-float difference: (x_hi - c_hi) + (x_lo - c_lo)
@@ -606,29 +640,26 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
                     }
                 }
             }
-            // The buffer is refilled in the next-but-one tile. A wait of tile k that ran out in
-            // any thread ends the tile loop (the sums are void).
-            __syncthreads();
-            if (s_timed_out) break;
-        }
-        if (s_timed_out) {
-            // Copies that may still be landing: tile k's (its wait ran out) and tile k + 1's
-            // (issued before that wait). Thread 0 waits for both, bounded again, so no copy
-            // is in flight into the CTA's shared memory when it exits. Tile k's phase parity
-            // is its buffer's phase before the flip above, tile k + 1's its buffer's current one.
-            if (tid == 0) {
-                const int buf = k & 1;
-                mbar_wait_bounded(&bar[buf], (buf == 0 ? phase0 : phase1) ^ 1u, a.err);
-                if (k + 1 < ntiles) mbar_wait_bounded(&bar[buf ^ 1], buf == 0 ? phase1 : phase0, a.err);
+            // Release the stage: every lane of the warp is done reading it. The warp that
+            // releases it last (the kWarps-th release of this tile) refills it with tile k + NS.
+            __syncwarp();
+            if (lane == 0) {
+                __threadfence_block();
+                if (atomicAdd(&s_done[buf], 1u) % kWarps == kWarps - 1 && k + NS < ntiles) {
+                    __threadfence_block();
+                    issue(k + NS, buf);
+                }
             }
-            return;
         }
 
+        const long long ttile_out = s_ttile;
+        const int chunk = s_chunk;
 #pragma unroll
         for (int t = 0; t < T; ++t) {
-            long long idx = ttile * TM + (FAST_FAR ? static_cast<long long>(tid) * T + t
-                                                   : static_cast<long long>(t) * kBsThreads + tid);
-            if (idx < J.M) {
+            const long long slot = ttile_out * TM + (FAST_FAR ? static_cast<long long>(tid) * T + t
+                                                              : static_cast<long long>(t) * kBsThreads + tid);
+            const long long idx = FAST_FAR ? bs_slot_target(J, slot) : slot;
+            if (slot < bs_slots(J) && idx < J.M) {
                 d3 u = mk(static_cast<double>(sx[t]) + static_cast<double>(cx[t]),
                           static_cast<double>(sy[t]) + static_cast<double>(cy[t]),
                           static_cast<double>(sz[t]) + static_cast<double>(cz[t]));
@@ -808,16 +839,7 @@ __device__ __forceinline__ void panel_unit2(const float* v, float2 X2h, float2 Y
     ux = uy = uz = bc(0.f);
     if (!n0 || !n1) {  // point doublet (panel.rs:82-96), unit strength
         const float2 e2s = make_float2(n0 ? 1.f : e2.x, n1 ? 1.f : e2.y);
-        const float2 e2f = add2(e2s, bc(FLT_MIN));
-        const float2 ir = make_float2(rsqrt_n(e2f.x), rsqrt_n(e2f.y));
-        const float2 ir2 = mul2(ir, ir);
-        const float2 sm = make_float2(n0 ? 0.f : v[35], n1 ? 0.f : v[35]);
-        const float2 sd = mul2(sm, mul2(mul2(ir2, ir2), ir));
-        const float nx = v[36], ny = v[37], nz = v[38];
-        const float2 h3 = mul2(bc(3.f), fma2(ex, bc(nx), fma2(ey, bc(ny), mul2(ez, bc(nz)))));
-        ux = mul2(sd, fma2(h3, ex, mul2(e2s, bc(-nx))));
-        uy = mul2(sd, fma2(h3, ey, mul2(e2s, bc(-ny))));
-        uz = mul2(sd, fma2(h3, ez, mul2(e2s, bc(-nz))));
+        doublet2(make_float2(n0 ? 0.f : v[35], n1 ? 0.f : v[35]), v, ex, ey, ez, e2s, ux, uy, uz);
     }
     if (n0 || n1) {  // vortex ring (panel.rs:99-118), unit strength
         ex = add2(ex, sub2s(X2l, v[32]));

@@ -277,7 +277,7 @@ __device__ void write_panel_records(const d3 (&pp)[4], double rc, double g, doub
         const double ff2 = t * t;
         for (int k = 0; k < 4; ++k) r.v[24 + k] = l2[k] > 0.0 ? static_cast<float>(1.0 / l2[k]) : 0.f;
         far_field_fields(ff2, c, &r.v[31], &r.v[kRec32FF2Lo], &r.v[kRec32FF2Band]);
-        r.v[35] = static_cast<float>(area * kFourPiInv);
+        r.v[35] = static_cast<float>(area * kFourPiInv * kInv3Sqrt3);
         r.v[36] = static_cast<float>(n.x);
         r.v[37] = static_cast<float>(n.y);
         r.v[38] = static_cast<float>(n.z);
@@ -311,7 +311,7 @@ __device__ void write_panel_records(const d3 (&pp)[4], double rc, double g, doub
         const float sp = (lf[0] + lf[1] + lf[2] + lf[3]) * 0.5f;
         // a degenerate quadrilateral can round the product below zero: area 0
         const float prod = fmaxf((sp - lf[0]) * (sp - lf[1]) * (sp - lf[2]) * (sp - lf[3]), 0.f);
-        r.v[35] = __fsqrt_rn(prod) * static_cast<float>(kFourPiInv);
+        r.v[35] = __fsqrt_rn(prod) * static_cast<float>(kFourPiInv * kInv3Sqrt3);
         const d3 a = pp[2] - pp[0], b = pp[3] - pp[1];
         const float ax = static_cast<float>(a.x), ay = static_cast<float>(a.y), az = static_cast<float>(a.z);
         const float bx = static_cast<float>(b.x), by = static_cast<float>(b.y), bz = static_cast<float>(b.z);

@@ -192,7 +192,7 @@ __device__ inline double foil_cd(const FoilP& f, double a) {
 //   [12..23] segment vectors d_k = p_{k+1} - p_k (rounded from f64)
 //   [24..27] 1/|d_k|^2 per ring segment k (0 for a degenerate segment)
 //   [28..30] centre hi, [31] far-field length squared (hi)
-//   [32..34] centre lo, [35] area / (4 pi)
+//   [32..34] centre lo, [35] area / (4 pi) / (3 sqrt 3) (the doublet's factor, see doublet2)
 //   [36..38] unit normal, [39] strength Gamma
 //   [40] core length^4, [41] wing index, [42..45] |d_k|^2,
 //   [46] far-field length squared lo (fl32(ff2 - hi), 0 when hi is infinite),
@@ -216,6 +216,7 @@ static_assert(sizeof(PanelRec<float>) == 192, "FP32 panel record is 192 bytes");
 static_assert(sizeof(PanelRec<double>) == 224, "FP64 panel record is 224 bytes");
 
 constexpr int kRec32Gamma = 39;  // strength slot of the FP32 record
+constexpr double kInv3Sqrt3 = 0.19245008972987526;  // 1 / (3 sqrt 3), folded into slot 35
 constexpr int kRec32DD = 42;     // |d_k|^2 of the FP32 record's four segments (slots 42..45)
 constexpr int kRec32FF2Lo = 46;    // lo part of the far-field length squared
 constexpr int kRec32FF2Band = 47;  // band of the hi-part near/far test (above)

@@ -11,6 +11,7 @@
 namespace sbgpu {
 
 constexpr int kBsThreads = 128;  // threads per Biot-Savart CTA
+constexpr int kMaxTargetGroups = 8;  // wings of a sweep's target order (BsJob::group_off)
 
 // One Biot-Savart sweep: velocities at M targets induced by panels [p_begin, p_end).
 // Its work items are (source chunk, target tile) pairs, chunk-major.
@@ -30,7 +31,30 @@ struct BsJob {
     const d3* base = nullptr;
     d3* out = nullptr;
     long long block_begin = 0;         // first block of this sweep in the batched reduce
+    // Order in which the FP32 far-field sweeps take their targets (sweeps over wake points):
+    // rows of row_pts points, each row made of n_groups groups (one wing's span points)
+    // starting at point group_off[g] (group_off[n_groups] = row_pts). Target slot s runs
+    // through the groups one after another and within a group through the rows, so that a
+    // warp's 64 targets are one wing's points on adjacent rows (a compact box) rather than a
+    // stretch of a row across two wings. slots = rows x row_pts >= M (a slot whose point is
+    // M or beyond is empty). n_groups == 0: slot s is target s; slots == 0: M slots.
+    long long slots = 0;
+    int row_pts = 0, n_groups = 0;
+    int group_off[kMaxTargetGroups + 1] = {};
 };
+
+// Target index of slot s (see BsJob::slots).
+__host__ __device__ inline long long bs_slot_target(const BsJob& J, long long s) {
+    if (J.n_groups == 0) return s;
+    const long long R = J.slots / J.row_pts;
+    int g = 0;
+    while (g + 1 < J.n_groups && s >= R * J.group_off[g + 1]) ++g;
+    const int off = J.group_off[g], n = J.group_off[g + 1] - off;
+    const long long t = s - R * off;
+    const long long r = t / n;
+    return r * J.row_pts + off + (t - r * n);
+}
+__host__ __device__ inline long long bs_slots(const BsJob& J) { return J.slots > 0 ? J.slots : J.M; }
 
 // A sweep launch: one job (job0, jobs == nullptr) or a list of jobs in device memory
 // whose items are handed out in list order (the batch puts the costliest items first).

@@ -477,6 +477,7 @@ struct sb_sim {
         chord_len.upload(cl); span_len_local.upload(sl);
         wing_of_line.upload(wol); wing_start.upload(ws); wing_end.upload(we);
         wing_of_line_h = wol;
+        wing_start_h = ws;
         is_virtual.upload(virt); foils.upload(fo);
         sp_line.upload(spl); sp_end.upload(spe); sp_a.upload(spa); sp_b.upload(spb);
 
@@ -729,7 +730,23 @@ struct sb_sim {
         const void* src = nullptr;  // chain records, or nullptr for the panel records
         bool chain = false;
         double segments = 0.0;      // segment evaluations per target
+        bool wake_targets = false;  // the targets are the wake points (rows of Np points)
     };
+
+    // Target order of a sweep over the wake points (BsJob::slots): wing by wing, rows within a
+    // wing, so that the far-field fast path sees compact warp boxes. Other sweeps, and one wing
+    // (whose natural order is that already), keep the index order.
+    void target_layout(const SweepDesc& d, BsJob& J) const {
+        J.slots = d.M;
+        J.row_pts = 0;
+        J.n_groups = 0;
+        if (!d.wake_targets || d.chain || S < 2 || S > kMaxTargetGroups || d.M <= 0) return;
+        J.slots = (d.M + Np - 1) / Np * static_cast<long long>(Np);
+        J.row_pts = Np;
+        J.n_groups = S;
+        for (int w = 0; w < S; ++w) J.group_off[w] = wing_start_h[w] + w;  // a wing's first point
+        J.group_off[S] = Np;
+    }
 
     // Biot-Savart sweep into out[0..M) (+ base), base only for [M, M_total).
     void sweep(const SweepDesc& d, int counter_slot) {
@@ -742,10 +759,11 @@ struct sb_sim {
         int neglect = twing ? 1 : 0;
         long long P = p1 - p0;
         if (M > 0 && P > 0) {
-            SweepPlan sp = plan_sweep(M, P, sym, neglect);
+            BsArgs a;
+            target_layout(d, a.job0);
+            SweepPlan sp = plan_sweep(bs_slots(a.job0), P, sym, neglect);
             size_t need = static_cast<size_t>(sp.n_chunks) * static_cast<size_t>(M) * 3;
             if (partial.n < need) partial.alloc(need);
-            BsArgs a;
             a.job0.panels = d.src ? d.src : precision == 2 ? static_cast<const void*>(rec64.p) : static_cast<const void*>(rec32.p);
             a.chain = d.chain ? 1 : 0;
             a.job0.p_begin = p0;
@@ -822,7 +840,7 @@ struct sb_sim {
                     (R + 1.0) * N + R * Np};
         }
         return {pts[cur].p, e, 0, active_panels(), nullptr, wake_fs, P_pts, vel.p, nullptr, false,
-                4.0 * static_cast<double>(active_panels())};
+                4.0 * static_cast<double>(active_panels()), true};
     }
 
     void after_fixed_sweep() {
@@ -1077,6 +1095,7 @@ struct sb_sim {
     // background thread.
     std::unique_ptr<sbhost::WakeFileWriter> wake_writer;
     std::vector<int> wing_of_line_h;
+    std::vector<int> wing_start_h;  // first line of each wing
     std::vector<double> panel_core_h;
 
     void push_wake_file() {
