@@ -489,28 +489,36 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
             {
                 if constexpr (F32) {
                     float2 TX = bc(0.f), TY = bc(0.f), TZ = bc(0.f);
-                    // Far-field fast path: when the box of the tile's panel centres lies farther from
-                    // the box of the warp's targets than the tile's largest far-field radius (with a
-                    // margin well beyond the FP32 rounding of the per-pair distance), every pair of
-                    // the tile is a point doublet (panel.rs:53-57, 82-96) and the per-pair test
-                    // below would decide so for every lane: the warp evaluates the doublets alone,
-                    // without the test and the votes.
-                    bool all_far = false;
+                    // Far-field fast path, per quarter of the tile (a sub-tile of TILE / 4 panels):
+                    // when the box of the sub-tile's panel centres lies farther from the box of the
+                    // warp's targets than the sub-tile's largest far-field radius (with a margin well
+                    // beyond the FP32 rounding of the per-pair distance), every pair of it is a point
+                    // doublet (panel.rs:53-57, 82-96) and the per-pair test below would decide so for
+                    // every lane: the warp evaluates the doublets alone, without the test and the
+                    // votes. Quarters keep the boxes compact where a tile holds the end of one wing's
+                    // row of panels and the start of the next.
+                    unsigned far_mask = 0;  // bit q: sub-tile q is all far
                     if constexpr (FAST_FAR) {
+                        static_assert(TILE % 32 == 0, "the fast path's sub-tiles are 8 lanes x TILE / 32 panels");
+                        constexpr int PPL = TILE / 32;  // panels per lane; sub-tile q = lanes 8q .. 8q + 7
                         float c7[7] = {CUDART_INF_F, CUDART_INF_F, CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F,
                                        0.f};
-                        for (int q = lane; q < np; q += 32) {
-                            const float4 c = *reinterpret_cast<const float4*>(&tile[buf][q].v[28]);  // centre hi, ff2
-                            c7[0] = fminf(c7[0], c.x);
-                            c7[1] = fminf(c7[1], c.y);
-                            c7[2] = fminf(c7[2], c.z);
-                            c7[3] = fmaxf(c7[3], c.x);
-                            c7[4] = fmaxf(c7[4], c.y);
-                            c7[5] = fmaxf(c7[5], c.z);
-                            c7[6] = fmaxf(c7[6], c.w);
+#pragma unroll
+                        for (int j = 0; j < PPL; ++j) {
+                            const int q = PPL * lane + j;
+                            if (q < np) {
+                                const float4 c = *reinterpret_cast<const float4*>(&tile[buf][q].v[28]);  // centre hi, ff2
+                                c7[0] = fminf(c7[0], c.x);
+                                c7[1] = fminf(c7[1], c.y);
+                                c7[2] = fminf(c7[2], c.z);
+                                c7[3] = fmaxf(c7[3], c.x);
+                                c7[4] = fmaxf(c7[4], c.y);
+                                c7[5] = fmaxf(c7[5], c.z);
+                                c7[6] = fmaxf(c7[6], c.w);
+                            }
                         }
 #pragma unroll
-                        for (int o = 16; o > 0; o >>= 1)
+                        for (int o = 4; o > 0; o >>= 1)
 #pragma unroll
                             for (int q = 0; q < 7; ++q) {
                                 const float w = __shfl_xor_sync(0xffffffffu, c7[q], o);
@@ -518,23 +526,29 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
                             }
                         const float* wb = s_wbox[tid >> 5];
                         // the boxes are of hi parts, each within 2^-24 |x| of its point: the gaps
-                        // shrink by both sides' bound before the test
+                        // shrink by both sides' bound before the test (an empty sub-tile's box
+                        // gives a gap of 0: not far, and no panels to take)
                         auto gap = [&](int q) {
                             const float m = fmaxf(fmaxf(fabsf(c7[q]), fabsf(c7[q + 3])), fmaxf(fabsf(wb[q]), fabsf(wb[q + 3])));
                             return fmaxf(0.f, fmaxf(c7[q] - wb[q + 3], wb[q] - c7[q + 3]) - 0x1p-23f * m);
                         };
                         const float gx = gap(0), gy = gap(1), gz = gap(2);
-                        // (the reduced values are the same in every lane; the vote tells the compiler
-                        // the branch is warp-uniform, which keeps the register count of the kernel)
-                        all_far = __all_sync(0xffffffffu, c7[6] < CUDART_INF_F && gx * gx + gy * gy + gz * gz > 1.001f * c7[6]);
+                        const unsigned b =
+                            __ballot_sync(0xffffffffu, c7[6] < CUDART_INF_F && gx * gx + gy * gy + gz * gz > 1.001f * c7[6]);
+                        far_mask = (b & 1u) | ((b >> 7) & 2u) | ((b >> 14) & 4u) | ((b >> 21) & 8u);
                     }
-                    if (all_far) {
+                    constexpr int NSUB = FAST_FAR ? 4 : 1;
+                    constexpr int SUB = TILE / NSUB;
+#pragma unroll 1
+                    for (int sq = 0; sq < NSUB; ++sq) {
+                    const int pa = sq * SUB, pz = min(np, pa + SUB);
+                    if ((far_mask >> sq) & 1u) {
                         // lanes of targets past the end compute values that are never stored; four
                         // panels per trip give the scheduler independent chains to interleave. A
                         // zero-strength panel must be skipped: only its strength slot is written
                         // (its other fields may hold anything, and 0 times NaN is NaN)
 #pragma unroll 4
-                        for (int p = 0; p < np; ++p) {
+                        for (int p = pa; p < pz; ++p) {
                             const float* v = reinterpret_cast<const float*>(tile[buf][p].v);
                             const float gam = v[kRec32Gamma];
                             if (gam == 0.f) continue;  // uniform across the CTA
@@ -544,8 +558,9 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
                             const float2 e2s = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
                             doublet2(bc(v[35] * gam), v, ex, ey, ez, e2s, TX, TY, TZ);
                         }
+                        continue;
                     }
-                    for (int p = 0; p < (all_far ? 0 : np); ++p) {
+                    for (int p = pa; p < pz; ++p) {
                         const float* v = reinterpret_cast<const float*>(tile[buf][p].v);
                         if constexpr (CHAIN) {  // every pair near-field: the chain's segments
                             if (v[kChainAny] == 0.f) continue;  // uniform across the CTA
@@ -600,6 +615,7 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
                             TY = fma2(gm, ay, TY);
                             TZ = fma2(gm, az, TZ);
                         }
+                    }
                     }
                     const float txa[2] = {TX.x, TX.y}, tya[2] = {TY.x, TY.y}, tza[2] = {TZ.x, TZ.y};
 #pragma unroll
