@@ -329,6 +329,11 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
     __shared__ __align__(8) uint64_t bar[NS];
     __shared__ unsigned s_done[NS];    // releases of the stage in this launch (kWarps per tile)
     __shared__ unsigned s_issued[NS];  // copies issued into the stage in this launch
+    // FP32 panel sweeps (capped at 96 registers): a thread's running sums and compensations (x,
+    // y, z sums of its two targets, then their compensations) between tiles. Touched once a
+    // tile, they leave the registers to the tile loop. (The chain sweeps keep them in registers.)
+    constexpr bool SMEM_ACC = F32 && !CHAIN;
+    __shared__ float s_acc[SMEM_ACC ? 12 : 1][kBsThreads];
     __shared__ long long s_item;
     // the item's target tile, source chunk and panel range (read from shared memory where used,
     // so that no register holds them through the tile loop)
@@ -418,10 +423,15 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
                 tw[u] = tw[t];
             }
         }
-        // running sums and compensations; for FP32 lane j of a float2 is target j
+        // running sums and compensations; for FP32 lane j of a float2 is target j (s_acc)
         R sx[TT], sy[TT], sz[TT], cx[TT], cy[TT], cz[TT];
+        if constexpr (SMEM_ACC) {
 #pragma unroll
-        for (int t = 0; t < TT; ++t) sx[t] = sy[t] = sz[t] = cx[t] = cy[t] = cz[t] = R(0);
+            for (int q = 0; q < 12; ++q) s_acc[q][tid] = 0.f;
+        } else {
+#pragma unroll
+            for (int t = 0; t < TT; ++t) sx[t] = sy[t] = sz[t] = cx[t] = cy[t] = cz[t] = R(0);
+        }
         float2 X2h, Y2h, Z2h, X2l, Y2l, Z2l;
         if constexpr (F32) {
             X2h = make_float2(xh[0], xh[1]); Y2h = make_float2(yh[0], yh[1]); Z2h = make_float2(zh[0], zh[1]);
@@ -497,16 +507,19 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
                     // every lane: the warp evaluates the doublets alone, without the test and the
                     // votes. Quarters keep the boxes compact where a tile holds the end of one wing's
                     // row of panels and the start of the next.
-                    unsigned far_mask = 0;  // bit q: sub-tile q is all far
+                    unsigned far_mask = 0;   // bit q: sub-tile q is all far
+                    unsigned zero_mask = 0;  // bit q: sub-tile q holds a zero-strength panel
                     if constexpr (FAST_FAR) {
                         static_assert(TILE % 32 == 0, "the fast path's sub-tiles are 8 lanes x TILE / 32 panels");
                         constexpr int PPL = TILE / 32;  // panels per lane; sub-tile q = lanes 8q .. 8q + 7
                         float c7[7] = {CUDART_INF_F, CUDART_INF_F, CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F,
                                        0.f};
+                        bool zero = false;  // a zero-strength panel: skipped, so not in the box
 #pragma unroll
                         for (int j = 0; j < PPL; ++j) {
                             const int q = PPL * lane + j;
-                            if (q < np) {
+                            if (q < np && tile[buf][q].v[kRec32Gamma] == 0.f) zero = true;
+                            else if (q < np) {
                                 const float4 c = *reinterpret_cast<const float4*>(&tile[buf][q].v[28]);  // centre hi, ff2
                                 c7[0] = fminf(c7[0], c.x);
                                 c7[1] = fminf(c7[1], c.y);
@@ -536,6 +549,9 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
                         const unsigned b =
                             __ballot_sync(0xffffffffu, c7[6] < CUDART_INF_F && gx * gx + gy * gy + gz * gz > 1.001f * c7[6]);
                         far_mask = (b & 1u) | ((b >> 7) & 2u) | ((b >> 14) & 4u) | ((b >> 21) & 8u);
+                        const unsigned z = __ballot_sync(0xffffffffu, zero);
+                        zero_mask = ((z & 0xffu) ? 1u : 0u) | ((z & 0xff00u) ? 2u : 0u) | ((z & 0xff0000u) ? 4u : 0u) |
+                                    ((z & 0xff000000u) ? 8u : 0u);
                     }
                     constexpr int NSUB = FAST_FAR ? 4 : 1;
                     constexpr int SUB = TILE / NSUB;
@@ -544,8 +560,22 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
                     const int pa = sq * SUB, pz = min(np, pa + SUB);
                     if ((far_mask >> sq) & 1u) {
                         // lanes of targets past the end compute values that are never stored; four
-                        // panels per trip give the scheduler independent chains to interleave. A
-                        // zero-strength panel must be skipped: only its strength slot is written
+                        // panels per trip give the scheduler independent chains to interleave, which
+                        // it can only do without a branch per panel: a sub-tile with no
+                        // zero-strength panel takes every panel
+                        if (!((zero_mask >> sq) & 1u)) {
+#pragma unroll 4
+                            for (int p = pa; p < pz; ++p) {
+                                const float* v = reinterpret_cast<const float*>(tile[buf][p].v);
+                                const float2 ex = sub2s(X2h, v[28]);
+                                const float2 ey = sub2s(Y2h, v[29]);
+                                const float2 ez = sub2s(Z2h, v[30]);
+                                const float2 e2s = fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
+                                doublet2(bc(v[35] * v[kRec32Gamma]), v, ex, ey, ez, e2s, TX, TY, TZ);
+                            }
+                            continue;
+                        }
+                        // a zero-strength panel must be skipped: only its strength slot is written
                         // (its other fields may hold anything, and 0 times NaN is NaN)
 #pragma unroll 4
                         for (int p = pa; p < pz; ++p) {
@@ -620,14 +650,34 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
                     const float txa[2] = {TX.x, TX.y}, tya[2] = {TY.x, TY.y}, tza[2] = {TZ.x, TZ.y};
 #pragma unroll
                     for (int t = 0; t < 2; ++t) {
-                        if (KAHAN) {
-                            two_sum_acc(sx[t], cx[t], static_cast<R>(txa[t]));
-                            two_sum_acc(sy[t], cy[t], static_cast<R>(tya[t]));
-                            two_sum_acc(sz[t], cz[t], static_cast<R>(tza[t]));
+                        if constexpr (!SMEM_ACC) {
+                            if (KAHAN) {
+                                two_sum_acc(sx[t], cx[t], txa[t]);
+                                two_sum_acc(sy[t], cy[t], tya[t]);
+                                two_sum_acc(sz[t], cz[t], tza[t]);
+                            } else {
+                                sx[t] += txa[t];
+                                sy[t] += tya[t];
+                                sz[t] += tza[t];
+                            }
                         } else {
-                            sx[t] += static_cast<R>(txa[t]);
-                            sy[t] += static_cast<R>(tya[t]);
-                            sz[t] += static_cast<R>(tza[t]);
+                            float ax = s_acc[t][tid], ay = s_acc[2 + t][tid], az = s_acc[4 + t][tid];
+                            if (KAHAN) {
+                                float bx = s_acc[6 + t][tid], by = s_acc[8 + t][tid], bz = s_acc[10 + t][tid];
+                                two_sum_acc(ax, bx, txa[t]);
+                                two_sum_acc(ay, by, tya[t]);
+                                two_sum_acc(az, bz, tza[t]);
+                                s_acc[6 + t][tid] = bx;
+                                s_acc[8 + t][tid] = by;
+                                s_acc[10 + t][tid] = bz;
+                            } else {
+                                ax += txa[t];
+                                ay += tya[t];
+                                az += tza[t];
+                            }
+                            s_acc[t][tid] = ax;
+                            s_acc[2 + t][tid] = ay;
+                            s_acc[4 + t][tid] = az;
                         }
                     }
                 } else {
@@ -670,6 +720,17 @@ __global__ void __launch_bounds__(kBsThreads, (sizeof(R) == 4 && !CHAIN) ? 5 : 1
 
         const long long ttile_out = s_ttile;
         const int chunk = s_chunk;
+        if constexpr (SMEM_ACC) {
+#pragma unroll
+            for (int t = 0; t < TT; ++t) {
+                sx[t] = s_acc[t][tid];
+                sy[t] = s_acc[2 + t][tid];
+                sz[t] = s_acc[4 + t][tid];
+                cx[t] = s_acc[6 + t][tid];
+                cy[t] = s_acc[8 + t][tid];
+                cz[t] = s_acc[10 + t][tid];
+            }
+        }
 #pragma unroll
         for (int t = 0; t < T; ++t) {
             const long long slot = ttile_out * TM + (FAST_FAR ? static_cast<long long>(tid) * T + t
