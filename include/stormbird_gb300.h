@@ -281,9 +281,10 @@ int sb_panel_sweep(int device, const double* corners, const double* strengths, c
  * sizes: SB_ERR_SIZE). Work is enqueued on `stream` (a cudaStream_t, NULL = the legacy
  * default stream) and the call returns when it has finished; the caller's current device is
  * the same after the call as before it. The first call on a device (and the first after
- * that device's context has been reset) resolves the array's device address; make that
- * first call before any stream capture begins. Every call shares the array: calls that
- * overlap on the GPU race and must be serialised.
+ * that device's context has been reset) resolves the array's device address. No call may
+ * be made while a stream is being captured: every call reads the error word back into host
+ * memory and synchronises `stream` before it returns. Every call shares the array: calls
+ * that overlap on the GPU race and must be serialised.
  */
 #define SB_NO_ALLOC_MAX_PANELS 16384
 #define SB_NO_ALLOC_MAX_TARGETS 65536
