@@ -398,7 +398,7 @@ int sb_batch_info(const sb_batch* batch, double* info, size_t n);
  * predicts, per panel, a correction to the solution extrapolated linearly in time, from
  * per-panel features the batch builds on the GPU. The SimpleIterative solve evaluates the
  * residual of the plain start, of the extrapolation and of extrapolation plus correction
- * and starts from the lowest, so the solver stays the judge of the result; the batch
+ * and starts from the lowest, so the solver alone decides the result; the batch
  * reports per case which start was taken.
  * =================================================================================== */
 typedef struct sb_mlp sb_mlp;

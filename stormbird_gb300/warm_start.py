@@ -8,7 +8,7 @@ plus a correction a network predicts per panel from features the batch builds on
 (previous solution and its neighbours, its last change, freestream change, geometric angle of
 attack, span position, sail index and counts, wake fill). The solve evaluates the residual of
 the plain start, of the extrapolation and of extrapolation plus correction and starts from
-the lowest, so the fallback is decided per case and step and the solver remains the judge of
+the lowest, so the fallback is decided per case and step and the solver alone decides
 the result.
 A network whose output layer is zero gives the extrapolation alone (`extrapolation_only`),
 the ablation that separates what the trained network adds.
